@@ -1,0 +1,221 @@
+/*
+ * svgpu.h -- C ABI of libsvgpu.so, the sm_103a (GB300) implementation of the
+ * scaled Vecchia hot path (Katzfuss, Guinness & Lawrence 2020/22).
+ *
+ * Every entry point is a plain C function over caller-owned DEVICE buffers
+ * (pointers + sizes), stream-ordered on `stream` (NULL = legacy default
+ * stream).  Nothing here allocates device memory: each call that needs
+ * scratch memory takes a caller-provided workspace whose size is returned by
+ * the matching *_workspace_bytes query.  Errors detected on the device (a
+ * failed block Cholesky, a wait that ran out of its iteration limit) are
+ * written to a caller-provided device `info` word array and become visible
+ * once the stream is synchronised; launch/argument errors are returned
+ * directly.  No C++ exception crosses this boundary.
+ *
+ * Each declaration names the reference function (jdtuck/pyscaledvecchia,
+ * paths relative to src/scaled_vecchia/) whose behaviour it reproduces.
+ */
+#ifndef SVGPU_H
+#define SVGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* sv_stream_t; /* identical to cudaStream_t */
+
+/* status codes (returned, and in info[0]) */
+#define SV_OK 0
+#define SV_EINVAL 1   /* bad argument / unsupported size -> ValueError */
+#define SV_ECHOL 2    /* block Cholesky failed even with jitter -> LinAlgError */
+#define SV_ETIMEOUT 3 /* a bounded device wait ran out -> RuntimeError */
+#define SV_ECUDA 4    /* CUDA runtime error (see sv_last_cuda_error) */
+#define SV_ENOSPC 5   /* workspace too small */
+
+/* layout of the device `info` array used by the calls below (int32[4]) */
+#define SV_INFO_STATUS 0     /* SV_* status of the device work */
+#define SV_INFO_BLOCK 1      /* first failing block / row, or -1 */
+#define SV_INFO_JITTER 2     /* largest jitter level used (0 = none, 1..9 = 1e-12..1e-4) */
+#define SV_INFO_AUX 3
+
+const char* sv_status_string(int status);
+int sv_abi_version(void);
+/* last cudaError_t recorded by a call that returned SV_ECUDA */
+int sv_last_cuda_error(void);
+
+/* ---------------------------------------------------------------------- */
+/* Ordering (ordering.py)                                                  */
+/* ---------------------------------------------------------------------- */
+
+/* Exact maximin ordering: replaces ordering.py:27-59 (_maximin_core; the
+ * caller supplies `first` as ordering.py:72 computes it).  X is (n, d)
+ * row-major float64; order receives n int64 indices.  Bit-exact: IEEE
+ * sequential squared distances without FMA, correctly rounded sqrt, strict
+ * '>' argmax with the smallest index winning ties, strict '<' updates. */
+size_t sv_maximin_workspace_bytes(int64_t n, int32_t d);
+int sv_maximin_order(const double* X, int64_t n, int32_t d, int64_t first, int64_t* order,
+                     int32_t* info, void* workspace, size_t workspace_bytes, sv_stream_t stream);
+
+/* Ordered nearest neighbours: replaces ordering.py:76-116 (find_ordered_nn).
+ * nn is (n, m+1) int64: column 0 = row index, columns 1..min(i,m) the nearest
+ * rows j < i (nearest first, ties to the smaller index), -1 padding; rows
+ * 1..start-1 keep only their self column, as in the reference. */
+size_t sv_ordered_knn_workspace_bytes(int64_t n, int32_t d);
+int sv_ordered_knn(const double* X, int64_t n, int32_t d, int32_t m, int64_t start, int64_t* nn,
+                   int32_t* info, void* workspace, size_t workspace_bytes, sv_stream_t stream);
+
+/* k nearest reference rows of every query row, sorted nearest first:
+ * replaces gp.py:253-255 (cKDTree(X_tr / lambda).query(X_star / lambda, k=m)).
+ * nb is (nq, k) int64. */
+size_t sv_knn_query_workspace_bytes(int64_t nref, int64_t nq, int32_t d);
+int sv_knn_query(const double* Xref, int64_t nref, const double* Xq, int64_t nq, int32_t d,
+                 int32_t k, int64_t* nb, int32_t* info, void* workspace, size_t workspace_bytes,
+                 sv_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Likelihood (likelihood.py)                                              */
+/* ---------------------------------------------------------------------- */
+
+typedef struct sv_loglik_desc {
+  int64_t n;            /* rows of X, y, Z (Vecchia order)                      */
+  int64_t nblk;         /* conditioning blocks                                  */
+  int64_t nblk_warp;    /* leading blocks with k+1 <= 32 (warp kernel);        */
+                        /* the rest (k+1 > 32) go to the CTA kernel            */
+  int32_t d;            /* input dimension                                      */
+  int32_t q;            /* trend columns (0 = none)                             */
+  int32_t ldnbr;        /* row stride of nbr                                    */
+  int32_t kmax;         /* largest conditioning-set size k                      */
+  int32_t need_grad;    /* 1: score and Fisher information too                 */
+  int32_t estimate_nu;  /* 1: theta = [log s2, log lam.., log nu, log tau]     */
+  int32_t chunked;      /* 1: chunk[] gives the jitter-sharing chunk of a block */
+  int32_t precision;    /* 0 = float64 throughout                               */
+  double nu;            /* fixed smoothness (estimate_nu = 0)                   */
+  double var_penalty;   /* likelihood.py:165-171                                */
+  double log_var_target;
+} sv_loglik_desc;
+
+/* Profile Vecchia log-likelihood, score and Fisher information with GLS
+ * profiling of the trend: replaces likelihood.py:66-175
+ * (vecchia_profile_loglik), including _block_cov / _block_cov_general,
+ * _batch_chol, _backsolve_LT and _forward_solve on its path.
+ *   theta : device float64[P], P = d+2 (+1 if estimate_nu)
+ *   block b: self row rowb[b], neighbours nbr[b*ldnbr + 0..kb[b]-1]
+ *   chunk : device int32[nblk] chunk ids (desc->chunked) or NULL
+ *   out   : device float64[1 + P + P*P + q] = ll, grad, fish (row-major), beta
+ *   info  : device int32[4] (SV_INFO_*) */
+size_t sv_loglik_workspace_bytes(const sv_loglik_desc* desc);
+int sv_vecchia_loglik(const sv_loglik_desc* desc, const double* theta, const double* X,
+                      const double* y, const double* Z, const int32_t* rowb, const int32_t* kb,
+                      const int32_t* nbr, const int32_t* chunk, double* out, int32_t* info,
+                      void* workspace, size_t workspace_bytes, sv_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Matern correlation (elementwise)                                        */
+/* ---------------------------------------------------------------------- */
+
+/* which = 0: M_nu(r); which = 1: g(r) = M_nu'(r)/r.
+ * general = 0: closed forms, nu in {0.5,1.5,2.5}: _covariance.py:49-72.
+ * general = 1: Bessel form 2^(1-nu)/Gamma(nu) c^nu K_nu(c), c = sqrt(2nu) r,
+ *              r floored at 1e-7: _matern_general.py:87-116. */
+int sv_matern_eval(const double* r, int64_t n, double nu, int32_t which, int32_t general,
+                   double* out, sv_stream_t stream);
+
+/* Modified Bessel function of the second kind K_nu(x) (device Temme/Steed
+ * evaluation; stands in for scipy.special.kv on the _matern_general.py path). */
+int sv_bessel_k(const double* x, int64_t n, double nu, double* out, sv_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Block-level routines (_covariance.py)                                   */
+/* ---------------------------------------------------------------------- */
+
+/* Sigma (B,K,K) and dSigma (B,P,K,K) of B blocks of K points:
+ * replaces _covariance.py:150-198 (_block_cov) and _matern_general.py:134-179
+ * (_block_cov_general).  Xb (B,K,d); ranges (d) host; nug_mask (B,K) or NULL.
+ * dS may be NULL (derivs=False).  estimate_nu adds the log-nu row (FD h). */
+int sv_block_cov(const double* Xb, int64_t B, int32_t K, int32_t d, const double* ranges_host,
+                 double variance, double nugget, double nu, int32_t general, int32_t estimate_nu,
+                 double nu_fd_h, const double* nug_mask, double* Sigma, double* dS,
+                 sv_stream_t stream);
+
+/* Batched lower Cholesky with the jitter retry of _covariance.py:235-252
+ * (_batch_chol): if any block fails, all blocks are retried with
+ * 10^p * mean(diag) for p = -12..-4 (the first p where every block succeeds).
+ * info[SV_INFO_JITTER] = level used; info[0] = SV_ECHOL if all fail. */
+size_t sv_batch_chol_workspace_bytes(int64_t B);
+int sv_batch_chol(const double* Sigma, int64_t B, int32_t K, double* L, int32_t* info,
+                  void* workspace, size_t workspace_bytes, sv_stream_t stream);
+
+/* Batched triangular solves: replaces _covariance.py:205-218 (_forward_solve,
+ * L X = B) and :220-232 (_backsolve_LT, L^T X = B).  L (b,K,K), B/X (b,K,nrhs). */
+int sv_forward_solve(const double* L, const double* Bm, int64_t b, int32_t K, int32_t nrhs,
+                     double* Xout, sv_stream_t stream);
+int sv_backsolve_LT(const double* L, const double* Bm, int64_t b, int32_t K, int32_t nrhs,
+                    double* Xout, sv_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Prediction (gp.py)                                                      */
+/* ---------------------------------------------------------------------- */
+
+typedef struct sv_pred_desc {
+  int64_t nall;     /* rows of Xall                                    */
+  int64_t nobs;     /* rows < nobs carry the nugget (observations)     */
+  int64_t nblk;     /* prediction blocks                               */
+  int32_t d;
+  int32_t k;        /* neighbours per block (block size K = k+1)       */
+  int32_t ldnbr;
+  int32_t general;  /* 1: Bessel Matern                                */
+  int32_t target_nugget; /* 1: the target row carries the nugget too     */
+                         /*    (prior / unconditional draws)              */
+  double nu;
+} sv_pred_desc;
+
+/* One prediction block per target row tgt[b] (noise-free unless
+ * desc->target_nugget) with neighbours nbr[b*ldnbr + 0..k-1] (rows of Xall;
+ * rows >= nobs are noise-free; a -1 ends a row with fewer neighbours):
+ * replaces the per-chunk work of gp.py:257-276 (_predict_scaled) and
+ * gp.py:329-348 (_joint_factor).
+ *   theta : device float64[d+2] = [log s2, log lam_1..d, log tau]
+ *   resid : device float64[nobs] residuals of the observations
+ *   mean, var : device float64[nblk] (may be NULL)
+ *             mean = -sum_{i<k, obs} a_i resid / a_K (marginal form when all
+ *             neighbours are observations), var = 1 / a_K^2
+ *   acol  : device float64[nblk * (k+1)] column a = L^-T e_K laid out as
+ *           [neighbour slots 0..k-1, target], absent slots 0 (may be NULL)
+ *   rhs   : device float64[nblk] = -sum_{obs i} a_i resid_i (may be NULL) */
+int sv_predict_blocks(const sv_pred_desc* desc, const double* theta, const double* Xall,
+                      const int32_t* tgt, const int32_t* nbr, const double* resid, double* mean,
+                      double* var, double* acol, double* rhs, int32_t* info, sv_stream_t stream);
+
+/* Sparse triangular solve U_pp^T X = R of gp.py:380-401 (scipy
+ * spsolve_triangular), from the block columns of sv_predict_blocks.  With
+ * nobs = 0 and the columns of an ordered Vecchia factor it also draws
+ * unconditional Vecchia samples y = U^-T eps (no reference counterpart: the
+ * reference only samples conditionally, gp.py:395-401):
+ * row c: acol[c*(k+1)+k] x_c + sum_{i<k, nbr_ic >= nobs} acol[c*(k+1)+i] x_{nbr_ic - nobs} = R_c
+ * (entries with nbr_ic < 0 are absent).
+ * R and X are (npred, nrhs) row-major; rows are processed in order with
+ * bounded waits on their predecessors (info[0] = SV_ETIMEOUT on expiry). */
+size_t sv_joint_solve_workspace_bytes(int64_t npred);
+int sv_joint_solve(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr, const int32_t* nbr,
+                   const double* acol, const double* R, int32_t nrhs, double* X, int32_t* info,
+                   void* workspace, size_t workspace_bytes, sv_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Measurement                                                             */
+/* ---------------------------------------------------------------------- */
+
+/* No reference counterpart: a float64 FMA throughput probe (8 independent
+ * chains of `iters` FMAs in each of sv_fp64_probe_threads() threads, one
+ * double written per thread to out), used to state the float64 peak that the
+ * block kernels are measured against. */
+int64_t sv_fp64_probe_threads(void);
+int sv_fp64_fma_probe(double* out, int32_t iters, sv_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVGPU_H */

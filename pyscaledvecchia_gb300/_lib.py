@@ -1,0 +1,159 @@
+"""ctypes binding of libsvgpu.so and the device-memory plumbing around it.
+
+Device buffers are torch CUDA tensors (torch is used only for allocation,
+streams and host<->device copies); every computation runs in the library's
+own sm_103a kernels.  There is no CPU fallback: without a CUDA device or
+without the built library every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import _build
+
+SV_OK, SV_EINVAL, SV_ECHOL, SV_ETIMEOUT, SV_ECUDA, SV_ENOSPC = range(6)
+
+_lock = threading.Lock()
+_lib = None
+
+c_i32, c_i64, c_dbl, c_sz, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_size_t, ctypes.c_void_p
+
+
+class LoglikDesc(ctypes.Structure):
+    """Mirror of sv_loglik_desc (include/svgpu.h)."""
+    _fields_ = [("n", c_i64), ("nblk", c_i64), ("nblk_warp", c_i64),
+                ("d", c_i32), ("q", c_i32), ("ldnbr", c_i32), ("kmax", c_i32),
+                ("need_grad", c_i32), ("estimate_nu", c_i32), ("chunked", c_i32),
+                ("precision", c_i32), ("nu", c_dbl), ("var_penalty", c_dbl),
+                ("log_var_target", c_dbl)]
+
+
+class PredDesc(ctypes.Structure):
+    """Mirror of sv_pred_desc (include/svgpu.h)."""
+    _fields_ = [("nall", c_i64), ("nobs", c_i64), ("nblk", c_i64), ("d", c_i32), ("k", c_i32),
+                ("ldnbr", c_i32), ("general", c_i32), ("target_nugget", c_i32), ("nu", c_dbl)]
+
+
+# name -> (restype, argtypes); every symbol declared in include/svgpu.h
+SIGNATURES = {
+    "sv_status_string": (ctypes.c_char_p, [c_i32]),
+    "sv_abi_version": (c_i32, []),
+    "sv_last_cuda_error": (c_i32, []),
+    "sv_maximin_workspace_bytes": (c_sz, [c_i64, c_i32]),
+    "sv_maximin_order": (c_i32, [c_vp, c_i64, c_i32, c_i64, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "sv_ordered_knn_workspace_bytes": (c_sz, [c_i64, c_i32]),
+    "sv_ordered_knn": (c_i32, [c_vp, c_i64, c_i32, c_i32, c_i64, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "sv_knn_query_workspace_bytes": (c_sz, [c_i64, c_i64, c_i32]),
+    "sv_knn_query": (c_i32, [c_vp, c_i64, c_vp, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "sv_loglik_workspace_bytes": (c_sz, [ctypes.POINTER(LoglikDesc)]),
+    "sv_vecchia_loglik": (c_i32, [ctypes.POINTER(LoglikDesc), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                  c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "sv_matern_eval": (c_i32, [c_vp, c_i64, c_dbl, c_i32, c_i32, c_vp, c_vp]),
+    "sv_bessel_k": (c_i32, [c_vp, c_i64, c_dbl, c_vp, c_vp]),
+    "sv_block_cov": (c_i32, [c_vp, c_i64, c_i32, c_i32, c_vp, c_dbl, c_dbl, c_dbl, c_i32, c_i32,
+                             c_dbl, c_vp, c_vp, c_vp, c_vp]),
+    "sv_batch_chol_workspace_bytes": (c_sz, [c_i64]),
+    "sv_batch_chol": (c_i32, [c_vp, c_i64, c_i32, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "sv_forward_solve": (c_i32, [c_vp, c_vp, c_i64, c_i32, c_i32, c_vp, c_vp]),
+    "sv_backsolve_LT": (c_i32, [c_vp, c_vp, c_i64, c_i32, c_i32, c_vp, c_vp]),
+    "sv_predict_blocks": (c_i32, [ctypes.POINTER(PredDesc), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                  c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "sv_joint_solve_workspace_bytes": (c_sz, [c_i64]),
+    "sv_fp64_probe_threads": (c_i64, []),
+    "sv_fp64_fma_probe": (c_i32, [c_vp, c_i32, c_vp]),
+    "sv_joint_solve": (c_i32, [c_i64, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp,
+                               c_vp, c_sz, c_vp]),
+}
+
+
+def library_path() -> str:
+    return _build.LIBPATH
+
+
+def load_library(check_current: bool = True):
+    """dlopen libsvgpu.so and attach the prototypes (no CUDA call is made)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIBPATH
+        if not os.path.exists(path):
+            raise RuntimeError(
+                f"{path} is missing: build the CUDA extension first "
+                "(python -c 'import __graft_entry__ as g; g.build()')")
+        if check_current and not _build.is_current():
+            raise RuntimeError(f"{path} is stale relative to csrc/: rebuild it")
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def device_ready():
+    """Load the library and make sure a CUDA device is present (else raise)."""
+    torch = _torch()
+    if not torch.cuda.is_available():
+        raise RuntimeError("scaled Vecchia GPU kernels need a CUDA device; none is available")
+    return load_library(), torch
+
+
+def stream_handle(torch):
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def to_dev(torch, arr, dtype):
+    """numpy -> device tensor (contiguous)."""
+    a = np.ascontiguousarray(arr, dtype=dtype)
+    t = torch.from_numpy(a)
+    if a.size:
+        t = t.pin_memory() if a.nbytes >= (1 << 20) else t
+    return t.to("cuda", non_blocking=True)
+
+
+def ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else ctypes.c_void_p(0)
+
+
+def new_info(torch):
+    return torch.zeros(4, dtype=torch.int32, device="cuda")
+
+
+def workspace(torch, nbytes):
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device="cuda")
+
+
+def check(lib, rc, what):
+    """Map a returned status to the reference's exceptions."""
+    if rc == SV_OK:
+        return
+    msg = lib.sv_status_string(rc).decode()
+    if rc == SV_EINVAL:
+        raise ValueError(f"{what}: {msg}")
+    if rc == SV_ECHOL:
+        raise np.linalg.LinAlgError("block Cholesky failed even with jitter")
+    if rc == SV_ECUDA:
+        raise RuntimeError(f"{what}: CUDA error {lib.sv_last_cuda_error()}")
+    raise RuntimeError(f"{what}: {msg}")
+
+
+def check_info(lib, info_host, what):
+    st = int(info_host[0])
+    if st == SV_OK:
+        return
+    if st == SV_ECHOL:
+        raise np.linalg.LinAlgError("block Cholesky failed even with jitter")
+    if st == SV_ETIMEOUT:
+        raise RuntimeError(f"{what}: a bounded device wait ran out (row/step {int(info_host[1])})")
+    check(lib, st, what)

@@ -1,0 +1,182 @@
+// Team-level building blocks of the Vecchia block kernels.
+//
+// A "team" of T threads owns one conditioning block at a time: T = 32 is one
+// warp (blocks of size K <= 32), T = blockDim.x is a whole CTA (K > 32).  All
+// of a team's data lives in shared memory; work inside a step is spread over
+// the team's lanes with a strided loop, steps are separated by team barriers.
+//
+// Storage of a K x K symmetric/lower matrix is the packed lower triangle,
+// row-major: entry (i, j), i >= j, at i(i+1)/2 + j.
+#pragma once
+#include "sv_common.cuh"
+#include "sv_matern.cuh"
+
+namespace sv {
+
+template <int T>
+struct Team {
+  // T == 32: one warp; T > 32: the whole CTA (T == blockDim.x)
+  __device__ __forceinline__ static int lane() { return T == 32 ? (threadIdx.x & 31) : threadIdx.x; }
+  __device__ __forceinline__ static void sync() {
+    if (T == 32)
+      __syncwarp();
+    else
+      __syncthreads();
+  }
+};
+
+// Matern evaluation mode of a block
+struct MaternMode {
+  int closed;          // 0/1/2 for nu = 0.5/1.5/2.5, -1 = general (Bessel)
+  int estimate_nu;     // also dM/dnu by central difference
+  double nu;           // smoothness
+  double log_coef;     // (1-nu) ln2 - lgamma(nu)
+  double nu_p, nu_m;   // nu +- h
+  double lc_p, lc_m;   // log_coef at nu +- h
+  double inv2h;        // 1 / (2h)
+};
+
+__device__ __forceinline__ void matern_eval(const MaternMode& mm, double r, double& M, double& g,
+                                            double& dMnu, bool want_g) {
+  if (mm.closed >= 0) {
+    matern_closed(mm.closed, r, M, g);
+    dMnu = 0.0;
+    return;
+  }
+  if (want_g) {
+    matern_general_Mg(r, mm.nu, mm.log_coef, M, g);
+  } else {
+    M = matern_general_M(r, mm.nu, mm.log_coef);
+    g = 0.0;
+  }
+  if (mm.estimate_nu) {
+    // _matern_general.py:170-176 (central difference in nu)
+    const double Mp = matern_general_M(r, mm.nu_p, mm.lc_p);
+    const double Mm = matern_general_M(r, mm.nu_m, mm.lc_m);
+    dMnu = (Mp - Mm) * mm.inv2h;
+  } else {
+    dMnu = 0.0;
+  }
+}
+
+// Assemble the packed lower triangle of Sigma (+ jitter on the diagonal) for
+// a block whose scaled coordinates u (K x d, row-major) are in shared memory.
+//   nug[i]  : nugget multiplier of entry i (1 observation, 0 noise-free)
+//   Gp, Dp  : optional packed -s2*g and s2*nu*dM/dnu (derivative factors)
+template <int T>
+__device__ void assemble_sigma(int K, int d, const double* u, const double* nugmask, double s2,
+                               double tau, double jit, const MaternMode& mm, double* Lp,
+                               double* Gp, double* Dp) {
+  const int lane = Team<T>::lane();
+  const int npair = K * (K + 1) / 2;
+  for (int t = lane; t < npair; t += T) {
+    int i, j;
+    tri_index(t, i, j);
+    const double* ui = u + i * d;
+    const double* uj = u + j * d;
+    double s = 0.0;
+    for (int l = 0; l < d; ++l) {
+      const double df = ui[l] - uj[l];
+      s += df * df;
+    }
+    const double r = sqrt(s);
+    double M, g, dMnu;
+    matern_eval(mm, r, M, g, dMnu, Gp != nullptr);
+    double nug = 0.0;
+    if (i == j) nug = tau * (nugmask ? nugmask[i] : 1.0);
+    double v = s2 * (M + nug);
+    if (i == j) v += jit;
+    Lp[t] = v;
+    if (Gp) Gp[t] = -s2 * g;
+    if (Dp) Dp[t] = s2 * mm.nu * dMnu;
+  }
+}
+
+// In-place right-looking Cholesky of the packed lower triangle.  Pivots
+// follow LAPACK dpotrf: a pivot that is not > 0 (or NaN) fails.  On success
+// invd[k] = 1/L_kk.  Returns true on success (team-uniform).
+template <int T>
+__device__ bool cholesky_packed(int K, double* Lp, double* invd, volatile int* flag) {
+  const int lane = Team<T>::lane();
+  for (int k = 0; k < K; ++k) {
+    const int kk = tri_off(k, k);
+    if (lane == 0) {
+      const double dkk = Lp[kk];
+      if (!(dkk > 0.0)) {
+        *flag = 1;
+      } else {
+        const double lkk = sqrt(dkk);
+        Lp[kk] = lkk;
+        invd[k] = 1.0 / lkk;
+      }
+    }
+    Team<T>::sync();
+    if (*flag) return false;
+    const double inv = invd[k];
+    for (int i = k + 1 + lane; i < K; i += T) Lp[tri_off(i, k)] *= inv;
+    Team<T>::sync();
+    const int m = K - k - 1;
+    const int cnt = m * (m + 1) / 2;
+    for (int t = lane; t < cnt; t += T) {
+      int ii, jj;
+      tri_index(t, ii, jj);
+      const int i = k + 1 + ii, j = k + 1 + jj;
+      Lp[tri_off(i, j)] -= Lp[tri_off(i, k)] * Lp[tri_off(j, k)];
+    }
+    Team<T>::sync();
+  }
+  return true;
+}
+
+// a = L^-T e_K (the block's column of the sparse inverse Cholesky factor).
+// acc is K doubles of scratch.
+template <int T>
+__device__ void backsolve_eK(int K, const double* Lp, const double* invd, double* a, double* acc) {
+  const int lane = Team<T>::lane();
+  for (int i = lane; i < K; i += T) acc[i] = (i == K - 1) ? 1.0 : 0.0;
+  Team<T>::sync();
+  for (int i = K - 1; i >= 0; --i) {
+    // a_i = acc_i / L_ii, then acc_j -= L_ij a_i for j < i
+    const double ai = acc[i] * invd[i];
+    for (int j = lane; j < i; j += T) acc[j] -= Lp[tri_off(i, j)] * ai;
+    if (lane == 0) a[i] = ai;
+    Team<T>::sync();
+  }
+}
+
+// Forward solve L W = R for NR right-hand sides stored column-major with
+// leading dimension ldr (R[c*ldr + i]), in place.
+template <int T>
+__device__ void forward_solve_multi(int K, const double* Lp, const double* invd, double* R, int NR,
+                                    int ldr) {
+  const int lane = Team<T>::lane();
+  for (int i = 0; i < K; ++i) {
+    for (int c = lane; c < NR; c += T) R[c * ldr + i] *= invd[i];
+    Team<T>::sync();
+    const int m = K - i - 1;
+    const int cnt = m * NR;
+    for (int t = lane; t < cnt; t += T) {
+      const int c = t / m;
+      const int j = i + 1 + (t - c * m);
+      R[c * ldr + j] -= Lp[tri_off(j, i)] * R[c * ldr + i];
+    }
+    Team<T>::sync();
+  }
+}
+
+// Team-wide sum of a per-lane value (result valid in every lane).
+template <int T>
+__device__ double team_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (T == 32) return v;
+  const int w = threadIdx.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int k = 0; k < T / 32; ++k) s += red[k];
+  __syncthreads();
+  return s;
+}
+
+}  // namespace sv

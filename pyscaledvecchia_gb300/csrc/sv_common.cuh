@@ -1,0 +1,62 @@
+// Shared definitions for the scaled Vecchia sm_103a kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/svgpu.h"
+
+#ifndef SV_HOST_DEVICE
+#define SV_HOST_DEVICE __host__ __device__ __forceinline__
+#endif
+
+#define SV_CUDA_TRY(expr)                                   \
+  do {                                                      \
+    cudaError_t e_ = (expr);                                \
+    if (e_ != cudaSuccess) return sv_record_cuda_error(e_); \
+  } while (0)
+
+// Bounded spin-waits: a wait that runs out of iterations sets this status in
+// the kernel's error word and the kernel returns instead of hanging.
+#define SV_SPIN_LIMIT (1u << 26)
+
+int sv_record_cuda_error(cudaError_t e);
+int sv_num_sms();
+
+namespace sv {
+
+__device__ __forceinline__ void set_error(int32_t* err, int32_t code) {
+  if (err) atomicCAS(err, 0, code);
+}
+
+// acquire / release accessors for inter-CTA flags (PTX memory model)
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_acquire_s32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_s32(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned atom_add_release_u32(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+// Row/column of the t-th entry of a packed lower triangle (row-major, i >= j).
+__device__ __forceinline__ void tri_index(int t, int& i, int& j) {
+  int r = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+  // correct the float estimate
+  while ((r + 1) * (r + 2) / 2 <= t) ++r;
+  while (r * (r + 1) / 2 > t) --r;
+  i = r;
+  j = t - r * (r + 1) / 2;
+}
+__device__ __forceinline__ int tri_off(int i, int j) { return i * (i + 1) / 2 + j; }
+
+}  // namespace sv

@@ -1,0 +1,344 @@
+// Exact k-nearest-neighbour searches on the GPU.
+//
+//   ordered : ordering.py:76-116 (find_ordered_nn): row i takes the min(i, m)
+//             nearest rows j < i;
+//   query   : gp.py:253-255 (cKDTree.query): each query row takes the k
+//             nearest reference rows.
+//
+// Tiled brute force.  A CTA owns a tile of Q query rows (one thread each,
+// coordinates in registers) and streams candidate tiles of C rows through
+// shared memory.  The screening distance is float32 on coordinates centred on
+// the centroid; a candidate whose float32 lower bound (same error analysis as
+// the maximin kernel: s32 >= (sqrt(s64_k)(1+(d+4)2^-53) + B_i + B_j)^2
+// (1+2^-24)^(D+2), formed with upward rounding) cannot beat the current k-th
+// best is skipped, every other one is measured exactly (IEEE sequential
+// float64, no FMA) and inserted into the thread's sorted list.  Candidates
+// are visited in increasing index order, so equal float64 distances keep the
+// smaller index: the selected set is the exact (distance, index) order.
+#include "sv_common.cuh"
+
+namespace sv {
+
+constexpr int kKnnQ = 128;  // queries per CTA (one per thread)
+constexpr int kKnnC = 128;  // candidates per shared-memory tile
+
+// prologue: centred float32 coordinates (zero padded to DP) and their bound
+__global__ void k_knn_prep(const double* X, int64_t n, int d, int DP, const double* centroid,
+                           float* v, float* B) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double e2 = 0.0;
+    for (int l = 0; l < DP; ++l) {
+      float f = 0.0f;
+      if (l < d) {
+        const double c = X[i * d + l] - centroid[l];
+        f = __double2float_rn(c);
+        e2 += c * c;
+      }
+      v[i * DP + l] = f;
+    }
+    B[i] = __double2float_ru(1.01 * 0x1p-24 * sqrt(e2));
+  }
+}
+
+__global__ void k_centroid2(const double* X, int64_t n, int d, double* c) {
+  const int l = blockIdx.x;
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += X[i * d + l];
+  __shared__ double red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) c[l] = n > 0 ? red[0] / (double)n : 0.0;
+}
+
+struct KnnArgs {
+  const double* Xq;    // query rows (float64)
+  const double* Xr;    // reference rows (float64)
+  const float* vq;     // query rows, centred float32 [nq][DP]
+  const float* vr;     // reference rows [nr][DP]
+  const float* Bq;
+  const float* Br;
+  int64_t nq, nr;
+  int d, k, m;
+  int64_t start;       // ordered: first row to fill
+  int64_t* out;        // ordered: (n, m+1); query: (nq, k)
+  float growth;        // (1+2^-24)^(DP+2) (1+2^-20), rounded up
+  int ordered;
+};
+
+__device__ __forceinline__ float knn_thr(double s64k, float Bi, int d) {
+  const double t = (sqrt(s64k) * (1.0 + (double)(d + 4) * 0x1p-53) + (double)Bi) * (1.0 + 0x1p-40);
+  return __double2float_ru(t);
+}
+
+template <int DP>
+__global__ void __launch_bounds__(kKnnQ) k_knn(KnnArgs A) {
+  extern __shared__ unsigned char smraw[];
+  float* tile = (float*)smraw;                     // [C][DP]
+  float* tileB = tile + kKnnC * DP;                // [C]
+  double* lsd = (double*)(tileB + kKnnC);          // [k][Q] squared distances
+  int* lsi = (int*)(lsd + (size_t)A.k * kKnnQ);    // [k][Q] indices
+
+  const int64_t ntile = (A.nq + kKnnQ - 1) / kKnnQ;
+  // largest tiles first (ordered search work grows with the row index)
+  const int64_t qt = A.ordered ? (ntile - 1 - blockIdx.x) : blockIdx.x;
+  const int64_t i = qt * kKnnQ + threadIdx.x;
+  const bool valid = i < A.nq;
+  const int tid = threadIdx.x;
+
+  int kq = A.k;
+  if (A.ordered) kq = (int)min((int64_t)A.m, i);
+  bool active = valid && kq > 0;
+  if (A.ordered && i < A.start) active = false;
+
+  float qv[DP];
+  float Bi = 0.0f;
+  const double* xq = A.Xq + (valid ? i : 0) * A.d;
+#pragma unroll
+  for (int l = 0; l < DP; ++l) qv[l] = valid ? A.vq[i * DP + l] : 0.0f;
+  if (valid) Bi = A.Bq[i];
+
+  int cnt = 0;
+  float T = __int_as_float(0x7f800000);  // +inf until the list is full
+
+  // candidate range
+  int64_t cend = A.nr;
+  if (A.ordered) cend = min(A.nq, (qt + 1) * kKnnQ);  // rows < last query of the tile
+  for (int64_t c0 = 0; c0 < cend; c0 += kKnnC) {
+    __syncthreads();
+    const int nc = (int)min((int64_t)kKnnC, cend - c0);
+    for (int e = tid; e < nc * DP; e += blockDim.x) tile[e] = A.vr[c0 * DP + e];
+    for (int e = tid; e < nc; e += blockDim.x) tileB[e] = A.Br[c0 + e];
+    __syncthreads();
+    if (!active) continue;
+    int cmax = nc;
+    if (A.ordered) {
+      const int64_t lim = i - c0;  // candidates j < i
+      if (lim <= 0) continue;
+      if (lim < cmax) cmax = (int)lim;
+    }
+    for (int c = 0; c < cmax; ++c) {
+      const float* tv = tile + c * DP;
+      float s32 = 0.0f;
+#pragma unroll
+      for (int l = 0; l < DP; l += 4) {
+        const float4 t4 = *reinterpret_cast<const float4*>(tv + l);
+        float df = __fsub_rn(qv[l], t4.x);
+        s32 = __fmaf_rn(df, df, s32);
+        df = __fsub_rn(qv[l + 1], t4.y);
+        s32 = __fmaf_rn(df, df, s32);
+        df = __fsub_rn(qv[l + 2], t4.z);
+        s32 = __fmaf_rn(df, df, s32);
+        df = __fsub_rn(qv[l + 3], t4.w);
+        s32 = __fmaf_rn(df, df, s32);
+      }
+      const float tb = __fadd_ru(T, tileB[c]);
+      const float bound = __fmul_ru(__fmul_ru(tb, tb), A.growth);
+      if (s32 >= bound) continue;
+      // exact float64 squared distance (IEEE sequential, no FMA)
+      const int64_t j = c0 + c;
+      const double* xr = A.Xr + j * A.d;
+      double s = 0.0;
+      for (int l = 0; l < A.d; ++l) {
+        const double df = __dsub_rn(xq[l], xr[l]);
+        s = __dadd_rn(s, __dmul_rn(df, df));
+      }
+      if (cnt == kq) {
+        if (!(s < lsd[(kq - 1) * kKnnQ + tid])) continue;  // later index loses ties
+        --cnt;
+      }
+      int p = cnt;
+      while (p > 0 && lsd[(p - 1) * kKnnQ + tid] > s) {
+        lsd[p * kKnnQ + tid] = lsd[(p - 1) * kKnnQ + tid];
+        lsi[p * kKnnQ + tid] = lsi[(p - 1) * kKnnQ + tid];
+        --p;
+      }
+      lsd[p * kKnnQ + tid] = s;
+      lsi[p * kKnnQ + tid] = (int)j;
+      ++cnt;
+      if (cnt == kq) T = knn_thr(lsd[(kq - 1) * kKnnQ + tid], Bi, A.d);
+    }
+  }
+  if (!valid) return;
+  if (A.ordered) {
+    int64_t* row = A.out + i * (int64_t)(A.m + 1);
+    row[0] = i;
+    for (int c = 0; c < A.m; ++c) row[1 + c] = (active && c < cnt) ? (int64_t)lsi[c * kKnnQ + tid] : -1;
+  } else {
+    int64_t* row = A.out + i * (int64_t)A.k;
+    for (int c = 0; c < A.k; ++c) row[c] = (c < cnt) ? (int64_t)lsi[c * kKnnQ + tid] : -1;
+  }
+}
+
+static int pad_dim(int d) {
+  if (d <= 4) return 4;
+  if (d <= 8) return 8;
+  if (d <= 12) return 12;
+  if (d <= 16) return 16;
+  if (d <= 24) return 24;
+  if (d <= 32) return 32;
+  if (d <= 48) return 48;
+  return 64;
+}
+
+static float growth_factor(int DP) {
+  double g = 1.0;
+  for (int i = 0; i < DP + 2; ++i) g *= (1.0 + 0x1p-24);
+  g *= (1.0 + 0x1p-20);
+  float gf = (float)g;
+  if ((double)gf < g) gf = nextafterf(gf, 2.0f);
+  return gf;
+}
+
+static int launch_knn(const KnnArgs& A, int DP, int64_t grid, size_t smem, cudaStream_t st) {
+  switch (DP) {
+#define SV_KNN_CASE(V)                                                                          \
+  case V:                                                                                       \
+    SV_CUDA_TRY(cudaFuncSetAttribute(k_knn<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     (int)smem));                                               \
+    k_knn<V><<<(unsigned)grid, kKnnQ, smem, st>>>(A);                                          \
+    break;
+    SV_KNN_CASE(4)
+    SV_KNN_CASE(8)
+    SV_KNN_CASE(12)
+    SV_KNN_CASE(16)
+    SV_KNN_CASE(24)
+    SV_KNN_CASE(32)
+    SV_KNN_CASE(48)
+    SV_KNN_CASE(64)
+#undef SV_KNN_CASE
+    default:
+      return SV_EINVAL;
+  }
+  SV_CUDA_TRY(cudaGetLastError());
+  return SV_OK;
+}
+
+static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace sv
+
+using namespace sv;
+
+extern "C" size_t sv_ordered_knn_workspace_bytes(int64_t n, int32_t d) {
+  const int DP = pad_dim(d > 0 ? d : 1);
+  return al256(sizeof(double) * 64) + al256(sizeof(float) * (size_t)(n > 0 ? n : 1) * DP) +
+         al256(sizeof(float) * (size_t)(n > 0 ? n : 1));
+}
+
+extern "C" size_t sv_knn_query_workspace_bytes(int64_t nref, int64_t nq, int32_t d) {
+  return sv_ordered_knn_workspace_bytes(nref, d) + sv_ordered_knn_workspace_bytes(nq, d);
+}
+
+static int knn_smem_ok(int DP, int k, size_t* smem) {
+  *smem = sizeof(float) * (size_t)kKnnC * DP + sizeof(float) * kKnnC +
+          (sizeof(double) + sizeof(int)) * (size_t)k * kKnnQ;
+  int dev = 0, maxsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return *smem <= (size_t)maxsm;
+}
+
+extern "C" int sv_ordered_knn(const double* X, int64_t n, int32_t d, int32_t m, int64_t start,
+                              int64_t* nn, int32_t* info, void* workspace, size_t workspace_bytes,
+                              sv_stream_t stream) {
+  if (n < 0 || d < 1 || d > 64 || m < 0 || start < 0 || (n > 0 && (!X || !nn)) || !info)
+    return SV_EINVAL;
+  if (n > 0x7fffffffLL) return SV_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  int32_t init_info[4] = {0, -1, 0, 0};
+  SV_CUDA_TRY(cudaMemcpyAsync(info, init_info, sizeof(init_info), cudaMemcpyHostToDevice, st));
+  if (n == 0) return SV_OK;
+  if (!workspace || workspace_bytes < sv_ordered_knn_workspace_bytes(n, d)) return SV_ENOSPC;
+  const int DP = pad_dim(d);
+  size_t smem;
+  if (!knn_smem_ok(DP, m > 0 ? m : 1, &smem)) return SV_EINVAL;
+  char* ws = (char*)workspace;
+  double* centroid = (double*)ws;
+  float* v = (float*)(ws + al256(sizeof(double) * 64));
+  float* B = (float*)((char*)v + al256(sizeof(float) * (size_t)n * DP));
+  k_centroid2<<<d, 256, 0, st>>>(X, n, d, centroid);
+  SV_CUDA_TRY(cudaGetLastError());
+  int64_t g = (n + 255) / 256;
+  if (g > 8LL * sv_num_sms()) g = 8LL * sv_num_sms();
+  k_knn_prep<<<(unsigned)g, 256, 0, st>>>(X, n, d, DP, centroid, v, B);
+  SV_CUDA_TRY(cudaGetLastError());
+  KnnArgs A;
+  A.Xq = X;
+  A.Xr = X;
+  A.vq = v;
+  A.vr = v;
+  A.Bq = B;
+  A.Br = B;
+  A.nq = n;
+  A.nr = n;
+  A.d = d;
+  A.k = m > 0 ? m : 1;
+  A.m = m;
+  A.start = start > 1 ? start : 1;
+  A.out = nn;
+  A.growth = growth_factor(DP);
+  A.ordered = 1;
+  const int64_t ntile = (n + kKnnQ - 1) / kKnnQ;
+  return launch_knn(A, DP, ntile, smem, st);
+}
+
+extern "C" int sv_knn_query(const double* Xref, int64_t nref, const double* Xq, int64_t nq,
+                            int32_t d, int32_t k, int64_t* nb, int32_t* info, void* workspace,
+                            size_t workspace_bytes, sv_stream_t stream) {
+  if (nref < 0 || nq < 0 || d < 1 || d > 64 || k < 1 || (nq > 0 && (!Xq || !nb)) ||
+      (nref > 0 && !Xref) || !info)
+    return SV_EINVAL;
+  if (nref > 0x7fffffffLL || nq > 0x7fffffffLL) return SV_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  int32_t init_info[4] = {0, -1, 0, 0};
+  SV_CUDA_TRY(cudaMemcpyAsync(info, init_info, sizeof(init_info), cudaMemcpyHostToDevice, st));
+  if (nq == 0) return SV_OK;
+  if (!workspace || workspace_bytes < sv_knn_query_workspace_bytes(nref, nq, d)) return SV_ENOSPC;
+  const int DP = pad_dim(d);
+  size_t smem;
+  if (!knn_smem_ok(DP, k, &smem)) return SV_EINVAL;
+  char* ws = (char*)workspace;
+  double* centroid = (double*)ws;
+  float* vr = (float*)(ws + al256(sizeof(double) * 64));
+  float* Br = (float*)((char*)vr + al256(sizeof(float) * (size_t)(nref > 0 ? nref : 1) * DP));
+  char* ws2 = ws + sv_ordered_knn_workspace_bytes(nref, d);
+  float* vq = (float*)(ws2 + al256(sizeof(double) * 64));
+  float* Bq = (float*)((char*)vq + al256(sizeof(float) * (size_t)nq * DP));
+  // one shift for both sets (the reference rows' centroid)
+  if (nref > 0) {
+    k_centroid2<<<d, 256, 0, st>>>(Xref, nref, d, centroid);
+  } else {
+    SV_CUDA_TRY(cudaMemsetAsync(centroid, 0, sizeof(double) * d, st));
+  }
+  SV_CUDA_TRY(cudaGetLastError());
+  int64_t g = (nref + 255) / 256;
+  if (g > 8LL * sv_num_sms()) g = 8LL * sv_num_sms();
+  if (nref > 0) k_knn_prep<<<(unsigned)(g > 0 ? g : 1), 256, 0, st>>>(Xref, nref, d, DP, centroid, vr, Br);
+  g = (nq + 255) / 256;
+  if (g > 8LL * sv_num_sms()) g = 8LL * sv_num_sms();
+  k_knn_prep<<<(unsigned)g, 256, 0, st>>>(Xq, nq, d, DP, centroid, vq, Bq);
+  SV_CUDA_TRY(cudaGetLastError());
+  KnnArgs A;
+  A.Xq = Xq;
+  A.Xr = Xref;
+  A.vq = vq;
+  A.vr = vr;
+  A.Bq = Bq;
+  A.Br = Br;
+  A.nq = nq;
+  A.nr = nref;
+  A.d = d;
+  A.k = k;
+  A.m = k;
+  A.start = 0;
+  A.out = nb;
+  A.growth = growth_factor(DP);
+  A.ordered = 0;
+  const int64_t ntile = (nq + kKnnQ - 1) / kKnnQ;
+  return launch_knn(A, DP, ntile, smem, st);
+}

@@ -1,0 +1,262 @@
+// Matern correlation M_nu(r), its radial factor g(r) = M_nu'(r)/r, and the
+// modified Bessel function K_nu used by the general-smoothness form.
+//
+// Closed forms (nu = 0.5, 1.5, 2.5) follow _covariance.py:49-72 and the
+// per-entry code of _covariance.py:111-147; the general form follows
+// _matern_general.py:87-116 (M = 2^(1-nu)/Gamma(nu) c^nu K_nu(c),
+// c = sqrt(2 nu) r, g via K_{nu-1}, r floored at 1e-7).
+//
+// K_nu(x) is evaluated with Temme's method (N. M. Temme, "On the numerical
+// evaluation of the modified Bessel function of the third kind", J. Comput.
+// Phys. 19 (1975) 324-337): write nu = N + mu with |mu| <= 1/2, get K_mu and
+// K_{mu+1} from Temme's power series (x <= 1.5) or from Steed's continued
+// fraction for the ratio together with Temme's normalising sum (x > 1.5), then
+// recur upward K_{a+1} = K_{a-1} + (2a/x) K_a.  The recurrence also yields
+// K_{nu-1}, which g needs.  1/Gamma(1 +- mu) come from the Taylor series of
+// 1/Gamma(1+z) about 0, whose coefficients were computed for this file to 20
+// digits with mpmath (they are the constants of Abramowitz & Stegun 6.1.34
+// shifted by one index).
+#pragma once
+#include <math.h>
+
+#ifndef SV_HD
+#define SV_HD __host__ __device__ __forceinline__
+#endif
+
+namespace sv {
+
+constexpr double kSqrt3 = 1.7320508075688772;
+constexpr double kSqrt5 = 2.23606797749979;
+constexpr double kPi = 3.141592653589793;
+constexpr double kLn2 = 0.6931471805599453;
+constexpr double kRFloor = 1e-7;  // _matern_general.py:87
+
+// 1/Gamma(1+z) = sum_k kRecipGammaTaylor[k] z^k, |z| <= 1/2
+SV_HD double recip_gamma_1p(double z) {
+  const double c[27] = {1.0,
+                        0.57721566490153286061,
+                        -0.65587807152025388108,
+                        -0.042002635034095235529,
+                        0.1665386113822914895,
+                        -0.042197734555544336748,
+                        -0.0096219715278769735621,
+                        0.0072189432466630995424,
+                        -0.0011651675918590651121,
+                        -0.00021524167411495097282,
+                        0.00012805028238811618615,
+                        -0.000020134854780788238656,
+                        -1.2504934821426706573e-6,
+                        1.1330272319816958824e-6,
+                        -2.0563384169776071035e-7,
+                        6.1160951044814158179e-9,
+                        5.0020076444692229301e-9,
+                        -1.1812745704870201446e-9,
+                        1.0434267116911005105e-10,
+                        7.782263439905071254e-12,
+                        -3.6968056186422057082e-12,
+                        5.100370287454475979e-13,
+                        -2.0583260535665067832e-14,
+                        -5.3481225394230179824e-15,
+                        1.2267786282382607902e-15,
+                        -1.1812593016974587695e-16,
+                        1.1866922547516003326e-18};
+  double s = c[26];
+  for (int k = 25; k >= 0; --k) s = s * z + c[k];
+  return s;
+}
+
+// Gamma_1(mu) = (1/Gamma(1-mu) - 1/Gamma(1+mu)) / (2 mu)   (odd part, no cancellation)
+// Gamma_2(mu) = (1/Gamma(1-mu) + 1/Gamma(1+mu)) / 2         (even part)
+SV_HD void temme_gammas(double mu, double& g1, double& g2, double& rg_plus, double& rg_minus) {
+  const double c[27] = {1.0,
+                        0.57721566490153286061,
+                        -0.65587807152025388108,
+                        -0.042002635034095235529,
+                        0.1665386113822914895,
+                        -0.042197734555544336748,
+                        -0.0096219715278769735621,
+                        0.0072189432466630995424,
+                        -0.0011651675918590651121,
+                        -0.00021524167411495097282,
+                        0.00012805028238811618615,
+                        -0.000020134854780788238656,
+                        -1.2504934821426706573e-6,
+                        1.1330272319816958824e-6,
+                        -2.0563384169776071035e-7,
+                        6.1160951044814158179e-9,
+                        5.0020076444692229301e-9,
+                        -1.1812745704870201446e-9,
+                        1.0434267116911005105e-10,
+                        7.782263439905071254e-12,
+                        -3.6968056186422057082e-12,
+                        5.100370287454475979e-13,
+                        -2.0583260535665067832e-14,
+                        -5.3481225394230179824e-15,
+                        1.2267786282382607902e-15,
+                        -1.1812593016974587695e-16,
+                        1.1866922547516003326e-18};
+  const double m2 = mu * mu;
+  // even part: c0 + c2 m^2 + c4 m^4 + ...
+  double ev = c[26];
+  for (int k = 24; k >= 0; k -= 2) ev = ev * m2 + c[k];
+  // odd part / mu: c1 + c3 m^2 + ...
+  double od = c[25];
+  for (int k = 23; k >= 1; k -= 2) od = od * m2 + c[k];
+  g1 = -od;
+  g2 = ev;
+  rg_plus = ev + mu * od;   // 1/Gamma(1+mu)
+  rg_minus = ev - mu * od;  // 1/Gamma(1-mu)
+}
+
+// K_mu(x) and K_{mu+1}(x) for |mu| <= 1/2, x > 0 (Temme 1975).
+SV_HD void bessel_k_pair(double mu, double x, double& kmu, double& kmu1) {
+  const double eps = 1e-17;
+  if (x <= 1.5) {
+    // Temme's series:  K_mu = sum c_k f_k,  K_{mu+1} = (2/x) sum c_k (p_k - k f_k)
+    double g1, g2, rgp, rgm;
+    temme_gammas(mu, g1, g2, rgp, rgm);
+    const double lnh = -log(0.5 * x);  // ln(2/x)
+    const double sig = mu * lnh;
+    const double pmu = kPi * mu;
+    const double fac = (fabs(pmu) < 1e-15) ? 1.0 : pmu / sin(pmu);
+    const double shr = (fabs(sig) < 1e-15) ? 1.0 : sinh(sig) / sig;
+    double f = fac * (g1 * cosh(sig) + g2 * shr * lnh);
+    const double es = exp(sig);       // (x/2)^(-mu)
+    double p = 0.5 * es / rgp;        // (1/2)(x/2)^(-mu) Gamma(1+mu)
+    double q = 0.5 / (es * rgm);      // (1/2)(x/2)^(mu) Gamma(1-mu)
+    double ck = 1.0;
+    const double y = 0.25 * x * x;
+    double s0 = f, s1 = p;
+    for (int k = 1; k < 500; ++k) {
+      const double dk = (double)k;
+      f = (dk * f + p + q) / (dk * dk - mu * mu);
+      ck *= y / dk;
+      p /= (dk - mu);
+      q /= (dk + mu);
+      const double t0 = ck * f;
+      s0 += t0;
+      s1 += ck * (p - dk * f);
+      if (fabs(t0) < fabs(s0) * eps) break;
+    }
+    kmu = s0;
+    kmu1 = s1 * (2.0 / x);
+  } else {
+    // Steed's continued fraction for the ratio, with Temme's normalising sum:
+    //   K_mu(x) = sqrt(pi/(2x)) e^{-x} / S
+    const double a1 = 0.25 - mu * mu;
+    double b = 2.0 * (1.0 + x);
+    double dd = 1.0 / b;
+    double del = dd, h = dd;
+    double qm1 = 0.0, qk = 1.0;
+    double ak = -a1;
+    double cc = a1, qs = a1;
+    double S = 1.0 + qs * del;
+    for (int i = 2; i < 1000; ++i) {
+      ak -= 2.0 * (double)(i - 1);
+      cc = -ak * cc / (double)i;
+      const double qn = (qm1 - b * qk) / ak;
+      qm1 = qk;
+      qk = qn;
+      qs += cc * qn;
+      b += 2.0;
+      dd = 1.0 / (b + ak * dd);
+      del = (b * dd - 1.0) * del;
+      h += del;
+      const double ds = qs * del;
+      S += ds;
+      if (fabs(ds) < fabs(S) * eps) break;
+    }
+    kmu = sqrt(kPi / (2.0 * x)) * exp(-x) / S;
+    kmu1 = kmu * (mu + x + 0.5 - a1 * h) / x;
+  }
+}
+
+// K_nu(x) and K_{nu-1}(x) for nu >= 0, x > 0.
+SV_HD void bessel_k_nu_and_prev(double nu, double x, double& knu, double& knum1) {
+  const int N = (int)floor(nu + 0.5);
+  const double mu = nu - (double)N;  // in [-1/2, 1/2)
+  double k0, k1;                     // K_mu, K_{mu+1}
+  bessel_k_pair(mu, x, k0, k1);
+  if (N == 0) {
+    knu = k0;
+    knum1 = k1 - (2.0 * mu / x) * k0;  // K_{mu-1}
+    return;
+  }
+  double km = k0, kc = k1;  // K_{mu+j-1}, K_{mu+j}, j = 1
+  for (int j = 1; j < N; ++j) {
+    const double kn = km + (2.0 * (mu + (double)j) / x) * kc;
+    km = kc;
+    kc = kn;
+  }
+  knu = kc;
+  knum1 = km;
+}
+
+SV_HD double bessel_k(double nu, double x) {
+  double a, b;
+  bessel_k_nu_and_prev(fabs(nu), x, a, b);
+  return a;
+}
+
+// ----------------------------------------------------------------------------
+// closed forms: returns M, g (g = M'(r)/r) for nu in {0.5, 1.5, 2.5}
+// nu_code: 0 -> 0.5, 1 -> 1.5, 2 -> 2.5
+SV_HD void matern_closed(int nu_code, double r, double& M, double& g) {
+  if (nu_code == 0) {
+    if (r > 0.0) {
+      const double e = exp(-r);
+      M = e;
+      g = -e / r;
+    } else {
+      M = 1.0;
+      g = 0.0;
+    }
+  } else if (nu_code == 1) {
+    const double c = kSqrt3 * r;
+    const double e = exp(-c);
+    M = (1.0 + c) * e;
+    g = -3.0 * e;
+  } else {
+    const double c = kSqrt5 * r;
+    const double e = exp(-c);
+    M = (1.0 + c + c * c / 3.0) * e;
+    g = -(5.0 / 3.0) * (1.0 + c) * e;
+  }
+}
+
+// general form, _matern_general.py:92-116.  log_coef = (1-nu) ln2 - lgamma(nu).
+SV_HD double matern_general_M(double r, double nu, double log_coef) {
+  if (r < kRFloor) return 1.0;
+  const double c = sqrt(2.0 * nu) * r;
+  double knu, knm1;
+  bessel_k_nu_and_prev(nu, c, knu, knm1);
+  return exp(log_coef + nu * log(c)) * knu;
+}
+
+SV_HD void matern_general_Mg(double r, double nu, double log_coef, double& M, double& g) {
+  const double rr = r < kRFloor ? kRFloor : r;
+  const double s2n = sqrt(2.0 * nu);
+  const double c = s2n * rr;
+  double knu, knm1;
+  bessel_k_nu_and_prev(nu, c, knu, knm1);
+  const double pre = exp(log_coef + nu * log(c));
+  if (r < kRFloor) {
+    M = 1.0;
+    g = 0.0;
+  } else {
+    M = pre * knu;
+    g = -(s2n / rr) * pre * knm1;
+  }
+}
+
+SV_HD double matern_log_coef(double nu) { return (1.0 - nu) * kLn2 - lgamma(nu); }
+
+// nu in {0.5, 1.5, 2.5} -> 0/1/2, else -1
+SV_HD int matern_closed_code(double nu) {
+  if (nu == 0.5) return 0;
+  if (nu == 1.5) return 1;
+  if (nu == 2.5) return 2;
+  return -1;
+}
+
+}  // namespace sv

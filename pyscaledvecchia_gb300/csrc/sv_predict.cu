@@ -1,0 +1,340 @@
+// Prediction blocks and the sparse triangular solve of the joint predictive
+// distribution.
+//
+//   k_pred_*      : gp.py:257-276 (_predict_scaled) and gp.py:329-348
+//                   (_joint_factor): per target, the block [neighbours, target]
+//                   with a noise-free target (nugget only on observation rows),
+//                   Cholesky with jitter retry, a = L^-T e_K; marginal mean
+//                   -a[:k].r / a_K and variance 1 / a_K^2, or the column a of
+//                   the sparse inverse Cholesky factor U.
+//   k_joint_solve : U_pp^T x = rhs (gp.py:380-401, scipy spsolve_triangular),
+//                   one warp per row, rows claimed in order, bounded waits on
+//                   the rows it depends on.
+#include "sv_block.cuh"
+
+namespace sv {
+
+struct PredArgs {
+  const double* theta;  // [log s2, log lam_1..d, log tau]
+  const double* Xall;
+  const int32_t* tgt;
+  const int32_t* nbr;
+  const double* resid;
+  double* mean;
+  double* var;
+  double* acol;
+  double* rhs;
+  int32_t* info;
+  int64_t nobs, nblk;
+  int d, k, ldnbr, kt;
+  int closed;
+  int target_nugget;
+  double nu;
+};
+
+struct PredPrm {
+  double s2, tau;
+  MaternMode mm;
+  double invlam[64];
+};
+
+__device__ void pred_params(const PredArgs& A, PredPrm* prm) {
+  if (threadIdx.x == 0) {
+    prm->s2 = exp(A.theta[0]);
+    prm->tau = exp(A.theta[1 + A.d]);
+    MaternMode mm;
+    mm.closed = A.closed;
+    mm.estimate_nu = 0;
+    mm.nu = A.nu;
+    mm.log_coef = A.closed < 0 ? matern_log_coef(A.nu) : 0.0;
+    mm.nu_p = mm.nu_m = mm.lc_p = mm.lc_m = 0.0;
+    mm.inv2h = 0.0;
+    prm->mm = mm;
+  }
+  for (int l = threadIdx.x; l < A.d; l += blockDim.x) prm->invlam[l] = exp(-A.theta[1 + l]);
+  __syncthreads();
+}
+
+__host__ __device__ inline int64_t pred_team_doubles(int kt, int d) {
+  return (int64_t)kt * d + (int64_t)kt * (kt + 1) / 2 + 5 * (int64_t)kt + (kt + 1) / 2 + 1 + 40;
+}
+
+template <int T>
+__device__ void pred_block(const PredArgs& A, const PredPrm* prm, int64_t b, double* sm) {
+  const int lane = Team<T>::lane();
+  const int d = A.d, kcap = A.k, kt = A.kt;
+  double* u = sm;
+  double* Lp = u + (int64_t)kt * d;
+  double* a = Lp + (int64_t)kt * (kt + 1) / 2;
+  double* invd = a + kt;
+  double* acc = invd + kt;
+  double* mask = acc + kt;
+  double* rv = mask + kt;
+  int* idx = (int*)(rv + kt);
+  volatile int* flag = idx + kt;
+  double* red = (double*)(rv + kt + (kt + 1) / 2 + 1);
+
+  // neighbours are packed at the front of the row; -1 marks absent entries
+  // (rows with fewer than k predecessors)
+  if (lane == 0) {
+    int kb = 0;
+    while (kb < kcap && A.nbr[b * A.ldnbr + kb] >= 0) ++kb;
+    *flag = kb;
+  }
+  Team<T>::sync();
+  const int k = *flag;
+  const int K = k + 1;
+  Team<T>::sync();
+  for (int i = lane; i < K; i += T) {
+    const int ix = (i < k) ? A.nbr[b * A.ldnbr + i] : A.tgt[b];
+    idx[i] = ix;
+    // gp.py:263-265, 336-339: nugget on observations only, target noise-free
+    // (a prior draw keeps the nugget on every row, target included)
+    mask[i] = ((i < k && ix < A.nobs) || (i == k && A.target_nugget)) ? 1.0 : 0.0;
+    rv[i] = (A.resid && i < k && ix < A.nobs) ? A.resid[ix] : 0.0;
+  }
+  Team<T>::sync();
+  for (int t = lane; t < K * d; t += T) {
+    const int i = t / d, l = t - (t / d) * d;
+    u[i * d + l] = A.Xall[(int64_t)idx[i] * d + l] * prm->invlam[l];
+  }
+  Team<T>::sync();
+  const double s2 = prm->s2, tau = prm->tau;
+  bool ok = false;
+  for (int lv = 0; lv <= 9; ++lv) {
+    double jit = 0.0;
+    if (lv > 0) {
+      // 10^p * mean(diag Sigma)   (_covariance.py:245-249)
+      double sc = 0.0;
+      for (int i = 0; i < K; ++i) sc += s2 * (1.0 + tau * mask[i]);
+      const double p10[10] = {0.0, 1e-12, 1e-11, 1e-10, 1e-9, 1e-8, 1e-7, 1e-6, 1e-5, 1e-4};
+      jit = p10[lv] * (sc / (double)K);
+    }
+    if (lane == 0) *flag = 0;
+    assemble_sigma<T>(K, d, u, mask, s2, tau, jit, prm->mm, Lp, nullptr, nullptr);
+    Team<T>::sync();
+    ok = cholesky_packed<T>(K, Lp, invd, flag);
+    Team<T>::sync();
+    if (ok) {
+      if (lv > 0 && lane == 0) atomicMax(A.info + SV_INFO_JITTER, lv);
+      break;
+    }
+  }
+  if (!ok) {
+    if (lane == 0) {
+      set_error(A.info + SV_INFO_STATUS, SV_ECHOL);
+      atomicCAS(A.info + SV_INFO_BLOCK, -1, (int)b);
+    }
+    return;
+  }
+  backsolve_eK<T>(K, Lp, invd, a, acc);
+  Team<T>::sync();
+  double s = 0.0;
+  for (int i = lane; i < k; i += T) s += a[i] * rv[i];
+  s = team_sum<T>(s, red);
+  if (lane == 0) {
+    const double aK = a[K - 1];
+    if (A.mean) A.mean[b] = -s / aK;
+    if (A.var) A.var[b] = 1.0 / (aK * aK);
+    if (A.rhs) A.rhs[b] = -s;
+  }
+  if (A.acol) {
+    // column of U laid out as [neighbour slots 0..kcap-1, target]; absent
+    // neighbour slots hold 0
+    const int Kc = kcap + 1;
+    for (int i = lane; i < Kc; i += T)
+      A.acol[b * (int64_t)Kc + i] = (i < k) ? a[i] : (i == kcap ? a[K - 1] : 0.0);
+  }
+}
+
+__global__ void k_pred_warp(PredArgs A) {
+  extern __shared__ double smem[];
+  PredPrm* prm = (PredPrm*)smem;
+  pred_params(A, prm);
+  const int64_t per = pred_team_doubles(32, A.d);
+  const int w = threadIdx.x >> 5;
+  double* sm = smem + (sizeof(PredPrm) + 7) / 8 + w * per;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t b = (int64_t)blockIdx.x * (blockDim.x >> 5) + w; b < A.nblk; b += nw) {
+    pred_block<32>(A, prm, b, sm);
+    __syncwarp();
+  }
+}
+
+__global__ void k_pred_cta(PredArgs A) {
+  extern __shared__ double smem[];
+  PredPrm* prm = (PredPrm*)smem;
+  pred_params(A, prm);
+  double* sm = smem + (sizeof(PredPrm) + 7) / 8;
+  for (int64_t b = blockIdx.x; b < A.nblk; b += gridDim.x) {
+    pred_block<128>(A, prm, b, sm);
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// sparse triangular solve  U_pp^T X = R
+// ---------------------------------------------------------------------------
+struct JsArgs {
+  int64_t npred, nobs;
+  int k, ldnbr, nrhs;
+  const int32_t* nbr;
+  const double* acol;
+  const double* R;
+  double* X;
+  int* ready;
+  unsigned* counter;
+  int32_t* info;
+};
+
+__global__ void k_joint_solve(JsArgs A) {
+  const int lane = threadIdx.x & 31;
+  const int K = A.k + 1;
+  while (true) {
+    int64_t c = 0;
+    if (lane == 0) c = (int64_t)atomicAdd(A.counter, 1u);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= A.npred) break;
+    const double* ac = A.acol + c * (int64_t)K;
+    bool timed_out = false;
+    for (int r0 = 0; r0 < A.nrhs; r0 += 32) {
+      const int r = r0 + lane;
+      double s = (r < A.nrhs) ? A.R[c * (int64_t)A.nrhs + r] : 0.0;
+      for (int i = 0; i < A.k; ++i) {
+        const int64_t ix = A.nbr[c * (int64_t)A.ldnbr + i];
+        if (ix < 0 || ix < A.nobs) continue;  // absent slot or observation
+        const int64_t p = ix - A.nobs;  // an earlier prediction row
+        if (r0 == 0) {
+          if (lane == 0) {
+            unsigned it = 0;
+            while (ld_acquire_s32(A.ready + p) == 0) {
+              if (++it > SV_SPIN_LIMIT) {
+                set_error(A.info + SV_INFO_STATUS, SV_ETIMEOUT);
+                atomicCAS(A.info + SV_INFO_BLOCK, -1, (int)c);
+                timed_out = true;
+                break;
+              }
+            }
+          }
+          timed_out = __shfl_sync(0xffffffffu, (int)timed_out, 0) != 0;
+          __syncwarp();
+        }
+        if (r < A.nrhs) s -= ac[i] * __ldcg(A.X + p * (int64_t)A.nrhs + r);
+      }
+      if (r < A.nrhs) A.X[c * (int64_t)A.nrhs + r] = s / ac[K - 1];
+    }
+    (void)timed_out;
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) st_release_s32(A.ready + c, 1);
+  }
+}
+
+}  // namespace sv
+
+using namespace sv;
+
+extern "C" int sv_predict_blocks(const sv_pred_desc* D, const double* theta, const double* Xall,
+                                 const int32_t* tgt, const int32_t* nbr, const double* resid,
+                                 double* mean, double* var, double* acol, double* rhs, int32_t* info,
+                                 sv_stream_t stream) {
+  if (!D || !theta || !Xall || !tgt || !info) return SV_EINVAL;
+  if (D->d < 1 || D->d > 64 || D->k < 0 || D->nblk < 0 || (D->k > 0 && (!nbr || D->ldnbr < D->k)))
+    return SV_EINVAL;
+  if (!(D->nu > 0.0)) return SV_EINVAL;
+  const int closed = matern_closed_code(D->nu);
+  if (!D->general && closed < 0) return SV_EINVAL;
+  if (D->nobs > 0 && !resid && (mean || rhs)) return SV_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  int32_t init_info[4] = {0, -1, 0, 0};
+  SV_CUDA_TRY(cudaMemcpyAsync(info, init_info, sizeof(init_info), cudaMemcpyHostToDevice, st));
+  if (D->nblk == 0) return SV_OK;
+  PredArgs A;
+  A.theta = theta;
+  A.Xall = Xall;
+  A.tgt = tgt;
+  A.nbr = nbr;
+  A.resid = resid;
+  A.mean = mean;
+  A.var = var;
+  A.acol = acol;
+  A.rhs = rhs;
+  A.info = info;
+  A.nobs = D->nobs;
+  A.nblk = D->nblk;
+  A.d = D->d;
+  A.k = D->k;
+  A.ldnbr = D->ldnbr;
+  A.closed = D->general ? -1 : closed;
+  A.target_nugget = D->target_nugget;
+  A.nu = D->nu;
+  int dev = 0, maxsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t prm = (sizeof(PredPrm) + 7) / 8 * 8;
+  const int nsm = sv_num_sms();
+  if (D->k + 1 <= 32) {
+    A.kt = 32;
+    const size_t team = sizeof(double) * pred_team_doubles(32, D->d);
+    int wpc = 8;
+    while (wpc > 1 && prm + wpc * team > (size_t)maxsm) --wpc;
+    const size_t smem = prm + wpc * team;
+    if (smem > (size_t)maxsm) return SV_EINVAL;
+    SV_CUDA_TRY(cudaFuncSetAttribute(k_pred_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int64_t grid = (D->nblk + wpc - 1) / wpc;
+    if (grid > 64LL * nsm) grid = 64LL * nsm;
+    k_pred_warp<<<(unsigned)grid, 32 * wpc, smem, st>>>(A);
+  } else {
+    A.kt = D->k + 1;
+    const size_t smem = prm + sizeof(double) * pred_team_doubles(A.kt, D->d);
+    if (smem > (size_t)maxsm) return SV_EINVAL;
+    SV_CUDA_TRY(cudaFuncSetAttribute(k_pred_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int64_t grid = D->nblk;
+    if (grid > 16LL * nsm) grid = 16LL * nsm;
+    k_pred_cta<<<(unsigned)grid, 128, smem, st>>>(A);
+  }
+  SV_CUDA_TRY(cudaGetLastError());
+  return SV_OK;
+}
+
+extern "C" size_t sv_joint_solve_workspace_bytes(int64_t npred) {
+  return 256 + ((sizeof(int) * (size_t)(npred > 0 ? npred : 1) + 255) & ~(size_t)255);
+}
+
+extern "C" int sv_joint_solve(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr,
+                              const int32_t* nbr, const double* acol, const double* R, int32_t nrhs,
+                              double* X, int32_t* info, void* workspace, size_t workspace_bytes,
+                              sv_stream_t stream) {
+  if (npred < 0 || nobs < 0 || k < 0 || nrhs < 1 || !info) return SV_EINVAL;
+  if (npred > 0 && (!acol || !R || !X || (k > 0 && (!nbr || ldnbr < k)))) return SV_EINVAL;
+  if (npred > 0x7fffffffLL) return SV_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  int32_t init_info[4] = {0, -1, 0, 0};
+  SV_CUDA_TRY(cudaMemcpyAsync(info, init_info, sizeof(init_info), cudaMemcpyHostToDevice, st));
+  if (npred == 0) return SV_OK;
+  if (!workspace || workspace_bytes < sv_joint_solve_workspace_bytes(npred)) return SV_ENOSPC;
+  unsigned* counter = (unsigned*)workspace;
+  int* ready = (int*)((char*)workspace + 256);
+  SV_CUDA_TRY(cudaMemsetAsync(workspace, 0, sv_joint_solve_workspace_bytes(npred), st));
+  JsArgs A;
+  A.npred = npred;
+  A.nobs = nobs;
+  A.k = k;
+  A.ldnbr = ldnbr;
+  A.nrhs = nrhs;
+  A.nbr = nbr;
+  A.acol = acol;
+  A.R = R;
+  A.X = X;
+  A.ready = ready;
+  A.counter = counter;
+  A.info = info;
+  const int nsm = sv_num_sms();
+  int64_t warps = npred;
+  if (warps > 16LL * nsm) warps = 16LL * nsm;
+  const int tpb = 256;
+  const int64_t grid = (warps * 32 + tpb - 1) / tpb;
+  k_joint_solve<<<(unsigned)grid, tpb, 0, st>>>(A);
+  SV_CUDA_TRY(cudaGetLastError());
+  return SV_OK;
+}

@@ -1,0 +1,195 @@
+"""Profile Vecchia log-likelihood, score and Fisher information on the GPU.
+
+Drop-in counterpart of the reference's ``scaled_vecchia.likelihood``
+(src/scaled_vecchia/likelihood.py:66-175).  For block U_i = (c(i), i) with
+covariance S = L L' and a = L^-T e_K (the block's column of the sparse inverse
+Cholesky factor):
+
+    l_i          = -1/2 (log 2 pi + 2 log L_KK + z_K^2),   z = L^-1 r
+    dl_i/dth_j   = -1/2 [ w^j_K (1 + z_K^2) - 2 z_K (w^j . z) ]
+    I_i[j, k]    =  1/2 [ 2 (w^j . w^k) - w^j_K w^k_K ],   w^j = L^-1 (dS_j a)
+
+with the trend coefficients beta profiled out by GLS on the whitened
+columns a.y, a.Z.  All of it runs in the fused block kernels of
+libsvgpu.so (sv_vecchia_loglik); the host only packs the conditioning sets.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib
+from ._covariance import _check_nu, _chunks
+
+__all__ = ["vecchia_profile_loglik"]
+
+_WARP_K = 32  # blocks with K = k+1 <= 32 run one per warp, larger ones one per CTA
+
+
+def pack_groups(groups, n=None):
+    """Flatten ``_nn_groups`` output into per-block arrays.
+
+    Returns (rowb int32 (B,), kb int32 (B,), nbr int32 (B, kmax), group_k list,
+    group_len list) with warp-sized blocks first (stable).
+    """
+    rows_l, k_l, nb_l = [], [], []
+    for rows, nb in groups:
+        rows = np.asarray(rows, dtype=np.int64).reshape(-1)
+        nb = np.asarray(nb, dtype=np.int64).reshape(rows.shape[0], -1)
+        rows_l.append(rows)
+        k_l.append(nb.shape[1])
+        nb_l.append(nb)
+    B = int(sum(r.shape[0] for r in rows_l))
+    kmax = max(k_l) if k_l else 0
+    rowb = np.empty(B, dtype=np.int32)
+    kb = np.empty(B, dtype=np.int32)
+    nbr = np.full((B, max(kmax, 1)), -1, dtype=np.int32)
+    gid = np.empty(B, dtype=np.int32)
+    o = 0
+    for g, (rows, k, nb) in enumerate(zip(rows_l, k_l, nb_l)):
+        c = rows.shape[0]
+        rowb[o:o + c] = rows
+        kb[o:o + c] = k
+        if k:
+            nbr[o:o + c, :k] = nb
+        gid[o:o + c] = g
+        o += c
+    if n is not None and B and (rowb.min() < 0 or rowb.max() >= n or
+                                (kmax and (nbr[nbr >= 0].max(initial=0) >= n))):
+        raise ValueError("conditioning sets reference rows outside the data")
+    big = (kb + 1) > _WARP_K
+    if big.any() and not np.all(np.diff(big.astype(np.int8)) >= 0):
+        perm = np.argsort(big, kind="stable")
+        rowb, kb, nbr, gid = rowb[perm], kb[perm], nbr[perm], gid[perm]
+    return rowb, kb, nbr, gid, k_l, [r.shape[0] for r in rows_l]
+
+
+def chunk_ids(gid, group_k, group_len, Pc):
+    """Jitter-sharing chunk of every block: the reference factorises each group
+    in chunks of ``_chunks(len(rows), K, Pc)`` rows and retries a whole chunk
+    with the same jitter (_covariance.py:235-259, likelihood.py:114)."""
+    ids_per_group = []
+    nxt = 0
+    for k, ln in zip(group_k, group_len):
+        ids = np.empty(ln, dtype=np.int32)
+        for a0, a1 in _chunks(ln, k + 1, Pc):
+            ids[a0:a1] = nxt
+            nxt += 1
+        ids_per_group.append(ids)
+    if gid.shape[0] == 0:
+        return np.zeros(0, dtype=np.int32)
+    # rank of each block inside its group (the stable warp/CTA split keeps it)
+    sort_idx = np.argsort(gid, kind="stable")
+    first = np.searchsorted(gid[sort_idx], np.arange(len(group_k)))
+    rank = np.empty(gid.shape[0], dtype=np.int64)
+    rank[sort_idx] = np.arange(gid.shape[0]) - first[gid[sort_idx]]
+    flat = np.concatenate(ids_per_group)
+    offs = np.concatenate([[0], np.cumsum(group_len)])[:-1].astype(np.int64)
+    return flat[offs[gid] + rank].astype(np.int32)
+
+
+class DeviceProblem:
+    """Device-resident inputs of one likelihood (X, y, Z in Vecchia order and
+    the packed conditioning sets), reused across objective evaluations."""
+
+    def __init__(self, Xo, yo, Zo, groups):
+        lib, torch = _lib.device_ready()
+        self.lib, self.torch = lib, torch
+        Xo = np.ascontiguousarray(Xo, dtype=np.float64)
+        self.n, self.d = Xo.shape
+        yo = np.ascontiguousarray(yo, dtype=np.float64).reshape(-1)
+        if yo.shape[0] != self.n:
+            raise ValueError("X and y have incompatible shapes")
+        self.has_Z = Zo is not None and np.asarray(Zo).ndim == 2 and np.asarray(Zo).shape[1] > 0
+        self.q = int(np.asarray(Zo).shape[1]) if self.has_Z else 0
+        self.X = _lib.to_dev(torch, Xo, np.float64)
+        self.y = _lib.to_dev(torch, yo, np.float64)
+        self.Z = _lib.to_dev(torch, np.asarray(Zo, dtype=np.float64), np.float64) if self.has_Z else None
+        rowb, kb, nbr, gid, gk, gl = pack_groups(groups, self.n)
+        self.nblk = rowb.shape[0]
+        self.kmax = int(kb.max()) if self.nblk else 0
+        self.nblk_warp = int(np.sum(kb + 1 <= _WARP_K))
+        self.rowb = _lib.to_dev(torch, rowb, np.int32)
+        self.kb = _lib.to_dev(torch, kb, np.int32)
+        self.nbr = _lib.to_dev(torch, nbr, np.int32)
+        self.ldnbr = nbr.shape[1]
+        self._gid, self._gk, self._gl = gid, gk, gl
+        self._chunks = {}
+        self._ws = None
+        self.out = None
+        self.info = _lib.new_info(torch)
+
+    def chunk_tensor(self, Pc):
+        if Pc not in self._chunks:
+            ids = chunk_ids(self._gid, self._gk, self._gl, Pc)
+            self._chunks[Pc] = _lib.to_dev(self.torch, ids, np.int32)
+        return self._chunks[Pc]
+
+    def launch(self, theta_dev, P, nu, estimate_nu, need_grad, var_penalty, log_var_target,
+               chunked=True, stream=None):
+        """Enqueue one evaluation; results land in self.out / self.info."""
+        torch, lib = self.torch, self.lib
+        D = _lib.LoglikDesc()
+        D.n, D.nblk, D.nblk_warp = self.n, self.nblk, self.nblk_warp
+        D.d, D.q, D.ldnbr, D.kmax = self.d, self.q, self.ldnbr, self.kmax
+        D.need_grad, D.estimate_nu = int(bool(need_grad)), int(bool(estimate_nu))
+        D.chunked = int(bool(chunked))
+        D.precision = 0
+        D.nu = float(nu) if nu is not None else 1.0
+        D.var_penalty, D.log_var_target = float(var_penalty), float(log_var_target)
+        nbytes = lib.sv_loglik_workspace_bytes(D)
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = _lib.workspace(torch, nbytes)
+        nout = 1 + P + P * P + self.q
+        if self.out is None or self.out.numel() != nout:
+            self.out = torch.empty(nout, dtype=torch.float64, device="cuda")
+        chunk = self.chunk_tensor(P if need_grad else 1) if chunked else None
+        st = stream if stream is not None else _lib.stream_handle(torch)
+        rc = lib.sv_vecchia_loglik(D, _lib.ptr(theta_dev), _lib.ptr(self.X), _lib.ptr(self.y),
+                                   _lib.ptr(self.Z), _lib.ptr(self.rowb), _lib.ptr(self.kb),
+                                   _lib.ptr(self.nbr), _lib.ptr(chunk), _lib.ptr(self.out),
+                                   _lib.ptr(self.info), _lib.ptr(self._ws), self._ws.numel(), st)
+        _lib.check(lib, rc, "sv_vecchia_loglik")
+
+    def evaluate(self, theta, nu, estimate_nu=False, need_grad=True, var_penalty=0.0,
+                 log_var_target=0.0, chunked=True):
+        torch = self.torch
+        theta = np.asarray(theta, dtype=float).reshape(-1)
+        d = self.d
+        P = d + 3 if estimate_nu else d + 2
+        if theta.shape[0] < P:
+            raise ValueError("theta has too few entries for this input dimension")
+        if not estimate_nu:
+            _check_nu(nu)
+        th = _lib.to_dev(torch, theta[:P], np.float64)
+        self.launch(th, P, nu, estimate_nu, need_grad, var_penalty, log_var_target, chunked)
+        res = torch.cat([self.out, self.info.to(torch.float64)]).cpu().numpy()
+        nout = 1 + P + P * P + self.q
+        _lib.check_info(self.lib, res[nout:].astype(np.int64), "sv_vecchia_loglik")
+        ll = float(res[0])
+        beta = res[1 + P + P * P:nout].copy() if self.has_Z else np.zeros(0)
+        if not need_grad:
+            return ll, None, None, beta
+        grad = res[1:1 + P].copy()
+        fish = res[1 + P:1 + P + P * P].reshape(P, P).copy()
+        return ll, grad, fish, beta
+
+
+def vecchia_profile_loglik(theta, Xo, yo, Zo, groups, nu, estimate_nu=False,
+                           need_grad=True, var_penalty=0.0, log_var_target=0.0):
+    """Profile Vecchia loglikelihood, its gradient and the Fisher information.
+
+    theta : (P,) log-scale parameters [log sigma^2, log lambda_1..d, log tau]
+            (P = d+2), or [log sigma^2, log lambda_1..d, log nu, log tau]
+            (P = d+3) with ``estimate_nu``.
+    Xo, yo, Zo : inputs, responses and trend design (or None) in Vecchia order.
+    groups : output of ``ordering._nn_groups``.
+    nu : fixed Matern smoothness (ignored with ``estimate_nu``).
+    Returns (ll, grad, fisher, beta); grad and fisher are None when
+    ``need_grad`` is False.  Raises numpy.linalg.LinAlgError when a block
+    cannot be factorised even with jitter.
+    """
+    theta = np.asarray(theta, dtype=float)
+    prob = DeviceProblem(Xo, yo, Zo, groups)
+    return prob.evaluate(theta, nu, estimate_nu=estimate_nu, need_grad=need_grad,
+                         var_penalty=var_penalty, log_var_target=log_var_target)
+
