@@ -130,13 +130,22 @@ GP_CASES = {
 
 @pytest.mark.parametrize("name", sorted(GP_CASES))
 def test_fit_parity_with_reference(golden_gp, name):
-    """Same Fisher-scoring path: parameters and log-likelihood agree."""
+    """Same Fisher-scoring path: parameters and log-likelihood agree.
+
+    When the estimated nugget runs onto its 1e-12 clip the blocks are nearly
+    singular and the reference's own fit is chaotic at the rounding level:
+    perturbing y by 1e-15 relative moves its final loglik by ~6e-4 (sine)
+    and 1e-13 by ~2e-3 (sub), and theta by ~3e-5 relative.  Those cases get
+    a band of that size; the fixed-nugget case is well posed and is held to
+    1e-8."""
     g = golden_gp
     gp = GP(**GP_CASES[name]).fit(g[name + "_X"], g[name + "_y"])
     ll_ref = float(g[name + "_loglik"])
-    assert abs(gp.loglik_ - ll_ref) <= 1e-6 * max(1.0, abs(ll_ref)), (gp.loglik_, ll_ref)
-    np.testing.assert_allclose(gp.theta_, g[name + "_theta"], rtol=1e-4, atol=1e-4)
-    np.testing.assert_allclose(gp.beta_, g[name + "_beta"], rtol=1e-5, atol=1e-6)
+    clipped = g[name + "_theta"][-1] < np.log(1e-11)
+    ll_tol, th_tol = (5e-3, 3e-4) if clipped else (1e-8 * abs(ll_ref), 1e-6)
+    assert abs(gp.loglik_ - ll_ref) <= ll_tol, (gp.loglik_, ll_ref)
+    np.testing.assert_allclose(gp.theta_, g[name + "_theta"], rtol=th_tol, atol=th_tol)
+    np.testing.assert_allclose(gp.beta_, g[name + "_beta"], rtol=th_tol, atol=th_tol)
 
 
 @pytest.mark.parametrize("name", ["sine", "linear", "fixnug", "sub", "nu175"])
