@@ -112,6 +112,24 @@ int sv_vecchia_loglik(const sv_loglik_desc* desc, const double* theta, const dou
                       const int32_t* nbr, const int32_t* chunk, double* out, int32_t* info,
                       void* workspace, size_t workspace_bytes, sv_stream_t stream);
 
+/* No counterpart in the reference.  The same evaluation as sv_vecchia_loglik
+ * for callers that cannot allocate device memory (an application whose fixed
+ * memory pool owns the GPU, or a loop that must not call cudaMalloc, which
+ * synchronises the device and can fail under memory pressure): inputs and
+ * outputs as above, but the scratch comes from a file-scope static device
+ * array of SV_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library
+ * until exit.  Returns SV_ENOSPC, launching nothing, when
+ * sv_loglik_workspace_bytes(desc) exceeds it (about 35,000 blocks at
+ * d = 10, m = 30).  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race, so serialise
+ * them. */
+#define SV_NOALLOC_SCRATCH_BYTES (32u << 20)
+int sv_vecchia_loglik_noalloc(const sv_loglik_desc* desc, const double* theta, const double* X,
+                              const double* y, const double* Z, const int32_t* rowb,
+                              const int32_t* kb, const int32_t* nbr, const int32_t* chunk,
+                              double* out, int32_t* info, sv_stream_t stream);
+
 /* ---------------------------------------------------------------------- */
 /* Matern correlation (elementwise)                                        */
 /* ---------------------------------------------------------------------- */

@@ -52,6 +52,8 @@ SIGNATURES = {
     "sv_loglik_workspace_bytes": (c_sz, [ctypes.POINTER(LoglikDesc)]),
     "sv_vecchia_loglik": (c_i32, [ctypes.POINTER(LoglikDesc), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
                                   c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "sv_vecchia_loglik_noalloc": (c_i32, [ctypes.POINTER(LoglikDesc), c_vp, c_vp, c_vp, c_vp, c_vp,
+                                          c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "sv_matern_eval": (c_i32, [c_vp, c_i64, c_dbl, c_i32, c_i32, c_vp, c_vp]),
     "sv_bessel_k": (c_i32, [c_vp, c_i64, c_dbl, c_vp, c_vp]),
     "sv_block_cov": (c_i32, [c_vp, c_i64, c_i32, c_i32, c_vp, c_dbl, c_dbl, c_dbl, c_i32, c_i32,

@@ -1,0 +1,85 @@
+"""sv_vecchia_loglik_noalloc: the likelihood evaluation for callers that
+cannot allocate device memory (an application whose own fixed pool owns the
+GPU's memory, or a loop that must not call cudaMalloc because it synchronises
+the device and can fail under memory pressure).  Its scratch is a fixed array
+inside the library instead of a caller-provided workspace; its results must
+be those of sv_vecchia_loglik on the same inputs.
+
+Two calls in a row on different problems (the second also uses the CTA
+kernel, K = 41) check that the contents the first call leaves in the shared
+array do not leak into the second.  Collected last so that a run stopping at
+the first failure has run every other test.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(seed, n, d, m):
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    from pyscaledvecchia_gb300.ordering import _nn_groups, find_ordered_nn, maximin_order
+    rng = np.random.default_rng(seed)
+    X = rng.random((n, d))
+    y = rng.standard_normal(n)
+    lam = np.exp(rng.uniform(math.log(0.1), math.log(3.0), d))
+    theta = np.concatenate([[math.log(1.4)], np.log(lam), [math.log(3e-3)]])
+    order = maximin_order(X / lam)
+    nn = find_ordered_nn((X / lam)[order], m)
+    prob = DeviceProblem(X[order], y[order], np.ones((n, 1)), _nn_groups(nn, m))
+    return prob, theta
+
+
+def _desc(prob, P):
+    from pyscaledvecchia_gb300 import _lib
+    D = _lib.LoglikDesc()
+    D.n, D.nblk, D.nblk_warp = prob.n, prob.nblk, prob.nblk_warp
+    D.d, D.q, D.ldnbr, D.kmax = prob.d, prob.q, prob.ldnbr, prob.kmax
+    D.need_grad, D.estimate_nu, D.chunked, D.precision = 1, 0, 1, 0
+    D.nu, D.var_penalty, D.log_var_target = 2.5, 0.0, 0.0
+    return D
+
+
+def _noalloc_call(prob, theta):
+    from pyscaledvecchia_gb300 import _lib
+    lib, torch = _lib.device_ready()
+    P = prob.d + 2
+    D = _desc(prob, P)
+    th = _lib.to_dev(torch, theta, np.float64)
+    out = torch.empty(1 + P + P * P + prob.q, dtype=torch.float64, device="cuda")
+    info = _lib.new_info(torch)
+    chunk = prob.chunk_tensor(P)
+    rc = lib.sv_vecchia_loglik_noalloc(D, _lib.ptr(th), _lib.ptr(prob.X), _lib.ptr(prob.y),
+                                       _lib.ptr(prob.Z), _lib.ptr(prob.rowb), _lib.ptr(prob.kb),
+                                       _lib.ptr(prob.nbr), _lib.ptr(chunk), _lib.ptr(out),
+                                       _lib.ptr(info), _lib.stream_handle(torch))
+    assert rc == 0, lib.sv_status_string(rc)
+    res = out.cpu().numpy()
+    assert int(info.cpu().numpy()[0]) == 0
+    return res[0], res[1:1 + P], res[1 + P:1 + P + P * P].reshape(P, P), res[1 + P + P * P:]
+
+
+def test_noalloc_matches_workspace_entry_point_on_two_calls():
+    for seed, n, d, m in ((1, 3000, 5, 20), (2, 1500, 3, 40)):
+        prob, theta = _problem(seed, n, d, m)
+        ll0, g0, F0, b0 = prob.evaluate(theta, 2.5)
+        ll, g, F, b = _noalloc_call(prob, theta)
+        assert abs(ll - ll0) <= 1e-10 * abs(ll0)
+        np.testing.assert_allclose(g, g0, rtol=1e-8, atol=1e-8 * np.abs(g0).max())
+        np.testing.assert_allclose(F, F0, rtol=1e-8, atol=1e-8 * np.abs(F0).max())
+        np.testing.assert_allclose(b, b0, rtol=1e-8, atol=1e-10)
+
+
+def test_noalloc_rejects_problems_beyond_the_fixed_scratch():
+    from pyscaledvecchia_gb300 import _lib
+    lib, torch = _lib.device_ready()
+    prob, theta = _problem(3, 500, 4, 10)
+    D = _desc(prob, 6)
+    D.nblk = D.nblk_warp = 40_000_000  # needs far more than 32 MiB of scratch
+    assert lib.sv_loglik_workspace_bytes(D) > (32 << 20)
+    info = _lib.new_info(torch)
+    rc = lib.sv_vecchia_loglik_noalloc(D, None, None, None, None, None, None, None, None, None,
+                                       _lib.ptr(info), _lib.stream_handle(torch))
+    assert rc == _lib.SV_ENOSPC
