@@ -253,30 +253,39 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
 
-    def step_device():
-        prob.launch(th_d, P, nu, False, True, 0.0, 0.0, True)
+    def time_form(precision, lanes, steps, warmup):
+        for _ in range(warmup):
+            prob.launch(th_d, P, nu, False, True, 0.0, 0.0, True, precision=precision,
+                        team_lanes=lanes)
+        torch.cuda.synchronize()
+        evs = []
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            prob.launch(th_d, P, nu, False, True, 0.0, 0.0, True, precision=precision,
+                        team_lanes=lanes)
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in evs]
 
-    for _ in range(args.warmup):
-        step_device()
-    torch.cuda.synchronize()
-    res = prob.evaluate(theta, nu)
+    # team width of the split kernel: pick the fastest on this problem
+    lane_ms = {}
+    for lanes in (4, 8, 16, 32):
+        lane_ms[lanes] = float(np.median(time_form("split", lanes, 2, 1)))
+    best_lanes = min(lane_ms, key=lane_ms.get)
+    res64 = prob.evaluate(theta, nu)
+    res = prob.evaluate(theta, nu, precision="split", team_lanes=best_lanes)
+    plain_ms = time_form("float64", 0, max(2, args.steps // 2), 1)
 
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks = Clocks(local)
-    evs = []
-    for _ in range(args.steps):
-        flush.zero_()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        step_device()
-        e1.record(stream)
-        evs.append((e0, e1))
-    torch.cuda.synchronize()
+    step_ms = time_form("split", best_lanes, args.steps, args.warmup)
     clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in evs]
     t_step = float(np.mean(step_ms)) * 1e-3
     if world > 1:
         tt = torch.tensor([t_step], device="cuda")
@@ -288,13 +297,13 @@ def main():
     h2d = Xo.nbytes + yo.nbytes + Zo.nbytes + prob.nblk * (4 + 4 + 4 * prob.ldnbr + 4) + 8 * len(theta)
     d2h = 8 * (1 + P + P * P + 1) + 16
     for _ in range(2):
-        sv.vecchia_profile_loglik(theta, Xo, yo, Zo, groups, nu)
+        sv.vecchia_profile_loglik(theta, Xo, yo, Zo, groups, nu, precision="split")
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        ll_e2e = sv.vecchia_profile_loglik(theta, Xo, yo, Zo, groups, nu)[0]
+        ll_e2e = sv.vecchia_profile_loglik(theta, Xo, yo, Zo, groups, nu, precision="split")[0]
     torch.cuda.synchronize()
     t_e2e = (time.perf_counter() - t0) / args.steps
     if world > 1:
@@ -311,10 +320,11 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "blocks/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 assembly/Gram + f64 factorisation (split form)",
         "data": "synthetic (seeded; y = Vecchia draw on the GPU)",
         "config": {"workload": f"loglik+score+Fisher, n={n}, d={d}, m={m}, nu={nu}, "
-                               "float64 (plain form)",
+                               "split-precision form",
                    "n": n, "d": d, "m": m, "nu": nu, "blocks_per_step": n,
                    "l2": "flushed between steps (256 MB write, outside the step time)",
                    "parallelism": f"{world} independent problem(s), one per GPU"},
@@ -326,8 +336,15 @@ def main():
                      "basis": "K^3/3 + (P+2)K^2 float64 flops per block (Cholesky, a, W, z); "
                               "peak = float64 FMA probe measured in this run"},
         "clocks": clk,
-        "extra": {"ll": res[0], "ll_e2e": ll_e2e, "maximin_s": t_maximin, "knn_s": t_knn,
-                  "step_ms_all": step_ms},
+        "extra": {"ll_split": res[0], "ll_float64": res64[0], "ll_e2e": ll_e2e,
+                  "rel_dll_split_vs_float64": abs(res[0] - res64[0]) / abs(res64[0]),
+                  "max_rel_dgrad": float(np.abs(res[1] - res64[1]).max() / np.abs(res64[1]).max()),
+                  "max_rel_dfisher": float(np.abs(res[2] - res64[2]).max() / np.abs(res64[2]).max()),
+                  "plain_float64_ms": float(np.mean(plain_ms)),
+                  "plain_float64_blocks_per_s": world * n / (float(np.mean(plain_ms)) * 1e-3),
+                  "plain_float64_roofline_frac": flops / (float(np.mean(plain_ms)) * 1e-3) / 1e12 / peak,
+                  "team_lanes_ms": lane_ms, "team_lanes": best_lanes,
+                  "maximin_s": t_maximin, "knn_s": t_knn, "step_ms_all": step_ms},
     }
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

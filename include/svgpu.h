@@ -39,7 +39,7 @@ typedef struct CUstream_st* sv_stream_t; /* identical to cudaStream_t */
 #define SV_INFO_STATUS 0     /* SV_* status of the device work */
 #define SV_INFO_BLOCK 1      /* first failing block / row, or -1 */
 #define SV_INFO_JITTER 2     /* largest jitter level used (0 = none, 1..9 = 1e-12..1e-4) */
-#define SV_INFO_AUX 3
+#define SV_INFO_AUX 3        /* split form: blocks re-evaluated in float64 */
 
 const char* sv_status_string(int status);
 int sv_abi_version(void);
@@ -91,7 +91,13 @@ typedef struct sv_loglik_desc {
   int32_t need_grad;    /* 1: score and Fisher information too                 */
   int32_t estimate_nu;  /* 1: theta = [log s2, log lam.., log nu, log tau]     */
   int32_t chunked;      /* 1: chunk[] gives the jitter-sharing chunk of a block */
-  int32_t precision;    /* 0 = float64 throughout                               */
+  int32_t precision;    /* 0 = float64 throughout; 1 = split: float32 assembly, */
+                        /*   dSigma.a and Gram products, float64 factorisation */
+                        /*   and solves (closed-form nu, k+1 <= 32 blocks)     */
+  int32_t team_lanes;   /* split form: lanes per block (4, 8, 16, 32; 0 = 8)   */
+  double split_rho_min; /* split form: blocks whose smallest pivot ratio      */
+                        /*   L_kk^2 / Sigma_kk is below this (0 = 1e-4) are    */
+                        /*   re-evaluated in float64; info[SV_INFO_AUX] counts */
   double nu;            /* fixed smoothness (estimate_nu = 0)                   */
   double var_penalty;   /* likelihood.py:165-171                                */
   double log_var_target;

@@ -28,7 +28,8 @@ class LoglikDesc(ctypes.Structure):
     _fields_ = [("n", c_i64), ("nblk", c_i64), ("nblk_warp", c_i64),
                 ("d", c_i32), ("q", c_i32), ("ldnbr", c_i32), ("kmax", c_i32),
                 ("need_grad", c_i32), ("estimate_nu", c_i32), ("chunked", c_i32),
-                ("precision", c_i32), ("nu", c_dbl), ("var_penalty", c_dbl),
+                ("precision", c_i32), ("team_lanes", c_i32), ("split_rho_min", c_dbl),
+                ("nu", c_dbl), ("var_penalty", c_dbl),
                 ("log_var_target", c_dbl)]
 
 

@@ -19,84 +19,9 @@
 // are bitwise reproducible run to run.
 #include <stdio.h>
 
-#include "sv_block.cuh"
+#include "sv_loglik.cuh"
 
 namespace sv {
-
-constexpr int kMaxD = 64;         // input dimensions supported by the block kernels
-constexpr int kMaxQ = 16;         // trend columns
-constexpr int kRedThreads = 256;  // reduction CTA size
-constexpr int kMaxP = kMaxD + 3;
-
-struct LikArgs {
-  const double* X;
-  const double* y;
-  const double* Z;
-  const int32_t* rowb;
-  const int32_t* kb;
-  const int32_t* nbr;
-  const int32_t* chunk;
-  const double* theta;
-  double* cache;
-  int8_t* level;
-  int32_t* chunk_max;
-  int32_t* flags;  // [0] = any block used jitter
-  int32_t* info;
-  int64_t n, b0, b1;
-  int d, q, ldnbr, P, NR, CS, kt;  // kt = team block capacity (32 or kmax+1)
-  int need_grad, estimate_nu, closed;
-  double nu_fixed, nu_fd_h;
-  int fixup;
-};
-
-// 10^p for jitter level lv = p + 13, p = -12..-4 (_covariance.py:247-249)
-__device__ __forceinline__ double jitter_pow10(int lv) {
-  switch (lv) {
-    case 1: return 1e-12;
-    case 2: return 1e-11;
-    case 3: return 1e-10;
-    case 4: return 1e-9;
-    case 5: return 1e-8;
-    case 6: return 1e-7;
-    case 7: return 1e-6;
-    case 8: return 1e-5;
-    default: return 1e-4;
-  }
-}
-
-// per-CTA parameter block in shared memory
-struct PrmSmem {
-  double s2, tau;
-  MaternMode mm;
-  double invlam[kMaxD];
-};
-
-__device__ void load_params(const LikArgs& A, PrmSmem* prm) {
-  if (threadIdx.x == 0) {
-    const int d = A.d;
-    prm->s2 = exp(A.theta[0]);
-    double nu = A.nu_fixed;
-    if (A.estimate_nu) {
-      nu = exp(A.theta[1 + d]);
-      prm->tau = exp(A.theta[2 + d]);
-    } else {
-      prm->tau = exp(A.theta[1 + d]);
-    }
-    MaternMode mm;
-    mm.closed = A.estimate_nu ? -1 : A.closed;
-    mm.estimate_nu = A.estimate_nu;
-    mm.nu = nu;
-    mm.log_coef = (mm.closed < 0) ? matern_log_coef(nu) : 0.0;
-    mm.nu_p = nu + A.nu_fd_h;
-    mm.nu_m = nu - A.nu_fd_h;
-    mm.lc_p = A.estimate_nu ? matern_log_coef(mm.nu_p) : 0.0;
-    mm.lc_m = A.estimate_nu ? matern_log_coef(mm.nu_m) : 0.0;
-    mm.inv2h = 1.0 / (2.0 * A.nu_fd_h);
-    prm->mm = mm;
-  }
-  for (int l = threadIdx.x; l < A.d; l += blockDim.x) prm->invlam[l] = exp(-A.theta[1 + l]);
-  __syncthreads();
-}
 
 // shared-memory footprint (doubles) of one team with block capacity kt
 __host__ __device__ inline int64_t team_smem_doubles(int kt, int d, int NR, int need_grad,
@@ -147,6 +72,8 @@ __device__ void block_pass1(const LikArgs& A, const PrmSmem* prm, int64_t b, dou
   int lv = 0;
   if (A.fixup) {
     lv = A.chunk_max[A.chunk[b]];
+  } else if (A.redo_mode) {
+    lv = A.level[b];
   }
   bool ok = false;
   for (; lv <= 9; ++lv) {
@@ -306,7 +233,9 @@ __global__ void k_block_warp(LikArgs A) {
   double* sm = smem + (sizeof(PrmSmem) + 7) / 8 + w * per_team;
   const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t b = A.b0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + w; b < A.b1; b += nw) {
-    if (A.fixup) {
+    if (A.redo_mode) {
+      if (!A.redo[b]) continue;
+    } else if (A.fixup) {
       if (A.chunk_max[A.chunk[b]] <= A.level[b]) continue;
     } else if (A.kb[b] + 1 > 32) {
       if ((threadIdx.x & 31) == 0) set_error(A.info + SV_INFO_STATUS, SV_EINVAL);
@@ -541,7 +470,7 @@ static int nred_ctas(int64_t nblk) {
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct WsLayout {
-  size_t cache, level, chunk_max, flags, part1, part2, beta, sums, total;
+  size_t cache, level, redo, chunk_max, flags, part1, part2, beta, sums, total;
 };
 
 static WsLayout ws_layout(const sv_loglik_desc* D) {
@@ -554,6 +483,8 @@ static WsLayout ws_layout(const sv_loglik_desc* D) {
   L.cache = off;
   off = align256(off + sizeof(double) * (size_t)CS * (size_t)(D->nblk > 0 ? D->nblk : 1));
   L.level = off;
+  off = align256(off + (size_t)(D->nblk > 0 ? D->nblk : 1));
+  L.redo = off;
   off = align256(off + (size_t)(D->nblk > 0 ? D->nblk : 1));
   L.chunk_max = off;
   off = align256(off + sizeof(int32_t) * (size_t)(D->nblk > 0 ? D->nblk : 1));
@@ -601,6 +532,7 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
   if (D->chunked && !chunk) return SV_EINVAL;
   const int closed = matern_closed_code(D->nu);
   if (!D->estimate_nu && !(D->nu > 0.0)) return SV_EINVAL;
+  if (D->precision != 0 && D->precision != 1) return SV_EINVAL;
   WsLayout W = ws_layout(D);
   if (!workspace || workspace_bytes < W.total) return SV_ENOSPC;
   cudaStream_t st = (cudaStream_t)stream;
@@ -633,6 +565,9 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
   A.nu_fixed = D->nu;
   A.nu_fd_h = 1e-3;  // _matern_general.py:135 (nu_fd_h)
   A.fixup = 0;
+  A.redo = (int8_t*)(ws + W.redo);
+  A.rho_min = D->split_rho_min > 0.0 ? D->split_rho_min : 1e-4;
+  A.redo_mode = 0;
 
   int32_t init_info[4] = {0, -1, 0, 0};
   SV_CUDA_TRY(cudaMemcpyAsync(info, init_info, sizeof(init_info), cudaMemcpyHostToDevice, st));
@@ -641,21 +576,31 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
 
   const int nsm = sv_num_sms();
   const size_t prm_bytes = (sizeof(PrmSmem) + 7) / 8 * 8;
-  // warp kernel: blocks [0, nblk_warp)
+  // warp-sized blocks [0, nblk_warp): float64 warp kernel or split kernel
+  // split form: closed-form nu and at most 32 right-hand sides (d + q <= 29);
+  // anything else runs the float64 kernels
+  const bool split = D->precision == 1 && !D->estimate_nu && closed >= 0 && A.NR <= 32;
+  const int lanes = D->team_lanes > 0 ? D->team_lanes : 8;
+  if (split && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32) return SV_EINVAL;
   if (D->nblk_warp > 0) {
     A.kt = 32;
     A.b0 = 0;
     A.b1 = D->nblk_warp;
-    const size_t team = sizeof(double) * team_smem_doubles(32, A.d, A.NR, A.need_grad, A.estimate_nu);
-    int wpc = 8;
-    while (wpc > 1 && prm_bytes + wpc * team > (size_t)max_smem_optin()) --wpc;
-    const size_t smem = prm_bytes + wpc * team;
-    if (smem > (size_t)max_smem_optin()) return SV_EINVAL;
-    SV_CUDA_TRY(cudaFuncSetAttribute(k_block_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int64_t grid = (D->nblk_warp + wpc - 1) / wpc;
-    if (grid > 64LL * nsm) grid = 64LL * nsm;
-    k_block_warp<<<(int)grid, 32 * wpc, smem, st>>>(A);
-    SV_CUDA_TRY(cudaGetLastError());
+    if (split) {
+      const int rc = launch_block_split(A, lanes, st);
+      if (rc != SV_OK) return rc;
+    } else {
+      const size_t team = sizeof(double) * team_smem_doubles(32, A.d, A.NR, A.need_grad, A.estimate_nu);
+      int wpc = 8;
+      while (wpc > 1 && prm_bytes + wpc * team > (size_t)max_smem_optin()) --wpc;
+      const size_t smem = prm_bytes + wpc * team;
+      if (smem > (size_t)max_smem_optin()) return SV_EINVAL;
+      SV_CUDA_TRY(cudaFuncSetAttribute(k_block_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      int64_t grid = (D->nblk_warp + wpc - 1) / wpc;
+      if (grid > 64LL * nsm) grid = 64LL * nsm;
+      k_block_warp<<<(int)grid, 32 * wpc, smem, st>>>(A);
+      SV_CUDA_TRY(cudaGetLastError());
+    }
   }
   // CTA kernel: blocks [nblk_warp, nblk)
   size_t cta_smem = 0;
@@ -681,12 +626,17 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
       A.kt = 32;
       A.b0 = 0;
       A.b1 = D->nblk_warp;
-      const size_t team = sizeof(double) * team_smem_doubles(32, A.d, A.NR, A.need_grad, A.estimate_nu);
-      int wpc = 8;
-      while (wpc > 1 && prm_bytes + wpc * team > (size_t)max_smem_optin()) --wpc;
-      k_block_warp<<<(int)((D->nblk_warp + wpc - 1) / wpc > 64LL * nsm ? 64LL * nsm : (D->nblk_warp + wpc - 1) / wpc),
-                     32 * wpc, prm_bytes + wpc * team, st>>>(A);
-      SV_CUDA_TRY(cudaGetLastError());
+      if (split) {
+        const int rc = launch_block_split(A, lanes, st);
+        if (rc != SV_OK) return rc;
+      } else {
+        const size_t team = sizeof(double) * team_smem_doubles(32, A.d, A.NR, A.need_grad, A.estimate_nu);
+        int wpc = 8;
+        while (wpc > 1 && prm_bytes + wpc * team > (size_t)max_smem_optin()) --wpc;
+        k_block_warp<<<(int)((D->nblk_warp + wpc - 1) / wpc > 64LL * nsm ? 64LL * nsm : (D->nblk_warp + wpc - 1) / wpc),
+                       32 * wpc, prm_bytes + wpc * team, st>>>(A);
+        SV_CUDA_TRY(cudaGetLastError());
+      }
     }
     if (D->nblk > D->nblk_warp) {
       A.kt = D->kmax + 1;
@@ -697,6 +647,25 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
       k_block_cta<<<(int)grid, 128, cta_smem, st>>>(A);
       SV_CUDA_TRY(cudaGetLastError());
     }
+  }
+
+  // split form: float64 re-evaluation of the blocks it flagged as ill-conditioned
+  if (split && D->nblk_warp > 0) {
+    A.fixup = 0;
+    A.redo_mode = 1;
+    A.kt = 32;
+    A.b0 = 0;
+    A.b1 = D->nblk_warp;
+    const size_t team = sizeof(double) * team_smem_doubles(32, A.d, A.NR, A.need_grad, A.estimate_nu);
+    int wpc = 8;
+    while (wpc > 1 && prm_bytes + wpc * team > (size_t)max_smem_optin()) --wpc;
+    const size_t smem = prm_bytes + wpc * team;
+    if (smem > (size_t)max_smem_optin()) return SV_EINVAL;
+    SV_CUDA_TRY(cudaFuncSetAttribute(k_block_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int64_t grid = (D->nblk_warp + wpc - 1) / wpc;
+    if (grid > 64LL * nsm) grid = 64LL * nsm;
+    k_block_warp<<<(int)grid, 32 * wpc, smem, st>>>(A);
+    SV_CUDA_TRY(cudaGetLastError());
   }
 
   RedArgs R;

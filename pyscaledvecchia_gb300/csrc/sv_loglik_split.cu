@@ -1,0 +1,464 @@
+// Split-precision block kernel of the Vecchia likelihood / score / Fisher
+// evaluation (blocks with K = k+1 <= 32, closed-form nu).
+//
+// Same per-block record as the float64 kernels (likelihood.py:111-144 of the
+// reference), computed with float64 only where conditioning needs it:
+//   float32 : centred scaled coordinates, distances, the correlation
+//             deficit 1 - M (accurate for close pairs) and g, the
+//             products dSigma_l a (K^2 d), the Fisher / score Gram products;
+//   float64 : the diagonal s2(1+tau) (+ jitter), the Cholesky factorisation,
+//             a = L^-T e_K, the forward solves W = L^-1 [dSigma a], L^-1 y,
+//             L^-1 Z, log L_KK and everything reduced afterwards.
+// On GB300 a float64 instruction costs 1/66 of the FP32 rate and a masked
+// lane costs as much as an active one, so a block is owned by a team of G
+// lanes and a warp holds 32/G blocks: the serial part of each Cholesky step
+// (the pivot square root and reciprocal) is shared by 32/G blocks, and the
+// pivot uses an FP32 reciprocal square root refined by two float64 Newton
+// steps (y <- y (3/2 - d y^2 / 2), quadratic convergence from 2^-22).
+//
+// Warp-uniform outer loops (up to the warp's largest K) with team-local
+// predication keep every __syncwarp reached by all lanes when the blocks of a
+// warp differ in size.
+#include "sv_loglik.cuh"
+
+namespace sv {
+
+constexpr int kSplitMaxThreads = 512;
+
+__device__ __forceinline__ void matern_closed_f32(int code, float r, float& M, float& g) {
+  if (code == 0) {
+    if (r > 0.0f) {
+      const float e = expf(-r);
+      M = e;
+      g = -e / r;
+    } else {
+      M = 1.0f;
+      g = 0.0f;
+    }
+  } else if (code == 1) {
+    const float c = 1.7320508075688772f * r;
+    const float e = expf(-c);
+    M = (1.0f + c) * e;
+    g = -3.0f * e;
+  } else {
+    const float c = 2.23606797749979f * r;
+    const float e = expf(-c);
+    M = (1.0f + c + c * c * (1.0f / 3.0f)) * e;
+    g = -(5.0f / 3.0f) * (1.0f + c) * e;
+  }
+}
+
+// Exponential-series tail E_m(c) = sum_{k >= m} c^k / k! for 0 <= c <= 2
+// (nested Horner form, positive terms only: no cancellation).
+__device__ __forceinline__ float exp_tail(float c, int m) {
+  float t = 1.0f;
+#pragma unroll
+  for (int k = 22; k > 0; --k)
+    if (k > m) t = fmaf(t, c * (1.0f / (float)k), 1.0f);
+  float p = 1.0f, f = 1.0f;
+  for (int k = 1; k <= m; ++k) {
+    p *= c;
+    f *= (float)k;
+  }
+  return t * (p / f);
+}
+
+// Correlation deficit D = 1 - M(r) with small relative error for every r
+// (for nearby points M is close to 1 and 1 - M would lose all of float32's
+// digits):  nu = 0.5: -expm1(-r);  nu = 1.5: e^-c E_2(c);
+// nu = 2.5: e^-c (c^2/6 + E_3(c)), c = sqrt(2 nu) r.
+__device__ __forceinline__ float matern_deficit_f32(int code, float r) {
+  if (code == 0) return -expm1f(-r);
+  const float c = (code == 1 ? 1.7320508075688772f : 2.23606797749979f) * r;
+  if (c > 2.0f) {
+    float M, g;
+    matern_closed_f32(code, r, M, g);
+    return 1.0f - M;
+  }
+  const float e = expf(-c);
+  if (code == 1) return e * exp_tail(c, 2);
+  return e * fmaf(c * c, 1.0f / 6.0f, exp_tail(c, 3));
+}
+
+// float64 pivot: lkk = sqrt(dkk), inv = 1/lkk
+__device__ __forceinline__ void pivot_rsqrt(double dkk, double& lkk, double& inv) {
+  if (dkk > 1e-30 && dkk < 1e30) {
+    double y = (double)rsqrtf((float)dkk);
+    const double h = 0.5 * dkk;
+    y = y * fma(-h, y * y, 1.5);
+    y = y * fma(-h, y * y, 1.5);
+    lkk = dkk * y;
+    inv = y;
+  } else {
+    lkk = sqrt(dkk);
+    inv = 1.0 / lkk;
+  }
+}
+
+// L is stored packed by columns with capacity 32: entry (i, j), i >= j, at
+// cstart(j) + i - j.  Column walks (scaling, trailing updates, forward
+// solves) then touch consecutive words, free of bank conflicts.
+__device__ __forceinline__ int cstart(int j) { return j * 32 - (j * (j - 1)) / 2; }
+__device__ __forceinline__ int cm(int i, int j) { return cstart(j) + (i - j); }
+
+template <int G>
+__global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, int wpc) {
+  extern __shared__ double smem[];
+  PrmSmem* prm = (PrmSmem*)smem;
+  load_params(A, prm);
+  constexpr int NB = 32 / G;
+  const unsigned full = 0xffffffffu;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tm = lane / G, tl = lane - (lane / G) * G;
+  const int d = A.d, q = A.q, P = A.P, NR = A.NR;
+  const int64_t slot = split_slot_doubles(d, NR);
+  double* Lp = smem + (sizeof(PrmSmem) + 7) / 8 + (int64_t)(warp * NB + tm) * slot;
+  double* R = Lp + 528;  // NR columns, stride 33
+  double* a = R + 33 * NR;
+  double* invd = a + 32;
+  float* a32 = (float*)(invd + 32);
+  float* u = a32 + 32;
+  int* idx = (int*)(u + 32 * d);
+  volatile int* tflag = idx + 32;
+  double* acc = R;            // column 0 of R is scratch during the a solve
+  float* R32 = (float*)Lp;    // float32 copy of R once L is no longer needed
+
+  const double s2 = prm->s2, tau = prm->tau;
+  const float s2f = (float)s2;
+  const int code = prm->mm.closed;
+  const double diag = s2 * (1.0 + tau);
+
+  const int64_t nb = A.b1 - A.b0;
+  const int64_t stride = (int64_t)gridDim.x * wpc * NB;
+  for (int64_t base = ((int64_t)blockIdx.x * wpc + warp) * NB; base < nb; base += stride) {
+    const int64_t b = A.b0 + base + tm;
+    bool active = (base + tm) < nb;
+    if (active && A.fixup) active = A.chunk_max[A.chunk[b]] > A.level[b];
+    const int K = active ? A.kb[b] + 1 : 0;
+    const int Kw = __reduce_max_sync(full, K);
+    if (Kw == 0) continue;
+    const int k = K - 1;
+
+    // ---- gather: neighbours first, self last; coordinates centred on self
+    if (active)
+      for (int i = tl; i < K; i += G) idx[i] = (i < k) ? A.nbr[b * A.ldnbr + i] : A.rowb[b];
+    __syncwarp();
+    if (active) {
+      const double* xs = A.X + (int64_t)idx[k] * d;
+      for (int t = tl; t < K * d; t += G) {
+        const int i = t / d, l = t - (t / d) * d;
+        u[t] = (float)((A.X[(int64_t)idx[i] * d + l] - xs[l]) * prm->invlam[l]);
+      }
+      if (A.need_grad)
+        for (int i = tl; i < K; i += G) {
+          R[P * 33 + i] = A.y[idx[i]];
+          for (int c = 0; c < q; ++c) R[(P + 1 + c) * 33 + i] = A.Z[(int64_t)idx[i] * q + c];
+        }
+    }
+    __syncwarp();
+
+    // ---- Sigma (float32 deficit, float64 entries) and Cholesky with the
+    //      jitter ladder of _covariance.py:235-252
+    int lv = (active && A.fixup) ? A.chunk_max[A.chunk[b]] : 0;
+    bool done = !active, failed = false;
+    double jit = 0.0;
+    double rho = 1.0;  // smallest pivot ratio L_kk^2 / Sigma_kk (team lane 0)
+    while (__any_sync(full, !done)) {
+      const bool need = !done;
+      if (need) {
+        jit = (lv > 0) ? jitter_pow10(lv) * diag : 0.0;  // 10^p * mean(diag)
+        const int npair = K * (K + 1) / 2;
+        for (int t = tl; t < npair; t += G) {
+          int i, j;
+          tri_index(t, i, j);
+          double v;
+          if (i == j) {
+            v = diag + jit;
+          } else {
+            float r2 = 0.0f;
+            for (int l = 0; l < d; ++l) {
+              const float df = u[i * d + l] - u[j * d + l];
+              r2 = fmaf(df, df, r2);
+            }
+            // s2 (1 - D): the deficit carries the information of close pairs
+            v = fma(-s2, (double)matern_deficit_f32(code, sqrtf(r2)), s2);
+          }
+          Lp[cm(i, j)] = v;
+        }
+        if (tl == 0) *tflag = 0;
+      }
+      __syncwarp();
+      // right-looking Cholesky by columns, warp-uniform step loop
+      for (int kk = 0; kk < Kw; ++kk) {
+        const bool go = need && kk < K;
+        if (go && tl == 0 && *tflag == 0) {
+          const int o = cm(kk, kk);
+          const double dkk = Lp[o];
+          if (!(dkk > 0.0)) {
+            *tflag = 1;
+          } else {
+            double lkk, inv;
+            rho = fmin(rho, dkk / (diag + jit));
+            pivot_rsqrt(dkk, lkk, inv);
+            Lp[o] = lkk;
+            invd[kk] = inv;
+          }
+        }
+        __syncwarp();
+        const bool go2 = go && *tflag == 0;
+        if (go2) {
+          const double inv = invd[kk];
+          double* colk = Lp + cstart(kk) - kk;  // colk[i] = L(i, kk)
+          for (int i = kk + 1 + tl; i < K; i += G) colk[i] *= inv;
+        }
+        __syncwarp();
+        if (go2) {
+          const int m = K - kk - 1;
+          const int cnt = m * (m + 1) / 2;
+          if (tl < cnt) {
+            const double* colk = Lp + cstart(kk) - kk;
+            int j = kk + 1, rem = tl;
+            while (rem >= K - j) {
+              rem -= K - j;
+              ++j;
+            }
+            for (int t = tl; t < cnt; t += G) {
+              Lp[cm(j + rem, j)] -= colk[j + rem] * colk[j];
+              rem += G;
+              while (j < K && rem >= K - j) {
+                rem -= K - j;
+                ++j;
+              }
+            }
+          }
+        }
+        __syncwarp();
+      }
+      if (need) {
+        if (*tflag == 0) {
+          done = true;
+        } else if (rho = 1.0, ++lv > 9) {
+          done = true;
+          failed = true;
+        }
+      }
+      __syncwarp();
+    }
+
+    double* rec = A.cache + b * (int64_t)A.CS;
+    if (failed) {
+      // not positive definite even with jitter after float32 assembly: the
+      // float64 pass decides (and reports a failure if it fails as well)
+      if (tl == 0) {
+        A.level[b] = 0;
+        A.redo[b] = 1;
+        atomicAdd(A.info + SV_INFO_AUX, 1);
+      }
+      for (int f = tl; f < A.CS; f += G) rec[f] = 0.0;
+    } else if (active && tl == 0) {
+      A.level[b] = (int8_t)lv;
+      if (lv > 0) {
+        atomicMax(A.info + SV_INFO_JITTER, lv);
+        A.flags[0] = 1;
+      }
+      // ill-conditioned blocks lose too much to float32 assembly: redo in float64
+      const bool again = rho < A.rho_min;
+      A.redo[b] = again ? 1 : 0;
+      if (again) atomicAdd(A.info + SV_INFO_AUX, 1);
+    }
+    const bool ok = active && !failed;
+
+    // ---- a = L^-T e_K (float64, right-looking over rows of L)
+    if (ok)
+      for (int i = tl; i < K; i += G) acc[i] = (i == k) ? 1.0 : 0.0;
+    __syncwarp();
+    for (int i = Kw - 1; i >= 0; --i) {
+      if (ok && i < K) {
+        const double ai = acc[i] * invd[i];
+        for (int j = tl; j < i; j += G) acc[j] -= Lp[cm(i, j)] * ai;
+        if (tl == 0) {
+          a[i] = ai;
+          a32[i] = (float)ai;
+        }
+      }
+      __syncwarp();
+    }
+
+    // ---- GLS parts (float64 team sums)
+    {
+      double vy = 0.0;
+      if (ok)
+        for (int i = tl; i < K; i += G) vy += a[i] * A.y[idx[i]];
+      for (int o = G / 2; o > 0; o >>= 1) vy += __shfl_xor_sync(full, vy, o);
+      if (ok && tl == 0) {
+        rec[0] = log(Lp[cm(k, k)]);
+        rec[1] = vy;
+      }
+      for (int c = 0; c < q; ++c) {
+        double vz = 0.0;
+        if (ok)
+          for (int i = tl; i < K; i += G) vz += a[i] * A.Z[(int64_t)idx[i] * q + c];
+        for (int o = G / 2; o > 0; o >>= 1) vz += __shfl_xor_sync(full, vz, o);
+        if (ok && tl == 0) rec[2 + c] = vz;
+      }
+    }
+    if (!A.need_grad) {
+      __syncwarp();
+      if (ok && tl == 0) {
+        rec[2 + q] = rec[1];
+        for (int c = 0; c < q; ++c) rec[3 + q + c] = rec[2 + c];
+      }
+      __syncwarp();
+      continue;
+    }
+    __syncwarp();
+
+    // ---- right-hand sides dSigma_p a
+    if (ok) {
+      // p = 0: Sigma (un-jittered) a = L_KK e_K - jit a
+      const double lKK = Lp[cm(k, k)];
+      for (int i = tl; i < K; i += G) R[i] = ((i == k) ? lKK : 0.0) - jit * a[i];
+      // p = 1..d (float32): -s2 sum_j g_ij a_j (u_il - u_jl)^2
+      for (int i = tl; i < K; i += G) {
+        float cj[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          float c = 0.0f;
+          if (j < K && j != i) {
+            float r2 = 0.0f;
+            for (int l = 0; l < d; ++l) {
+              const float df = u[i * d + l] - u[j * d + l];
+              r2 = fmaf(df, df, r2);
+            }
+            float M, g;
+            matern_closed_f32(code, sqrtf(r2), M, g);
+            c = g * a32[j];
+          }
+          cj[j] = c;
+        }
+        for (int l = 0; l < d; ++l) {
+          const float uil = u[i * d + l];
+          float s = 0.0f;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            if (j < K) {
+              const float df = uil - u[j * d + l];
+              s = fmaf(cj[j], df * df, s);
+            }
+          }
+          R[(1 + l) * 33 + i] = (double)(-s2f * s);
+        }
+      }
+      // nugget row: dSigma_tau = s2 tau I
+      for (int i = tl; i < K; i += G) R[(P - 1) * 33 + i] = s2 * tau * a[i];
+    }
+    __syncwarp();
+
+    // ---- forward solves (float64): W, L^-1 y, L^-1 Z; column walks
+    for (int i = 0; i < Kw; ++i) {
+      if (ok && i < K)
+        for (int c = tl; c < NR; c += G) R[c * 33 + i] *= invd[i];
+      __syncwarp();
+      if (ok && i < K - 1) {
+        const int m = K - i - 1;
+        const int cnt = m * NR;
+        if (tl < cnt) {
+          const double* coli = Lp + cstart(i) - i;  // coli[j] = L(j, i)
+          int c = tl / m, r = tl - (tl / m) * m;
+          for (int t = tl; t < cnt; t += G) {
+            const int j = i + 1 + r;
+            R[c * 33 + j] -= coli[j] * R[c * 33 + i];
+            r += G;
+            while (r >= m) {
+              r -= m;
+              ++c;
+            }
+          }
+        }
+      }
+      __syncwarp();
+    }
+
+    // ---- record: z parts, w_K (float64), Gram products (float32)
+    if (ok) {
+      for (int e = tl; e < NR * 33; e += G) {
+        const int c = e / 33, j = e - (e / 33) * 33;
+        R32[e] = (j < K) ? (float)R[c * 33 + j] : 0.0f;
+      }
+    }
+    __syncwarp();
+    if (ok) {
+      double* wK = rec + 3 + 2 * q;
+      double* wzy = wK + P;
+      double* wzZ = wzy + P;
+      double* F = wzZ + P * q;
+      for (int c = tl; c < 1 + q; c += G) rec[2 + q + c] = R[(P + c) * 33 + k];
+      for (int p = tl; p < P; p += G) wK[p] = R[p * 33 + k];
+      const int nf = P * (P + 1) / 2;
+      const int ntot = nf + P * (1 + q);
+      for (int t = tl; t < ntot; t += G) {
+        int c1, c2;
+        if (t < nf) {
+          tri_index(t, c1, c2);
+        } else {
+          const int s3 = t - nf;
+          c1 = s3 / (1 + q);
+          c2 = P + (s3 - c1 * (1 + q));
+        }
+        const float* r1 = R32 + c1 * 33;
+        const float* r2 = R32 + c2 * 33;
+        float sacc = 0.0f;
+        for (int i = 0; i < K; ++i) sacc = fmaf(r1[i], r2[i], sacc);
+        if (t < nf) {
+          F[t] = 0.5 * (2.0 * (double)sacc - R[c1 * 33 + k] * R[c2 * 33 + k]);
+        } else {
+          const int s3 = t - nf;
+          const int p = s3 / (1 + q);
+          const int cc = s3 - p * (1 + q);
+          if (cc == 0)
+            wzy[p] = (double)sacc;
+          else
+            wzZ[p * q + (cc - 1)] = (double)sacc;
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+int launch_block_split(const LikArgs& A, int lanes, cudaStream_t st) {
+  int dev = 0, maxsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t prm = (sizeof(PrmSmem) + 7) / 8 * 8;
+  const size_t per_warp = sizeof(double) * (size_t)split_slot_doubles(A.d, A.NR) * (32 / lanes);
+  int wpc = kSplitMaxThreads / 32;
+  while (wpc > 1 && prm + wpc * per_warp > (size_t)maxsm) --wpc;
+  const size_t smem = prm + wpc * per_warp;
+  if (smem > (size_t)maxsm) return SV_EINVAL;
+  const int64_t nb = A.b1 - A.b0;
+  const int64_t per_cta = (int64_t)wpc * (32 / lanes);
+  int64_t grid = (nb + per_cta - 1) / per_cta;
+  const int nsm = sv_num_sms();
+  if (grid > 64LL * nsm) grid = 64LL * nsm;
+  if (grid < 1) grid = 1;
+  switch (lanes) {
+#define SV_SPLIT_CASE(GV)                                                                          \
+  case GV:                                                                                         \
+    SV_CUDA_TRY(cudaFuncSetAttribute(k_block_split<GV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     (int)smem));                                                  \
+    k_block_split<GV><<<(unsigned)grid, 32 * wpc, smem, st>>>(A, wpc);                            \
+    break;
+    SV_SPLIT_CASE(4)
+    SV_SPLIT_CASE(8)
+    SV_SPLIT_CASE(16)
+    SV_SPLIT_CASE(32)
+#undef SV_SPLIT_CASE
+    default:
+      return SV_EINVAL;
+  }
+  SV_CUDA_TRY(cudaGetLastError());
+  return SV_OK;
+}
+
+}  // namespace sv

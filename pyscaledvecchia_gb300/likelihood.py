@@ -23,6 +23,7 @@ from ._covariance import _check_nu, _chunks
 __all__ = ["vecchia_profile_loglik"]
 
 _WARP_K = 32  # blocks with K = k+1 <= 32 run one per warp, larger ones one per CTA
+_PRECISION = {"float64": 0, "split": 1}
 
 
 def pack_groups(groups, n=None):
@@ -125,15 +126,21 @@ class DeviceProblem:
         return self._chunks[Pc]
 
     def launch(self, theta_dev, P, nu, estimate_nu, need_grad, var_penalty, log_var_target,
-               chunked=True, stream=None):
-        """Enqueue one evaluation; results land in self.out / self.info."""
+               chunked=True, stream=None, precision="float64", team_lanes=0):
+        """Enqueue one evaluation; results land in self.out / self.info.
+
+        precision "float64" is the reference's arithmetic; "split" computes
+        distances, Matern terms, dSigma.a and the Gram products in float32 and
+        keeps the factorisation, solves and log-determinants in float64
+        (closed-form nu; other cases fall back to float64 in the library)."""
         torch, lib = self.torch, self.lib
         D = _lib.LoglikDesc()
         D.n, D.nblk, D.nblk_warp = self.n, self.nblk, self.nblk_warp
         D.d, D.q, D.ldnbr, D.kmax = self.d, self.q, self.ldnbr, self.kmax
         D.need_grad, D.estimate_nu = int(bool(need_grad)), int(bool(estimate_nu))
         D.chunked = int(bool(chunked))
-        D.precision = 0
+        D.precision = _PRECISION[precision]
+        D.team_lanes = int(team_lanes)
         D.nu = float(nu) if nu is not None else 1.0
         D.var_penalty, D.log_var_target = float(var_penalty), float(log_var_target)
         nbytes = lib.sv_loglik_workspace_bytes(D)
@@ -151,7 +158,7 @@ class DeviceProblem:
         _lib.check(lib, rc, "sv_vecchia_loglik")
 
     def evaluate(self, theta, nu, estimate_nu=False, need_grad=True, var_penalty=0.0,
-                 log_var_target=0.0, chunked=True):
+                 log_var_target=0.0, chunked=True, precision="float64", team_lanes=0):
         torch = self.torch
         theta = np.asarray(theta, dtype=float).reshape(-1)
         d = self.d
@@ -161,10 +168,12 @@ class DeviceProblem:
         if not estimate_nu:
             _check_nu(nu)
         th = _lib.to_dev(torch, theta[:P], np.float64)
-        self.launch(th, P, nu, estimate_nu, need_grad, var_penalty, log_var_target, chunked)
+        self.launch(th, P, nu, estimate_nu, need_grad, var_penalty, log_var_target, chunked,
+                    precision=precision, team_lanes=team_lanes)
         res = torch.cat([self.out, self.info.to(torch.float64)]).cpu().numpy()
         nout = 1 + P + P * P + self.q
-        _lib.check_info(self.lib, res[nout:].astype(np.int64), "sv_vecchia_loglik")
+        self.last_info = res[nout:].astype(np.int64)
+        _lib.check_info(self.lib, self.last_info, "sv_vecchia_loglik")
         ll = float(res[0])
         beta = res[1 + P + P * P:nout].copy() if self.has_Z else np.zeros(0)
         if not need_grad:
@@ -175,7 +184,8 @@ class DeviceProblem:
 
 
 def vecchia_profile_loglik(theta, Xo, yo, Zo, groups, nu, estimate_nu=False,
-                           need_grad=True, var_penalty=0.0, log_var_target=0.0):
+                           need_grad=True, var_penalty=0.0, log_var_target=0.0, *,
+                           precision="float64"):
     """Profile Vecchia loglikelihood, its gradient and the Fisher information.
 
     theta : (P,) log-scale parameters [log sigma^2, log lambda_1..d, log tau]
@@ -184,12 +194,18 @@ def vecchia_profile_loglik(theta, Xo, yo, Zo, groups, nu, estimate_nu=False,
     Xo, yo, Zo : inputs, responses and trend design (or None) in Vecchia order.
     groups : output of ``ordering._nn_groups``.
     nu : fixed Matern smoothness (ignored with ``estimate_nu``).
+    precision (keyword only, not in the reference): "float64" (default, the
+            reference's arithmetic) or "split" (float32 assembly and Gram
+            products, float64 factorisation; see DeviceProblem.launch).
     Returns (ll, grad, fisher, beta); grad and fisher are None when
     ``need_grad`` is False.  Raises numpy.linalg.LinAlgError when a block
     cannot be factorised even with jitter.
     """
     theta = np.asarray(theta, dtype=float)
+    if precision not in _PRECISION:
+        raise ValueError("precision must be 'float64' or 'split'")
     prob = DeviceProblem(Xo, yo, Zo, groups)
     return prob.evaluate(theta, nu, estimate_nu=estimate_nu, need_grad=need_grad,
-                         var_penalty=var_penalty, log_var_target=log_var_target)
+                         var_penalty=var_penalty, log_var_target=log_var_target,
+                         precision=precision)
 
