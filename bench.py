@@ -246,9 +246,7 @@ def main():
     th_d = _lib.to_dev(torch, theta, np.float64)
     kb = np.minimum(np.arange(n), m)
     flops = block_flops(kb, P)
-    launches_per_step = (1 if prob.nblk_warp else 0) + (1 if prob.nblk > prob.nblk_warp else 0)
-    launches_per_step += 1 + (1 if prob.nblk_warp else 0) + (1 if prob.nblk > prob.nblk_warp else 0)
-    launches_per_step += 4
+    launches_per_step = prob.kernel_launches("split", nu=nu)
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()

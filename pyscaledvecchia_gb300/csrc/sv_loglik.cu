@@ -126,7 +126,7 @@ __device__ void block_pass1(const LikArgs& A, const PrmSmem* prm, int64_t b, dou
     for (int i = lane; i < K; i += T) vy += a[i] * A.y[idx[i]];
     vy = team_sum<T>(vy, red);
     if (lane == 0) {
-      rec[0] = log(Lp[tri_off(K - 1, K - 1)]);
+      rec[0] = Lp[tri_off(K - 1, K - 1)];  // L_KK; the log is taken in the reduction
       rec[1] = vy;
     }
     for (int c = 0; c < q; ++c) {
@@ -306,7 +306,7 @@ __global__ void k_reduce1(RedArgs R) {
   for (int f = threadIdx.x; f < nf; f += blockDim.x) {
     double s = 0.0;
     if (f == 0) {
-      for (int64_t b = b0; b < b1; ++b) s += R.cache[b * R.CS];
+      for (int64_t b = b0; b < b1; ++b) s += log(R.cache[b * R.CS]);
     } else if (f < 1 + q) {
       const int i = f - 1;
       for (int64_t b = b0; b < b1; ++b) s += R.cache[b * R.CS + 2 + i] * R.cache[b * R.CS + 1];
@@ -378,7 +378,7 @@ __global__ void k_reduce2(RedArgs R) {
     const double* c = R.cache + b * R.CS;
     double zK = c[2 + q];
     for (int i = 0; i < q; ++i) zK -= c[3 + q + i] * sbeta[i];
-    acc[0] -= 0.5 * (2.0 * c[0] + zK * zK);
+    acc[0] -= 0.5 * (2.0 * log(c[0]) + zK * zK);
     if (R.need_grad) {
       const double* wK = c + 3 + 2 * q;
       const double* wzy = wK + P;
@@ -470,7 +470,7 @@ static int nred_ctas(int64_t nblk) {
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct WsLayout {
-  size_t cache, level, redo, chunk_max, flags, part1, part2, beta, sums, total;
+  size_t cache, level, redo, chunk_max, flags, part1, part2, beta, sums, xhl, total;
 };
 
 static WsLayout ws_layout(const sv_loglik_desc* D) {
@@ -498,6 +498,8 @@ static WsLayout ws_layout(const sv_loglik_desc* D) {
   off = align256(off + sizeof(double) * (kMaxQ + 1));
   L.sums = off;
   off = align256(off + sizeof(double) * (size_t)nfield1(q, P, D->need_grad));
+  L.xhl = off;
+  if (D->precision == 1) off = align256(off + sizeof(float) * 2 * (size_t)D->n * (size_t)D->d);
   L.total = off;
   return L;
 }
@@ -568,6 +570,7 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
   A.redo = (int8_t*)(ws + W.redo);
   A.rho_min = D->split_rho_min > 0.0 ? D->split_rho_min : 1e-4;
   A.redo_mode = 0;
+  A.xhl = (float2*)(ws + W.xhl);
 
   int32_t init_info[4] = {0, -1, 0, 0};
   SV_CUDA_TRY(cudaMemcpyAsync(info, init_info, sizeof(init_info), cudaMemcpyHostToDevice, st));
@@ -587,7 +590,9 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
     A.b0 = 0;
     A.b1 = D->nblk_warp;
     if (split) {
-      const int rc = launch_block_split(A, lanes, st);
+      int rc = launch_split_prep(A, st);
+      if (rc != SV_OK) return rc;
+      rc = launch_block_split(A, lanes, st);
       if (rc != SV_OK) return rc;
     } else {
       const size_t team = sizeof(double) * team_smem_doubles(32, A.d, A.NR, A.need_grad, A.estimate_nu);

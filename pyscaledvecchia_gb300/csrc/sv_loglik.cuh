@@ -34,6 +34,8 @@ struct LikArgs {
   int8_t* redo;
   double rho_min;
   int redo_mode;  // float64 kernel: only blocks with redo[b] != 0
+  // split form: scaled coordinates x / lambda as float32 (hi, lo) pairs
+  float2* xhl;
 };
 
 // 10^p for jitter level lv = p + 13, p = -12..-4 (_covariance.py:247-249)
@@ -86,7 +88,7 @@ __device__ inline void load_params(const LikArgs& A, PrmSmem* prm) {
 }
 
 
-// block record layout (doubles): [log L_KK, a.y, a.Z(q), (L^-1 y)_K, (L^-1 Z)_K(q),
+// block record layout (doubles): [L_KK, a.y, a.Z(q), (L^-1 y)_K, (L^-1 Z)_K(q),
 // w_K(P), W(L^-1 y)(P), W(L^-1 Z)(P q), F(P(P+1)/2) packed lower]
 __host__ __device__ inline int record_stride(int q, int P, int need_grad) {
   return 3 + 2 * q + (need_grad ? (2 * P + P * q + P * (P + 1) / 2) : 0);
@@ -106,5 +108,8 @@ __host__ __device__ inline int split_slot_doubles(int d, int NR) {
 // launches the split-precision kernel over blocks [A.b0, A.b1) (all K <= 32,
 // closed-form nu); lanes = block team width (4, 8, 16 or 32)
 int launch_block_split(const LikArgs& A, int lanes, cudaStream_t st);
+
+// split form: fills A.xhl (n * d float2) from X and theta
+int launch_split_prep(const LikArgs& A, cudaStream_t st);
 
 }  // namespace sv

@@ -11,10 +11,13 @@
 //             L^-1 Z, log L_KK and everything reduced afterwards.
 // On GB300 a float64 instruction costs 1/66 of the FP32 rate and a masked
 // lane costs as much as an active one, so a block is owned by a team of G
-// lanes and a warp holds 32/G blocks: the serial part of each Cholesky step
-// (the pivot square root and reciprocal) is shared by 32/G blocks, and the
-// pivot uses an FP32 reciprocal square root refined by two float64 Newton
-// steps (y <- y (3/2 - d y^2 / 2), quadratic convergence from 2^-22).
+// lanes and a warp holds 32/G blocks: the serial part of each factorisation
+// step is shared by 32/G blocks.  The factorisation is LDL^T (unit lower L,
+// D = diag(d_k)), which needs one reciprocal per step (an FP32 seed and one
+// float64 Newton step) and no square roots; the Cholesky factor is
+// C = L D^(1/2), so a = C^-T e_K = L^-T e_K / sqrt(d_K), W = D^(-1/2) L^-1 V
+// (unit forward solves, the D^(-1/2) weights applied in the float32 Gram)
+// and L_KK = sqrt(d_K) (one float64 square root per block).
 //
 // Warp-uniform outer loops (up to the warp's largest K) with team-local
 // predication keep every __syncwarp reached by all lanes when the blocks of a
@@ -80,19 +83,23 @@ __device__ __forceinline__ float matern_deficit_f32(int code, float r) {
   return e * fmaf(c * c, 1.0f / 6.0f, exp_tail(c, 3));
 }
 
-// float64 pivot: lkk = sqrt(dkk), inv = 1/lkk
-__device__ __forceinline__ void pivot_rsqrt(double dkk, double& lkk, double& inv) {
-  if (dkk > 1e-30 && dkk < 1e30) {
-    double y = (double)rsqrtf((float)dkk);
-    const double h = 0.5 * dkk;
-    y = y * fma(-h, y * y, 1.5);
-    y = y * fma(-h, y * y, 1.5);
-    lkk = dkk * y;
-    inv = y;
-  } else {
-    lkk = sqrt(dkk);
-    inv = 1.0 / lkk;
+// Order tests on the bit patterns of positive doubles (integer pipe, not the
+// slow float64 pipe): for x, y >= 0, x < y <=> bits(x) < bits(y).
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+constexpr long long kBitsTiny = 0x39B4484BFEEBC2A0LL;  // 1e-30
+constexpr long long kBitsHuge = 0x46293E5939A08CEALL;  // 1e30
+constexpr long long kBitsInf = 0x7FF0000000000000LL;
+
+// float64 reciprocal of a pivot from the float32 reciprocal refined by one
+// Newton step y <- y + y (1 - d y): relative error about 2^-44, far below the
+// float32 assembly error of the split form; a chain of two float64 FMAs.
+__device__ __forceinline__ double pivot_rcp(double dkk) {
+  const long long bd = dbits(dkk);
+  if (bd > kBitsTiny && bd < kBitsHuge) {
+    const double y = (double)(1.0f / (float)dkk);
+    return fma(y, fma(-dkk, y, 1.0), y);
   }
+  return 1.0 / dkk;
 }
 
 // L is stored packed by columns with capacity 32: entry (i, j), i >= j, at
@@ -144,10 +151,14 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       for (int i = tl; i < K; i += G) idx[i] = (i < k) ? A.nbr[b * A.ldnbr + i] : A.rowb[b];
     __syncwarp();
     if (active) {
-      const double* xs = A.X + (int64_t)idx[k] * d;
+      // centred scaled coordinates from the (hi, lo) float32 pairs: the
+      // difference keeps ~24 bits relative to itself, however close the points
+      const float2* xs = A.xhl + (int64_t)idx[k] * d;
       for (int t = tl; t < K * d; t += G) {
         const int i = t / d, l = t - (t / d) * d;
-        u[t] = (float)((A.X[(int64_t)idx[i] * d + l] - xs[l]) * prm->invlam[l]);
+        const float2 v = A.xhl[(int64_t)idx[i] * d + l];
+        const float2 w = xs[l];
+        u[t] = (v.x - w.x) + (v.y - w.y);
       }
       if (A.need_grad)
         for (int i = tl; i < K; i += G) {
@@ -162,11 +173,13 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     int lv = (active && A.fixup) ? A.chunk_max[A.chunk[b]] : 0;
     bool done = !active, failed = false;
     double jit = 0.0;
-    double rho = 1.0;  // smallest pivot ratio L_kk^2 / Sigma_kk (team lane 0)
+    long long rho_bits = 0;
+    bool ill = false;  // a pivot ratio L_kk^2 / Sigma_kk fell below rho_min (team lane 0)
     while (__any_sync(full, !done)) {
       const bool need = !done;
       if (need) {
         jit = (lv > 0) ? jitter_pow10(lv) * diag : 0.0;  // 10^p * mean(diag)
+        rho_bits = dbits(A.rho_min * (diag + jit));
         const int npair = K * (K + 1) / 2;
         for (int t = tl; t < npair; t += G) {
           int i, j;
@@ -188,20 +201,19 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         if (tl == 0) *tflag = 0;
       }
       __syncwarp();
-      // right-looking Cholesky by columns, warp-uniform step loop
+      // right-looking LDL^T by columns, warp-uniform step loop; acc holds the
+      // unscaled pivot column of the current step
       for (int kk = 0; kk < Kw; ++kk) {
         const bool go = need && kk < K;
         if (go && tl == 0 && *tflag == 0) {
-          const int o = cm(kk, kk);
-          const double dkk = Lp[o];
-          if (!(dkk > 0.0)) {
+          const double dkk = Lp[cm(kk, kk)];
+          const long long bd = dbits(dkk);
+          // LAPACK criterion: a pivot that is not > 0 (negative, zero or NaN) fails
+          if (bd <= 0 || bd >= kBitsInf) {
             *tflag = 1;
           } else {
-            double lkk, inv;
-            rho = fmin(rho, dkk / (diag + jit));
-            pivot_rsqrt(dkk, lkk, inv);
-            Lp[o] = lkk;
-            invd[kk] = inv;
+            ill = ill || (bd < rho_bits);
+            invd[kk] = pivot_rcp(dkk);
           }
         }
         __syncwarp();
@@ -209,7 +221,11 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         if (go2) {
           const double inv = invd[kk];
           double* colk = Lp + cstart(kk) - kk;  // colk[i] = L(i, kk)
-          for (int i = kk + 1 + tl; i < K; i += G) colk[i] *= inv;
+          for (int i = kk + 1 + tl; i < K; i += G) {
+            const double v = colk[i];
+            acc[i] = v;
+            colk[i] = v * inv;
+          }
         }
         __syncwarp();
         if (go2) {
@@ -222,13 +238,31 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
               rem -= K - j;
               ++j;
             }
-            for (int t = tl; t < cnt; t += G) {
-              Lp[cm(j + rem, j)] -= colk[j + rem] * colk[j];
-              rem += G;
-              while (j < K && rem >= K - j) {
-                rem -= K - j;
-                ++j;
+            // four independent elements per round keep several float64 FMAs
+            // in flight per lane:  A(i, j) -= l(i, k) * A(j, k)
+            for (int t = tl; t < cnt; t += 4 * G) {
+              int jj[4], ii[4];
+#pragma unroll
+              for (int u4 = 0; u4 < 4; ++u4) {
+                jj[u4] = j;
+                ii[u4] = j + rem;
+                rem += G;
+                while (j < K && rem >= K - j) {
+                  rem -= K - j;
+                  ++j;
+                }
               }
+              double lik[4], ajk[4], aij[4];
+#pragma unroll
+              for (int u4 = 0; u4 < 4; ++u4)
+                if (t + u4 * G < cnt) {
+                  lik[u4] = colk[ii[u4]];
+                  ajk[u4] = acc[jj[u4]];
+                  aij[u4] = Lp[cm(ii[u4], jj[u4])];
+                }
+#pragma unroll
+              for (int u4 = 0; u4 < 4; ++u4)
+                if (t + u4 * G < cnt) Lp[cm(ii[u4], jj[u4])] = fma(-lik[u4], ajk[u4], aij[u4]);
             }
           }
         }
@@ -237,7 +271,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       if (need) {
         if (*tflag == 0) {
           done = true;
-        } else if (rho = 1.0, ++lv > 9) {
+        } else if (ill = false, ++lv > 9) {
           done = true;
           failed = true;
         }
@@ -262,27 +296,35 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         A.flags[0] = 1;
       }
       // ill-conditioned blocks lose too much to float32 assembly: redo in float64
-      const bool again = rho < A.rho_min;
+      const bool again = ill;
       A.redo[b] = again ? 1 : 0;
       if (again) atomicAdd(A.info + SV_INFO_AUX, 1);
     }
     const bool ok = active && !failed;
 
-    // ---- a = L^-T e_K (float64, right-looking over rows of L)
-    if (ok)
+    // ---- a = C^-T e_K = L^-T e_K / sqrt(d_K)  (float64, unit back substitution)
+    double lKK = 0.0, sK = 0.0;  // L_KK = sqrt(d_K) and its reciprocal
+    if (ok) {
+      lKK = sqrt(Lp[cm(k, k)]);
+      sK = 1.0 / lKK;
+      if (tl == 0) rec[0] = lKK;  // L_KK; the log is taken in the reduction
       for (int i = tl; i < K; i += G) acc[i] = (i == k) ? 1.0 : 0.0;
+    }
     __syncwarp();
     for (int i = Kw - 1; i >= 0; --i) {
       if (ok && i < K) {
-        const double ai = acc[i] * invd[i];
+        const double ai = acc[i];
         for (int j = tl; j < i; j += G) acc[j] -= Lp[cm(i, j)] * ai;
-        if (tl == 0) {
-          a[i] = ai;
-          a32[i] = (float)ai;
-        }
       }
       __syncwarp();
     }
+    if (ok)
+      for (int i = tl; i < K; i += G) {
+        const double ai = acc[i] * sK;
+        a[i] = ai;
+        a32[i] = (float)ai;
+      }
+    __syncwarp();
 
     // ---- GLS parts (float64 team sums)
     {
@@ -290,10 +332,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       if (ok)
         for (int i = tl; i < K; i += G) vy += a[i] * A.y[idx[i]];
       for (int o = G / 2; o > 0; o >>= 1) vy += __shfl_xor_sync(full, vy, o);
-      if (ok && tl == 0) {
-        rec[0] = log(Lp[cm(k, k)]);
-        rec[1] = vy;
-      }
+      if (ok && tl == 0) rec[1] = vy;
       for (int c = 0; c < q; ++c) {
         double vz = 0.0;
         if (ok)
@@ -316,7 +355,6 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     // ---- right-hand sides dSigma_p a
     if (ok) {
       // p = 0: Sigma (un-jittered) a = L_KK e_K - jit a
-      const double lKK = Lp[cm(k, k)];
       for (int i = tl; i < K; i += G) R[i] = ((i == k) ? lKK : 0.0) - jit * a[i];
       // p = 1..d (float32): -s2 sum_j g_ij a_j (u_il - u_jl)^2
       for (int i = tl; i < K; i += G) {
@@ -354,36 +392,59 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     }
     __syncwarp();
 
-    // ---- forward solves (float64): W, L^-1 y, L^-1 Z; column walks
-    for (int i = 0; i < Kw; ++i) {
-      if (ok && i < K)
-        for (int c = tl; c < NR; c += G) R[c * 33 + i] *= invd[i];
-      __syncwarp();
+    // ---- forward solves (float64) with the unit factor: L^-1 [dSigma a, y, Z];
+    // W = D^(-1/2) L^-1 dSigma a.  Without jitter Sigma a = L_KK e_K, whose
+    // solution is sqrt(d_K) e_K, so that column is left out of the solve.
+    const int c0 = (jit == 0.0) ? 1 : 0;
+    for (int i = 0; i < Kw - 1; ++i) {
       if (ok && i < K - 1) {
         const int m = K - i - 1;
-        const int cnt = m * NR;
+        const int cnt = m * (NR - c0);
         if (tl < cnt) {
           const double* coli = Lp + cstart(i) - i;  // coli[j] = L(j, i)
-          int c = tl / m, r = tl - (tl / m) * m;
-          for (int t = tl; t < cnt; t += G) {
-            const int j = i + 1 + r;
-            R[c * 33 + j] -= coli[j] * R[c * 33 + i];
-            r += G;
-            while (r >= m) {
-              r -= m;
-              ++c;
+          int c = c0 + tl / m, r = tl - (tl / m) * m;
+          for (int t = tl; t < cnt; t += 4 * G) {
+            int cc[4], jj[4];
+#pragma unroll
+            for (int u4 = 0; u4 < 4; ++u4) {
+              cc[u4] = c;
+              jj[u4] = i + 1 + r;
+              r += G;
+              while (r >= m) {
+                r -= m;
+                ++c;
+              }
             }
+            double lji[4], rci[4], rcj[4];
+#pragma unroll
+            for (int u4 = 0; u4 < 4; ++u4)
+              if (t + u4 * G < cnt) {
+                lji[u4] = coli[jj[u4]];
+                rci[u4] = R[cc[u4] * 33 + i];
+                rcj[u4] = R[cc[u4] * 33 + jj[u4]];
+              }
+#pragma unroll
+            for (int u4 = 0; u4 < 4; ++u4)
+              if (t + u4 * G < cnt) R[cc[u4] * 33 + jj[u4]] = fma(-lji[u4], rci[u4], rcj[u4]);
           }
         }
       }
       __syncwarp();
     }
+    if (ok) {
+      if (c0 == 1)
+        for (int i = tl; i < K; i += G) R[i] = (i == k) ? lKK : 0.0;
+      // a32 is free now: it takes the float32 weights d_j^(-1/2)
+      for (int j = tl; j < K; j += G) a32[j] = sqrtf((float)invd[j]);
+    }
+    __syncwarp();
 
-    // ---- record: z parts, w_K (float64), Gram products (float32)
+    // ---- record: z parts, w_K (float64), Gram products (float32) of the
+    //      D^(-1/2)-weighted solutions
     if (ok) {
       for (int e = tl; e < NR * 33; e += G) {
         const int c = e / 33, j = e - (e / 33) * 33;
-        R32[e] = (j < K) ? (float)R[c * 33 + j] : 0.0f;
+        R32[e] = (j < K) ? (float)R[c * 33 + j] * a32[j] : 0.0f;
       }
     }
     __syncwarp();
@@ -392,8 +453,8 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       double* wzy = wK + P;
       double* wzZ = wzy + P;
       double* F = wzZ + P * q;
-      for (int c = tl; c < 1 + q; c += G) rec[2 + q + c] = R[(P + c) * 33 + k];
-      for (int p = tl; p < P; p += G) wK[p] = R[p * 33 + k];
+      for (int c = tl; c < 1 + q; c += G) rec[2 + q + c] = R[(P + c) * 33 + k] * sK;
+      for (int p = tl; p < P; p += G) wK[p] = R[p * 33 + k] * sK;
       const int nf = P * (P + 1) / 2;
       const int ntot = nf + P * (1 + q);
       for (int t = tl; t < ntot; t += G) {
@@ -410,7 +471,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         float sacc = 0.0f;
         for (int i = 0; i < K; ++i) sacc = fmaf(r1[i], r2[i], sacc);
         if (t < nf) {
-          F[t] = 0.5 * (2.0 * (double)sacc - R[c1 * 33 + k] * R[c2 * 33 + k]);
+          F[t] = 0.5 * (2.0 * (double)sacc - (R[c1 * 33 + k] * sK) * (R[c2 * 33 + k] * sK));
         } else {
           const int s3 = t - nf;
           const int p = s3 / (1 + q);
@@ -424,6 +485,28 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     }
     __syncwarp();
   }
+}
+
+// (hi, lo) float32 pairs of x / lambda: hi = fl32(v), lo = fl32(v - hi)
+__global__ void k_split_prep(const double* X, const double* theta, int64_t n, int d, float2* xhl) {
+  const int64_t tot = n * d;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int l = (int)(e % d);
+    const double v = X[e] * exp(-theta[1 + l]);
+    const float hi = (float)v;
+    xhl[e] = make_float2(hi, (float)(v - (double)hi));
+  }
+}
+
+int launch_split_prep(const LikArgs& A, cudaStream_t st) {
+  const int64_t tot = A.n * A.d;
+  if (tot == 0) return SV_OK;
+  int64_t grid = (tot + 255) / 256;
+  if (grid > 16LL * sv_num_sms()) grid = 16LL * sv_num_sms();
+  k_split_prep<<<(unsigned)grid, 256, 0, st>>>(A.X, A.theta, A.n, A.d, A.xhl);
+  SV_CUDA_TRY(cudaGetLastError());
+  return SV_OK;
 }
 
 int launch_block_split(const LikArgs& A, int lanes, cudaStream_t st) {

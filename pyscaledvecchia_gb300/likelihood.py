@@ -119,6 +119,21 @@ class DeviceProblem:
         self.out = None
         self.info = _lib.new_info(torch)
 
+    def kernel_launches(self, precision="float64", chunked=True, estimate_nu=False, nu=2.5):
+        """Number of library kernels one evaluation launches."""
+        warp = self.nblk_warp > 0
+        cta = self.nblk > self.nblk_warp
+        split = (precision == "split" and not estimate_nu and nu in (0.5, 1.5, 2.5)
+                 and self.d + 3 + self.q <= 32)
+        n = (1 if warp else 0) + (1 if cta else 0)
+        if split and warp:
+            n += 1  # coordinate pre-pass
+        if chunked:
+            n += 1 + (1 if warp else 0) + (1 if cta else 0)
+        if split and warp:
+            n += 1  # float64 re-evaluation of flagged blocks
+        return n + 4
+
     def chunk_tensor(self, Pc):
         if Pc not in self._chunks:
             ids = chunk_ids(self._gid, self._gk, self._gl, Pc)
