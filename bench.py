@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--m", type=int, default=30)
     ap.add_argument("--nu", type=float, default=2.5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fits-problems", type=int, default=256,
+                    help="problems of the batched-fits workload (0 = skip it)")
+    ap.add_argument("--fits-dump", default="",
+                    help="write per-problem results of the batched-fits workload to this .npz")
     return ap.parse_args()
 
 
@@ -192,6 +196,136 @@ def run_reference(args):
         "e2e": {"value": v, "unit": "blocks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def make_fit_problems(nprob, seed=2):
+    """The batched-fits workload: nprob independent problems, n log-uniform
+    in [500, 20000], d uniform in {3..12}, m in {10, 20, 30}, X uniform in
+    [0,1]^d, lambda log-uniform in [0.05, 100], Matern 2.5 Vecchia draws
+    (sigma^2 = 1); the first half hold a fixed nugget of 1e-8 (and are drawn
+    with tau = 1e-8), the second half estimate it (drawn with tau
+    log-uniform in [1e-4, 1e-1])."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(nprob):
+        n = int(round(math.exp(rng.uniform(math.log(500), math.log(20000)))))
+        d = int(rng.integers(3, 13))
+        m = int(rng.choice([10, 20, 30]))
+        X = rng.random((n, d))
+        lam = np.exp(rng.uniform(math.log(0.05), math.log(100.0), d))
+        fixed = i < nprob // 2
+        tau = 1e-8 if fixed else float(np.exp(rng.uniform(math.log(1e-4), math.log(1e-1))))
+        eps = rng.standard_normal(n)
+        out.append(dict(n=n, d=d, m=m, X=X, lam=lam, tau=tau, fixed=fixed, eps=eps))
+    return out
+
+
+def draw_fit_responses(torch, lib, probs):
+    """y of every problem: unconditional Vecchia draw in its own maximin
+    order (the method's sample_joint prior), returned in the rows' order."""
+    from pyscaledvecchia_gb300 import _lib
+    from pyscaledvecchia_gb300.ordering import maximin_order_device, ordered_nn_device
+    from pyscaledvecchia_gb300.sampling import vecchia_prior_sample_device
+    ys = []
+    for pr in probs:
+        X, lam, n, m = pr["X"], pr["lam"], pr["n"], pr["m"]
+        Xs = X / lam
+        first = int(np.argmin(((Xs - Xs.mean(0)) ** 2).sum(1)))
+        Xs_d = _lib.to_dev(torch, Xs, np.float64)
+        order_d, info = maximin_order_device(torch, Xs_d, first)
+        _lib.check_info(lib, info.cpu().numpy(), "maximin")
+        nn_d, info = ordered_nn_device(torch, Xs_d[order_d].contiguous(), m)
+        _lib.check_info(lib, info.cpu().numpy(), "knn")
+        order = order_d.cpu().numpy()
+        theta = np.concatenate([[0.0], np.log(lam), [math.log(pr["tau"])]])
+        yo = vecchia_prior_sample_device(torch, _lib.to_dev(torch, X[order], np.float64), nn_d, theta,
+                                         2.5, _lib.to_dev(torch, pr["eps"].reshape(n, 1), np.float64))
+        y = np.empty(n)
+        y[order] = yo.reshape(-1).cpu().numpy()
+        ys.append(y)
+    return ys
+
+
+def run_fits(torch, lib, nprob, dump=""):
+    """Batched-fits workload: plain form (ScaledVecchiaGP.fit one problem at
+    a time, float64, default start, no graphs) against the chosen form
+    (fit_batched: all problems together, split-precision iterations with a
+    float64 polish, batched device reorders, CUDA-graph replay)."""
+    from pyscaledvecchia_gb300 import ScaledVecchiaGP
+    from pyscaledvecchia_gb300.fit_batched import fit_batched
+    probs = make_fit_problems(nprob)
+    t0 = time.perf_counter()
+    ys = draw_fit_responses(torch, lib, probs)
+    t_draw = time.perf_counter() - t0
+
+    def model(pr):
+        return ScaledVecchiaGP(m_est=pr["m"], n_est=None, nu=2.5,
+                               nugget=1e-8 if pr["fixed"] else None, var_correction=False)
+
+    Xs = [pr["X"] for pr in probs]
+    # warm-up of both paths on two small problems (library load, graphs)
+    small = sorted(range(nprob), key=lambda i: probs[i]["n"])[:2]
+    for i in small:
+        model(probs[i]).fit(Xs[i], ys[i])
+    fit_batched([model(probs[i]) for i in small], [Xs[i] for i in small], [ys[i] for i in small])
+    torch.cuda.synchronize()
+
+    t0 = time.perf_counter()
+    plain = [model(pr).fit(X, y) for pr, X, y in zip(probs, Xs, ys)]
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+
+    st = {}
+    t0 = time.perf_counter()
+    chosen = fit_batched([model(pr) for pr in probs], Xs, ys, precision="split", graphs=True, stats=st)
+    torch.cuda.synchronize()
+    t_chosen = time.perf_counter() - t0
+
+    ll_p = np.array([g.loglik_ for g in plain])
+    ll_c = np.array([g.loglik_ for g in chosen])
+    dll = ll_c - ll_p
+    rel = np.abs(dll) / np.maximum(np.abs(ll_p), 1.0)
+    # split form vs float64 at every chosen final state (same ordering)
+    BL = st.pop("batch")
+    th = st.pop("thetas")
+    th_obj = [g._objective_theta(t, g.d_, False) for g, t in zip(chosen, th)]
+    r64 = BL.evaluate(th_obj, active=np.ones(nprob, bool), precision="float64")
+    r32 = BL.evaluate(th_obj, active=np.ones(nprob, bool), precision="split")
+    e_ll = max(abs(a[1] - b[1]) / abs(b[1]) for a, b in zip(r32, r64))
+    # score error in units of its standard deviation sqrt(F_ii) (the score
+    # itself is ~0 at the optimum, so a relative error says nothing there)
+    e_g = max(float(np.max(np.abs(a[2] - b[2]) / np.sqrt(np.maximum(np.diag(b[3]), 1e-300))))
+              for a, b in zip(r32, r64))
+    e_f = max(float(np.abs(a[3] - b[3]).max() / max(np.abs(b[3]).max(), 1e-300)) for a, b in zip(r32, r64))
+    e_b = max(float(np.abs(a[4] - b[4]).max() / max(np.abs(b[4]).max(), 1e-300)) for a, b in zip(r32, r64))
+    evals_c = sum(g.fit_stats_["split"] + g.fit_stats_["float64"] for g in chosen)
+    if dump:
+        np.savez_compressed(
+            dump, n=np.array([p["n"] for p in probs]), d=np.array([p["d"] for p in probs]),
+            m=np.array([p["m"] for p in probs]), fixed=np.array([p["fixed"] for p in probs]),
+            tau=np.array([p["tau"] for p in probs]), ll_plain=ll_p, ll_chosen=ll_c,
+            theta_plain=np.array([np.pad(g.theta_, (0, 14 - g.theta_.size)) for g in plain]),
+            theta_chosen=np.array([np.pad(g.theta_, (0, 14 - g.theta_.size)) for g in chosen]),
+            evals_split=np.array([g.fit_stats_["split"] for g in chosen]),
+            evals_f64=np.array([g.fit_stats_["float64"] for g in chosen]),
+            ll_final_split=np.array([a[1] for a in r32]), ll_final_f64=np.array([b[1] for b in r64]))
+    return {
+        "workload": f"{nprob} independent fits, n log-U[500,20000] (total "
+                    f"{sum(p['n'] for p in probs)} points), d U{{3..12}}, m in {{10,20,30}}, "
+                    "nu = 2.5, half fixed nugget 1e-8, n_est = None, var_correction off",
+        "plain_fits_per_s": nprob / t_plain, "chosen_fits_per_s": nprob / t_chosen,
+        "speedup": t_plain / t_chosen, "plain_s": t_plain, "chosen_s": t_chosen,
+        "dll_abs_max": float(np.abs(dll).max()), "dll_abs_median": float(np.median(np.abs(dll))),
+        "dll_rel_max": float(rel.max()),
+        "frac_abs_dll_below_1e-6": float(np.mean(np.abs(dll) < 1e-6)),
+        "frac_rel_dll_below_1e-6": float(np.mean(rel < 1e-6)),
+        "frac_chosen_not_worse": float(np.mean(dll >= -1e-6)),
+        "split_vs_float64_at_final_state": {"ll_rel_max": e_ll, "score_err_max_in_sd": e_g,
+                                            "fisher_rel_max": e_f, "beta_rel_max": e_b},
+        "chosen_objective_evals": int(evals_c),
+        "schedule": {k: (float(v) if isinstance(v, float) else v) for k, v in st.items()},
+        "draw_s": t_draw,
+    }
 
 
 def main():
@@ -354,6 +488,8 @@ def main():
                                 "sample": f"one full evaluation of all {n} blocks "
                                           "(C restatement of the reference's Numba loops, OpenMP)"}
         line["extra"]["ll_cpu"] = out[0]
+    if args.fits_problems > 0:
+        line["fits"] = run_fits(torch, lib, args.fits_problems, args.fits_dump)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

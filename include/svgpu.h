@@ -75,6 +75,43 @@ int sv_knn_query(const double* Xref, int64_t nref, const double* Xq, int64_t nq,
                  int32_t k, int64_t* nb, int32_t* info, void* workspace, size_t workspace_bytes,
                  sv_stream_t stream);
 
+/* Batched rebuild of many problems' Vecchia structure: gp.py:182-191 (the
+ * fit's `rebuild`: Xs = X_e / ranges, maximin_order(Xs), find_ordered_nn of
+ * Xs[order], _nn_groups, X_e/y_e/Z_e[order]) for every listed problem in one
+ * call.  No counterpart in the reference, which rebuilds one fit at a time;
+ * the per-problem results are the reference's own (bit-exact ordering and
+ * neighbour sets).  Problem p reads rows from Xe/ye/Ze at its *e_off offsets
+ * and writes the reordered rows to X/y/Z at x_off/y_off/z_off, its maximin
+ * order (indices into its own rows) to order at its running row offset
+ * (problems in call order; order may be NULL), and row i's min(i, m)
+ * neighbours, nearest first, to nbr[(blk_off + i) * ldnbr ..], -1 padded.
+ * probs and ranges (nprob x dmax: exp(log lambda) as the caller computed it)
+ * are HOST arrays; the library stages them into the workspace.  A problem
+ * must fit one thread-block cluster: n <= sv_maximin_cluster_max_rows(d).
+ * info is device int32[4 * nprob]. */
+typedef struct sv_reorder_prob {
+  int64_t n;
+  int64_t xe_off, ye_off, ze_off;  /* source rows (any order)                */
+  int64_t x_off, y_off, z_off;     /* destination rows (maximin order)       */
+  int64_t blk_off;                 /* likelihood block of row 0              */
+  int64_t first;                   /* first row of the ordering (ordering.py:72) */
+  int32_t d, q, m, pad;
+} sv_reorder_prob;
+
+typedef struct sv_reorder_desc {
+  int64_t nprob;
+  int32_t dmax;   /* row stride of ranges                                   */
+  int32_t ldnbr;  /* row stride of nbr (>= every m)                          */
+} sv_reorder_desc;
+
+int64_t sv_maximin_cluster_max_rows(int32_t d);
+size_t sv_reorder_batched_workspace_bytes(const sv_reorder_desc* desc, const sv_reorder_prob* probs);
+int sv_reorder_batched(const sv_reorder_desc* desc, const sv_reorder_prob* probs,
+                       const double* ranges, const double* Xe, const double* ye, const double* Ze,
+                       double* X, double* y, double* Z, int32_t* nbr, int64_t* order,
+                       int32_t* info, void* workspace, size_t workspace_bytes,
+                       sv_stream_t stream);
+
 /* ---------------------------------------------------------------------- */
 /* Likelihood (likelihood.py)                                              */
 /* ---------------------------------------------------------------------- */
@@ -118,6 +155,51 @@ int sv_vecchia_loglik(const sv_loglik_desc* desc, const double* theta, const dou
                       const int32_t* nbr, const int32_t* chunk, double* out, int32_t* info,
                       void* workspace, size_t workspace_bytes, sv_stream_t stream);
 
+/* Batched form: many independent problems evaluated by one set of launches
+ * (the spec batched fits; the reference fits problems one at a time, so
+ * the per-problem arithmetic is likelihood.py:66-175 unchanged).  Problem p
+ * has its own inputs (offsets into the concatenated X, y, Z), its own
+ * contiguous run of blocks [blk_off, blk_off + nblk) with row indices local
+ * to the problem, its own parameter vector theta[p * theta_stride ..] and its
+ * own output out[p * out_stride ..] = ll, grad(P_p), fish(P_p * P_p), beta(q_p)
+ * and info[4 p .. 4 p + 3].  bprob gives each block's problem; wlist / clist
+ * list the blocks with k+1 <= 32 / k+1 > 32.  Only kernels and memsets are
+ * enqueued, so the call can be captured in a CUDA graph and replayed with new
+ * theta values. */
+typedef struct sv_prob_desc {
+  int64_t n;            /* rows of the problem                               */
+  int64_t x_off;        /* offset (doubles) of its X (n x d, row-major)      */
+  int64_t y_off;        /* offset (doubles) of its y                         */
+  int64_t z_off;        /* offset (doubles) of its Z (n x q)                 */
+  int64_t blk_off;      /* first block                                      */
+  int64_t nblk;         /* number of blocks                                 */
+  int32_t d, q;
+  int32_t estimate_nu;
+  int32_t skip;         /* nonzero: not evaluated by this call; its out and   */
+                        /* info entries are left as they were               */
+  double nu, var_penalty, log_var_target;
+} sv_prob_desc;
+
+typedef struct sv_batch_desc {
+  int64_t nprob, nblk;  /* problems, blocks in all                          */
+  int64_t nwarp, ncta;  /* lengths of wlist and clist (sum = nblk)          */
+  int64_t nx;           /* doubles in X                                     */
+  int32_t dmax, qmax, kmax, ldnbr;
+  int32_t need_grad, any_estimate_nu, chunked, precision, team_lanes;
+  int32_t theta_stride, out_stride, pad;
+  double split_rho_min;
+  int64_t nblk_max;     /* blocks of the largest problem (sizes the reductions) */
+} sv_batch_desc;
+
+size_t sv_loglik_batched_workspace_bytes(const sv_batch_desc* desc);
+int sv_vecchia_loglik_batched(const sv_batch_desc* desc, const sv_prob_desc* probs,
+                              const double* theta, const double* X, const double* y,
+                              const double* Z, const int32_t* rowb, const int32_t* kb,
+                              const int32_t* nbr, const int32_t* bprob, const int32_t* wlist,
+                              const int32_t* clist, const int32_t* chunk, double* out,
+                              int32_t* info, void* workspace, size_t workspace_bytes,
+                              sv_stream_t stream);
+
 /* No counterpart in the reference.  The same evaluation as sv_vecchia_loglik
  * for callers that cannot allocate device memory (an application whose fixed
  * memory pool owns the GPU, or a loop that must not call cudaMalloc, which
@@ -135,6 +217,38 @@ int sv_vecchia_loglik_noalloc(const sv_loglik_desc* desc, const double* theta, c
                               const double* y, const double* Z, const int32_t* rowb,
                               const int32_t* kb, const int32_t* nbr, const int32_t* chunk,
                               double* out, int32_t* info, sv_stream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Learned warm start (set encoder)                                        */
+/* ---------------------------------------------------------------------- */
+
+/* No counterpart in the reference: a DeepSets encoder whose output replaces
+ * the default starting point of Fisher scoring (gp.py:169-177); the fit
+ * itself is unchanged.  Sets of S points (S a multiple of 128), 16 bfloat16
+ * features per point (x_1..x_12 zero padded, y, three zeros); cnt[b] valid
+ * points in set b.  Parameters: a flat float32 vector of
+ * sv_encoder_param_count() entries, W1[128][16] b1[128] W2[128][128] b2[128]
+ * W3[128][128] b3[128] W4[16][128] b4[16], and its bfloat16 copy
+ * (sv_encoder_to_bf16); weights are read as bfloat16, biases as float32, all
+ * sums accumulate in float32.  out is float32 [nset][16].  The backward also
+ * takes target and weights [nset][16] (loss = sum w (out - target)^2) and
+ * writes the loss (1 float) and the float32 gradient (param_count floats). */
+int64_t sv_encoder_param_count(void);
+size_t sv_encoder_workspace_bytes(int64_t nset, int32_t S, int32_t train);
+int sv_encoder_pack(const double* features, int64_t n, uint16_t* x_bf16, sv_stream_t stream);
+int sv_encoder_to_bf16(const float* params, uint16_t* params_bf16, int64_t n, sv_stream_t stream);
+int sv_encoder_forward(int64_t nset, int32_t S, const uint16_t* x, const int32_t* cnt,
+                       const float* params, const uint16_t* params_bf16, float* out,
+                       void* workspace, size_t workspace_bytes, sv_stream_t stream);
+int sv_encoder_backward(int64_t nset, int32_t S, const uint16_t* x, const int32_t* cnt,
+                        const float* params, const uint16_t* params_bf16, const float* target,
+                        const float* weights, float* out, float* loss, float* grad,
+                        void* workspace, size_t workspace_bytes, sv_stream_t stream);
+/* Adam step (bias-corrected, decoupled weight decay added to the gradient)
+ * on the float32 master parameters; refreshes the bfloat16 copy. */
+int sv_encoder_adam(float* params, const float* grad, float* m, float* v, uint16_t* params_bf16,
+                    int64_t n, float lr, float beta1, float beta2, float eps, int32_t step,
+                    float weight_decay, sv_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
 /* Matern correlation (elementwise)                                        */

@@ -33,6 +33,36 @@ class LoglikDesc(ctypes.Structure):
                 ("log_var_target", c_dbl)]
 
 
+class ProbDesc(ctypes.Structure):
+    """Mirror of sv_prob_desc (include/svgpu.h)."""
+    _fields_ = [("n", c_i64), ("x_off", c_i64), ("y_off", c_i64), ("z_off", c_i64),
+                ("blk_off", c_i64), ("nblk", c_i64), ("d", c_i32), ("q", c_i32),
+                ("estimate_nu", c_i32), ("skip", c_i32), ("nu", c_dbl), ("var_penalty", c_dbl),
+                ("log_var_target", c_dbl)]
+
+
+class BatchDesc(ctypes.Structure):
+    """Mirror of sv_batch_desc (include/svgpu.h)."""
+    _fields_ = [("nprob", c_i64), ("nblk", c_i64), ("nwarp", c_i64), ("ncta", c_i64),
+                ("nx", c_i64), ("dmax", c_i32), ("qmax", c_i32), ("kmax", c_i32),
+                ("ldnbr", c_i32), ("need_grad", c_i32), ("any_estimate_nu", c_i32),
+                ("chunked", c_i32), ("precision", c_i32), ("team_lanes", c_i32),
+                ("theta_stride", c_i32), ("out_stride", c_i32), ("pad", c_i32),
+                ("split_rho_min", c_dbl), ("nblk_max", c_i64)]
+
+
+class ReorderProb(ctypes.Structure):
+    """Mirror of sv_reorder_prob (include/svgpu.h)."""
+    _fields_ = [("n", c_i64), ("xe_off", c_i64), ("ye_off", c_i64), ("ze_off", c_i64),
+                ("x_off", c_i64), ("y_off", c_i64), ("z_off", c_i64), ("blk_off", c_i64),
+                ("first", c_i64), ("d", c_i32), ("q", c_i32), ("m", c_i32), ("pad", c_i32)]
+
+
+class ReorderDesc(ctypes.Structure):
+    """Mirror of sv_reorder_desc (include/svgpu.h)."""
+    _fields_ = [("nprob", c_i64), ("dmax", c_i32), ("ldnbr", c_i32)]
+
+
 class PredDesc(ctypes.Structure):
     """Mirror of sv_pred_desc (include/svgpu.h)."""
     _fields_ = [("nall", c_i64), ("nobs", c_i64), ("nblk", c_i64), ("d", c_i32), ("k", c_i32),
@@ -50,11 +80,24 @@ SIGNATURES = {
     "sv_ordered_knn": (c_i32, [c_vp, c_i64, c_i32, c_i32, c_i64, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "sv_knn_query_workspace_bytes": (c_sz, [c_i64, c_i64, c_i32]),
     "sv_knn_query": (c_i32, [c_vp, c_i64, c_vp, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "sv_maximin_cluster_max_rows": (c_i64, [c_i32]),
+    "sv_reorder_batched_workspace_bytes": (c_sz, [ctypes.POINTER(ReorderDesc), c_vp]),
+    "sv_reorder_batched": (c_i32, [ctypes.POINTER(ReorderDesc), c_vp, c_vp] + [c_vp] * 10 + [c_sz, c_vp]),
     "sv_loglik_workspace_bytes": (c_sz, [ctypes.POINTER(LoglikDesc)]),
     "sv_vecchia_loglik": (c_i32, [ctypes.POINTER(LoglikDesc), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
                                   c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "sv_loglik_batched_workspace_bytes": (c_sz, [ctypes.POINTER(BatchDesc)]),
+    "sv_vecchia_loglik_batched": (c_i32, [ctypes.POINTER(BatchDesc)] + [c_vp] * 15 + [c_sz, c_vp]),
     "sv_vecchia_loglik_noalloc": (c_i32, [ctypes.POINTER(LoglikDesc), c_vp, c_vp, c_vp, c_vp, c_vp,
                                           c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "sv_encoder_param_count": (c_i64, []),
+    "sv_encoder_workspace_bytes": (c_sz, [c_i64, c_i32, c_i32]),
+    "sv_encoder_pack": (c_i32, [c_vp, c_i64, c_vp, c_vp]),
+    "sv_encoder_to_bf16": (c_i32, [c_vp, c_vp, c_i64, c_vp]),
+    "sv_encoder_forward": (c_i32, [c_i64, c_i32] + [c_vp] * 6 + [c_sz, c_vp]),
+    "sv_encoder_backward": (c_i32, [c_i64, c_i32] + [c_vp] * 10 + [c_sz, c_vp]),
+    "sv_encoder_adam": (c_i32, [c_vp] * 5 + [c_i64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                             ctypes.c_float, c_i32, ctypes.c_float, c_vp]),
     "sv_matern_eval": (c_i32, [c_vp, c_i64, c_dbl, c_i32, c_i32, c_vp, c_vp]),
     "sv_bessel_k": (c_i32, [c_vp, c_i64, c_dbl, c_vp, c_vp]),
     "sv_block_cov": (c_i32, [c_vp, c_i64, c_i32, c_i32, c_vp, c_dbl, c_dbl, c_dbl, c_i32, c_i32,

@@ -59,4 +59,23 @@ __device__ __forceinline__ void tri_index(int t, int& i, int& j) {
 }
 __device__ __forceinline__ int tri_off(int i, int j) { return i * (i + 1) / 2 + j; }
 
+// exact maximin / kNN arithmetic (ordering.py:52-57): squared distance in
+// IEEE sequential float64, no FMA contraction
+__device__ __forceinline__ double sqdist_exact(const double* a, const double* b, int d) {
+  double s = 0.0;
+  for (int l = 0; l < d; ++l) {
+    const double df = __dsub_rn(a[l], b[l]);
+    s = __dadd_rn(s, __dmul_rn(df, df));
+  }
+  return s;
+}
+
+// maximin float32 skip threshold: an upper bound of
+// dist * (1 + (d+4) 2^-53) + B_p as a float32, rounded up
+__device__ __forceinline__ float thr_base(double dist, double Bp, int d) {
+  if (isinf(dist)) return __int_as_float(0x7f800000);
+  const double t = (dist * (1.0 + (double)(d + 4) * 0x1p-53) + Bp) * (1.0 + 0x1p-40);
+  return __double2float_ru(t);
+}
+
 }  // namespace sv

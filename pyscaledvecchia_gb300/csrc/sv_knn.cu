@@ -15,7 +15,7 @@
 // float64, no FMA) and inserted into the thread's sorted list.  Candidates
 // are visited in increasing index order, so equal float64 distances keep the
 // smaller index: the selected set is the exact (distance, index) order.
-#include "sv_common.cuh"
+#include "sv_reorder.cuh"
 
 namespace sv {
 
@@ -68,6 +68,9 @@ struct KnnArgs {
   int64_t* out;        // ordered: (n, m+1); query: (nq, k)
   float growth;        // (1+2^-24)^(DP+2) (1+2^-20), rounded up
   int ordered;
+  int32_t* nbr;        // ordered, block form: neighbour columns of blocks b0 + i
+  int64_t b0;
+  int ldnbr;
 };
 
 __device__ __forceinline__ float knn_thr(double s64k, float Bi, int d) {
@@ -75,17 +78,17 @@ __device__ __forceinline__ float knn_thr(double s64k, float Bi, int d) {
   return __double2float_ru(t);
 }
 
+// One query tile: qt = tile index, rows [qt Q, qt Q + Q) of the query set.
+// Ordered searches write the reference's (n, m+1) rows, or, when A.nbr is
+// set, the neighbour columns of the likelihood blocks (block b0 + i holds
+// row i's neighbours, -1 padded to ldnbr).
 template <int DP>
-__global__ void __launch_bounds__(kKnnQ) k_knn(KnnArgs A) {
-  extern __shared__ unsigned char smraw[];
+__device__ __forceinline__ void knn_tile(const KnnArgs& A, int64_t qt, unsigned char* smraw) {
   float* tile = (float*)smraw;                     // [C][DP]
   float* tileB = tile + kKnnC * DP;                // [C]
   double* lsd = (double*)(tileB + kKnnC);          // [k][Q] squared distances
   int* lsi = (int*)(lsd + (size_t)A.k * kKnnQ);    // [k][Q] indices
 
-  const int64_t ntile = (A.nq + kKnnQ - 1) / kKnnQ;
-  // largest tiles first (ordered search work grows with the row index)
-  const int64_t qt = A.ordered ? (ntile - 1 - blockIdx.x) : blockIdx.x;
   const int64_t i = qt * kKnnQ + threadIdx.x;
   const bool valid = i < A.nq;
   const int tid = threadIdx.x;
@@ -164,7 +167,10 @@ __global__ void __launch_bounds__(kKnnQ) k_knn(KnnArgs A) {
     }
   }
   if (!valid) return;
-  if (A.ordered) {
+  if (A.nbr) {
+    int32_t* row = A.nbr + (A.b0 + i) * (int64_t)A.ldnbr;
+    for (int c = 0; c < A.ldnbr; ++c) row[c] = (active && c < cnt) ? lsi[c * kKnnQ + tid] : -1;
+  } else if (A.ordered) {
     int64_t* row = A.out + i * (int64_t)(A.m + 1);
     row[0] = i;
     for (int c = 0; c < A.m; ++c) row[1 + c] = (active && c < cnt) ? (int64_t)lsi[c * kKnnQ + tid] : -1;
@@ -172,6 +178,15 @@ __global__ void __launch_bounds__(kKnnQ) k_knn(KnnArgs A) {
     int64_t* row = A.out + i * (int64_t)A.k;
     for (int c = 0; c < A.k; ++c) row[c] = (c < cnt) ? (int64_t)lsi[c * kKnnQ + tid] : -1;
   }
+}
+
+template <int DP>
+__global__ void __launch_bounds__(kKnnQ) k_knn(KnnArgs A) {
+  extern __shared__ unsigned char smraw[];
+  const int64_t ntile = (A.nq + kKnnQ - 1) / kKnnQ;
+  // largest tiles first (ordered search work grows with the row index)
+  const int64_t qt = A.ordered ? (ntile - 1 - blockIdx.x) : blockIdx.x;
+  knn_tile<DP>(A, qt, smraw);
 }
 
 static int pad_dim(int d) {
@@ -219,6 +234,74 @@ static int launch_knn(const KnnArgs& A, int DP, int64_t grid, size_t smem, cudaS
 }
 
 static size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// batched ordered search: entry t of the tile table is (problem, query tile)
+template <int DP>
+__global__ void __launch_bounds__(kKnnQ) k_knn_batched(const KnnBatchProb* probs, const int2* tiles,
+                                                        const double* Xs, const float* v,
+                                                        const float* B, int32_t* nbr, int ldnbr,
+                                                        int kcap, float growth) {
+  extern __shared__ unsigned char smraw[];
+  const int2 te = tiles[blockIdx.x];
+  const KnnBatchProb& P = probs[te.x];
+  KnnArgs A;
+  A.Xq = Xs + P.xs_off;
+  A.Xr = A.Xq;
+  A.vq = v + P.v_off;
+  A.vr = A.vq;
+  A.Bq = B + P.row_off;
+  A.Br = A.Bq;
+  A.nq = P.n;
+  A.nr = P.n;
+  A.d = P.d;
+  A.k = kcap;
+  A.m = P.m;
+  A.start = 1;
+  A.out = nullptr;
+  A.growth = growth;
+  A.ordered = 1;
+  A.nbr = nbr;
+  A.b0 = P.blk_off;
+  A.ldnbr = ldnbr;
+  knn_tile<DP>(A, te.y, smraw);
+}
+
+int knn_pad_dim(int d) { return pad_dim(d); }
+
+int launch_knn_batched(int DP, const KnnBatchProb* probs, const int2* tiles, int64_t ntiles,
+                       const double* Xs, const float* v, const float* B, int32_t* nbr, int ldnbr,
+                       int kcap, cudaStream_t st) {
+  if (ntiles <= 0) return SV_OK;
+  const size_t smem = sizeof(float) * (size_t)kKnnC * DP + sizeof(float) * kKnnC +
+                      (sizeof(double) + sizeof(int)) * (size_t)kcap * kKnnQ;
+  int dev = 0, maxsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (smem > (size_t)maxsm) return SV_EINVAL;
+  const float g = growth_factor(DP);
+  switch (DP) {
+#define SV_KNNB_CASE(V)                                                                           \
+  case V:                                                                                        \
+    SV_CUDA_TRY(cudaFuncSetAttribute(k_knn_batched<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     (int)smem));                                                \
+    k_knn_batched<V><<<(unsigned)ntiles, kKnnQ, smem, st>>>(probs, tiles, Xs, v, B, nbr, ldnbr,  \
+                                                             kcap, g);                           \
+    break;
+    SV_KNNB_CASE(4)
+    SV_KNNB_CASE(8)
+    SV_KNNB_CASE(12)
+    SV_KNNB_CASE(16)
+    SV_KNNB_CASE(24)
+    SV_KNNB_CASE(32)
+    SV_KNNB_CASE(48)
+    SV_KNNB_CASE(64)
+#undef SV_KNNB_CASE
+    default:
+      return SV_EINVAL;
+  }
+  SV_CUDA_TRY(cudaGetLastError());
+  return SV_OK;
+}
 
 }  // namespace sv
 
@@ -283,6 +366,9 @@ extern "C" int sv_ordered_knn(const double* X, int64_t n, int32_t d, int32_t m, 
   A.out = nn;
   A.growth = growth_factor(DP);
   A.ordered = 1;
+  A.nbr = nullptr;
+  A.b0 = 0;
+  A.ldnbr = 0;
   const int64_t ntile = (n + kKnnQ - 1) / kKnnQ;
   return launch_knn(A, DP, ntile, smem, st);
 }
@@ -339,6 +425,9 @@ extern "C" int sv_knn_query(const double* Xref, int64_t nref, const double* Xq, 
   A.out = nb;
   A.growth = growth_factor(DP);
   A.ordered = 0;
+  A.nbr = nullptr;
+  A.b0 = 0;
+  A.ldnbr = 0;
   const int64_t ntile = (nq + kKnnQ - 1) / kKnnQ;
   return launch_knn(A, DP, ntile, smem, st);
 }

@@ -12,16 +12,81 @@
 // W (L^-1 y) and W (L^-1 Z) instead of L and W, so pass 2 is a light
 // reduction over that per-block record.
 //
-// Kernels: k_block_warp (one warp per block, K <= 32), k_block_cta (one CTA
-// per block, K > 32), k_chunk_max / fixup (reference chunk-wide jitter),
-// k_reduce1 / k_final1 (GLS + Fisher sums, beta), k_reduce2 / k_final2
-// (ll, score, variance penalty).  Reductions are in a fixed order, so results
-// are bitwise reproducible run to run.
+// An evaluation covers a batch of independent problems (one for
+// sv_vecchia_loglik): every block carries its problem index, so one launch of
+// the block kernel processes the blocks of all problems.
+//
+// Kernels: k_prob_params (theta -> per-problem parameters), k_block_warp (one
+// warp per block, K <= 32), k_block_cta (one CTA per block, K > 32),
+// k_chunk_max / fix-up pass (reference chunk-wide jitter), k_reduce1 /
+// k_final1 (GLS + Fisher sums, beta), k_reduce2 / k_final2 (ll, score,
+// variance penalty).  Reductions are in a fixed order, so results are bitwise
+// reproducible run to run.  Only kernels and memsets are enqueued, so a
+// batched evaluation can be captured in a CUDA graph.
 #include <stdio.h>
 
 #include "sv_loglik.cuh"
 
 namespace sv {
+
+// theta -> per-problem parameters (sigma^2, tau, nu, 1/lambda)
+__global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, int tstride,
+                              int nprob, ProbInfo* out) {
+  const int p = blockIdx.x;
+  if (p >= nprob) return;
+  const sv_prob_desc& D = descs[p];
+  ProbInfo& I = out[p];
+  const double* th = theta + (int64_t)p * tstride;
+  const int d = D.d;
+  if (threadIdx.x == 0) {
+    I.n = D.n;
+    I.x_off = D.x_off;
+    I.y_off = D.y_off;
+    I.z_off = D.z_off;
+    I.blk_off = D.blk_off;
+    I.nblk = D.nblk;
+    I.d = d;
+    I.q = D.q;
+    I.estimate_nu = D.estimate_nu;
+    I.skip = D.skip;
+    I.P = d + 2 + (D.estimate_nu ? 1 : 0);
+    I.nu_fixed = D.nu;
+    I.var_penalty = D.var_penalty;
+    I.log_var_target = D.log_var_target;
+    I.s2 = exp(th[0]);
+    double nu = D.nu;
+    if (D.estimate_nu) {
+      nu = exp(th[1 + d]);
+      I.tau = exp(th[2 + d]);
+    } else {
+      I.tau = exp(th[1 + d]);
+    }
+    MaternMode mm;
+    mm.closed = D.estimate_nu ? -1 : matern_closed_code(D.nu);
+    I.closed = mm.closed;
+    mm.estimate_nu = D.estimate_nu;
+    mm.nu = nu;
+    mm.log_coef = (mm.closed < 0) ? matern_log_coef(nu) : 0.0;
+    const double h = 1e-3;  // _matern_general.py:135 (nu_fd_h)
+    mm.nu_p = nu + h;
+    mm.nu_m = nu - h;
+    mm.lc_p = D.estimate_nu ? matern_log_coef(mm.nu_p) : 0.0;
+    mm.lc_m = D.estimate_nu ? matern_log_coef(mm.nu_m) : 0.0;
+    mm.inv2h = 1.0 / (2.0 * h);
+    I.mm = mm;
+  }
+  for (int l = threadIdx.x; l < d; l += blockDim.x) I.invlam[l] = exp(-th[1 + l]);
+}
+
+// info words of every problem: status 0, first failing block -1, jitter 0, aux 0
+__global__ void k_info_init(int32_t* info, int nprob) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nprob; p += gridDim.x * blockDim.x) {
+    info[4 * p + 0] = 0;
+    info[4 * p + 1] = -1;
+    info[4 * p + 2] = 0;
+    info[4 * p + 3] = 0;
+  }
+}
 
 // shared-memory footprint (doubles) of one team with block capacity kt
 __host__ __device__ inline int64_t team_smem_doubles(int kt, int d, int NR, int need_grad,
@@ -38,37 +103,44 @@ __host__ __device__ inline int64_t team_smem_doubles(int kt, int d, int NR, int 
   return s;
 }
 
-// One block, processed by a team.  Writes the block's record to the cache.
+// One block, processed by a team (float64 throughout).  Writes the block's record.
 template <int T>
-__device__ void block_pass1(const LikArgs& A, const PrmSmem* prm, int64_t b, double* sm) {
+__device__ void block_pass1(const LikArgs& A, int64_t b, double* sm) {
   const int lane = Team<T>::lane();
-  const int d = A.d, q = A.q, P = A.P, NR = A.NR, kt = A.kt;
+  const int p = block_problem(A, b);
+  const ProbInfo& PI = A.probs[p];
+  const int d = PI.d, q = PI.q, P = PI.P, NR = A.need_grad ? (P + 1 + q) : 0, kt = A.kt;
+  const int dmax = A.dmax;
   const int k = A.kb[b];
   const int K = k + 1;
   const int64_t tri = (int64_t)kt * (kt + 1) / 2;
   double* u = sm;
-  double* Lp = u + (int64_t)kt * d;
+  double* Lp = u + (int64_t)kt * dmax;
   double* Gp = A.need_grad ? Lp + tri : nullptr;
-  double* Dp = A.estimate_nu ? (Lp + tri * (A.need_grad ? 2 : 1)) : nullptr;
-  double* R = Lp + tri * (1 + (A.need_grad ? 1 : 0) + (A.estimate_nu ? 1 : 0));
-  double* a = R + (int64_t)NR * kt;
+  double* Dp = (A.any_estimate_nu && PI.estimate_nu) ? (Lp + tri * (A.need_grad ? 2 : 1)) : nullptr;
+  double* R = Lp + tri * (1 + (A.need_grad ? 1 : 0) + (A.any_estimate_nu ? 1 : 0));
+  double* a = R + (int64_t)A.NRmax * kt;
   double* invd = a + kt;
   double* acc = invd + kt;
   int* idx = (int*)(acc + kt);
   volatile int* flag = idx + kt;
   double* red = (double*)(acc + kt + (kt + 1) / 2 + 1);
+  const double* X = A.X + PI.x_off;
+  const double* Y = A.y + PI.y_off;
+  const double* Zm = A.Z + PI.z_off;
+  int32_t* info = A.info + 4 * p;
 
   // ---- gather: neighbours first, self last (likelihood.py:113)
   for (int i = lane; i < K; i += T) idx[i] = (i < k) ? A.nbr[b * A.ldnbr + i] : A.rowb[b];
   Team<T>::sync();
   for (int t = lane; t < K * d; t += T) {
     const int i = t / d, l = t - (t / d) * d;
-    u[i * d + l] = A.X[(int64_t)idx[i] * d + l] * prm->invlam[l];
+    u[i * d + l] = X[(int64_t)idx[i] * d + l] * PI.invlam[l];
   }
   Team<T>::sync();
 
   // ---- Sigma, Cholesky, jitter retry (_covariance.py:235-252)
-  const double s2 = prm->s2, tau = prm->tau;
+  const double s2 = PI.s2, tau = PI.tau;
   int lv = 0;
   if (A.fixup) {
     lv = A.chunk_max[A.chunk[b]];
@@ -86,7 +158,7 @@ __device__ void block_pass1(const LikArgs& A, const PrmSmem* prm, int64_t b, dou
       jit = jitter_pow10(lv) * sc;
     }
     if (lane == 0) *flag = 0;
-    assemble_sigma<T>(K, d, u, nullptr, s2, tau, jit, prm->mm, Lp, Gp, Dp);
+    assemble_sigma<T>(K, d, u, nullptr, s2, tau, jit, PI.mm, Lp, Gp, Dp);
     Team<T>::sync();
     ok = cholesky_packed<T>(K, Lp, invd, flag);
     Team<T>::sync();
@@ -95,8 +167,8 @@ __device__ void block_pass1(const LikArgs& A, const PrmSmem* prm, int64_t b, dou
   double* rec = A.cache + b * (int64_t)A.CS;
   if (!ok) {
     if (lane == 0) {
-      set_error(A.info + SV_INFO_STATUS, SV_ECHOL);
-      atomicCAS(A.info + SV_INFO_BLOCK, -1, (int)b);
+      set_error(info + SV_INFO_STATUS, SV_ECHOL);
+      atomicCAS(info + SV_INFO_BLOCK, -1, (int)(b - PI.blk_off));
     }
     if (lane == 0) A.level[b] = 10;
     for (int f = lane; f < A.CS; f += T) rec[f] = 0.0;
@@ -105,7 +177,7 @@ __device__ void block_pass1(const LikArgs& A, const PrmSmem* prm, int64_t b, dou
   if (lane == 0) {
     A.level[b] = (int8_t)lv;
     if (lv > 0) {
-      atomicMax(A.info + SV_INFO_JITTER, lv);
+      atomicMax(info + SV_INFO_JITTER, lv);
       A.flags[0] = 1;
     }
   }
@@ -123,7 +195,7 @@ __device__ void block_pass1(const LikArgs& A, const PrmSmem* prm, int64_t b, dou
   // ---- GLS parts a.y, a.Z (likelihood.py:129-134)
   {
     double vy = 0.0;
-    for (int i = lane; i < K; i += T) vy += a[i] * A.y[idx[i]];
+    for (int i = lane; i < K; i += T) vy += a[i] * Y[idx[i]];
     vy = team_sum<T>(vy, red);
     if (lane == 0) {
       rec[0] = Lp[tri_off(K - 1, K - 1)];  // L_KK; the log is taken in the reduction
@@ -131,7 +203,7 @@ __device__ void block_pass1(const LikArgs& A, const PrmSmem* prm, int64_t b, dou
     }
     for (int c = 0; c < q; ++c) {
       double vz = 0.0;
-      for (int i = lane; i < K; i += T) vz += a[i] * A.Z[(int64_t)idx[i] * q + c];
+      for (int i = lane; i < K; i += T) vz += a[i] * Zm[(int64_t)idx[i] * q + c];
       vz = team_sum<T>(vz, red);
       if (lane == 0) rec[2 + c] = vz;
     }
@@ -163,20 +235,20 @@ __device__ void block_pass1(const LikArgs& A, const PrmSmem* prm, int64_t b, dou
     }
     R[(1 + l) * ldr + i] = s;
   }
-  int p = 1 + d;
-  if (A.estimate_nu) {
+  int pr = 1 + d;
+  if (PI.estimate_nu) {
     for (int i = lane; i < K; i += T) {
       double s = 0.0;
       for (int j = 0; j < K; ++j) s += ((i >= j) ? Dp[tri_off(i, j)] : Dp[tri_off(j, i)]) * a[j];
-      R[p * ldr + i] = s;
+      R[pr * ldr + i] = s;
     }
-    ++p;
+    ++pr;
   }
   // nugget row: dSigma_tau = s2 * tau * I
-  for (int i = lane; i < K; i += T) R[p * ldr + i] = s2 * tau * a[i];
+  for (int i = lane; i < K; i += T) R[pr * ldr + i] = s2 * tau * a[i];
   for (int i = lane; i < K; i += T) {
-    R[P * ldr + i] = A.y[idx[i]];
-    for (int c = 0; c < q; ++c) R[(P + 1 + c) * ldr + i] = A.Z[(int64_t)idx[i] * q + c];
+    R[P * ldr + i] = Y[idx[i]];
+    for (int c = 0; c < q; ++c) R[(P + 1 + c) * ldr + i] = Zm[(int64_t)idx[i] * q + c];
   }
   Team<T>::sync();
 
@@ -224,41 +296,43 @@ __device__ void block_pass1(const LikArgs& A, const PrmSmem* prm, int64_t b, dou
   }
 }
 
+// which blocks a launch of the block kernels processes
+__device__ __forceinline__ bool block_selected(const LikArgs& A, int64_t b, int kcap) {
+  if (A.redo_mode) return A.redo[b] != 0;
+  if (A.fixup) return A.chunk_max[A.chunk[b]] > A.level[b];
+  return A.kb[b] + 1 <= kcap;
+}
+
 __global__ void k_block_warp(LikArgs A) {
   extern __shared__ double smem[];
-  PrmSmem* prm = (PrmSmem*)smem;
-  load_params(A, prm);
-  const int64_t per_team = team_smem_doubles(32, A.d, A.NR, A.need_grad, A.estimate_nu);
+  const int64_t per_team = team_smem_doubles(32, A.dmax, A.NRmax, A.need_grad, A.any_estimate_nu);
   const int w = threadIdx.x >> 5;
-  double* sm = smem + (sizeof(PrmSmem) + 7) / 8 + w * per_team;
+  double* sm = smem + w * per_team;
   const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t b = A.b0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + w; b < A.b1; b += nw) {
-    if (A.redo_mode) {
-      if (!A.redo[b]) continue;
-    } else if (A.fixup) {
-      if (A.chunk_max[A.chunk[b]] <= A.level[b]) continue;
-    } else if (A.kb[b] + 1 > 32) {
-      if ((threadIdx.x & 31) == 0) set_error(A.info + SV_INFO_STATUS, SV_EINVAL);
+  for (int64_t t = A.b0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + w; t < A.b1; t += nw) {
+    const int64_t b = launch_block(A, t);
+    if (A.probs[block_problem(A, b)].skip) continue;
+    if (!block_selected(A, b, 32)) {
+      if (!A.redo_mode && !A.fixup && (threadIdx.x & 31) == 0)
+        set_error(A.info + 4 * block_problem(A, b) + SV_INFO_STATUS, SV_EINVAL);
       continue;
     }
-    block_pass1<32>(A, prm, b, sm);
+    block_pass1<32>(A, b, sm);
     __syncwarp();
   }
 }
 
 __global__ void k_block_cta(LikArgs A) {
   extern __shared__ double smem[];
-  PrmSmem* prm = (PrmSmem*)smem;
-  load_params(A, prm);
-  double* sm = smem + (sizeof(PrmSmem) + 7) / 8;
-  for (int64_t b = A.b0 + blockIdx.x; b < A.b1; b += gridDim.x) {
-    if (A.fixup) {
-      if (A.chunk_max[A.chunk[b]] <= A.level[b]) continue;
-    } else if (A.kb[b] + 1 > A.kt) {
-      if (threadIdx.x == 0) set_error(A.info + SV_INFO_STATUS, SV_EINVAL);
+  for (int64_t t = A.b0 + blockIdx.x; t < A.b1; t += gridDim.x) {
+    const int64_t b = launch_block(A, t);
+    if (A.probs[block_problem(A, b)].skip) continue;
+    if (!block_selected(A, b, A.kt)) {
+      if (!A.redo_mode && !A.fixup && threadIdx.x == 0)
+        set_error(A.info + 4 * block_problem(A, b) + SV_INFO_STATUS, SV_EINVAL);
       continue;
     }
-    block_pass1<128>(A, prm, b, sm);
+    block_pass1<128>(A, b, smem);
     __syncthreads();
   }
 }
@@ -275,70 +349,92 @@ __global__ void k_chunk_max(const int32_t* flags, const int32_t* chunk, const in
 }
 
 // ---------------------------------------------------------------------------
-// reductions
+// reductions (grid row = problem, R.parts partitions of its blocks)
 // ---------------------------------------------------------------------------
 struct RedArgs {
   const double* cache;
-  int64_t nblk;
-  int CS, q, P, need_grad;
-  double* part1;  // [nctas][nfield1]
-  double* part2;  // [nctas][1 + P]
-  double* beta;   // [q]
-  double* sums;   // [nfield1] final pass-1 sums
+  const ProbInfo* probs;
+  int CS, need_grad, nfmax, qmax, Pmax;
+  int parts;      // partitions of every problem's blocks
+  double* part1;  // [nprob][parts][nfmax]
+  double* part2;  // [nprob][parts][Pmax + 1]
+  double* beta;   // [nprob][qmax + 1]
+  double* sums;   // [nprob][nfmax]
   const double* theta;
-  double var_penalty, log_var_target;
-  int64_t n;
+  int tstride;
   double* out;
-  int32_t* info;
+  int ostride;
 };
 
-// pass-1 fields: logdet, Zty[q], XtX[q*q], F[P(P+1)/2]
+// pass-1 fields of a problem: logdet, Zty[q], XtX[q*q], F[P(P+1)/2]
 __host__ __device__ inline int nfield1(int q, int P, int need_grad) {
   return 1 + q + q * q + (need_grad ? P * (P + 1) / 2 : 0);
 }
 
+// Pass-1 sums of one partition: warp w takes the partition's blocks
+// w, w + nwarp, ..., its lanes the fields; each (warp, field) accumulator in
+// shared memory has one owner, and the warps' rows are added in a fixed order.
 __global__ void k_reduce1(RedArgs R) {
-  const int nf = nfield1(R.q, R.P, R.need_grad);
-  const int64_t per = (R.nblk + gridDim.x - 1) / gridDim.x;
-  const int64_t b0 = blockIdx.x * per;
-  const int64_t b1 = min(R.nblk, b0 + per);
-  const int q = R.q;
+  extern __shared__ double racc[];  // [nwarp][nfmax]
+  const int p = blockIdx.y;
+  const ProbInfo& PI = R.probs[p];
+  if (PI.skip) return;
+  const int q = PI.q, P = PI.P;
+  const int nf = nfield1(q, P, R.need_grad);
+  const int nwarp = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t per = (PI.nblk + R.parts - 1) / R.parts;
+  const int64_t b0 = PI.blk_off + blockIdx.x * per;
+  const int64_t b1 = min(PI.blk_off + PI.nblk, b0 + per);
+  double* acc = racc + (int64_t)w * R.nfmax;
+  for (int f = lane; f < nf; f += 32) acc[f] = 0.0;
+  const int foff = 3 + 2 * q + P * (2 + q);
+  for (int64_t b = b0 + w; b < b1; b += nwarp) {
+    const double* c = R.cache + b * R.CS;
+    for (int f = lane; f < nf; f += 32) {
+      double v;
+      if (f == 0) {
+        v = log(c[0]);
+      } else if (f < 1 + q) {
+        v = c[2 + (f - 1)] * c[1];
+      } else if (f < 1 + q + q * q) {
+        const int e = f - 1 - q;
+        const int i = e / q, jj = e - (e / q) * q;
+        v = c[2 + i] * c[2 + jj];
+      } else {
+        v = c[foff + (f - 1 - q - q * q)];
+      }
+      acc[f] += v;
+    }
+  }
+  __syncthreads();
+  double* part = R.part1 + ((int64_t)p * R.parts + blockIdx.x) * R.nfmax;
   for (int f = threadIdx.x; f < nf; f += blockDim.x) {
     double s = 0.0;
-    if (f == 0) {
-      for (int64_t b = b0; b < b1; ++b) s += log(R.cache[b * R.CS]);
-    } else if (f < 1 + q) {
-      const int i = f - 1;
-      for (int64_t b = b0; b < b1; ++b) s += R.cache[b * R.CS + 2 + i] * R.cache[b * R.CS + 1];
-    } else if (f < 1 + q + q * q) {
-      const int e = f - 1 - q;
-      const int i = e / q, j = e - (e / q) * q;
-      for (int64_t b = b0; b < b1; ++b)
-        s += R.cache[b * R.CS + 2 + i] * R.cache[b * R.CS + 2 + j];
-    } else {
-      const int e = f - 1 - q - q * q;
-      const int off = 3 + 2 * q + R.P * (2 + q) + e;
-      for (int64_t b = b0; b < b1; ++b) s += R.cache[b * R.CS + off];
-    }
-    R.part1[blockIdx.x * (int64_t)nf + f] = s;
+    for (int k = 0; k < nwarp; ++k) s += racc[(int64_t)k * R.nfmax + f];
+    part[f] = s;
   }
 }
 
-__global__ void k_final1(RedArgs R, int nparts) {
-  const int nf = nfield1(R.q, R.P, R.need_grad);
+__global__ void k_final1(RedArgs R) {
+  const int p = blockIdx.x;
+  const ProbInfo& PI = R.probs[p];
+  if (PI.skip) return;
+  const int q = PI.q, P = PI.P;
+  const int nf = nfield1(q, P, R.need_grad);
+  double* sums = R.sums + (int64_t)p * R.nfmax;
   for (int f = threadIdx.x; f < nf; f += blockDim.x) {
     double s = 0.0;
-    for (int c = 0; c < nparts; ++c) s += R.part1[c * (int64_t)nf + f];
-    R.sums[f] = s;
+    for (int c = 0; c < R.parts; ++c) s += R.part1[((int64_t)p * R.parts + c) * R.nfmax + f];
+    sums[f] = s;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     // beta = solve(XtX + 1e-12 I, Zty): Gaussian elimination, partial pivoting
-    const int q = R.q;
+    double* beta = R.beta + (int64_t)p * (R.qmax + 1);
     double M[kMaxQ][kMaxQ + 1];
     for (int i = 0; i < q; ++i) {
-      for (int j = 0; j < q; ++j) M[i][j] = R.sums[1 + q + i * q + j] + (i == j ? 1e-12 : 0.0);
-      M[i][q] = R.sums[1 + i];
+      for (int j = 0; j < q; ++j) M[i][j] = sums[1 + q + i * q + j] + (i == j ? 1e-12 : 0.0);
+      M[i][q] = sums[1 + i];
     }
     for (int c = 0; c < q; ++c) {
       int piv = c;
@@ -357,8 +453,8 @@ __global__ void k_final1(RedArgs R, int nparts) {
     }
     for (int c = q - 1; c >= 0; --c) {
       double s = M[c][q];
-      for (int j = c + 1; j < q; ++j) s -= M[c][j] * R.beta[j];
-      R.beta[c] = s / M[c][c];
+      for (int j = c + 1; j < q; ++j) s -= M[c][j] * beta[j];
+      beta[c] = s / M[c][c];
     }
   }
 }
@@ -366,12 +462,15 @@ __global__ void k_final1(RedArgs R, int nparts) {
 __global__ void k_reduce2(RedArgs R) {
   __shared__ double sbeta[kMaxQ];
   __shared__ double red[kRedThreads / 32][kMaxP + 1];
-  const int q = R.q, P = R.P, np = R.need_grad ? P : 0;
-  for (int i = threadIdx.x; i < q; i += blockDim.x) sbeta[i] = R.beta[i];
+  const int p = blockIdx.y;
+  const ProbInfo& PI = R.probs[p];
+  if (PI.skip) return;
+  const int q = PI.q, P = PI.P, np = R.need_grad ? P : 0;
+  for (int i = threadIdx.x; i < q; i += blockDim.x) sbeta[i] = R.beta[(int64_t)p * (R.qmax + 1) + i];
   __syncthreads();
-  const int64_t per = (R.nblk + gridDim.x - 1) / gridDim.x;
-  const int64_t b0 = blockIdx.x * per;
-  const int64_t b1 = min(R.nblk, b0 + per);
+  const int64_t per = (PI.nblk + R.parts - 1) / R.parts;
+  const int64_t b0 = PI.blk_off + blockIdx.x * per;
+  const int64_t b1 = min(PI.blk_off + PI.nblk, b0 + per);
   double acc[kMaxP + 1];
   for (int i = 0; i <= np; ++i) acc[i] = 0.0;
   for (int64_t b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
@@ -383,10 +482,10 @@ __global__ void k_reduce2(RedArgs R) {
       const double* wK = c + 3 + 2 * q;
       const double* wzy = wK + P;
       const double* wzZ = wzy + P;
-      for (int p = 0; p < P; ++p) {
-        double wz = wzy[p];
-        for (int i = 0; i < q; ++i) wz -= wzZ[p * q + i] * sbeta[i];
-        acc[1 + p] -= 0.5 * (wK[p] * (1.0 + zK * zK) - 2.0 * zK * wz);
+      for (int pp = 0; pp < P; ++pp) {
+        double wz = wzy[pp];
+        for (int i = 0; i < q; ++i) wz -= wzZ[pp * q + i] * sbeta[i];
+        acc[1 + pp] -= 0.5 * (wK[pp] * (1.0 + zK * zK) - 2.0 * zK * wz);
       }
     }
   }
@@ -401,116 +500,125 @@ __global__ void k_reduce2(RedArgs R) {
   for (int i = threadIdx.x; i <= np; i += blockDim.x) {
     double s = 0.0;
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k][i];
-    R.part2[blockIdx.x * (int64_t)(1 + np) + i] = s;
+    R.part2[((int64_t)p * R.parts + blockIdx.x) * (R.Pmax + 1) + i] = s;
   }
 }
 
-__global__ void k_final2(RedArgs R, int nparts) {
-  const int P = R.P, q = R.q, np = R.need_grad ? P : 0;
-  const int nf = nfield1(q, P, R.need_grad);
+__global__ void k_final2(RedArgs R) {
+  const int p = blockIdx.x;
+  const ProbInfo& PI = R.probs[p];
+  if (PI.skip) return;
+  const int P = PI.P, q = PI.q, np = R.need_grad ? P : 0;
   __shared__ double tot[kMaxP + 1];
   for (int i = threadIdx.x; i <= np; i += blockDim.x) {
     double s = 0.0;
-    for (int c = 0; c < nparts; ++c) s += R.part2[c * (int64_t)(1 + np) + i];
+    for (int c = 0; c < R.parts; ++c) s += R.part2[((int64_t)p * R.parts + c) * (R.Pmax + 1) + i];
     tot[i] = s;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
+    double* out = R.out + (int64_t)p * R.ostride;
+    const double* sums = R.sums + (int64_t)p * R.nfmax;
+    const double* th = R.theta + (int64_t)p * R.tstride;
     // ll = -n/2 log(2pi) - sum_b (log L_KK + z_K^2 / 2)  (likelihood.py:149-156)
-    double ll = -0.5 * (double)R.n * 1.8378770664093453 + tot[0];
+    double ll = -0.5 * (double)PI.n * 1.8378770664093453 + tot[0];
     double g0 = np ? tot[1] : 0.0;
     double f00_add = 0.0;
-    if (R.var_penalty > 0.0) {  // likelihood.py:165-171
-      double excess = R.theta[0] - R.log_var_target;
+    if (PI.var_penalty > 0.0) {  // likelihood.py:165-171
+      double excess = th[0] - PI.log_var_target;
       if (excess < 0.0) excess = 0.0;
-      ll -= 0.5 * R.var_penalty * excess * excess;
-      g0 -= R.var_penalty * excess;
-      if (excess > 0.0) f00_add = R.var_penalty;
+      ll -= 0.5 * PI.var_penalty * excess * excess;
+      g0 -= PI.var_penalty * excess;
+      if (excess > 0.0) f00_add = PI.var_penalty;
     }
-    R.out[0] = ll;
+    out[0] = ll;
     if (np) {
-      R.out[1] = g0;
-      for (int p = 1; p < P; ++p) R.out[1 + p] = tot[1 + p];
-    }
-    (void)f00_add;
-    if (np) {
+      out[1] = g0;
+      for (int pp = 1; pp < P; ++pp) out[1 + pp] = tot[1 + pp];
       // Fisher: sums hold the packed lower triangle
-      double* fish = R.out + 1 + P;
+      double* fish = out + 1 + P;
       const int foff = 1 + q + q * q;
       for (int i = 0; i < P; ++i)
         for (int j = 0; j <= i; ++j) {
-          const double v = R.sums[foff + i * (i + 1) / 2 + j];
+          const double v = sums[foff + i * (i + 1) / 2 + j];
           fish[i * P + j] = v;
           fish[j * P + i] = v;
         }
       fish[0] += f00_add;
+    } else {
+      for (int i = 0; i < P + P * P; ++i) out[1 + i] = 0.0;
     }
-    if (!np)
-      for (int i = 0; i < P + P * P; ++i) R.out[1 + i] = 0.0;
-    double* bo = R.out + 1 + P + P * P;
-    for (int i = 0; i < q; ++i) bo[i] = R.beta[i];
+    double* bo = out + 1 + P + P * P;
+    for (int i = 0; i < q; ++i) bo[i] = R.beta[(int64_t)p * (R.qmax + 1) + i];
   }
-  (void)nf;
 }
 
 }  // namespace sv
 
 // ---------------------------------------------------------------------------
-// C ABI
+// evaluation driver shared by the single-problem and batched entry points
 // ---------------------------------------------------------------------------
 using namespace sv;
 
-static int nred_ctas(int64_t nblk) {
-  int64_t c = (nblk + 1023) / 1024;
-  if (c < 1) c = 1;
-  if (c > 4 * (int64_t)sv_num_sms()) c = 4 * (int64_t)sv_num_sms();
-  return (int)c;
-}
-
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-struct WsLayout {
-  size_t cache, level, redo, chunk_max, flags, part1, part2, beta, sums, xhl, total;
+namespace {
+
+struct EvalShape {
+  int64_t nprob, nblk, nx, nblk_max;
+  int dmax, qmax, Pmax, kmax, need_grad, any_est, precision;
 };
 
-static WsLayout ws_layout(const sv_loglik_desc* D) {
-  const int P = D->d + 2 + (D->estimate_nu ? 1 : 0);
-  const int q = D->q;
-  const int CS = 3 + 2 * q + (D->need_grad ? (2 * P + P * q + P * (P + 1) / 2) : 0);
-  const int nr = nred_ctas(D->nblk);
+// reduction partitions per problem: about 1024 blocks each for the largest
+int red_parts(const EvalShape& S) {
+  int64_t parts = (S.nblk_max + 1023) / 1024;
+  if (parts < 8) parts = 8;
+  if (parts > 4096) parts = 4096;
+  return (int)parts;
+}
+
+struct WsLayout {
+  size_t desc, probs, cache, level, redo, chunk_max, flags, part1, part2, beta, sums, xhl, total;
+  int CS, nfmax;
+};
+
+WsLayout ws_layout(const EvalShape& S) {
   WsLayout L;
+  const int P = S.Pmax, q = S.qmax;
+  L.CS = record_stride(q, P, S.need_grad);
+  L.nfmax = nfield1(q, P, S.need_grad);
+  const size_t nb = (size_t)(S.nblk > 0 ? S.nblk : 1);
   size_t off = 0;
+  L.desc = off;
+  off = align256(off + sizeof(sv_prob_desc));
+  L.probs = off;
+  off = align256(off + sizeof(ProbInfo) * (size_t)S.nprob);
   L.cache = off;
-  off = align256(off + sizeof(double) * (size_t)CS * (size_t)(D->nblk > 0 ? D->nblk : 1));
+  off = align256(off + sizeof(double) * (size_t)L.CS * nb);
   L.level = off;
-  off = align256(off + (size_t)(D->nblk > 0 ? D->nblk : 1));
+  off = align256(off + nb);
   L.redo = off;
-  off = align256(off + (size_t)(D->nblk > 0 ? D->nblk : 1));
+  off = align256(off + nb);
   L.chunk_max = off;
-  off = align256(off + sizeof(int32_t) * (size_t)(D->nblk > 0 ? D->nblk : 1));
+  off = align256(off + sizeof(int32_t) * nb);
   L.flags = off;
   off = align256(off + 4 * sizeof(int32_t));
   L.part1 = off;
-  off = align256(off + sizeof(double) * (size_t)nr * nfield1(q, P, D->need_grad));
+  off = align256(off + sizeof(double) * (size_t)S.nprob * red_parts(S) * L.nfmax);
   L.part2 = off;
-  off = align256(off + sizeof(double) * (size_t)nr * (P + 1));
+  off = align256(off + sizeof(double) * (size_t)S.nprob * red_parts(S) * (P + 1));
   L.beta = off;
-  off = align256(off + sizeof(double) * (kMaxQ + 1));
+  off = align256(off + sizeof(double) * (size_t)S.nprob * (q + 1));
   L.sums = off;
-  off = align256(off + sizeof(double) * (size_t)nfield1(q, P, D->need_grad));
+  off = align256(off + sizeof(double) * (size_t)S.nprob * L.nfmax);
   L.xhl = off;
-  if (D->precision == 1) off = align256(off + sizeof(float) * 2 * (size_t)D->n * (size_t)D->d);
+  if (S.precision == 1) off = align256(off + sizeof(float) * 2 * (size_t)S.nx);
   L.total = off;
   return L;
 }
 
-extern "C" size_t sv_loglik_workspace_bytes(const sv_loglik_desc* D) {
-  if (!D) return 0;
-  return ws_layout(D).total;
-}
-
-static int g_max_smem_optin = -1;
-static int max_smem_optin() {
+int g_max_smem_optin = -1;
+int max_smem_optin() {
   if (g_max_smem_optin < 0) {
     int dev = 0, v = 0;
     cudaGetDevice(&dev);
@@ -518,6 +626,220 @@ static int max_smem_optin() {
     g_max_smem_optin = v;
   }
   return g_max_smem_optin;
+}
+
+struct EvalCall {
+  EvalShape S;
+  const sv_prob_desc* probs;  // device
+  const double* theta;        // device, nprob x tstride
+  int tstride;
+  const double *X, *y, *Z;
+  const int32_t *rowb, *kb, *nbr, *chunk, *bprob, *wlist, *clist;
+  int64_t nwarp, ncta;  // list lengths (lists nullptr: ranges [0,nwarp), [nwarp,nwarp+ncta))
+  int ldnbr, chunked, team_lanes;
+  double rho_min;
+  double* out;
+  int ostride;
+  int32_t* info;
+  char* ws;
+};
+
+int launch_warp_kernel(LikArgs A, cudaStream_t st) {
+  const int nsm = sv_num_sms();
+  const size_t team = sizeof(double) * team_smem_doubles(32, A.dmax, A.NRmax, A.need_grad, A.any_estimate_nu);
+  int wpc = 8;
+  while (wpc > 1 && wpc * team > (size_t)max_smem_optin()) --wpc;
+  const size_t smem = wpc * team;
+  if (smem > (size_t)max_smem_optin()) return SV_EINVAL;
+  SV_CUDA_TRY(cudaFuncSetAttribute(k_block_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int64_t grid = (A.b1 - A.b0 + wpc - 1) / wpc;
+  if (grid > 64LL * nsm) grid = 64LL * nsm;
+  if (grid < 1) grid = 1;
+  k_block_warp<<<(int)grid, 32 * wpc, smem, st>>>(A);
+  SV_CUDA_TRY(cudaGetLastError());
+  return SV_OK;
+}
+
+int launch_cta_kernel(LikArgs A, cudaStream_t st) {
+  const int nsm = sv_num_sms();
+  const size_t smem = sizeof(double) * team_smem_doubles(A.kt, A.dmax, A.NRmax, A.need_grad, A.any_estimate_nu);
+  if (smem > (size_t)max_smem_optin()) return SV_EINVAL;
+  SV_CUDA_TRY(cudaFuncSetAttribute(k_block_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int64_t grid = A.b1 - A.b0;
+  if (grid > 8LL * nsm) grid = 8LL * nsm;
+  if (grid < 1) grid = 1;
+  k_block_cta<<<(int)grid, 128, smem, st>>>(A);
+  SV_CUDA_TRY(cudaGetLastError());
+  return SV_OK;
+}
+
+// Enqueues one evaluation.  Only kernels and memsets: capturable in a graph.
+int run_eval(const EvalCall& C, cudaStream_t st) {
+  const EvalShape& S = C.S;
+  WsLayout W = ws_layout(S);
+  char* ws = C.ws;
+  ProbInfo* probs = (ProbInfo*)(ws + W.probs);
+
+  LikArgs A;
+  A.X = C.X;
+  A.y = C.y;
+  A.Z = C.Z;
+  A.rowb = C.rowb;
+  A.kb = C.kb;
+  A.nbr = C.nbr;
+  A.chunk = C.chunk;
+  A.bprob = C.bprob;
+  A.list = nullptr;
+  A.probs = probs;
+  A.cache = (double*)(ws + W.cache);
+  A.level = (int8_t*)(ws + W.level);
+  A.redo = (int8_t*)(ws + W.redo);
+  A.chunk_max = (int32_t*)(ws + W.chunk_max);
+  A.flags = (int32_t*)(ws + W.flags);
+  A.info = C.info;
+  A.b0 = 0;
+  A.b1 = 0;
+  A.nprob = (int)S.nprob;
+  A.ldnbr = C.ldnbr;
+  A.CS = W.CS;
+  A.kt = 32;
+  A.dmax = S.dmax;
+  A.NRmax = S.need_grad ? (S.Pmax + 1 + S.qmax) : 0;
+  A.need_grad = S.need_grad;
+  A.any_estimate_nu = S.any_est;
+  A.fixup = 0;
+  A.redo_mode = 0;
+  A.rho_min = C.rho_min > 0.0 ? C.rho_min : 1e-4;
+  A.xhl = (float2*)(ws + W.xhl);
+
+  k_info_init<<<(int)((S.nprob + 255) / 256), 256, 0, st>>>(C.info, (int)S.nprob);
+  SV_CUDA_TRY(cudaGetLastError());
+  SV_CUDA_TRY(cudaMemsetAsync(A.flags, 0, 4 * sizeof(int32_t), st));
+  if (C.chunked)
+    SV_CUDA_TRY(cudaMemsetAsync(A.chunk_max, 0, sizeof(int32_t) * (S.nblk > 0 ? S.nblk : 1), st));
+  k_prob_params<<<(int)S.nprob, 64, 0, st>>>(C.probs, C.theta, C.tstride, (int)S.nprob, probs);
+  SV_CUDA_TRY(cudaGetLastError());
+
+  // split form: closed-form nu for every problem and at most 32 right-hand
+  // sides (d + q <= 29); anything else runs the float64 kernels
+  const bool split = S.precision == 1 && !S.any_est && A.NRmax <= 32;
+  const int lanes = C.team_lanes > 0 ? C.team_lanes : 8;
+  if (split && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32) return SV_EINVAL;
+
+  auto warp_pass = [&](LikArgs B) -> int {
+    B.kt = 32;
+    B.list = C.wlist;
+    B.b0 = 0;
+    B.b1 = C.nwarp;
+    if (C.nwarp <= 0) return SV_OK;
+    if (split && !B.redo_mode) return launch_block_split(B, lanes, st);
+    return launch_warp_kernel(B, st);
+  };
+  auto cta_pass = [&](LikArgs B) -> int {
+    B.kt = S.kmax + 1;
+    B.list = C.clist;
+    B.b0 = C.clist ? 0 : C.nwarp;
+    B.b1 = C.clist ? C.ncta : C.nwarp + C.ncta;
+    if (C.ncta <= 0) return SV_OK;
+    return launch_cta_kernel(B, st);
+  };
+
+  int rc;
+  if (split && C.nwarp > 0) {
+    rc = launch_split_prep(A, S.nx, st);
+    if (rc != SV_OK) return rc;
+  }
+  if ((rc = warp_pass(A)) != SV_OK) return rc;
+  if ((rc = cta_pass(A)) != SV_OK) return rc;
+  // reference chunk-wide jitter: redo blocks whose chunk needed a larger level
+  if (C.chunked && S.nblk > 0) {
+    int64_t g = (S.nblk + 255) / 256;
+    if (g > 4096) g = 4096;
+    k_chunk_max<<<(int)g, 256, 0, st>>>(A.flags, C.chunk, A.level, S.nblk, A.chunk_max);
+    SV_CUDA_TRY(cudaGetLastError());
+    LikArgs B = A;
+    B.fixup = 1;
+    if ((rc = warp_pass(B)) != SV_OK) return rc;
+    if ((rc = cta_pass(B)) != SV_OK) return rc;
+  }
+  // split form: float64 re-evaluation of the blocks it flagged as ill-conditioned
+  if (split && C.nwarp > 0) {
+    LikArgs B = A;
+    B.redo_mode = 1;
+    if ((rc = warp_pass(B)) != SV_OK) return rc;
+  }
+
+  RedArgs R;
+  R.cache = A.cache;
+  R.probs = probs;
+  R.CS = W.CS;
+  R.need_grad = S.need_grad;
+  R.nfmax = W.nfmax;
+  R.qmax = S.qmax;
+  R.Pmax = S.Pmax;
+  R.part1 = (double*)(ws + W.part1);
+  R.part2 = (double*)(ws + W.part2);
+  R.beta = (double*)(ws + W.beta);
+  R.sums = (double*)(ws + W.sums);
+  R.theta = C.theta;
+  R.tstride = C.tstride;
+  R.out = C.out;
+  R.ostride = C.ostride;
+  R.parts = red_parts(S);
+  const dim3 rgrid((unsigned)R.parts, (unsigned)S.nprob);
+  int rwarps = kRedThreads / 32;
+  while (rwarps > 1 && sizeof(double) * (size_t)rwarps * W.nfmax > (size_t)max_smem_optin()) --rwarps;
+  const size_t rsmem = sizeof(double) * (size_t)rwarps * W.nfmax;
+  if (rsmem > (size_t)max_smem_optin()) return SV_EINVAL;
+  SV_CUDA_TRY(cudaFuncSetAttribute(k_reduce1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
+  k_reduce1<<<rgrid, 32 * rwarps, rsmem, st>>>(R);
+  SV_CUDA_TRY(cudaGetLastError());
+  k_final1<<<(unsigned)S.nprob, kRedThreads, 0, st>>>(R);
+  SV_CUDA_TRY(cudaGetLastError());
+  k_reduce2<<<rgrid, kRedThreads, 0, st>>>(R);
+  SV_CUDA_TRY(cudaGetLastError());
+  k_final2<<<(unsigned)S.nprob, 64, 0, st>>>(R);
+  SV_CUDA_TRY(cudaGetLastError());
+  return SV_OK;
+}
+
+EvalShape single_shape(const sv_loglik_desc* D) {
+  EvalShape S;
+  S.nprob = 1;
+  S.nblk = D->nblk;
+  S.nblk_max = D->nblk;
+  S.nx = D->n * D->d;
+  S.dmax = D->d;
+  S.qmax = D->q;
+  S.Pmax = D->d + 2 + (D->estimate_nu ? 1 : 0);
+  S.kmax = D->kmax;
+  S.need_grad = D->need_grad;
+  S.any_est = D->estimate_nu;
+  S.precision = D->precision;
+  return S;
+}
+
+EvalShape batch_shape(const sv_batch_desc* B) {
+  EvalShape S;
+  S.nprob = B->nprob;
+  S.nblk = B->nblk;
+  S.nblk_max = B->nblk_max > 0 ? B->nblk_max : B->nblk;
+  S.nx = B->nx;
+  S.dmax = B->dmax;
+  S.qmax = B->qmax;
+  S.Pmax = B->dmax + 2 + (B->any_estimate_nu ? 1 : 0);
+  S.kmax = B->kmax;
+  S.need_grad = B->need_grad;
+  S.any_est = B->any_estimate_nu;
+  S.precision = B->precision;
+  return S;
+}
+
+}  // namespace
+
+extern "C" size_t sv_loglik_workspace_bytes(const sv_loglik_desc* D) {
+  if (!D) return 0;
+  return ws_layout(single_shape(D)).total;
 }
 
 extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, const double* X,
@@ -532,172 +854,109 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
   if (D->nblk_warp < 0 || D->nblk_warp > D->nblk) return SV_EINVAL;
   if (D->kmax > 0 && (!nbr || D->ldnbr < D->kmax)) return SV_EINVAL;
   if (D->chunked && !chunk) return SV_EINVAL;
-  const int closed = matern_closed_code(D->nu);
   if (!D->estimate_nu && !(D->nu > 0.0)) return SV_EINVAL;
   if (D->precision != 0 && D->precision != 1) return SV_EINVAL;
-  WsLayout W = ws_layout(D);
+  const EvalShape S = single_shape(D);
+  WsLayout W = ws_layout(S);
   if (!workspace || workspace_bytes < W.total) return SV_ENOSPC;
   cudaStream_t st = (cudaStream_t)stream;
   char* ws = (char*)workspace;
+  // the problem table of a one-problem batch lives in the workspace
+  sv_prob_desc pd;
+  pd.n = D->n;
+  pd.x_off = 0;
+  pd.y_off = 0;
+  pd.z_off = 0;
+  pd.blk_off = 0;
+  pd.nblk = D->nblk;
+  pd.d = D->d;
+  pd.q = D->q;
+  pd.estimate_nu = D->estimate_nu;
+  pd.skip = 0;
+  pd.nu = D->nu;
+  pd.var_penalty = D->var_penalty;
+  pd.log_var_target = D->log_var_target;
+  SV_CUDA_TRY(cudaMemcpyAsync(ws + W.desc, &pd, sizeof(pd), cudaMemcpyHostToDevice, st));
+  EvalCall C;
+  C.S = S;
+  C.probs = (const sv_prob_desc*)(ws + W.desc);
+  C.theta = theta;
+  C.tstride = S.Pmax;
+  C.X = X;
+  C.y = y;
+  C.Z = Z;
+  C.rowb = rowb;
+  C.kb = kb;
+  C.nbr = nbr;
+  C.chunk = chunk;
+  C.bprob = nullptr;
+  C.wlist = nullptr;
+  C.clist = nullptr;
+  C.nwarp = D->nblk_warp;
+  C.ncta = D->nblk - D->nblk_warp;
+  C.ldnbr = D->ldnbr;
+  C.chunked = D->chunked;
+  C.team_lanes = D->team_lanes;
+  C.rho_min = D->split_rho_min;
+  C.out = out;
+  C.ostride = 1 + S.Pmax + S.Pmax * S.Pmax + S.qmax;
+  C.info = info;
+  C.ws = ws;
+  return run_eval(C, st);
+}
 
-  LikArgs A;
-  A.X = X;
-  A.y = y;
-  A.Z = Z;
-  A.rowb = rowb;
-  A.kb = kb;
-  A.nbr = nbr;
-  A.chunk = chunk;
-  A.theta = theta;
-  A.cache = (double*)(ws + W.cache);
-  A.level = (int8_t*)(ws + W.level);
-  A.chunk_max = (int32_t*)(ws + W.chunk_max);
-  A.flags = (int32_t*)(ws + W.flags);
-  A.info = info;
-  A.n = D->n;
-  A.d = D->d;
-  A.q = D->q;
-  A.ldnbr = D->ldnbr;
-  A.P = D->d + 2 + (D->estimate_nu ? 1 : 0);
-  A.NR = D->need_grad ? (A.P + 1 + A.q) : 0;
-  A.CS = 3 + 2 * A.q + (D->need_grad ? (2 * A.P + A.P * A.q + A.P * (A.P + 1) / 2) : 0);
-  A.need_grad = D->need_grad;
-  A.estimate_nu = D->estimate_nu;
-  A.closed = closed;
-  A.nu_fixed = D->nu;
-  A.nu_fd_h = 1e-3;  // _matern_general.py:135 (nu_fd_h)
-  A.fixup = 0;
-  A.redo = (int8_t*)(ws + W.redo);
-  A.rho_min = D->split_rho_min > 0.0 ? D->split_rho_min : 1e-4;
-  A.redo_mode = 0;
-  A.xhl = (float2*)(ws + W.xhl);
+extern "C" size_t sv_loglik_batched_workspace_bytes(const sv_batch_desc* B) {
+  if (!B) return 0;
+  return ws_layout(batch_shape(B)).total;
+}
 
-  int32_t init_info[4] = {0, -1, 0, 0};
-  SV_CUDA_TRY(cudaMemcpyAsync(info, init_info, sizeof(init_info), cudaMemcpyHostToDevice, st));
-  SV_CUDA_TRY(cudaMemsetAsync(A.flags, 0, 4 * sizeof(int32_t), st));
-  if (D->chunked) SV_CUDA_TRY(cudaMemsetAsync(A.chunk_max, 0, sizeof(int32_t) * D->nblk, st));
-
-  const int nsm = sv_num_sms();
-  const size_t prm_bytes = (sizeof(PrmSmem) + 7) / 8 * 8;
-  // warp-sized blocks [0, nblk_warp): float64 warp kernel or split kernel
-  // split form: closed-form nu and at most 32 right-hand sides (d + q <= 29);
-  // anything else runs the float64 kernels
-  const bool split = D->precision == 1 && !D->estimate_nu && closed >= 0 && A.NR <= 32;
-  const int lanes = D->team_lanes > 0 ? D->team_lanes : 8;
-  if (split && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32) return SV_EINVAL;
-  if (D->nblk_warp > 0) {
-    A.kt = 32;
-    A.b0 = 0;
-    A.b1 = D->nblk_warp;
-    if (split) {
-      int rc = launch_split_prep(A, st);
-      if (rc != SV_OK) return rc;
-      rc = launch_block_split(A, lanes, st);
-      if (rc != SV_OK) return rc;
-    } else {
-      const size_t team = sizeof(double) * team_smem_doubles(32, A.d, A.NR, A.need_grad, A.estimate_nu);
-      int wpc = 8;
-      while (wpc > 1 && prm_bytes + wpc * team > (size_t)max_smem_optin()) --wpc;
-      const size_t smem = prm_bytes + wpc * team;
-      if (smem > (size_t)max_smem_optin()) return SV_EINVAL;
-      SV_CUDA_TRY(cudaFuncSetAttribute(k_block_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      int64_t grid = (D->nblk_warp + wpc - 1) / wpc;
-      if (grid > 64LL * nsm) grid = 64LL * nsm;
-      k_block_warp<<<(int)grid, 32 * wpc, smem, st>>>(A);
-      SV_CUDA_TRY(cudaGetLastError());
-    }
-  }
-  // CTA kernel: blocks [nblk_warp, nblk)
-  size_t cta_smem = 0;
-  if (D->nblk > D->nblk_warp) {
-    A.kt = D->kmax + 1;
-    A.b0 = D->nblk_warp;
-    A.b1 = D->nblk;
-    cta_smem = prm_bytes + sizeof(double) * team_smem_doubles(A.kt, A.d, A.NR, A.need_grad, A.estimate_nu);
-    if (cta_smem > (size_t)max_smem_optin()) return SV_EINVAL;
-    SV_CUDA_TRY(cudaFuncSetAttribute(k_block_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cta_smem));
-    int64_t grid = D->nblk - D->nblk_warp;
-    if (grid > 8LL * nsm) grid = 8LL * nsm;
-    k_block_cta<<<(int)grid, 128, cta_smem, st>>>(A);
-    SV_CUDA_TRY(cudaGetLastError());
-  }
-  // reference chunk-wide jitter: redo blocks whose chunk needed a larger level
-  if (D->chunked && D->nblk > 0) {
-    k_chunk_max<<<(int)((D->nblk + 255) / 256 > 4096 ? 4096 : (D->nblk + 255) / 256), 256, 0, st>>>(
-        A.flags, chunk, A.level, D->nblk, A.chunk_max);
-    SV_CUDA_TRY(cudaGetLastError());
-    A.fixup = 1;
-    if (D->nblk_warp > 0) {
-      A.kt = 32;
-      A.b0 = 0;
-      A.b1 = D->nblk_warp;
-      if (split) {
-        const int rc = launch_block_split(A, lanes, st);
-        if (rc != SV_OK) return rc;
-      } else {
-        const size_t team = sizeof(double) * team_smem_doubles(32, A.d, A.NR, A.need_grad, A.estimate_nu);
-        int wpc = 8;
-        while (wpc > 1 && prm_bytes + wpc * team > (size_t)max_smem_optin()) --wpc;
-        k_block_warp<<<(int)((D->nblk_warp + wpc - 1) / wpc > 64LL * nsm ? 64LL * nsm : (D->nblk_warp + wpc - 1) / wpc),
-                       32 * wpc, prm_bytes + wpc * team, st>>>(A);
-        SV_CUDA_TRY(cudaGetLastError());
-      }
-    }
-    if (D->nblk > D->nblk_warp) {
-      A.kt = D->kmax + 1;
-      A.b0 = D->nblk_warp;
-      A.b1 = D->nblk;
-      int64_t grid = D->nblk - D->nblk_warp;
-      if (grid > 8LL * nsm) grid = 8LL * nsm;
-      k_block_cta<<<(int)grid, 128, cta_smem, st>>>(A);
-      SV_CUDA_TRY(cudaGetLastError());
-    }
-  }
-
-  // split form: float64 re-evaluation of the blocks it flagged as ill-conditioned
-  if (split && D->nblk_warp > 0) {
-    A.fixup = 0;
-    A.redo_mode = 1;
-    A.kt = 32;
-    A.b0 = 0;
-    A.b1 = D->nblk_warp;
-    const size_t team = sizeof(double) * team_smem_doubles(32, A.d, A.NR, A.need_grad, A.estimate_nu);
-    int wpc = 8;
-    while (wpc > 1 && prm_bytes + wpc * team > (size_t)max_smem_optin()) --wpc;
-    const size_t smem = prm_bytes + wpc * team;
-    if (smem > (size_t)max_smem_optin()) return SV_EINVAL;
-    SV_CUDA_TRY(cudaFuncSetAttribute(k_block_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int64_t grid = (D->nblk_warp + wpc - 1) / wpc;
-    if (grid > 64LL * nsm) grid = 64LL * nsm;
-    k_block_warp<<<(int)grid, 32 * wpc, smem, st>>>(A);
-    SV_CUDA_TRY(cudaGetLastError());
-  }
-
-  RedArgs R;
-  R.cache = A.cache;
-  R.nblk = D->nblk;
-  R.CS = A.CS;
-  R.q = A.q;
-  R.P = A.P;
-  R.need_grad = A.need_grad;
-  R.part1 = (double*)(ws + W.part1);
-  R.part2 = (double*)(ws + W.part2);
-  R.beta = (double*)(ws + W.beta);
-  R.sums = (double*)(ws + W.sums);
-  R.theta = theta;
-  R.var_penalty = D->var_penalty;
-  R.log_var_target = D->log_var_target;
-  R.n = D->n;
-  R.out = out;
-  R.info = info;
-  const int nr = nred_ctas(D->nblk);
-  k_reduce1<<<nr, kRedThreads, 0, st>>>(R);
-  SV_CUDA_TRY(cudaGetLastError());
-  k_final1<<<1, kRedThreads, 0, st>>>(R, nr);
-  SV_CUDA_TRY(cudaGetLastError());
-  k_reduce2<<<nr, kRedThreads, 0, st>>>(R);
-  SV_CUDA_TRY(cudaGetLastError());
-  k_final2<<<1, 64, 0, st>>>(R, nr);
-  SV_CUDA_TRY(cudaGetLastError());
-  return SV_OK;
+extern "C" int sv_vecchia_loglik_batched(const sv_batch_desc* B, const sv_prob_desc* probs,
+                                         const double* theta, const double* X, const double* y,
+                                         const double* Z, const int32_t* rowb, const int32_t* kb,
+                                         const int32_t* nbr, const int32_t* bprob,
+                                         const int32_t* wlist, const int32_t* clist,
+                                         const int32_t* chunk, double* out, int32_t* info,
+                                         void* workspace, size_t workspace_bytes,
+                                         sv_stream_t stream) {
+  if (!B || !probs || !theta || !X || !y || !rowb || !kb || !bprob || !out || !info)
+    return SV_EINVAL;
+  if (B->nprob < 1 || B->nblk < 0 || B->dmax < 1 || B->dmax > kMaxD || B->qmax < 0 ||
+      B->qmax > kMaxQ || B->nwarp < 0 || B->ncta < 0 || B->nwarp + B->ncta != B->nblk)
+    return SV_EINVAL;
+  if (B->qmax > 0 && !Z) return SV_EINVAL;
+  if (B->kmax > 0 && (!nbr || B->ldnbr < B->kmax)) return SV_EINVAL;
+  if ((B->nwarp > 0 && !wlist) || (B->ncta > 0 && !clist)) return SV_EINVAL;
+  if (B->chunked && !chunk) return SV_EINVAL;
+  if (B->precision != 0 && B->precision != 1) return SV_EINVAL;
+  const int Pmax = B->dmax + 2 + (B->any_estimate_nu ? 1 : 0);
+  if (B->theta_stride < Pmax || B->out_stride < 1 + Pmax + Pmax * Pmax + B->qmax) return SV_EINVAL;
+  const EvalShape S = batch_shape(B);
+  WsLayout W = ws_layout(S);
+  if (!workspace || workspace_bytes < W.total) return SV_ENOSPC;
+  EvalCall C;
+  C.S = S;
+  C.probs = probs;
+  C.theta = theta;
+  C.tstride = B->theta_stride;
+  C.X = X;
+  C.y = y;
+  C.Z = Z;
+  C.rowb = rowb;
+  C.kb = kb;
+  C.nbr = nbr;
+  C.chunk = chunk;
+  C.bprob = bprob;
+  C.wlist = wlist;
+  C.clist = clist;
+  C.nwarp = B->nwarp;
+  C.ncta = B->ncta;
+  C.ldnbr = B->ldnbr;
+  C.chunked = B->chunked;
+  C.team_lanes = B->team_lanes;
+  C.rho_min = B->split_rho_min;
+  C.out = out;
+  C.ostride = B->out_stride;
+  C.info = info;
+  C.ws = (char*)workspace;
+  return run_eval(C, (cudaStream_t)stream);
 }

@@ -1,5 +1,11 @@
 // Shared definitions of the likelihood kernels (float64 plain form in
 // sv_loglik.cu, split-precision form in sv_loglik_split.cu).
+//
+// Every evaluation is a batch of independent problems (one problem for
+// sv_vecchia_loglik, many for sv_vecchia_loglik_batched).  Each problem has
+// its own inputs (offsets into concatenated X, y, Z), its own contiguous run
+// of conditioning blocks and its own parameter vector; a per-block problem
+// index lets one launch process the blocks of all problems together.
 #pragma once
 #include "sv_block.cuh"
 
@@ -10,6 +16,17 @@ constexpr int kMaxQ = 16;         // trend columns
 constexpr int kRedThreads = 256;  // reduction CTA size
 constexpr int kMaxP = kMaxD + 3;
 
+// Per-problem data in device memory: the layout from sv_prob_desc and the
+// parameters derived from theta (filled by k_prob_params every evaluation).
+struct ProbInfo {
+  int64_t n, x_off, y_off, z_off, blk_off, nblk;
+  int32_t d, q, P, estimate_nu, closed, skip;
+  double nu_fixed, var_penalty, log_var_target;
+  double s2, tau;
+  MaternMode mm;
+  double invlam[kMaxD];
+};
+
 struct LikArgs {
   const double* X;
   const double* y;
@@ -18,25 +35,31 @@ struct LikArgs {
   const int32_t* kb;
   const int32_t* nbr;
   const int32_t* chunk;
-  const double* theta;
-  double* cache;
+  const int32_t* bprob;   // problem of each block (nullptr: all problem 0)
+  const int32_t* list;    // blocks this launch processes (nullptr: [b0, b1))
+  const ProbInfo* probs;
+  double* cache;          // per-block records, stride CS
   int8_t* level;
-  int32_t* chunk_max;
-  int32_t* flags;  // [0] = any block used jitter
-  int32_t* info;
-  int64_t n, b0, b1;
-  int d, q, ldnbr, P, NR, CS, kt;  // kt = team block capacity (32 or kmax+1)
-  int need_grad, estimate_nu, closed;
-  double nu_fixed, nu_fd_h;
-  int fixup;
-  // split form: blocks whose smallest pivot ratio L_kk^2 / Sigma_kk falls
-  // below rho_min are flagged in redo[] and re-evaluated in float64
   int8_t* redo;
+  int32_t* chunk_max;
+  int32_t* flags;         // [0] = any block used jitter
+  int32_t* info;          // 4 words per problem
+  int64_t b0, b1;         // list range (indices into list, or block ids)
+  int nprob, ldnbr, CS, kt, dmax, NRmax;  // kt = team block capacity (32 or kmax+1)
+  int need_grad, any_estimate_nu;
+  int fixup;              // only blocks whose chunk needs a larger jitter level
+  int redo_mode;          // float64 kernel: only blocks flagged by the split kernel
   double rho_min;
-  int redo_mode;  // float64 kernel: only blocks with redo[b] != 0
-  // split form: scaled coordinates x / lambda as float32 (hi, lo) pairs
-  float2* xhl;
+  float2* xhl;            // split form: x / lambda as float32 (hi, lo) pairs
 };
+
+// block id of the t-th entry handled by a launch
+__device__ __forceinline__ int64_t launch_block(const LikArgs& A, int64_t t) {
+  return A.list ? (int64_t)A.list[t] : t;
+}
+__device__ __forceinline__ int block_problem(const LikArgs& A, int64_t b) {
+  return A.bprob ? A.bprob[b] : 0;
+}
 
 // 10^p for jitter level lv = p + 13, p = -12..-4 (_covariance.py:247-249)
 __device__ __forceinline__ double jitter_pow10(int lv) {
@@ -52,41 +75,6 @@ __device__ __forceinline__ double jitter_pow10(int lv) {
     default: return 1e-4;
   }
 }
-
-// per-CTA parameter block in shared memory
-struct PrmSmem {
-  double s2, tau;
-  MaternMode mm;
-  double invlam[kMaxD];
-};
-
-__device__ inline void load_params(const LikArgs& A, PrmSmem* prm) {
-  if (threadIdx.x == 0) {
-    const int d = A.d;
-    prm->s2 = exp(A.theta[0]);
-    double nu = A.nu_fixed;
-    if (A.estimate_nu) {
-      nu = exp(A.theta[1 + d]);
-      prm->tau = exp(A.theta[2 + d]);
-    } else {
-      prm->tau = exp(A.theta[1 + d]);
-    }
-    MaternMode mm;
-    mm.closed = A.estimate_nu ? -1 : A.closed;
-    mm.estimate_nu = A.estimate_nu;
-    mm.nu = nu;
-    mm.log_coef = (mm.closed < 0) ? matern_log_coef(nu) : 0.0;
-    mm.nu_p = nu + A.nu_fd_h;
-    mm.nu_m = nu - A.nu_fd_h;
-    mm.lc_p = A.estimate_nu ? matern_log_coef(mm.nu_p) : 0.0;
-    mm.lc_m = A.estimate_nu ? matern_log_coef(mm.nu_m) : 0.0;
-    mm.inv2h = 1.0 / (2.0 * A.nu_fd_h);
-    prm->mm = mm;
-  }
-  for (int l = threadIdx.x; l < A.d; l += blockDim.x) prm->invlam[l] = exp(-A.theta[1 + l]);
-  __syncthreads();
-}
-
 
 // block record layout (doubles): [L_KK, a.y, a.Z(q), (L^-1 y)_K, (L^-1 Z)_K(q),
 // w_K(P), W(L^-1 y)(P), W(L^-1 Z)(P q), F(P(P+1)/2) packed lower]
@@ -105,11 +93,11 @@ __host__ __device__ inline int split_slot_doubles(int d, int NR) {
   return s;
 }
 
-// launches the split-precision kernel over blocks [A.b0, A.b1) (all K <= 32,
-// closed-form nu); lanes = block team width (4, 8, 16 or 32)
+// launches the split-precision kernel over list entries [A.b0, A.b1) (all
+// K <= 32, closed-form nu); lanes = block team width (4, 8, 16 or 32)
 int launch_block_split(const LikArgs& A, int lanes, cudaStream_t st);
 
-// split form: fills A.xhl (n * d float2) from X and theta
-int launch_split_prep(const LikArgs& A, cudaStream_t st);
+// split form: fills A.xhl (X's n * d entries as float2) for every problem
+int launch_split_prep(const LikArgs& A, int64_t nx, cudaStream_t st);
 
 }  // namespace sv

@@ -111,40 +111,47 @@ __device__ __forceinline__ int cm(int i, int j) { return cstart(j) + (i - j); }
 template <int G>
 __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, int wpc) {
   extern __shared__ double smem[];
-  PrmSmem* prm = (PrmSmem*)smem;
-  load_params(A, prm);
   constexpr int NB = 32 / G;
   const unsigned full = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tm = lane / G, tl = lane - (lane / G) * G;
-  const int d = A.d, q = A.q, P = A.P, NR = A.NR;
-  const int64_t slot = split_slot_doubles(d, NR);
-  double* Lp = smem + (sizeof(PrmSmem) + 7) / 8 + (int64_t)(warp * NB + tm) * slot;
+  const int dmax = A.dmax;
+  const int64_t slot = split_slot_doubles(dmax, A.NRmax);
+  double* Lp = smem + (int64_t)(warp * NB + tm) * slot;
   double* R = Lp + 528;  // NR columns, stride 33
-  double* a = R + 33 * NR;
+  double* a = R + 33 * A.NRmax;
   double* invd = a + 32;
   float* a32 = (float*)(invd + 32);
   float* u = a32 + 32;
-  int* idx = (int*)(u + 32 * d);
+  int* idx = (int*)(u + 32 * dmax);
   volatile int* tflag = idx + 32;
   double* acc = R;            // column 0 of R is scratch during the a solve
   float* R32 = (float*)Lp;    // float32 copy of R once L is no longer needed
 
-  const double s2 = prm->s2, tau = prm->tau;
-  const float s2f = (float)s2;
-  const int code = prm->mm.closed;
-  const double diag = s2 * (1.0 + tau);
-
   const int64_t nb = A.b1 - A.b0;
   const int64_t stride = (int64_t)gridDim.x * wpc * NB;
   for (int64_t base = ((int64_t)blockIdx.x * wpc + warp) * NB; base < nb; base += stride) {
-    const int64_t b = A.b0 + base + tm;
-    bool active = (base + tm) < nb;
+    const int64_t tix = base + tm;
+    bool active = tix < nb;
+    const int64_t b = active ? launch_block(A, A.b0 + tix) : 0;
+    if (active && A.probs[block_problem(A, b)].skip) active = false;
     if (active && A.fixup) active = A.chunk_max[A.chunk[b]] > A.level[b];
     const int K = active ? A.kb[b] + 1 : 0;
     const int Kw = __reduce_max_sync(full, K);
     if (Kw == 0) continue;
     const int k = K - 1;
+    // this team's problem
+    const int pid = active ? block_problem(A, b) : 0;
+    const ProbInfo& PI = A.probs[pid];
+    const int d = PI.d, q = PI.q, P = PI.P, NR = P + 1 + q;
+    const double s2 = PI.s2, tau = PI.tau;
+    const float s2f = (float)s2;
+    const int code = PI.closed;
+    const double diag = s2 * (1.0 + tau);
+    const double* Y = A.y + PI.y_off;
+    const double* Zm = A.Z + PI.z_off;
+    const float2* XH = A.xhl + PI.x_off;
+    int32_t* info = A.info + 4 * pid;
 
     // ---- gather: neighbours first, self last; coordinates centred on self
     if (active)
@@ -153,17 +160,17 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     if (active) {
       // centred scaled coordinates from the (hi, lo) float32 pairs: the
       // difference keeps ~24 bits relative to itself, however close the points
-      const float2* xs = A.xhl + (int64_t)idx[k] * d;
+      const float2* xs = XH + (int64_t)idx[k] * d;
       for (int t = tl; t < K * d; t += G) {
         const int i = t / d, l = t - (t / d) * d;
-        const float2 v = A.xhl[(int64_t)idx[i] * d + l];
+        const float2 v = XH[(int64_t)idx[i] * d + l];
         const float2 w = xs[l];
         u[t] = (v.x - w.x) + (v.y - w.y);
       }
       if (A.need_grad)
         for (int i = tl; i < K; i += G) {
-          R[P * 33 + i] = A.y[idx[i]];
-          for (int c = 0; c < q; ++c) R[(P + 1 + c) * 33 + i] = A.Z[(int64_t)idx[i] * q + c];
+          R[P * 33 + i] = Y[idx[i]];
+          for (int c = 0; c < q; ++c) R[(P + 1 + c) * 33 + i] = Zm[(int64_t)idx[i] * q + c];
         }
     }
     __syncwarp();
@@ -286,19 +293,19 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       if (tl == 0) {
         A.level[b] = 0;
         A.redo[b] = 1;
-        atomicAdd(A.info + SV_INFO_AUX, 1);
+        atomicAdd(info + SV_INFO_AUX, 1);
       }
       for (int f = tl; f < A.CS; f += G) rec[f] = 0.0;
     } else if (active && tl == 0) {
       A.level[b] = (int8_t)lv;
       if (lv > 0) {
-        atomicMax(A.info + SV_INFO_JITTER, lv);
+        atomicMax(info + SV_INFO_JITTER, lv);
         A.flags[0] = 1;
       }
       // ill-conditioned blocks lose too much to float32 assembly: redo in float64
       const bool again = ill;
       A.redo[b] = again ? 1 : 0;
-      if (again) atomicAdd(A.info + SV_INFO_AUX, 1);
+      if (again) atomicAdd(info + SV_INFO_AUX, 1);
     }
     const bool ok = active && !failed;
 
@@ -330,15 +337,18 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     {
       double vy = 0.0;
       if (ok)
-        for (int i = tl; i < K; i += G) vy += a[i] * A.y[idx[i]];
+        for (int i = tl; i < K; i += G) vy += a[i] * Y[idx[i]];
       for (int o = G / 2; o > 0; o >>= 1) vy += __shfl_xor_sync(full, vy, o);
       if (ok && tl == 0) rec[1] = vy;
-      for (int c = 0; c < q; ++c) {
+      // teams of one warp may belong to problems with different q: the
+      // shuffles run to the warp's largest q
+      const int qw = __reduce_max_sync(full, active ? q : 0);
+      for (int c = 0; c < qw; ++c) {
         double vz = 0.0;
-        if (ok)
-          for (int i = tl; i < K; i += G) vz += a[i] * A.Z[(int64_t)idx[i] * q + c];
+        if (ok && c < q)
+          for (int i = tl; i < K; i += G) vz += a[i] * Zm[(int64_t)idx[i] * q + c];
         for (int o = G / 2; o > 0; o >>= 1) vz += __shfl_xor_sync(full, vz, o);
-        if (ok && tl == 0) rec[2 + c] = vz;
+        if (ok && c < q && tl == 0) rec[2 + c] = vz;
       }
     }
     if (!A.need_grad) {
@@ -487,24 +497,30 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
   }
 }
 
-// (hi, lo) float32 pairs of x / lambda: hi = fl32(v), lo = fl32(v - hi)
-__global__ void k_split_prep(const double* X, const double* theta, int64_t n, int d, float2* xhl) {
-  const int64_t tot = n * d;
+// (hi, lo) float32 pairs of x / lambda: hi = fl32(v), lo = fl32(v - hi);
+// grid row = problem
+__global__ void k_split_prep(const double* X, const ProbInfo* probs, float2* xhl) {
+  const ProbInfo& PI = probs[blockIdx.y];
+  if (PI.skip) return;
+  const int d = PI.d;
+  const int64_t tot = PI.n * d;
+  const double* Xp = X + PI.x_off;
+  float2* out = xhl + PI.x_off;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot;
        e += (int64_t)gridDim.x * blockDim.x) {
     const int l = (int)(e % d);
-    const double v = X[e] * exp(-theta[1 + l]);
+    const double v = Xp[e] * PI.invlam[l];
     const float hi = (float)v;
-    xhl[e] = make_float2(hi, (float)(v - (double)hi));
+    out[e] = make_float2(hi, (float)(v - (double)hi));
   }
 }
 
-int launch_split_prep(const LikArgs& A, cudaStream_t st) {
-  const int64_t tot = A.n * A.d;
-  if (tot == 0) return SV_OK;
-  int64_t grid = (tot + 255) / 256;
-  if (grid > 16LL * sv_num_sms()) grid = 16LL * sv_num_sms();
-  k_split_prep<<<(unsigned)grid, 256, 0, st>>>(A.X, A.theta, A.n, A.d, A.xhl);
+int launch_split_prep(const LikArgs& A, int64_t nx, cudaStream_t st) {
+  if (nx == 0) return SV_OK;
+  int64_t gx = (nx / A.nprob + 255) / 256;
+  if (gx > 4LL * sv_num_sms()) gx = 4LL * sv_num_sms();
+  if (gx < 1) gx = 1;
+  k_split_prep<<<dim3((unsigned)gx, (unsigned)A.nprob), 256, 0, st>>>(A.X, A.probs, A.xhl);
   SV_CUDA_TRY(cudaGetLastError());
   return SV_OK;
 }
@@ -513,11 +529,10 @@ int launch_block_split(const LikArgs& A, int lanes, cudaStream_t st) {
   int dev = 0, maxsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t prm = (sizeof(PrmSmem) + 7) / 8 * 8;
-  const size_t per_warp = sizeof(double) * (size_t)split_slot_doubles(A.d, A.NR) * (32 / lanes);
+  const size_t per_warp = sizeof(double) * (size_t)split_slot_doubles(A.dmax, A.NRmax) * (32 / lanes);
   int wpc = kSplitMaxThreads / 32;
-  while (wpc > 1 && prm + wpc * per_warp > (size_t)maxsm) --wpc;
-  const size_t smem = prm + wpc * per_warp;
+  while (wpc > 1 && wpc * per_warp > (size_t)maxsm) --wpc;
+  const size_t smem = wpc * per_warp;
   if (smem > (size_t)maxsm) return SV_EINVAL;
   const int64_t nb = A.b1 - A.b0;
   const int64_t per_cta = (int64_t)wpc * (32 / lanes);

@@ -22,7 +22,7 @@
 // slot array and a monotone arrival counter; waits are bounded
 // (SV_ETIMEOUT).  Every CTA reduces the same candidates in the same way, so
 // all agree on the next pivot.
-#include "sv_common.cuh"
+#include "sv_reorder.cuh"
 
 namespace sv {
 
@@ -43,21 +43,6 @@ struct MmArgs {
   float growth;            // (1+2^-24)^(d+2) (1+2^-20), rounded up
 };
 
-__device__ __forceinline__ double sqdist_exact(const double* a, const double* b, int d) {
-  double s = 0.0;
-  for (int l = 0; l < d; ++l) {
-    const double df = __dsub_rn(a[l], b[l]);
-    s = __dadd_rn(s, __dmul_rn(df, df));
-  }
-  return s;
-}
-
-// float32 value bound of (dist * (1 + (d+4) 2^-53) + B_p), rounded up
-__device__ __forceinline__ float thr_base(double dist, double Bp, int d) {
-  if (isinf(dist)) return __int_as_float(0x7f800000);
-  const double t = (dist * (1.0 + (double)(d + 4) * 0x1p-53) + Bp) * (1.0 + 0x1p-40);
-  return __double2float_ru(t);
-}
 
 __global__ void __launch_bounds__(kMmThreads) k_maximin(MmArgs A) {
   extern __shared__ unsigned char smraw[];
@@ -235,6 +220,14 @@ __global__ void __launch_bounds__(kMmThreads) k_maximin(MmArgs A) {
       }
       __syncthreads();
     }
+    // no finite candidate left (NaN inputs): report instead of indexing with it
+    if (s_pivot == 0x7fffffffffffffffLL) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        set_error(A.info + SV_INFO_STATUS, SV_EINVAL);
+        A.info[SV_INFO_BLOCK] = (int)t;
+      }
+      return;
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) A.order[t + 1] = s_pivot;
   }
 }
@@ -282,6 +275,10 @@ extern "C" int sv_maximin_order(const double* X, int64_t n, int32_t d, int64_t f
     return SV_OK;
   }
   if (!workspace || workspace_bytes < sv_maximin_workspace_bytes(n, d)) return SV_ENOSPC;
+  // problems that fit one thread-block cluster: hardware cluster barrier per
+  // step instead of the grid-wide exchange below
+  if (n <= maximin_cluster_max_rows(d))
+    return maximin_cluster_single(X, n, d, first, order, info, (char*)workspace, st);
   const int nsm = sv_num_sms();
   char* ws = (char*)workspace;
   double* centroid = (double*)ws;

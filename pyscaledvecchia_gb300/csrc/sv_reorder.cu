@@ -1,0 +1,548 @@
+// Batched reorder of many independent problems: the rebuild step of the fit
+// (gp.py:182-191) for every problem of a batched fit in one call.
+//
+// Per problem p with inputs X_e (n x d, subsample order), y_e, Z_e and
+// ranges r (host values, so the division below sees numpy's exp bits):
+//   Xs   = X_e / r                                (gp.py:184, IEEE division)
+//   ord  = maximin order of Xs from row `first`   (ordering.py:27-73)
+//   X, y, Z <- X_e[ord], y_e[ord], Z_e[ord]        (gp.py:189-191)
+//   nbr  <- ordered kNN of Xs[ord], m neighbours   (ordering.py:76-116), written
+//           straight into the likelihood's block columns: block blk_off + i
+//           holds row i's min(i, m) neighbours, nearest first, -1 padded
+//           (the _nn_groups layout, ordering.py:119-127, with row i = block i).
+//
+// Maximin runs one thread-block cluster per problem.  The cluster's CTAs
+// split the problem's points; each keeps, in shared memory, the float64
+// distances, float32 skip thresholds and float32 coordinates centred on the
+// first row, and makes every update decision exactly as the single-problem
+// kernel (sv_maximin.cu) does: float32 screening with a rigorous bound, the
+// float64 distance in IEEE sequential arithmetic wherever the bound cannot
+// exclude an update.  Per step the CTAs' candidates (distance bits, index)
+// meet through distributed shared memory after one hardware cluster barrier
+// (double-buffered by step parity), so there is no spin-wait at all.
+// Problems are grouped by cluster size (1, 2, 4 or 8 CTAs, the smallest
+// whose shared memory holds the problem), one launch per group, largest
+// problems first.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "sv_reorder.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace sv {
+
+constexpr int kMcThreads = 512;
+constexpr int kMcStaticSmem = 64 * 8 * 2 + 64 * 4 + 4 + 2 * 8 * (kMcThreads / 32) + 4 * 8 + 8 + 64;
+
+struct RoProb {
+  int64_t n, xe_off, ye_off, ze_off, x_off, y_off, z_off, blk_off, first;
+  int64_t xs_off;   // doubles: this call's scaled rows (and their maximin-order copy)
+  int64_t v_off;    // floats: centred float32 rows [n][DP]
+  int64_t row_off;  // rows: order, B
+  int32_t d, q, m, DP, C, pad;
+};
+
+// per-point shared memory of the cluster maximin: dist f64, thr f32, B f32, v f32[d]
+__host__ __device__ inline int64_t mc_point_bytes(int d) { return 16 + 4 * (int64_t)d; }
+
+__device__ __forceinline__ void cand_better(long long ob, long long oi, long long& bb, long long& bi) {
+  if (ob > bb || (ob == bb && oi < bi)) {
+    bb = ob;
+    bi = oi;
+  }
+}
+
+// (1+2^-24)^(d+2) (1+2^-20) as a float32 rounded up
+__device__ __forceinline__ float mc_growth(int d) {
+  double g = 1.0;
+  for (int i = 0; i < d + 2; ++i) g *= (1.0 + 0x1p-24);
+  return __double2float_ru(g * (1.0 + 0x1p-20));
+}
+
+__global__ void k_ro_info_init(int32_t* info, int nprob) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nprob; p += gridDim.x * blockDim.x) {
+    info[4 * p + 0] = 0;
+    info[4 * p + 1] = -1;
+    info[4 * p + 2] = 0;
+    info[4 * p + 3] = 0;
+  }
+}
+
+// Xs = X_e / r; grid row = problem
+__global__ void k_ro_scale(const RoProb* probs, const double* ranges, int dmax, const double* Xe,
+                           double* Xs) {
+  const RoProb& P = probs[blockIdx.y];
+  const int d = P.d;
+  const int64_t tot = P.n * d;
+  const double* r = ranges + (int64_t)blockIdx.y * dmax;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot;
+       e += (int64_t)gridDim.x * blockDim.x)
+    Xs[P.xs_off + e] = __ddiv_rn(Xe[P.xe_off + e], r[e % d]);
+}
+
+// warp 0: exact pivot row, its float32 image and rounding bound
+__device__ __forceinline__ void mc_load_pivot(const double* X, long long j, int d, const double* cen,
+                                              double* xj, float* vj, float* Bj) {
+  const int lane = threadIdx.x & 31;
+  double e2 = 0.0;
+  for (int l = lane; l < d; l += 32) {
+    const double x = X[j * d + l];
+    const double c = x - cen[l];
+    xj[l] = x;
+    vj[l] = __double2float_rn(c);
+    e2 += c * c;
+  }
+  for (int o = 16; o > 0; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+  if (lane == 0) *Bj = __double2float_ru(1.01 * 0x1p-24 * sqrt(e2));
+}
+
+__global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* probs,
+                                                                const int32_t* plist,
+                                                                const double* Xs, int64_t* ord,
+                                                                int32_t* info) {
+  extern __shared__ unsigned char smraw[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int r = (int)cluster.block_rank();
+  const int pid = plist[blockIdx.x / C];
+  const RoProb& P = probs[pid];
+  const int64_t n = P.n;
+  const int d = P.d;
+  const double* X = Xs + P.xs_off;
+  int64_t* order = ord + P.row_off;
+  const int64_t per = (n + C - 1) / C;
+  const int64_t p0 = (int64_t)r * per;
+  const int64_t p1 = min(n, p0 + per);
+  const int S = (int)max((int64_t)0, p1 - p0);
+  const int Sc = (int)per;
+  double* dist = (double*)smraw;
+  float* thr = (float*)(dist + Sc);
+  float* Bp = thr + Sc;
+  float* v = Bp + Sc;
+  __shared__ double xj[64], cen[64];
+  __shared__ float vj[64];
+  __shared__ float Bj_f;
+  __shared__ long long red_bits[kMcThreads / 32], red_idx[kMcThreads / 32];
+  __shared__ long long cand_bits[2], cand_idx[2];
+  __shared__ long long s_pivot;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarp = blockDim.x >> 5;
+  const float growth = mc_growth(d);
+
+  // centre: the first row (any shift serves the float32 screen)
+  for (int l = threadIdx.x; l < d; l += blockDim.x) cen[l] = X[P.first * d + l];
+  __syncthreads();
+  for (int p = threadIdx.x; p < S; p += blockDim.x) {
+    const double* xp = X + (p0 + p) * d;
+    double e2 = 0.0;
+    for (int l = 0; l < d; ++l) {
+      const double c = xp[l] - cen[l];
+      v[l * Sc + p] = __double2float_rn(c);
+      e2 += c * c;
+    }
+    Bp[p] = __double2float_ru(1.01 * 0x1p-24 * sqrt(e2));
+    dist[p] = __longlong_as_double(0x7ff0000000000000LL);  // +inf: first pass is exact
+    thr[p] = __int_as_float(0x7f800000);
+  }
+  if (threadIdx.x == 0) {
+    s_pivot = P.first;
+    if (r == 0) order[0] = P.first;
+  }
+  if (warp == 0) mc_load_pivot(X, P.first, d, cen, xj, vj, &Bj_f);
+  __syncthreads();
+
+  for (int64_t t = 0; t + 1 < n; ++t) {
+    const long long j = s_pivot;
+    const float bj = Bj_f;
+    long long best_bits = -1LL;  // below every non-negative double
+    long long best_idx = 0x7fffffffffffffffLL;
+    for (int p = threadIdx.x; p < S; p += blockDim.x) {
+      double dp = dist[p];
+      if (__double_as_longlong(dp) < 0) continue;  // already ordered (ordering.py:50-51)
+      const long long gp = p0 + p;
+      if (gp == j) {
+        dist[p] = -1.0;  // ordering.py:58
+        continue;
+      }
+      float s32 = 0.0f;
+      for (int l = 0; l < d; ++l) {
+        const float df = __fsub_rn(v[l * Sc + p], vj[l]);
+        s32 = __fmaf_rn(df, df, s32);
+      }
+      const float tb = __fadd_ru(thr[p], bj);
+      const float bound = __fmul_ru(__fmul_ru(tb, tb), growth);
+      if (!(s32 >= bound)) {
+        // possible update: decide exactly (ordering.py:52-57)
+        const double dj = __dsqrt_rn(sqdist_exact(X + gp * d, xj, d));
+        if (dj < dp) {
+          dp = dj;
+          dist[p] = dj;
+          thr[p] = thr_base(dj, (double)Bp[p], d);
+        }
+      }
+      const long long bits = __double_as_longlong(dp);
+      if (bits > best_bits && bits <= 0x7ff0000000000000LL) {
+        best_bits = bits;
+        best_idx = gp;
+      }
+    }
+    // larger distance wins, then the smaller index (np.argmax's first maximum)
+    for (int o = 16; o > 0; o >>= 1)
+      cand_better(__shfl_xor_sync(0xffffffffu, best_bits, o), __shfl_xor_sync(0xffffffffu, best_idx, o),
+                  best_bits, best_idx);
+    if (lane == 0) {
+      red_bits[warp] = best_bits;
+      red_idx[warp] = best_idx;
+    }
+    __syncthreads();
+    const int par = (int)(t & 1);
+    long long bb = -1LL, bi = 0x7fffffffffffffffLL;
+    if (warp == 0) {
+      if (lane < nwarp) {
+        bb = red_bits[lane];
+        bi = red_idx[lane];
+      }
+      for (int o = 16; o > 0; o >>= 1)
+        cand_better(__shfl_xor_sync(0xffffffffu, bb, o), __shfl_xor_sync(0xffffffffu, bi, o), bb, bi);
+      if (C > 1 && lane == 0) {
+        cand_bits[par] = bb;
+        cand_idx[par] = bi;
+      }
+    }
+    if (C > 1) {
+      // every CTA's candidate of this step is visible after the barrier; the
+      // slots of step t are rewritten at t + 2, after the next barrier, which
+      // no CTA passes before all have read them
+      cluster.sync();
+      if (warp == 0) {
+        bb = -1LL;
+        bi = 0x7fffffffffffffffLL;
+        if (lane < C) {
+          bb = cluster.map_shared_rank(cand_bits, lane)[par];
+          bi = cluster.map_shared_rank(cand_idx, lane)[par];
+        }
+        for (int o = 16; o > 0; o >>= 1)
+          cand_better(__shfl_xor_sync(0xffffffffu, bb, o), __shfl_xor_sync(0xffffffffu, bi, o), bb, bi);
+      }
+    }
+    if (warp == 0) {
+      if (lane == 0) s_pivot = bi;
+      if (bi != 0x7fffffffffffffffLL) {
+        if (r == 0 && lane == 0) order[t + 1] = bi;
+        mc_load_pivot(X, bi, d, cen, xj, vj, &Bj_f);
+      } else if (r == 0 && lane == 0) {
+        // no finite candidate left (NaN inputs): report and stop
+        set_error(info + 4 * pid + SV_INFO_STATUS, SV_EINVAL);
+        info[4 * pid + SV_INFO_BLOCK] = (int)t;
+      }
+    }
+    __syncthreads();
+    if (s_pivot == 0x7fffffffffffffffLL) break;  // the same value in every CTA
+  }
+  // keep this CTA's shared memory alive until every remote read is done
+  if (C > 1) cluster.sync();
+}
+
+// X, y, Z <- rows of X_e, y_e, Z_e in maximin order; Xso <- Xs in that order;
+// grid row = problem
+__global__ void k_ro_permute(const RoProb* probs, const int64_t* ord, const double* Xe,
+                             const double* ye, const double* Ze, const double* Xs, double* X,
+                             double* y, double* Z, double* Xso, int64_t* order_out) {
+  const RoProb& P = probs[blockIdx.y];
+  const int d = P.d, q = P.q;
+  const int64_t* o = ord + P.row_off;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t src = o[i];
+    for (int l = 0; l < d; ++l) {
+      X[P.x_off + i * d + l] = Xe[P.xe_off + src * d + l];
+      Xso[P.xs_off + P.n * d + i * d + l] = Xs[P.xs_off + src * d + l];
+    }
+    y[P.y_off + i] = ye[P.ye_off + src];
+    for (int c = 0; c < q; ++c) Z[P.z_off + i * q + c] = Ze[P.ze_off + src * q + c];
+    if (order_out) order_out[P.row_off + i] = src;
+  }
+}
+
+// centred float32 rows (zero padded to DP) and their rounding bound for the
+// kNN screen, centre = row 0 of the ordered problem; grid row = problem
+__global__ void k_ro_knn_prep(const RoProb* probs, const double* Xso, float* v, float* B) {
+  const RoProb& P = probs[blockIdx.y];
+  const int d = P.d, DP = P.DP;
+  const double* X = Xso + P.xs_off + P.n * d;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double e2 = 0.0;
+    for (int l = 0; l < DP; ++l) {
+      float f = 0.0f;
+      if (l < d) {
+        const double c = X[i * d + l] - X[l];
+        f = __double2float_rn(c);
+        e2 += c * c;
+      }
+      v[P.v_off + i * DP + l] = f;
+    }
+    B[P.row_off + i] = __double2float_ru(1.01 * 0x1p-24 * sqrt(e2));
+  }
+}
+
+static size_t ro_align(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static int ro_max_smem() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return v;
+}
+
+// cluster size for n rows of dimension d: 1, 2, 4 or 8, or 0 when none fits
+static int mc_cluster_size(int64_t n, int d, int maxsm) {
+  const int64_t budget = (int64_t)maxsm - kMcStaticSmem;
+  for (int C = 1; C <= 8; C *= 2) {
+    const int64_t per = (n + C - 1) / C;
+    if (per * mc_point_bytes(d) <= budget) return C;
+  }
+  return 0;
+}
+
+struct RoPlan {
+  std::vector<RoProb> probs;
+  std::vector<KnnBatchProb> kprobs;
+  std::vector<int32_t> plist[4];   // problems per cluster size 1, 2, 4, 8
+  size_t smem[4] = {0, 0, 0, 0};
+  std::vector<int2> tiles[8];      // kNN tiles per padded dimension
+  int DPs[8] = {4, 8, 12, 16, 24, 32, 48, 64};
+  int kcap[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int64_t nrows = 0, nxs = 0, nv = 0;
+  // workspace layout
+  size_t o_probs, o_kprobs, o_plist[4], o_tiles[8], o_ranges, o_xs, o_v, o_b, o_ord, total, staged;
+};
+
+static int ro_plan(const sv_reorder_desc* D, const sv_reorder_prob* hp, RoPlan& L) {
+  const int maxsm = ro_max_smem();
+  const int64_t np = D->nprob;
+  L.probs.resize(np);
+  L.kprobs.resize(np);
+  for (int64_t i = 0; i < np; ++i) {
+    const sv_reorder_prob& U = hp[i];
+    if (U.n < 0 || U.d < 1 || U.d > D->dmax || U.d > 64 || U.q < 0 || U.m < 0 || U.m > D->ldnbr ||
+        (U.n > 0 && (U.first < 0 || U.first >= U.n)) || U.n > 0x7fffffffLL)
+      return SV_EINVAL;
+    RoProb& R = L.probs[i];
+    R.n = U.n;
+    R.xe_off = U.xe_off;
+    R.ye_off = U.ye_off;
+    R.ze_off = U.ze_off;
+    R.x_off = U.x_off;
+    R.y_off = U.y_off;
+    R.z_off = U.z_off;
+    R.blk_off = U.blk_off;
+    R.first = U.first;
+    R.d = U.d;
+    R.q = U.q;
+    R.m = U.m;
+    R.DP = knn_pad_dim(U.d);
+    R.C = mc_cluster_size(U.n, U.d, maxsm);
+    if (R.C == 0) return SV_EINVAL;
+    R.xs_off = L.nxs;
+    L.nxs += 2 * U.n * U.d;  // scaled rows, then the same rows in maximin order
+    R.v_off = L.nv;
+    L.nv += U.n * R.DP;
+    R.row_off = L.nrows;
+    L.nrows += U.n;
+    R.pad = 0;
+    KnnBatchProb& K = L.kprobs[i];
+    K.xs_off = R.xs_off + U.n * U.d;
+    K.v_off = R.v_off;
+    K.row_off = R.row_off;
+    K.n = U.n;
+    K.blk_off = U.blk_off;
+    K.d = U.d;
+    K.m = U.m;
+  }
+  // largest problems first in every launch
+  std::vector<int32_t> byn(np);
+  for (int64_t i = 0; i < np; ++i) byn[i] = (int32_t)i;
+  std::stable_sort(byn.begin(), byn.end(),
+                   [&](int32_t a, int32_t b) { return L.probs[a].n > L.probs[b].n; });
+  for (int32_t i : byn) {
+    const RoProb& R = L.probs[i];
+    if (R.n < 1) continue;
+    const int g = R.C == 1 ? 0 : R.C == 2 ? 1 : R.C == 4 ? 2 : 3;
+    L.plist[g].push_back(i);
+    const size_t sm = (size_t)((R.n + R.C - 1) / R.C) * (size_t)mc_point_bytes(R.d);
+    L.smem[g] = std::max(L.smem[g], sm);
+    if (R.m < 1 || R.n < 2) continue;
+    int gi = 0;
+    while (L.DPs[gi] != R.DP) ++gi;
+    L.kcap[gi] = std::max(L.kcap[gi], R.m);
+    const int64_t nt = (R.n + 127) / 128;
+    for (int64_t t = nt - 1; t >= 0; --t) L.tiles[gi].push_back(make_int2(i, (int)t));
+  }
+  // workspace: staged tables first, then the arrays
+  size_t off = 0;
+  L.o_probs = off;
+  off = ro_align(off + sizeof(RoProb) * (size_t)np);
+  L.o_kprobs = off;
+  off = ro_align(off + sizeof(KnnBatchProb) * (size_t)np);
+  for (int g = 0; g < 4; ++g) {
+    L.o_plist[g] = off;
+    off = ro_align(off + sizeof(int32_t) * L.plist[g].size());
+  }
+  for (int g = 0; g < 8; ++g) {
+    L.o_tiles[g] = off;
+    off = ro_align(off + sizeof(int2) * L.tiles[g].size());
+  }
+  L.o_ranges = off;
+  off = ro_align(off + sizeof(double) * (size_t)np * D->dmax);
+  L.staged = off;
+  L.o_xs = off;
+  off = ro_align(off + sizeof(double) * (size_t)L.nxs);
+  L.o_v = off;
+  off = ro_align(off + sizeof(float) * (size_t)L.nv);
+  L.o_b = off;
+  off = ro_align(off + sizeof(float) * (size_t)L.nrows);
+  L.o_ord = off;
+  off = ro_align(off + sizeof(int64_t) * (size_t)L.nrows);
+  L.total = off;
+  return SV_OK;
+}
+
+static int launch_maximin_cluster(int C, size_t smem, unsigned nclusters, const RoProb* probs,
+                                  const int32_t* plist, const double* Xs, int64_t* ord,
+                                  int32_t* info, cudaStream_t st) {
+  SV_CUDA_TRY(cudaFuncSetAttribute(k_maximin_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nclusters * (unsigned)C);
+  cfg.blockDim = dim3(kMcThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  SV_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_maximin_cluster, probs, plist, Xs, ord, info));
+  return SV_OK;
+}
+
+// One problem through the cluster kernel (sv_maximin_order for n that fits
+// one cluster).  ws: 256 bytes of device scratch.
+int maximin_cluster_single(const double* X, int64_t n, int d, int64_t first, int64_t* order,
+                           int32_t* info, char* ws, cudaStream_t st) {
+  const int C = mc_cluster_size(n, d, ro_max_smem());
+  if (C == 0) return SV_EINVAL;
+  struct {
+    RoProb p;
+    int32_t plist[4];
+  } h;
+  memset(&h, 0, sizeof(h));
+  h.p.n = n;
+  h.p.first = first;
+  h.p.d = d;
+  h.p.C = C;
+  SV_CUDA_TRY(cudaMemcpyAsync(ws, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+  const size_t smem = (size_t)((n + C - 1) / C) * (size_t)mc_point_bytes(d);
+  return launch_maximin_cluster(C, smem, 1, (const RoProb*)ws, (const int32_t*)(ws + sizeof(RoProb)),
+                                X, order, info, st);
+}
+
+int64_t maximin_cluster_max_rows(int d) {
+  if (d < 1 || d > 64) return 0;
+  const int64_t budget = (int64_t)ro_max_smem() - kMcStaticSmem;
+  return 8 * (budget / mc_point_bytes(d));
+}
+
+}  // namespace sv
+
+using namespace sv;
+
+extern "C" int64_t sv_maximin_cluster_max_rows(int32_t d) { return maximin_cluster_max_rows(d); }
+
+extern "C" size_t sv_reorder_batched_workspace_bytes(const sv_reorder_desc* D,
+                                                     const sv_reorder_prob* probs) {
+  if (!D || (D->nprob > 0 && !probs) || D->nprob < 0) return 0;
+  RoPlan L;
+  if (ro_plan(D, probs, L) != SV_OK) return 0;
+  return L.total;
+}
+
+extern "C" int sv_reorder_batched(const sv_reorder_desc* D, const sv_reorder_prob* probs,
+                                  const double* ranges, const double* Xe, const double* ye,
+                                  const double* Ze, double* X, double* y, double* Z, int32_t* nbr,
+                                  int64_t* order, int32_t* info, void* workspace,
+                                  size_t workspace_bytes, sv_stream_t stream) {
+  if (!D || D->nprob < 0 || D->dmax < 1 || D->dmax > 64 || D->ldnbr < 0 || !info) return SV_EINVAL;
+  if (D->nprob == 0) return SV_OK;
+  if (!probs || !ranges || !Xe || !ye || !X || !y) return SV_EINVAL;
+  RoPlan L;
+  int rc = ro_plan(D, probs, L);
+  if (rc != SV_OK) return rc;
+  bool anyq = false, anym = false;
+  for (const RoProb& R : L.probs) {
+    anyq = anyq || R.q > 0;
+    anym = anym || (R.m > 0 && R.n > 1);
+  }
+  if ((anyq && (!Ze || !Z)) || (anym && (!nbr || D->ldnbr < 1))) return SV_EINVAL;
+  if (!workspace || workspace_bytes < L.total) return SV_ENOSPC;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* ws = (char*)workspace;
+  const int np = (int)D->nprob;
+
+  // one staged copy of every table
+  std::vector<char> host(L.staged, 0);
+  memcpy(host.data() + L.o_probs, L.probs.data(), sizeof(RoProb) * np);
+  memcpy(host.data() + L.o_kprobs, L.kprobs.data(), sizeof(KnnBatchProb) * np);
+  for (int g = 0; g < 4; ++g)
+    if (!L.plist[g].empty())
+      memcpy(host.data() + L.o_plist[g], L.plist[g].data(), sizeof(int32_t) * L.plist[g].size());
+  for (int g = 0; g < 8; ++g)
+    if (!L.tiles[g].empty())
+      memcpy(host.data() + L.o_tiles[g], L.tiles[g].data(), sizeof(int2) * L.tiles[g].size());
+  memcpy(host.data() + L.o_ranges, ranges, sizeof(double) * (size_t)np * D->dmax);
+  SV_CUDA_TRY(cudaMemcpyAsync(ws, host.data(), L.staged, cudaMemcpyHostToDevice, st));
+  const RoProb* dprobs = (const RoProb*)(ws + L.o_probs);
+  double* Xs = (double*)(ws + L.o_xs);
+  float* v = (float*)(ws + L.o_v);
+  float* B = (float*)(ws + L.o_b);
+  int64_t* ord = (int64_t*)(ws + L.o_ord);
+
+  k_ro_info_init<<<(np + 255) / 256, 256, 0, st>>>(info, np);
+  SV_CUDA_TRY(cudaGetLastError());
+  int64_t maxn = 0;
+  for (const RoProb& R : L.probs) maxn = std::max(maxn, R.n);
+  int64_t gx = (maxn * D->dmax + 255) / 256;
+  gx = std::max<int64_t>(1, std::min<int64_t>(gx, 64));
+  k_ro_scale<<<dim3((unsigned)gx, np), 256, 0, st>>>(dprobs, (const double*)(ws + L.o_ranges),
+                                                      D->dmax, Xe, Xs);
+  SV_CUDA_TRY(cudaGetLastError());
+
+  // maximin: one launch per cluster size
+  for (int g = 0; g < 4; ++g) {
+    if (L.plist[g].empty()) continue;
+    rc = launch_maximin_cluster(1 << g, L.smem[g], (unsigned)L.plist[g].size(), dprobs,
+                                (const int32_t*)(ws + L.o_plist[g]), (const double*)Xs, ord, info, st);
+    if (rc != SV_OK) return rc;
+  }
+
+  gx = (maxn + 255) / 256;
+  gx = std::max<int64_t>(1, std::min<int64_t>(gx, 64));
+  k_ro_permute<<<dim3((unsigned)gx, np), 256, 0, st>>>(dprobs, ord, Xe, ye, Ze, Xs, X, y, Z, Xs, order);
+  SV_CUDA_TRY(cudaGetLastError());
+  k_ro_knn_prep<<<dim3((unsigned)gx, np), 256, 0, st>>>(dprobs, Xs, v, B);
+  SV_CUDA_TRY(cudaGetLastError());
+  for (int g = 0; g < 8; ++g) {
+    if (L.tiles[g].empty()) continue;
+    rc = launch_knn_batched(L.DPs[g], (const KnnBatchProb*)(ws + L.o_kprobs),
+                            (const int2*)(ws + L.o_tiles[g]), (int64_t)L.tiles[g].size(), Xs, v, B,
+                            nbr, D->ldnbr, L.kcap[g], st);
+    if (rc != SV_OK) return rc;
+  }
+  return SV_OK;
+}

@@ -1,0 +1,33 @@
+// Internal interface between the batched reorder (sv_reorder.cu) and the kNN
+// kernels (sv_knn.cu).
+#pragma once
+#include "sv_common.cuh"
+
+namespace sv {
+
+// one problem of a batched ordered kNN search
+struct KnnBatchProb {
+  int64_t xs_off;   // doubles: its rows (maximin order, scaled) in Xs
+  int64_t v_off;    // floats: its centred float32 rows [n][DP] in v
+  int64_t row_off;  // its rows in B
+  int64_t n;
+  int64_t blk_off;  // block of row 0 (row i -> block blk_off + i)
+  int32_t d, m;
+};
+
+// padded dimension of the float32 screening rows (4, 8, 12, 16, 24, 32, 48, 64)
+int knn_pad_dim(int d);
+
+// ordered kNN of every (problem, query tile) entry of tiles (one CTA each);
+// all problems of the launch share DP; kcap >= every m
+int launch_knn_batched(int DP, const KnnBatchProb* probs, const int2* tiles, int64_t ntiles,
+                       const double* Xs, const float* v, const float* B, int32_t* nbr, int ldnbr,
+                       int kcap, cudaStream_t st);
+
+// single-problem maximin through the cluster kernel (n <= maximin_cluster_max_rows(d));
+// ws: 256 bytes of device scratch
+int maximin_cluster_single(const double* X, int64_t n, int d, int64_t first, int64_t* order,
+                           int32_t* info, char* ws, cudaStream_t st);
+int64_t maximin_cluster_max_rows(int d);
+
+}  // namespace sv

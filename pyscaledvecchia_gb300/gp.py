@@ -115,6 +115,45 @@ class ScaledVecchiaGP:
 
     # ---------------- fitting ----------------------------------------------
     def fit(self, X, y):
+        st = self._fit_prepare(X, y)
+        d, estimate_nu = st["d"], st["estimate_nu"]
+        theta = st["theta0"]
+        state = {}
+
+        def rebuild(th):
+            order, groups = self._order_and_neighbours(st["Xe"], th, d, st["m"])
+            state["order"] = order
+            state["groups"] = groups
+            state["prob"] = DeviceProblem(st["Xe"][order], st["ye"][order], st["Ze"][order], groups)
+
+        rebuild(theta)
+        last_ranges = np.exp(theta[1:1 + d]).copy()
+
+        def objective(th):
+            th = self._objective_theta(th, d, estimate_nu)
+            ll, g, M, beta = state["prob"].evaluate(
+                th, self.nu, estimate_nu=estimate_nu, need_grad=True,
+                var_penalty=self.var_penalty, log_var_target=st["log_var_target"])
+            g, M = self._freeze_nugget(g, M)
+            return ll, g, M, beta
+
+        def reorder_hook(th, k):
+            nonlocal last_ranges
+            r = self._reorder_ranges(th, d, estimate_nu, last_ranges, k)
+            if r is None:
+                return False
+            rebuild(th)
+            last_ranges = r.copy()
+            return True
+
+        theta, ll, beta = _fisher_scoring(
+            theta, objective, max_iter=self.max_iter, tol=self.tol,
+            verbose=self.verbose, reorder_hook=reorder_hook)
+        return self._fit_finish(st, theta, ll, beta)
+
+    # ---------------- pieces of fit shared with the batched fitter ----------
+    def _fit_prepare(self, X, y):
+        """Standardisation, subsample and initial theta (gp.py:139-177)."""
         X = np.ascontiguousarray(np.atleast_2d(X), dtype=float)
         y = np.asarray(y, dtype=float).ravel()
         n, d = X.shape
@@ -151,65 +190,61 @@ class ScaledVecchiaGP:
             theta[1 + d] = math.log(1.5)
         theta[-1] = math.log(self.nugget if fixed_nug else 0.1)
         theta = self._clip_theta(theta, d, estimate_nu)
+        return {"n": n, "d": d, "estimate_nu": estimate_nu, "rng": rng, "Xe": Xe, "ye": ye,
+                "Ze": Ze, "m": m, "theta0": theta,
+                "log_var_target": math.log(max(ye.var(), 1e-8))}
 
+    @staticmethod
+    def _order_and_neighbours(Xe, th, d, m):
+        """Maximin ordering and neighbours in the scaled space (gp.py:182-191);
+        the scaled inputs are formed with the reference's own expression so
+        the exact searches see the same bits."""
         lib, torch = _lib.device_ready()
-        state = {}
+        Xs = Xe / np.exp(th[1:1 + d])
+        first = int(np.argmin(((Xs - Xs.mean(0)) ** 2).sum(1)))
+        Xs_dev = _lib.to_dev(torch, Xs, np.float64)
+        order_d, info = maximin_order_device(torch, Xs_dev, first)
+        nn_d, info2 = ordered_nn_device(torch, Xs_dev[order_d].contiguous(), m)
+        order = order_d.cpu().numpy()
+        nn = nn_d.cpu().numpy()
+        _lib.check_info(lib, info.cpu().numpy(), "sv_maximin_order")
+        _lib.check_info(lib, info2.cpu().numpy(), "sv_ordered_knn")
+        return order, _nn_groups(nn, m)
 
-        def rebuild(th):
-            # ordering and neighbours in the scaled space (gp.py:182-191); the
-            # scaled inputs are formed with the reference's own expression so
-            # the exact searches see the same bits
-            Xs = Xe / np.exp(th[1:1 + d])
-            first = int(np.argmin(((Xs - Xs.mean(0)) ** 2).sum(1)))
-            Xs_dev = _lib.to_dev(torch, Xs, np.float64)
-            order_d, info = maximin_order_device(torch, Xs_dev, first)
-            nn_d, info2 = ordered_nn_device(torch, Xs_dev[order_d].contiguous(), m)
-            order = order_d.cpu().numpy()
-            nn = nn_d.cpu().numpy()
-            _lib.check_info(lib, info.cpu().numpy(), "sv_maximin_order")
-            _lib.check_info(lib, info2.cpu().numpy(), "sv_ordered_knn")
-            state["order"] = order
-            state["groups"] = _nn_groups(nn, m)
-            state["prob"] = DeviceProblem(Xe[order], ye[order], Ze[order], state["groups"])
+    def _objective_theta(self, th, d, estimate_nu):
+        """theta as the objective sees it: clipped, nugget held (gp.py:197-199)."""
+        th = self._clip_theta(np.array(th, dtype=float), d, estimate_nu)
+        if self.nugget is not None:
+            th[-1] = math.log(self.nugget)
+        return th
 
-        rebuild(theta)
-        last_ranges = np.exp(theta[1:1 + d]).copy()
-        log_var_target = math.log(max(ye.var(), 1e-8))
+    def _freeze_nugget(self, g, M):
+        """Fixed nugget: zero its score and decouple its Fisher row (gp.py:206-208)."""
+        if g is not None and self.nugget is not None:
+            g = g.copy()
+            g[-1] = 0.0
+            M = M.copy()
+            M[-1, :] = 0.0
+            M[:, -1] = 0.0
+            M[-1, -1] = 1.0
+        return g, M
 
-        def objective(th):
-            th = self._clip_theta(np.array(th, dtype=float), d, estimate_nu)
-            if fixed_nug:
-                th[-1] = math.log(self.nugget)
-            ll, g, M, beta = state["prob"].evaluate(
-                th, self.nu, estimate_nu=estimate_nu, need_grad=True,
-                var_penalty=self.var_penalty, log_var_target=log_var_target)
-            if g is not None and fixed_nug:
-                g = g.copy()
-                g[-1] = 0.0
-                M = M.copy()
-                M[-1, :] = 0.0
-                M[:, -1] = 0.0
-                M[-1, -1] = 1.0
-            return ll, g, M, beta
+    def _reorder_ranges(self, th, d, estimate_nu, last_ranges, k):
+        """Ranges to reorder with, or None when they moved less than 1e-3 in
+        log scale since the last ordering (gp.py:211-221)."""
+        r = np.exp(self._clip_theta(np.array(th), d, estimate_nu)[1:1 + d])
+        if np.max(np.abs(np.log(r / last_ranges))) < 1e-3:
+            return None
+        if self.verbose:
+            print(f"    [reorder at iter {k}] ranges = "
+                  + np.array2string(r, precision=3))
+        return r
 
-        def reorder_hook(th, k):
-            nonlocal last_ranges
-            r = np.exp(self._clip_theta(np.array(th), d, estimate_nu)[1:1 + d])
-            if np.max(np.abs(np.log(r / last_ranges))) < 1e-3:
-                return False
-            if self.verbose:
-                print(f"    [reorder at iter {k}] ranges = "
-                      + np.array2string(r, precision=3))
-            rebuild(th)
-            last_ranges = r.copy()
-            return True
-
-        theta, ll, beta = _fisher_scoring(
-            theta, objective, max_iter=self.max_iter, tol=self.tol,
-            verbose=self.verbose, reorder_hook=reorder_hook)
-
+    def _fit_finish(self, st, theta, ll, beta):
+        """Fitted attributes and the variance correction (gp.py:227-239)."""
+        d, estimate_nu = st["d"], st["estimate_nu"]
         theta = self._clip_theta(np.array(theta), d, estimate_nu)
-        if fixed_nug:
+        if self.nugget is not None:
             theta[-1] = math.log(self.nugget)
         self.theta_ = theta
         self.beta_ = beta
@@ -217,8 +252,8 @@ class ScaledVecchiaGP:
         self._nu_fit = math.exp(theta[1 + d]) if estimate_nu else self.nu
 
         self.b_ = 1.0
-        if self.var_correction and n >= 200:
-            self.b_ = self._estimate_b(rng)
+        if self.var_correction and st["n"] >= 200:
+            self.b_ = self._estimate_b(st["rng"])
         return self
 
     # ---------------- prediction -------------------------------------------

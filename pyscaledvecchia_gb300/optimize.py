@@ -6,13 +6,28 @@ agree: a Fisher direction ridged (x10 from 1e-6, up to 12 tries) until it
 ascends, else the normalised gradient; the step capped at ``max_step`` in
 norm; up to 20 halvings of alpha, a LinAlgError counting as a failed try;
 stop when no step ascends or |alpha step . g| < tol; reorder at
-k = 2, 4, 8, 16, ...  Each objective call is one GPU likelihood evaluation.
+k = 2, 4, 8, 16, ...
+
+The iteration is written once, as a generator that asks its driver for
+objective values (``("eval", theta)``) and reorders (``("reorder", theta,
+k)``).  ``_fisher_scoring`` drives it with a direct objective call (one GPU
+likelihood evaluation each); the batched driver (batched.py) advances many
+problems' generators together and answers all their evaluation requests
+with one batched launch.
 """
 from __future__ import annotations
 
 import numpy as np
 
-__all__ = ["_fisher_scoring"]
+__all__ = ["_fisher_scoring", "fisher_scoring_steps"]
+
+
+class EvalFailed:
+    """Sent to a generator in place of an objective value when the
+    evaluation raised numpy.linalg.LinAlgError."""
+
+
+EVAL_FAILED = EvalFailed()
 
 
 def _scoring_direction(M, g):
@@ -30,22 +45,30 @@ def _scoring_direction(M, g):
     return g / max(np.linalg.norm(g), 1e-12)
 
 
-def _fisher_scoring(theta0, objective, max_iter=40, tol=1e-4, verbose=False,
-                    reorder_hook=None, max_step=3.0):
-    """Maximise ``objective(theta) -> (loglik, grad, fisher, beta)``.
+def fisher_scoring_steps(theta0, max_iter=40, tol=1e-4, verbose=False, reorder=True,
+                         max_step=3.0):
+    """Generator form of the Fisher-scoring iteration.
 
-    ``reorder_hook(theta, k)`` is called at k = 2, 4, 8, ...; when it returns
-    True the objective changed and is re-evaluated at the current theta.
-    Returns (theta, loglik, beta).
+    Yields ("eval", theta) and expects (ll, grad, fisher, beta) back, or
+    EVAL_FAILED when the objective raised LinAlgError (only tolerated in the
+    line search, as in the reference); yields ("reorder", theta, k) and
+    expects a bool.  Returns (theta, ll, beta).
     """
     theta = np.array(theta0, dtype=float)
-    ll, g, M, beta = objective(theta)
+    res = yield ("eval", theta.copy())
+    if res is EVAL_FAILED:
+        raise np.linalg.LinAlgError("block Cholesky failed even with jitter")
+    ll, g, M, beta = res
     reorder_at = 2
     for k in range(1, max_iter + 1):
-        if reorder_hook is not None and k == reorder_at:
+        if reorder and k == reorder_at:
             reorder_at *= 2
-            if reorder_hook(theta, k):
-                ll, g, M, beta = objective(theta)
+            changed = yield ("reorder", theta.copy(), k)
+            if changed:
+                res = yield ("eval", theta.copy())
+                if res is EVAL_FAILED:
+                    raise np.linalg.LinAlgError("block Cholesky failed even with jitter")
+                ll, g, M, beta = res
 
         step = _scoring_direction(M, g)
         nrm = np.linalg.norm(step)
@@ -54,11 +77,11 @@ def _fisher_scoring(theta0, objective, max_iter=40, tol=1e-4, verbose=False,
 
         alpha, accepted = 1.0, False
         for _ in range(20):
-            try:
-                c_ll, c_g, c_M, c_beta = objective(theta + alpha * step)
-            except np.linalg.LinAlgError:
+            res = yield ("eval", theta + alpha * step)
+            if res is EVAL_FAILED:
                 alpha *= 0.5
                 continue
+            c_ll, c_g, c_M, c_beta = res
             if np.isfinite(c_ll) and c_ll > ll:
                 theta = theta + alpha * step
                 ll, g, M, beta = c_ll, c_g, c_M, c_beta
@@ -73,3 +96,28 @@ def _fisher_scoring(theta0, objective, max_iter=40, tol=1e-4, verbose=False,
         if abs(np.dot(alpha * step, g)) < tol:
             break
     return theta, ll, beta
+
+
+def _fisher_scoring(theta0, objective, max_iter=40, tol=1e-4, verbose=False,
+                    reorder_hook=None, max_step=3.0):
+    """Maximise ``objective(theta) -> (loglik, grad, fisher, beta)``.
+
+    ``reorder_hook(theta, k)`` is called at k = 2, 4, 8, ...; when it returns
+    True the objective changed and is re-evaluated at the current theta.
+    Returns (theta, loglik, beta).
+    """
+    gen = fisher_scoring_steps(theta0, max_iter=max_iter, tol=tol, verbose=verbose,
+                               reorder=reorder_hook is not None, max_step=max_step)
+    msg = next(gen)
+    while True:
+        if msg[0] == "eval":
+            try:
+                reply = objective(msg[1])
+            except np.linalg.LinAlgError:
+                reply = EVAL_FAILED
+        else:
+            reply = bool(reorder_hook(msg[1], msg[2]))
+        try:
+            msg = gen.send(reply)
+        except StopIteration as stop:
+            return stop.value

@@ -238,17 +238,39 @@ def gen_gp(R, out):
     np.savez_compressed(os.path.join(out, "gp.npz"), **cases)
 
 
+def gen_optimize(R, out):
+    """Traces of the reference's Fisher scoring (optimize.py:11-73) on the
+    toy objectives of toy_objectives.py: every evaluated theta, every reorder
+    call and the result."""
+    sys.path.insert(0, HERE)
+    import toy_objectives as T
+    from scaled_vecchia import optimize
+    cases = {}
+    for name in T.CASES:
+        toy, theta0, max_step = T.make(name)
+        th, ll, beta = optimize._fisher_scoring(theta0, toy.objective, max_iter=25, tol=1e-6,
+                                                reorder_hook=toy.reorder_hook, max_step=max_step)
+        cases[f"{name}_theta0"] = theta0
+        cases[f"{name}_trace"] = np.array(toy.trace)
+        cases[f"{name}_reorder_k"] = np.array([k for k, _ in toy.reorders], dtype=np.int64)
+        cases[f"{name}_reorder_th"] = np.array([t for _, t in toy.reorders]).reshape(len(toy.reorders), -1)
+        cases[f"{name}_theta"] = th
+        cases[f"{name}_ll"] = np.array(ll)
+        cases[f"{name}_beta"] = beta
+    np.savez_compressed(os.path.join(out, "optimize.npz"), **cases)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--only", default="")
     a = ap.parse_args()
     R = import_reference(a.ref)
-    which = a.only.split(",") if a.only else ["ordering", "blocks", "likelihood", "gp"]
+    which = a.only.split(",") if a.only else ["ordering", "blocks", "likelihood", "gp", "optimize"]
     for w in which:
         t0 = time.time()
         {"ordering": gen_ordering, "blocks": gen_blocks,
-         "likelihood": gen_likelihood, "gp": gen_gp}[w](R, HERE)
+         "likelihood": gen_likelihood, "gp": gen_gp, "optimize": gen_optimize}[w](R, HERE)
         print(f"{w}: {time.time() - t0:.1f}s")
 
 

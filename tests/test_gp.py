@@ -135,14 +135,20 @@ def test_fit_parity_with_reference(golden_gp, name):
     When the estimated nugget runs onto its 1e-12 clip the blocks are nearly
     singular and the reference's own fit is chaotic at the rounding level:
     perturbing y by 1e-15 relative moves its final loglik by ~6e-4 (sine)
-    and 1e-13 by ~2e-3 (sub), and theta by ~3e-5 relative.  Those cases get
-    a band of that size; the fixed-nugget case is well posed and is held to
-    1e-8."""
+    and 1e-13 by ~2e-3 (sub), and theta by ~3e-5 relative.  The Bessel case
+    (nu = 1.75) is more sensitive still: eight perturbations of y between
+    1e-15 and 1e-14 relative moved the reference's loglik by up to 9.5e-3
+    (spread 1.55e-2), theta by up to 1.2e-4 and beta by up to 2.7e-4
+    relative.  Those cases get bands of about twice that size; the
+    fixed-nugget case is well posed and is held to 1e-8."""
     g = golden_gp
     gp = GP(**GP_CASES[name]).fit(g[name + "_X"], g[name + "_y"])
     ll_ref = float(g[name + "_loglik"])
     clipped = g[name + "_theta"][-1] < np.log(1e-11)
-    ll_tol, th_tol = (5e-3, 3e-4) if clipped else (1e-8 * abs(ll_ref), 1e-6)
+    if clipped:
+        ll_tol, th_tol = (2e-2, 5e-4) if name == "nu175" else (5e-3, 3e-4)
+    else:
+        ll_tol, th_tol = 1e-8 * abs(ll_ref), 1e-6
     assert abs(gp.loglik_ - ll_ref) <= ll_tol, (gp.loglik_, ll_ref)
     np.testing.assert_allclose(gp.theta_, g[name + "_theta"], rtol=th_tol, atol=th_tol)
     np.testing.assert_allclose(gp.beta_, g[name + "_beta"], rtol=th_tol, atol=th_tol)
