@@ -58,6 +58,7 @@ def parse():
                     help="problems of the batched-fits workload (0 = skip it)")
     ap.add_argument("--fits-dump", default="",
                     help="write per-problem results of the batched-fits workload to this .npz")
+    ap.add_argument("--no-predict", action="store_true", help="skip the prediction workload")
     return ap.parse_args()
 
 
@@ -246,13 +247,34 @@ def draw_fit_responses(torch, lib, probs):
     return ys
 
 
+def _form_stats(ref, models, t, nprob):
+    ll_r = np.array([g.loglik_ for g in ref])
+    ll_m = np.array([g.loglik_ for g in models])
+    dll = ll_m - ll_r
+    rel = np.abs(dll) / np.maximum(np.abs(ll_r), 1.0)
+    same = sum(bool(np.array_equal(a.theta_, b.theta_) and a.loglik_ == b.loglik_)
+               for a, b in zip(ref, models))
+    ev = np.array([g.fit_stats_["split"] + g.fit_stats_["float64"] for g in models])
+    return {"fits_per_s": nprob / t, "s": t, "objective_evals_mean": float(ev.mean()),
+            "dll_abs_max": float(np.abs(dll).max()), "dll_abs_median": float(np.median(np.abs(dll))),
+            "dll_rel_max": float(rel.max()),
+            "frac_abs_dll_below_1e-6": float(np.mean(np.abs(dll) < 1e-6)),
+            "frac_not_worse_than_plain": float(np.mean(dll >= -1e-6 * np.maximum(np.abs(ll_r), 1.0))),
+            "bitwise_equal_to_plain": int(same)}
+
+
 def run_fits(torch, lib, nprob, dump=""):
-    """Batched-fits workload: plain form (ScaledVecchiaGP.fit one problem at
-    a time, float64, default start, no graphs) against the chosen form
-    (fit_batched: all problems together, split-precision iterations with a
-    float64 polish, batched device reorders, CUDA-graph replay)."""
+    """Batched-fits workload.  Forms: plain (ScaledVecchiaGP.fit one problem
+    at a time, float64, default start, no graphs); batched_float64
+    (fit_batched: all problems per launch, CUDA-graph replay, batched device
+    reorders, float64 evaluations: the plain form's iterates bit for bit);
+    batched_split (split-precision iterations + float64 polish); and, when
+    trained weights ship, batched_split_warm (the same from the encoder's
+    starting point).  "chosen" is the fastest form whose loglik agrees with
+    the plain form's within 1e-6 on every problem."""
     from pyscaledvecchia_gb300 import ScaledVecchiaGP
     from pyscaledvecchia_gb300.fit_batched import fit_batched
+    from pyscaledvecchia_gb300 import warmstart
     probs = make_fit_problems(nprob)
     t0 = time.perf_counter()
     ys = draw_fit_responses(torch, lib, probs)
@@ -262,33 +284,44 @@ def run_fits(torch, lib, nprob, dump=""):
         return ScaledVecchiaGP(m_est=pr["m"], n_est=None, nu=2.5,
                                nugget=1e-8 if pr["fixed"] else None, var_correction=False)
 
+    enc = warmstart.SetEncoder.load() if os.path.exists(warmstart.DEFAULT_WEIGHTS) else None
     Xs = [pr["X"] for pr in probs]
-    # warm-up of both paths on two small problems (library load, graphs)
+    # warm-up of every path on two small problems (library load, graphs)
     small = sorted(range(nprob), key=lambda i: probs[i]["n"])[:2]
     for i in small:
         model(probs[i]).fit(Xs[i], ys[i])
-    fit_batched([model(probs[i]) for i in small], [Xs[i] for i in small], [ys[i] for i in small])
+    for prec in ("float64", "split"):
+        fit_batched([model(probs[i]) for i in small], [Xs[i] for i in small], [ys[i] for i in small],
+                    precision=prec, warm_start=enc)
     torch.cuda.synchronize()
 
-    t0 = time.perf_counter()
-    plain = [model(pr).fit(X, y) for pr, X, y in zip(probs, Xs, ys)]
-    torch.cuda.synchronize()
-    t_plain = time.perf_counter() - t0
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
 
+    plain, t_plain = timed(lambda: [model(pr).fit(X, y) for pr, X, y in zip(probs, Xs, ys)])
+    forms = {}
+    b64, t = timed(lambda: fit_batched([model(pr) for pr in probs], Xs, ys, precision="float64"))
+    forms["batched_float64"] = _form_stats(plain, b64, t, nprob)
     st = {}
-    t0 = time.perf_counter()
-    chosen = fit_batched([model(pr) for pr in probs], Xs, ys, precision="split", graphs=True, stats=st)
-    torch.cuda.synchronize()
-    t_chosen = time.perf_counter() - t0
+    spl, t = timed(lambda: fit_batched([model(pr) for pr in probs], Xs, ys, precision="split", stats=st))
+    forms["batched_split"] = _form_stats(plain, spl, t, nprob)
+    forms["batched_split"]["schedule"] = {k: (float(v) if isinstance(v, float) else v)
+                                          for k, v in st.items() if k not in ("batch", "thetas")}
+    if enc is not None:
+        stw = {}
+        warm, t = timed(lambda: fit_batched([model(pr) for pr in probs], Xs, ys, precision="split",
+                                            warm_start=enc, stats=stw))
+        forms["batched_split_warm"] = _form_stats(plain, warm, t, nprob)
+        forms["batched_split_warm"]["schedule"] = {k: (float(v) if isinstance(v, float) else v)
+                                                   for k, v in stw.items() if k not in ("batch", "thetas")}
 
-    ll_p = np.array([g.loglik_ for g in plain])
-    ll_c = np.array([g.loglik_ for g in chosen])
-    dll = ll_c - ll_p
-    rel = np.abs(dll) / np.maximum(np.abs(ll_p), 1.0)
-    # split form vs float64 at every chosen final state (same ordering)
-    BL = st.pop("batch")
-    th = st.pop("thetas")
-    th_obj = [g._objective_theta(t, g.d_, False) for g, t in zip(chosen, th)]
+    # split form vs float64 at every final state of the split fits (same ordering)
+    BL = st["batch"]
+    th_obj = [g._objective_theta(t_, g.d_, False) for g, t_ in zip(spl, st["thetas"])]
     r64 = BL.evaluate(th_obj, active=np.ones(nprob, bool), precision="float64")
     r32 = BL.evaluate(th_obj, active=np.ones(nprob, bool), precision="split")
     e_ll = max(abs(a[1] - b[1]) / abs(b[1]) for a, b in zip(r32, r64))
@@ -298,34 +331,86 @@ def run_fits(torch, lib, nprob, dump=""):
               for a, b in zip(r32, r64))
     e_f = max(float(np.abs(a[3] - b[3]).max() / max(np.abs(b[3]).max(), 1e-300)) for a, b in zip(r32, r64))
     e_b = max(float(np.abs(a[4] - b[4]).max() / max(np.abs(b[4]).max(), 1e-300)) for a, b in zip(r32, r64))
-    evals_c = sum(g.fit_stats_["split"] + g.fit_stats_["float64"] for g in chosen)
     if dump:
         np.savez_compressed(
             dump, n=np.array([p["n"] for p in probs]), d=np.array([p["d"] for p in probs]),
             m=np.array([p["m"] for p in probs]), fixed=np.array([p["fixed"] for p in probs]),
-            tau=np.array([p["tau"] for p in probs]), ll_plain=ll_p, ll_chosen=ll_c,
-            theta_plain=np.array([np.pad(g.theta_, (0, 14 - g.theta_.size)) for g in plain]),
-            theta_chosen=np.array([np.pad(g.theta_, (0, 14 - g.theta_.size)) for g in chosen]),
-            evals_split=np.array([g.fit_stats_["split"] for g in chosen]),
-            evals_f64=np.array([g.fit_stats_["float64"] for g in chosen]),
-            ll_final_split=np.array([a[1] for a in r32]), ll_final_f64=np.array([b[1] for b in r64]))
+            ll_plain=np.array([g.loglik_ for g in plain]), ll_b64=np.array([g.loglik_ for g in b64]),
+            ll_split=np.array([g.loglik_ for g in spl]),
+            evals_plain=np.array([g.fit_stats_["float64"] for g in plain]),
+            evals_split=np.array([g.fit_stats_["split"] for g in spl]),
+            evals_polish=np.array([g.fit_stats_["float64"] for g in spl]),
+            **({"ll_warm": np.array([g.loglik_ for g in warm]),
+                "evals_warm": np.array([g.fit_stats_["split"] + g.fit_stats_["float64"] for g in warm])}
+               if enc is not None else {}))
+    ok = [k for k, v in forms.items() if v["frac_abs_dll_below_1e-6"] == 1.0 or
+          v["dll_rel_max"] < 1e-6]
+    chosen = max(ok, key=lambda k: forms[k]["fits_per_s"]) if ok else None
+    fastest = max(forms, key=lambda k: forms[k]["fits_per_s"])
     return {
         "workload": f"{nprob} independent fits, n log-U[500,20000] (total "
                     f"{sum(p['n'] for p in probs)} points), d U{{3..12}}, m in {{10,20,30}}, "
                     "nu = 2.5, half fixed nugget 1e-8, n_est = None, var_correction off",
-        "plain_fits_per_s": nprob / t_plain, "chosen_fits_per_s": nprob / t_chosen,
-        "speedup": t_plain / t_chosen, "plain_s": t_plain, "chosen_s": t_chosen,
-        "dll_abs_max": float(np.abs(dll).max()), "dll_abs_median": float(np.median(np.abs(dll))),
-        "dll_rel_max": float(rel.max()),
-        "frac_abs_dll_below_1e-6": float(np.mean(np.abs(dll) < 1e-6)),
-        "frac_rel_dll_below_1e-6": float(np.mean(rel < 1e-6)),
-        "frac_chosen_not_worse": float(np.mean(dll >= -1e-6)),
+        "plain_fits_per_s": nprob / t_plain, "plain_s": t_plain,
+        "plain_objective_evals_mean": float(np.mean([g.fit_stats_["float64"] for g in plain])),
+        "forms": forms,
+        "chosen_form": chosen, "chosen_fits_per_s": forms[chosen]["fits_per_s"] if chosen else None,
+        "chosen_speedup": (forms[chosen]["fits_per_s"] * t_plain / nprob) if chosen else None,
+        "fastest_form": fastest, "fastest_speedup": forms[fastest]["fits_per_s"] * t_plain / nprob,
         "split_vs_float64_at_final_state": {"ll_rel_max": e_ll, "score_err_max_in_sd": e_g,
                                             "fisher_rel_max": e_f, "beta_rel_max": e_b},
-        "chosen_objective_evals": int(evals_c),
-        "schedule": {k: (float(v) if isinstance(v, float) else v) for k, v in st.items()},
         "draw_s": t_draw,
     }
+
+
+def run_predict(torch, lib):
+    """Prediction and joint sampling: n_train = 100,000 points in [0,1]^6,
+    y a Matern-2.5 Vecchia draw with lambda = (0.1, 0.2, 0.4, 0.8, 5, 100),
+    sigma^2 = 1, tau = 1e-6 (seed 3); the default fit (m_est 30, n_est 5000,
+    variance correction b on the reference's inner split); then 50,000 test
+    points in [-0.1, 1.1]^6: marginal mean/sd with m_pred = 140 (141-point
+    blocks) and 100 joint sample paths."""
+    from pyscaledvecchia_gb300 import ScaledVecchiaGP, _lib as L
+    from pyscaledvecchia_gb300.ordering import maximin_order_device, ordered_nn_device
+    from pyscaledvecchia_gb300.sampling import vecchia_prior_sample_device
+    rng = np.random.default_rng(3)
+    ntr, nte, d = 100_000, 50_000, 6
+    X = rng.random((ntr, d))
+    Xte = rng.uniform(-0.1, 1.1, (nte, d))
+    lam = np.array([0.1, 0.2, 0.4, 0.8, 5.0, 100.0])
+    eps = rng.standard_normal(ntr)
+    Xs = X / lam
+    first = int(np.argmin(((Xs - Xs.mean(0)) ** 2).sum(1)))
+    Xs_d = L.to_dev(torch, Xs, np.float64)
+    od, _ = maximin_order_device(torch, Xs_d, first)
+    nd, _ = ordered_nn_device(torch, Xs_d[od].contiguous(), 30)
+    o = od.cpu().numpy()
+    th = np.concatenate([[0.0], np.log(lam), [math.log(1e-6)]])
+    yo = vecchia_prior_sample_device(torch, L.to_dev(torch, X[o], np.float64), nd, th, 2.5,
+                                     L.to_dev(torch, eps.reshape(ntr, 1), np.float64))
+    y = np.empty(ntr)
+    y[o] = yo.reshape(-1).cpu().numpy()
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    gp = ScaledVecchiaGP(m_est=30, m_pred=140, nu=2.5)
+    _, t_fit = timed(lambda: gp.fit(X, y))
+    gp.predict(Xte[:2000], return_std=True)  # warm-up
+    (mu, sd), t_pred = timed(lambda: gp.predict(Xte, return_std=True))
+    samples, t_joint = timed(lambda: gp.sample_joint(Xte, n_sim=100, random_state=0))
+    K = 141
+    flops = nte * (K ** 3 / 3 + K ** 2)
+    return {"workload": "n_train 100000 x 6, n_test 50000, m_pred 140, 100 joint paths, nu 2.5",
+            "fit_s": t_fit, "predict_s": t_pred, "predict_points_per_s": nte / t_pred,
+            "predict_fp64_tflops": flops / t_pred / 1e12,
+            "sample_joint_s": t_joint, "b": float(gp.b_),
+            "fitted_ranges": [float(v) for v in gp.ranges_], "nugget": float(gp.nugget_),
+            "sd_finite": bool(np.all(np.isfinite(sd))), "samples_shape": list(samples.shape)}
 
 
 def main():
@@ -490,6 +575,8 @@ def main():
         line["extra"]["ll_cpu"] = out[0]
     if args.fits_problems > 0:
         line["fits"] = run_fits(torch, lib, args.fits_problems, args.fits_dump)
+    if not args.no_predict:
+        line["predict"] = run_predict(torch, lib)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -237,9 +237,13 @@ int64_t sv_encoder_param_count(void);
 size_t sv_encoder_workspace_bytes(int64_t nset, int32_t S, int32_t train);
 int sv_encoder_pack(const double* features, int64_t n, uint16_t* x_bf16, sv_stream_t stream);
 int sv_encoder_to_bf16(const float* params, uint16_t* params_bf16, int64_t n, sv_stream_t stream);
+/* variant 0: per-point layers on tcgen05 (tensor memory accumulators);
+ * variant 1: on mma.sync (the training path's forward).  A tcgen05 wait that
+ * runs out leaves NaN outputs. */
 int sv_encoder_forward(int64_t nset, int32_t S, const uint16_t* x, const int32_t* cnt,
                        const float* params, const uint16_t* params_bf16, float* out,
-                       void* workspace, size_t workspace_bytes, sv_stream_t stream);
+                       int32_t variant, void* workspace, size_t workspace_bytes,
+                       sv_stream_t stream);
 int sv_encoder_backward(int64_t nset, int32_t S, const uint16_t* x, const int32_t* cnt,
                         const float* params, const uint16_t* params_bf16, const float* target,
                         const float* weights, float* out, float* loss, float* grad,

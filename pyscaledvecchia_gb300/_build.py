@@ -46,7 +46,9 @@ def _digest() -> str:
         h.update(os.path.basename(f).encode())
         with open(f, "rb") as fh:
             h.update(fh.read())
-    h.update(" ".join(ARCH + NVCC_FLAGS).encode())
+    # flags without the include path: the same tree reached through another
+    # path (a symlink) is the same build
+    h.update(" ".join(ARCH + [f for f in NVCC_FLAGS if not f.startswith("-I")]).encode())
     return h.hexdigest()
 
 

@@ -94,7 +94,7 @@ SIGNATURES = {
     "sv_encoder_workspace_bytes": (c_sz, [c_i64, c_i32, c_i32]),
     "sv_encoder_pack": (c_i32, [c_vp, c_i64, c_vp, c_vp]),
     "sv_encoder_to_bf16": (c_i32, [c_vp, c_vp, c_i64, c_vp]),
-    "sv_encoder_forward": (c_i32, [c_i64, c_i32] + [c_vp] * 6 + [c_sz, c_vp]),
+    "sv_encoder_forward": (c_i32, [c_i64, c_i32] + [c_vp] * 5 + [c_i32, c_vp, c_sz, c_vp]),
     "sv_encoder_backward": (c_i32, [c_i64, c_i32] + [c_vp] * 10 + [c_sz, c_vp]),
     "sv_encoder_adam": (c_i32, [c_vp] * 5 + [c_i64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                              ctypes.c_float, c_i32, ctypes.c_float, c_vp]),

@@ -10,9 +10,11 @@
 //   head  g = GELU(W3 pool + b3)  128,   out = W4 g + b4   16 (14 used)
 //
 // Weights are bfloat16 copies of float32 master weights; every product
-// accumulates in float32.  The per-point layers run on the tensor cores
-// (mma.sync m16n8k16 bf16 -> f32), one CTA per 128-point tile, 8 warps of
-// 16 points; the backward recomputes the tile's forward and produces
+// accumulates in float32.  The per-point layers run on the tensor cores, one
+// CTA per 128-point tile: the inference forward on tcgen05 (operands in
+// shared memory, accumulators in tensor memory), the training forward and
+// backward on mma.sync m16n8k16 (8 warps of 16 points, float32 fragments in
+// registers, which the fused backward needs); the backward recomputes the tile's forward and produces
 // per-tile weight-gradient partials that a separate kernel sums in a fixed
 // order (no float atomics: results are bitwise reproducible).  The head is
 // float32 SIMT, one CTA per set.
@@ -379,9 +381,199 @@ __global__ void __launch_bounds__(kEThreads, 1) k_enc_points_bwd(EncArgs A) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Forward per-point layers on the 5th-generation tensor cores (tcgen05):
+// one CTA of 4 warps per 128-point tile; operands in shared memory in the
+// canonical no-swizzle K-major layout (8-row x 16-byte core matrices, core
+// matrices along K 128 bytes apart, 8-row groups KG * 128 bytes apart),
+// accumulators in tensor memory (128 lanes = points, 256 columns = two
+// 128-wide float32 results), one thread issuing the MMAs, completion
+// signalled through an mbarrier, epilogues read back with tcgen05.ld.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t umma_off(int r, int k, int KG) {
+  return (uint32_t)((r >> 3) * (KG * 128) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
+// offsets in 16-byte units, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// instruction descriptor of kind::f16: D float32, A and B bfloat16, both
+// K-major, M x N
+__host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+      :: "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+               :: "r"(mbar) : "memory");
+}
+
+// bounded wait for the mbarrier phase; false when the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+  for (uint32_t it = 0; it < (1u << 22); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.b32 %0, 1, 0, p;\n}\n"
+        : "=r"(done) : "r"(mbar), "r"(phase) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+#define SV_TC_LD32(taddr, v)                                                                      \
+  asm volatile(                                                                                    \
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14," \
+      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"              \
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),      \
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),  \
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),            \
+        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),            \
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])             \
+      : "r"(taddr))
+
+struct EncTcSmem {
+  alignas(128) unsigned char x[kET * kEF * 2];   // canonical, KG = 2
+  alignas(128) unsigned char w1[kEH * kEF * 2];  // canonical, KG = 2
+  alignas(128) unsigned char w2[kEH * kEH * 2];  // canonical, KG = 16
+  alignas(128) unsigned char h1[kET * kEH * 2];  // canonical, KG = 16
+  float colsum[4][kEH];
+  uint64_t mbar;
+  uint32_t tmem_base;
+};
+
+// 16-byte chunk c of a row-major [rows][K] bfloat16 matrix into the canonical layout
+__device__ __forceinline__ void umma_stage(unsigned char* dst, const bf16* src, int rows, int K) {
+  const int KG = K / 8;
+  for (int c = threadIdx.x; c < rows * KG; c += blockDim.x) {
+    const int r = c / KG, kg = c - (c / KG) * KG;
+    *reinterpret_cast<uint4*>(dst + umma_off(r, kg * 8, KG)) =
+        *reinterpret_cast<const uint4*>(src + (int64_t)r * K + kg * 8);
+  }
+}
+
+__global__ void __launch_bounds__(128, 1) k_enc_points_fwd_tc(EncArgs A, int32_t* err) {
+  extern __shared__ __align__(16) unsigned char tc_smraw[];
+  // 128-byte aligned base inside the launch's slack
+  const uint32_t pad = (128u - (smem_u32(tc_smraw) & 127u)) & 127u;
+  EncTcSmem& s = *reinterpret_cast<EncTcSmem*>(tc_smraw + pad);
+  const int tile = blockIdx.x, set = blockIdx.y;
+  const int ntile = A.S / kET;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cnt = A.cnt[set];
+  const uint32_t mbar = smem_u32(&s.mbar);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(smem_u32(&s.tmem_base)), "r"(256));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(mbar), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  umma_stage(s.w1, A.pb + kOffW1, kEH, kEF);
+  umma_stage(s.w2, A.pb + kOffW2, kEH, kEH);
+  umma_stage(s.x, A.x + ((int64_t)set * A.S + (int64_t)tile * kET) * kEF, kET, kEF);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tbase = s.tmem_base;
+  const uint32_t idesc = umma_idesc_bf16(kET, kEH);
+  bool ok = true;
+
+  // layer 1: D1 = X W1^T (K = 16, one instruction)
+  if (threadIdx.x == 0) {
+    umma_bf16(tbase, umma_desc(smem_u32(s.x), 128, 256), umma_desc(smem_u32(s.w1), 128, 256), idesc, 0);
+    umma_commit(mbar);
+  }
+  ok = __all_sync(0xffffffffu, mbar_wait(mbar, 0));  // warp-uniform before tcgen05.ld
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const int row = warp * 32 + lane;  // this thread's point in the tile
+  const uint32_t tlane = tbase + ((uint32_t)(warp * 32) << 16);
+  if (ok) {
+    // epilogue 1: h1 = bf16(GELU(z1 + b1)) into the canonical A operand of layer 2
+    for (int c0 = 0; c0 < kEH; c0 += 32) {
+      uint32_t v[32];
+      SV_TC_LD32(tlane + c0, v);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int c = 0; c < 32; c += 8) {
+        uint32_t w[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          w[e] = pack2(gelu_f(__uint_as_float(v[c + 2 * e]) + A.pf[kOffB1 + c0 + c + 2 * e]),
+                       gelu_f(__uint_as_float(v[c + 2 * e + 1]) + A.pf[kOffB1 + c0 + c + 2 * e + 1]));
+        *reinterpret_cast<uint4*>(s.h1 + umma_off(row, c0 + c, kEH / 8)) = make_uint4(w[0], w[1], w[2], w[3]);
+      }
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  ok = __syncthreads_and(ok);
+
+  // layer 2: D2 = H1 W2^T (K = 128, eight instructions of K = 16)
+  if (ok && threadIdx.x == 0) {
+    for (int kk = 0; kk < kEH / 16; ++kk)
+      umma_bf16(tbase + kEH, umma_desc(smem_u32(s.h1) + kk * 256, 128, 2048),
+                umma_desc(smem_u32(s.w2) + kk * 256, 128, 2048), idesc, kk > 0 ? 1u : 0u);
+    umma_commit(mbar);
+  }
+  if (ok) ok = __all_sync(0xffffffffu, mbar_wait(mbar, 1));
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const bool valid = tile * kET + row < cnt;
+  for (int c0 = 0; c0 < kEH; c0 += 32) {
+    uint32_t v[32];
+    if (ok) {
+      SV_TC_LD32(tlane + kEH + c0, v);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    }
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+      float h = (ok && valid) ? gelu_f(__uint_as_float(v[c]) + A.pf[kOffB2 + c0 + c]) : 0.0f;
+      for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+      if (lane == 0) s.colsum[warp][c0 + c] = h;
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (threadIdx.x < kEH) {
+    const float v = ((s.colsum[0][threadIdx.x] + s.colsum[1][threadIdx.x]) + s.colsum[2][threadIdx.x]) +
+                    s.colsum[3][threadIdx.x];
+    A.part[((int64_t)set * ntile + tile) * kEH + threadIdx.x] = v;
+  }
+  if (!ok && threadIdx.x == 0) atomicExch(err, SV_ETIMEOUT);
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tbase), "r"(256));
+  }
+}
+
 // head, one CTA (128 threads) per set: pool, g, out; with targets also the
 // loss terms and the vectors the weight gradients need
 struct HeadArgs {
+  const int32_t* err;  // nonzero: the per-point forward failed (outputs NaN)
   const float* part;
   const int32_t* cnt;
   int ntile, nset;
@@ -415,7 +607,7 @@ __global__ void __launch_bounds__(kEH) k_enc_head(HeadArgs H) {
   if (j < kEO) {
     float o = H.pf[kOffB4 + j];
     for (int i = 0; i < kEH; ++i) o += __bfloat162float(H.pb[kOffW4 + j * kEH + i]) * gs[i];
-    H.out[(int64_t)b * kEO + j] = o;
+    H.out[(int64_t)b * kEO + j] = (H.err && *H.err) ? __int_as_float(0x7fc00000) : o;
     if (H.target) {
       const float w = H.wts[(int64_t)b * kEO + j];
       const float r = o - H.target[(int64_t)b * kEO + j];
@@ -524,13 +716,15 @@ __global__ void k_enc_pack(const double* f, bf16* x, int64_t n) {
 static size_t enc_align(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct EncWs {
-  size_t part, pool, gv, dzg, dout, dpool, loss_set, gpart, total;
+  size_t err, part, pool, gv, dzg, dout, dpool, loss_set, gpart, total;
 };
 
 static EncWs enc_ws(int64_t nset, int S, int train) {
   EncWs W;
   const int64_t ntile = S / kET;
   size_t off = 0;
+  W.err = off;
+  off = enc_align(off + sizeof(int32_t));
   W.part = off;
   off = enc_align(off + sizeof(float) * nset * ntile * kEH);
   W.pool = off;
@@ -590,6 +784,7 @@ static int enc_common(int64_t nset, int32_t S, const uint16_t* x, const int32_t*
   A.part = (float*)(w + W.part);
   A.dpool = (const float*)(w + W.dpool);
   A.gpart = (float*)(w + W.gpart);
+  H.err = (const int32_t*)(w + W.err);
   H.part = A.part;
   H.cnt = cnt;
   H.ntile = S / kET;
@@ -610,17 +805,28 @@ static int enc_common(int64_t nset, int32_t S, const uint16_t* x, const int32_t*
 
 extern "C" int sv_encoder_forward(int64_t nset, int32_t S, const uint16_t* x, const int32_t* cnt,
                                   const float* params, const uint16_t* params_bf16, float* out,
-                                  void* workspace, size_t workspace_bytes, sv_stream_t stream) {
+                                  int32_t variant, void* workspace, size_t workspace_bytes,
+                                  sv_stream_t stream) {
   EncArgs A;
   HeadArgs H;
   EncWs W;
+  if (variant != 0 && variant != 1) return SV_EINVAL;
   int rc = enc_common(nset, S, x, cnt, params, params_bf16, out, workspace, workspace_bytes, 0, A,
                       H, W);
   if (rc != SV_OK) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  const size_t smem = sizeof(EncSmem);
-  SV_CUDA_TRY(cudaFuncSetAttribute(k_enc_points_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_enc_points_fwd<<<dim3((unsigned)(S / kET), (unsigned)nset), kEThreads, smem, st>>>(A);
+  const dim3 grid((unsigned)(S / kET), (unsigned)nset);
+  int32_t* err = (int32_t*)((char*)workspace + W.err);
+  SV_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int32_t), st));
+  if (variant == 0) {
+    const size_t smem = sizeof(EncTcSmem) + 128;  // + alignment slack of the dynamic base
+    SV_CUDA_TRY(cudaFuncSetAttribute(k_enc_points_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_enc_points_fwd_tc<<<grid, 128, smem, st>>>(A, err);
+  } else {
+    const size_t smem = sizeof(EncSmem);
+    SV_CUDA_TRY(cudaFuncSetAttribute(k_enc_points_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_enc_points_fwd<<<grid, kEThreads, smem, st>>>(A);
+  }
   SV_CUDA_TRY(cudaGetLastError());
   k_enc_head<<<(unsigned)nset, kEH, 0, st>>>(H);
   SV_CUDA_TRY(cudaGetLastError());
@@ -646,6 +852,7 @@ extern "C" int sv_encoder_backward(int64_t nset, int32_t S, const uint16_t* x, c
   SV_CUDA_TRY(cudaFuncSetAttribute(k_enc_points_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   SV_CUDA_TRY(cudaFuncSetAttribute(k_enc_points_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const dim3 grid((unsigned)(S / kET), (unsigned)nset);
+  SV_CUDA_TRY(cudaMemsetAsync((char*)workspace + W.err, 0, sizeof(int32_t), st));
   k_enc_points_fwd<<<grid, kEThreads, smem, st>>>(A);
   SV_CUDA_TRY(cudaGetLastError());
   k_enc_head<<<(unsigned)nset, kEH, 0, st>>>(H);

@@ -35,7 +35,9 @@ namespace cg = cooperative_groups;
 namespace sv {
 
 constexpr int kMcThreads = 512;
-constexpr int kMcStaticSmem = 64 * 8 * 2 + 64 * 4 + 4 + 2 * 8 * (kMcThreads / 32) + 4 * 8 + 8 + 64;
+constexpr int kMcStaticSmem =
+    64 * 8 * 2 + 64 * 4 + 4 + 2 * 8 * (kMcThreads / 32) + 4 * 8 + 2 * 64 * 8 + 8 + 64;
+constexpr int kMcMaxCluster = 16;
 
 struct RoProb {
   int64_t n, xe_off, ye_off, ze_off, x_off, y_off, z_off, blk_off, first;
@@ -45,8 +47,9 @@ struct RoProb {
   int32_t d, q, m, DP, C, pad;
 };
 
-// per-point shared memory of the cluster maximin: dist f64, thr f32, B f32, v f32[d]
-__host__ __device__ inline int64_t mc_point_bytes(int d) { return 16 + 4 * (int64_t)d; }
+// per-point shared memory of the cluster maximin: dist f64, exact coordinates
+// f64[d], thr f32, B f32, float32 centred coordinates f32[d]
+__host__ __device__ inline int64_t mc_point_bytes(int d) { return 16 + 12 * (int64_t)d; }
 
 __device__ __forceinline__ void cand_better(long long ob, long long oi, long long& bb, long long& bi) {
   if (ob > bb || (ob == bb && oi < bi)) {
@@ -99,6 +102,22 @@ __device__ __forceinline__ void mc_load_pivot(const double* X, long long j, int 
   if (lane == 0) *Bj = __double2float_ru(1.01 * 0x1p-24 * sqrt(e2));
 }
 
+// warp 0: pivot row from a row of d doubles (shared or distributed shared memory)
+__device__ __forceinline__ void mc_pivot_from(const double* src, int d, const double* cen, double* xj,
+                                              float* vj, float* Bj) {
+  const int lane = threadIdx.x & 31;
+  double e2 = 0.0;
+  for (int l = lane; l < d; l += 32) {
+    const double x = src[l];
+    const double c = x - cen[l];
+    xj[l] = x;
+    vj[l] = __double2float_rn(c);
+    e2 += c * c;
+  }
+  for (int o = 16; o > 0; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+  if (lane == 0) *Bj = __double2float_ru(1.01 * 0x1p-24 * sqrt(e2));
+}
+
 __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* probs,
                                                                 const int32_t* plist,
                                                                 const double* Xs, int64_t* ord,
@@ -119,7 +138,8 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
   const int S = (int)max((int64_t)0, p1 - p0);
   const int Sc = (int)per;
   double* dist = (double*)smraw;
-  float* thr = (float*)(dist + Sc);
+  double* xs = dist + Sc;  // exact coordinates of the CTA's points, row-major
+  float* thr = (float*)(xs + (int64_t)Sc * d);
   float* Bp = thr + Sc;
   float* v = Bp + Sc;
   __shared__ double xj[64], cen[64];
@@ -127,6 +147,7 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
   __shared__ float Bj_f;
   __shared__ long long red_bits[kMcThreads / 32], red_idx[kMcThreads / 32];
   __shared__ long long cand_bits[2], cand_idx[2];
+  __shared__ double cand_x[2][64];  // the CTA candidate's exact coordinates
   __shared__ long long s_pivot;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarp = blockDim.x >> 5;
@@ -135,6 +156,7 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
   // centre: the first row (any shift serves the float32 screen)
   for (int l = threadIdx.x; l < d; l += blockDim.x) cen[l] = X[P.first * d + l];
   __syncthreads();
+  for (int e = threadIdx.x; e < S * d; e += blockDim.x) xs[e] = X[p0 * d + e];
   for (int p = threadIdx.x; p < S; p += blockDim.x) {
     const double* xp = X + (p0 + p) * d;
     double e2 = 0.0;
@@ -176,7 +198,7 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
       const float bound = __fmul_ru(__fmul_ru(tb, tb), growth);
       if (!(s32 >= bound)) {
         // possible update: decide exactly (ordering.py:52-57)
-        const double dj = __dsqrt_rn(sqdist_exact(X + gp * d, xj, d));
+        const double dj = __dsqrt_rn(sqdist_exact(xs + (int64_t)p * d, xj, d));
         if (dj < dp) {
           dp = dj;
           dist[p] = dj;
@@ -207,9 +229,13 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
       }
       for (int o = 16; o > 0; o >>= 1)
         cand_better(__shfl_xor_sync(0xffffffffu, bb, o), __shfl_xor_sync(0xffffffffu, bi, o), bb, bi);
-      if (C > 1 && lane == 0) {
-        cand_bits[par] = bb;
-        cand_idx[par] = bi;
+      if (C > 1) {
+        if (lane == 0) {
+          cand_bits[par] = bb;
+          cand_idx[par] = bi;
+        }
+        if (bi != 0x7fffffffffffffffLL)
+          for (int l = lane; l < d; l += 32) cand_x[par][l] = xs[(bi - p0) * d + l];
       }
     }
     if (C > 1) {
@@ -232,7 +258,11 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
       if (lane == 0) s_pivot = bi;
       if (bi != 0x7fffffffffffffffLL) {
         if (r == 0 && lane == 0) order[t + 1] = bi;
-        mc_load_pivot(X, bi, d, cen, xj, vj, &Bj_f);
+        // the winner's exact row: from this CTA's points, or published by its owner
+        const int owner = (int)(bi / per);
+        const double* src = (C == 1 || owner == r) ? xs + (bi - p0) * d
+                                                   : cluster.map_shared_rank(&cand_x[par][0], owner);
+        mc_pivot_from(src, d, cen, xj, vj, &Bj_f);
       } else if (r == 0 && lane == 0) {
         // no finite candidate left (NaN inputs): report and stop
         set_error(info + 4 * pid + SV_INFO_STATUS, SV_EINVAL);
@@ -298,10 +328,45 @@ static int ro_max_smem() {
   return v;
 }
 
-// cluster size for n rows of dimension d: 1, 2, 4 or 8, or 0 when none fits
+static int launch_maximin_cluster(int C, size_t smem, unsigned nclusters, const RoProb* probs,
+                                  const int32_t* plist, const double* Xs, int64_t* ord,
+                                  int32_t* info, cudaStream_t st);
+
+// largest cluster the device can schedule with a full shared-memory budget
+// per CTA (16 needs the non-portable cluster size; else 8)
+static int g_mc_max_cluster = 0;
+static int mc_max_cluster() {
+  if (g_mc_max_cluster) return g_mc_max_cluster;
+  int C = 8;
+  if (cudaFuncSetAttribute(k_maximin_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+      cudaSuccess) {
+    const int smem = ro_max_smem() - kMcStaticSmem;
+    cudaFuncSetAttribute(k_maximin_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kMcMaxCluster);
+    cfg.blockDim = dim3(kMcThreads);
+    cfg.dynamicSmemBytes = (size_t)smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kMcMaxCluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclus = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclus, (void*)k_maximin_cluster, &cfg) == cudaSuccess && nclus > 0)
+      C = kMcMaxCluster;
+  }
+  cudaGetLastError();  // a refused query leaves no error behind
+  g_mc_max_cluster = C;
+  return C;
+}
+
+// cluster size for n rows of dimension d: 1, 2, 4, 8 (or 16), or 0 when none fits
 static int mc_cluster_size(int64_t n, int d, int maxsm) {
   const int64_t budget = (int64_t)maxsm - kMcStaticSmem;
-  for (int C = 1; C <= 8; C *= 2) {
+  const int cmax = mc_max_cluster();
+  for (int C = 1; C <= cmax; C *= 2) {
     const int64_t per = (n + C - 1) / C;
     if (per * mc_point_bytes(d) <= budget) return C;
   }
@@ -311,14 +376,14 @@ static int mc_cluster_size(int64_t n, int d, int maxsm) {
 struct RoPlan {
   std::vector<RoProb> probs;
   std::vector<KnnBatchProb> kprobs;
-  std::vector<int32_t> plist[4];   // problems per cluster size 1, 2, 4, 8
-  size_t smem[4] = {0, 0, 0, 0};
+  std::vector<int32_t> plist[5];   // problems per cluster size 1, 2, 4, 8, 16
+  size_t smem[5] = {0, 0, 0, 0, 0};
   std::vector<int2> tiles[8];      // kNN tiles per padded dimension
   int DPs[8] = {4, 8, 12, 16, 24, 32, 48, 64};
   int kcap[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int64_t nrows = 0, nxs = 0, nv = 0;
   // workspace layout
-  size_t o_probs, o_kprobs, o_plist[4], o_tiles[8], o_ranges, o_xs, o_v, o_b, o_ord, total, staged;
+  size_t o_probs, o_kprobs, o_plist[5], o_tiles[8], o_ranges, o_xs, o_v, o_b, o_ord, total, staged;
 };
 
 static int ro_plan(const sv_reorder_desc* D, const sv_reorder_prob* hp, RoPlan& L) {
@@ -371,7 +436,7 @@ static int ro_plan(const sv_reorder_desc* D, const sv_reorder_prob* hp, RoPlan& 
   for (int32_t i : byn) {
     const RoProb& R = L.probs[i];
     if (R.n < 1) continue;
-    const int g = R.C == 1 ? 0 : R.C == 2 ? 1 : R.C == 4 ? 2 : 3;
+    const int g = R.C == 1 ? 0 : R.C == 2 ? 1 : R.C == 4 ? 2 : R.C == 8 ? 3 : 4;
     L.plist[g].push_back(i);
     const size_t sm = (size_t)((R.n + R.C - 1) / R.C) * (size_t)mc_point_bytes(R.d);
     L.smem[g] = std::max(L.smem[g], sm);
@@ -388,7 +453,7 @@ static int ro_plan(const sv_reorder_desc* D, const sv_reorder_prob* hp, RoPlan& 
   off = ro_align(off + sizeof(RoProb) * (size_t)np);
   L.o_kprobs = off;
   off = ro_align(off + sizeof(KnnBatchProb) * (size_t)np);
-  for (int g = 0; g < 4; ++g) {
+  for (int g = 0; g < 5; ++g) {
     L.o_plist[g] = off;
     off = ro_align(off + sizeof(int32_t) * L.plist[g].size());
   }
@@ -456,7 +521,7 @@ int maximin_cluster_single(const double* X, int64_t n, int d, int64_t first, int
 int64_t maximin_cluster_max_rows(int d) {
   if (d < 1 || d > 64) return 0;
   const int64_t budget = (int64_t)ro_max_smem() - kMcStaticSmem;
-  return 8 * (budget / mc_point_bytes(d));
+  return (int64_t)mc_max_cluster() * (budget / mc_point_bytes(d));
 }
 
 }  // namespace sv
@@ -499,7 +564,7 @@ extern "C" int sv_reorder_batched(const sv_reorder_desc* D, const sv_reorder_pro
   std::vector<char> host(L.staged, 0);
   memcpy(host.data() + L.o_probs, L.probs.data(), sizeof(RoProb) * np);
   memcpy(host.data() + L.o_kprobs, L.kprobs.data(), sizeof(KnnBatchProb) * np);
-  for (int g = 0; g < 4; ++g)
+  for (int g = 0; g < 5; ++g)
     if (!L.plist[g].empty())
       memcpy(host.data() + L.o_plist[g], L.plist[g].data(), sizeof(int32_t) * L.plist[g].size());
   for (int g = 0; g < 8; ++g)
@@ -524,7 +589,7 @@ extern "C" int sv_reorder_batched(const sv_reorder_desc* D, const sv_reorder_pro
   SV_CUDA_TRY(cudaGetLastError());
 
   // maximin: one launch per cluster size
-  for (int g = 0; g < 4; ++g) {
+  for (int g = 0; g < 5; ++g) {
     if (L.plist[g].empty()) continue;
     rc = launch_maximin_cluster(1 << g, L.smem[g], (unsigned)L.plist[g].size(), dprobs,
                                 (const int32_t*)(ws + L.o_plist[g]), (const double*)Xs, ord, info, st);

@@ -58,12 +58,16 @@ class _Fit:
 
 
 def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=None,
-                warm_start=None, team_lanes=0, verbose=False, stats=None):
+                warm_start=None, team_lanes=0, polish_iter=5, verbose=False, stats=None):
     """Fit ``models[i]`` to ``(Xs[i], ys[i])`` for every i, together.
 
     models : ScaledVecchiaGP instances (each keeps its own settings)
     precision : "split" (split-precision iterations + float64 polish) or
-            "float64"
+            "float64" (every evaluation in float64: the fitted parameters are
+            bit for bit those of ScaledVecchiaGP.fit)
+    polish_iter : float64 Fisher-scoring iterations after the split phase
+            (it re-anchors the split iterate in float64; near parameter
+            clips the iteration can crawl for its whole budget)
     graphs : replay each batched evaluation from a captured CUDA graph
     init_thetas : optional per-model starting log-parameters (a warm start);
             None entries use the model's default initialisation
@@ -148,7 +152,7 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
                 # float64 polish from the split iterate, no reorders
                 f.phase = "polish"
                 f.prec = "float64"
-                f.gen = fisher_scoring_steps(theta, max_iter=f.model.max_iter,
+                f.gen = fisher_scoring_steps(theta, max_iter=min(f.model.max_iter, polish_iter),
                                              tol=f.model.tol, reorder=False)
                 f.msg = next(f.gen)
             else:

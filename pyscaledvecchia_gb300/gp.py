@@ -129,7 +129,10 @@ class ScaledVecchiaGP:
         rebuild(theta)
         last_ranges = np.exp(theta[1:1 + d]).copy()
 
+        nev = [0]
+
         def objective(th):
+            nev[0] += 1
             th = self._objective_theta(th, d, estimate_nu)
             ll, g, M, beta = state["prob"].evaluate(
                 th, self.nu, estimate_nu=estimate_nu, need_grad=True,
@@ -149,6 +152,7 @@ class ScaledVecchiaGP:
         theta, ll, beta = _fisher_scoring(
             theta, objective, max_iter=self.max_iter, tol=self.tol,
             verbose=self.verbose, reorder_hook=reorder_hook)
+        self.fit_stats_ = {"split": 0, "float64": nev[0]}
         return self._fit_finish(st, theta, ll, beta)
 
     # ---------------- pieces of fit shared with the batched fitter ----------

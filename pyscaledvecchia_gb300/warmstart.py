@@ -185,20 +185,24 @@ class SetEncoder:
             self._ws = _lib.workspace(self.torch, nb)
         return self._ws
 
-    def forward_dev(self, x, cnt_d, nset, S=S_POINTS):
+    def forward_dev(self, x, cnt_d, nset, S=S_POINTS, variant="tcgen05"):
         torch = self.torch
         out = torch.empty((nset, N_OUT), dtype=torch.float32, device="cuda")
         ws = self._workspace(nset, S, False)
+        v = {"tcgen05": 0, "mma_sync": 1}[variant]
         rc = self.lib.sv_encoder_forward(nset, S, _lib.ptr(x), _lib.ptr(cnt_d), _lib.ptr(self.p),
-                                         _lib.ptr(self.pb), _lib.ptr(out), _lib.ptr(ws), ws.numel(),
+                                         _lib.ptr(self.pb), _lib.ptr(out), v, _lib.ptr(ws), ws.numel(),
                                          self._st)
         _lib.check(self.lib, rc, "sv_encoder_forward")
         return out
 
-    def forward(self, feats, cnt):
+    def forward(self, feats, cnt, variant="tcgen05"):
+        """Encoder outputs (nset, 16) for host features; variant "tcgen05"
+        (inference kernels) or "mma_sync" (the training forward)."""
         x = self.pack(feats)
         cnt_d = _lib.to_dev(self.torch, np.asarray(cnt, dtype=np.int32), np.int32)
-        return self.forward_dev(x, cnt_d, feats.shape[0], feats.shape[1]).cpu().numpy().astype(np.float64)
+        return self.forward_dev(x, cnt_d, feats.shape[0], feats.shape[1],
+                                variant).cpu().numpy().astype(np.float64)
 
     def loss_grad_dev(self, x, cnt_d, tgt_d, wts_d, nset, S=S_POINTS):
         torch = self.torch
@@ -301,7 +305,34 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--infer", type=int, default=0,
+                    help="only run the inference forward (tcgen05) on this many random sets "
+                         "with the saved weights, timed, and exit")
     a = ap.parse_args(argv)
+    if a.infer:
+        import torch
+        enc = SetEncoder.load(a.out) if os.path.exists(a.out) else SetEncoder(seed=a.seed)
+        rng = np.random.default_rng(a.seed)
+        feats = np.zeros((a.infer, S_POINTS, N_FEAT))
+        feats[:, :, :MAX_D] = rng.random((a.infer, S_POINTS, MAX_D))
+        feats[:, :, MAX_D] = rng.standard_normal((a.infer, S_POINTS))
+        x = enc.pack(feats)
+        cnt = _lib.to_dev(torch, np.full(a.infer, S_POINTS, dtype=np.int32), np.int32)
+        for variant in ("tcgen05", "mma_sync"):
+            for _ in range(3):
+                enc.forward_dev(x, cnt, a.infer, variant=variant)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(10):
+                enc.forward_dev(x, cnt, a.infer, variant=variant)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / 10
+            flops = 2.0 * a.infer * S_POINTS * (N_FEAT * 128 + 128 * 128)
+            print(f"{variant}: {a.infer} sets x {S_POINTS} points: {ms:.3f} ms per forward, "
+                  f"{flops / ms / 1e9:.1f} TFLOP/s in the per-point layers (incl. head)")
+        return
     t0 = time.time()
     feats, cnt, tg, wt, dims = draw_training_problems(a.problems, seed=a.seed, n=a.n)
     t_draw = time.time() - t0

@@ -33,6 +33,25 @@ def test_binding_table_covers_the_header():
     assert set(declared_functions()) == set(_lib.SIGNATURES)
 
 
+def declared_arities():
+    """name -> number of parameters, from the prototypes in the header."""
+    src = open(os.path.join(ROOT, "include", "svgpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(sv_[a-zA-Z0-9_]+)\s*\(([^;{]*?)\)\s*;", src, flags=re.S):
+        args = m.group(2).strip()
+        out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_binding_argument_counts_match_the_prototypes():
+    from pyscaledvecchia_gb300 import _lib
+    ar = declared_arities()
+    assert set(ar) == set(_lib.SIGNATURES)
+    for name, (_, argtypes) in _lib.SIGNATURES.items():
+        assert len(argtypes) == ar[name], (name, len(argtypes), ar[name])
+
+
 def test_status_strings(lib):
     assert lib.sv_abi_version() == 1
     assert lib.sv_status_string(0) == b"ok"
