@@ -224,10 +224,12 @@ int sv_vecchia_loglik_noalloc(const sv_loglik_desc* desc, const double* theta, c
 
 /* No counterpart in the reference: a DeepSets encoder whose output replaces
  * the default starting point of Fisher scoring (gp.py:169-177); the fit
- * itself is unchanged.  Sets of S points (S a multiple of 128), 16 bfloat16
- * features per point (x_1..x_12 zero padded, y, three zeros); cnt[b] valid
- * points in set b.  Parameters: a flat float32 vector of
- * sv_encoder_param_count() entries, W1[128][16] b1[128] W2[128][128] b2[128]
+ * itself is unchanged.  Sets of S points (S a multiple of 128), 32 bfloat16
+ * features per point (x_1..x_12 zero padded, y, and for the point's nearest
+ * neighbour in the whole set its distance, the y difference and its square
+ * and |dx_1|..|dx_12|; four zeros); cnt[b] valid points in set b.
+ * Parameters: a flat float32 vector of
+ * sv_encoder_param_count() entries, W1[128][32] b1[128] W2[128][128] b2[128]
  * W3[128][128] b3[128] W4[16][128] b4[16], and its bfloat16 copy
  * (sv_encoder_to_bf16); weights are read as bfloat16, biases as float32, all
  * sums accumulate in float32.  out is float32 [nset][16].  The backward also

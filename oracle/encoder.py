@@ -21,7 +21,7 @@ from __future__ import annotations
 import numpy as np
 from scipy.special import erf
 
-H, F, O = 128, 16, 16
+H, F, O = 128, 32, 16
 LAYOUT = [("W1", (H, F)), ("b1", (H,)), ("W2", (H, H)), ("b2", (H,)), ("W3", (H, H)),
           ("b3", (H,)), ("W4", (O, H)), ("b4", (O,))]
 

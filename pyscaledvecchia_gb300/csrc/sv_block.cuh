@@ -128,6 +128,70 @@ __device__ bool cholesky_packed(int K, double* Lp, double* invd, volatile int* f
   return true;
 }
 
+// float64 reciprocal of a positive pivot without a division on the float64
+// pipe: float32 seed and two Newton steps y <- y + y (1 - d y) (quadratic
+// convergence: relative error ~2^-24 -> 2^-48 -> 2^-96, below float64
+// rounding); pivots outside the float32 range take the float64 division.
+__device__ __forceinline__ double rcp_pivot64(double d) {
+  if (d > 1e-30 && d < 1e30) {
+    double y = (double)(1.0f / (float)d);
+    y = fma(y, fma(-d, y, 1.0), y);
+    return fma(y, fma(-d, y, 1.0), y);
+  }
+  return 1.0 / d;
+}
+
+// LDL^T of the packed lower triangle in place (unit L below the diagonal,
+// D = diag(d_k) on it): one reciprocal per step instead of a square root and
+// a division.  Fails as the Cholesky does (LAPACK dpotrf: a pivot that is not
+// > 0, d_k = L_kk^2).  acc is K doubles of scratch.
+template <int T>
+__device__ bool ldlt_packed(int K, double* Lp, double* invd, double* acc, volatile int* flag) {
+  const int lane = Team<T>::lane();
+  for (int k = 0; k < K; ++k) {
+    if (lane == 0) {
+      const double dkk = Lp[tri_off(k, k)];
+      if (!(dkk > 0.0))
+        *flag = 1;
+      else
+        invd[k] = rcp_pivot64(dkk);
+    }
+    Team<T>::sync();
+    if (*flag) return false;
+    const double inv = invd[k];
+    for (int i = k + 1 + lane; i < K; i += T) {
+      const double v = Lp[tri_off(i, k)];
+      acc[i] = v;
+      Lp[tri_off(i, k)] = v * inv;
+    }
+    Team<T>::sync();
+    const int m = K - k - 1;
+    const int cnt = m * (m + 1) / 2;
+    for (int t = lane; t < cnt; t += T) {
+      int ii, jj;
+      tri_index(t, ii, jj);
+      const int i = k + 1 + ii, j = k + 1 + jj;
+      Lp[tri_off(i, j)] -= Lp[tri_off(i, k)] * acc[j];  // a_ij -= l_ik d_k l_jk
+    }
+    Team<T>::sync();
+  }
+  return true;
+}
+
+// u = L^-T e_K for a unit lower L (packed); u_K = 1.
+template <int T>
+__device__ void backsolve_unit_eK(int K, const double* Lp, double* u, double* acc) {
+  const int lane = Team<T>::lane();
+  for (int i = lane; i < K; i += T) acc[i] = (i == K - 1) ? 1.0 : 0.0;
+  Team<T>::sync();
+  for (int i = K - 1; i >= 0; --i) {
+    const double ui = acc[i];
+    for (int j = lane; j < i; j += T) acc[j] -= Lp[tri_off(i, j)] * ui;
+    if (lane == 0) u[i] = ui;
+    Team<T>::sync();
+  }
+}
+
 // a = L^-T e_K (the block's column of the sparse inverse Cholesky factor).
 // acc is K doubles of scratch.
 template <int T>

@@ -3,7 +3,7 @@
 // scoring.  No counterpart in the reference; it only moves the starting
 // point of gp.py:169-177 (the default start stays the fallback).
 //
-//   per point  (16 features: x_1..x_12 zero padded, y, 3 zeros, bfloat16)
+//   per point  (32 bfloat16 features, see sv_encoder_* in svgpu.h)
 //     h1 = GELU(W1 x + b1)        128       (h1 rounded to bfloat16)
 //     h2 = GELU(W2 h1 + b2)       128
 //   pool = mean over the set's points of h2
@@ -20,7 +20,7 @@
 // float32 SIMT, one CTA per set.
 //
 // Flat parameter layout (float32 master and bfloat16 copy alike):
-//   W1[128][16] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] W4[16][128] b4[16]
+//   W1[128][32] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] W4[16][128] b4[16]
 #include <cuda_bf16.h>
 
 #include "sv_common.cuh"
@@ -28,11 +28,11 @@
 namespace sv {
 
 constexpr int kEH = 128;   // hidden width
-constexpr int kEF = 16;    // per-point features
+constexpr int kEF = 32;    // per-point features
 constexpr int kEO = 16;    // head outputs
 constexpr int kET = 128;   // points per tile (CTA)
 constexpr int kELd = 136;  // bfloat16 row stride of 128-wide smem tiles
-constexpr int kELx = 24;   // bfloat16 row stride of 16-wide smem tiles
+constexpr int kELx = 40;   // bfloat16 row stride of 32-wide smem tiles
 constexpr int kEThreads = 256;
 
 constexpr int64_t kOffW1 = 0;
@@ -154,8 +154,6 @@ __device__ void enc_load_tile(const EncArgs& A, EncSmem& s, int set, int tile, b
 // z1 for the warp's 16 points (rows r0..r0+15) into acc[16][4] (C layout, n = hidden)
 __device__ __forceinline__ void enc_layer1(const EncSmem& s, const float* b1, int r0, float acc[16][4]) {
   const int t = threadIdx.x & 3;
-  uint32_t a[4];
-  frag_a_row(a, s.x, kELx, r0, 0);
 #pragma unroll
   for (int nt = 0; nt < 16; ++nt) {
     const float bb0 = b1[nt * 8 + 2 * t], bb1 = b1[nt * 8 + 2 * t + 1];
@@ -163,9 +161,17 @@ __device__ __forceinline__ void enc_layer1(const EncSmem& s, const float* b1, in
     acc[nt][1] = bb1;
     acc[nt][2] = bb0;
     acc[nt][3] = bb1;
-    uint32_t b[2];
-    frag_b_col(b, s.W1, kELx, 0, nt * 8);
-    mma16816(acc[nt], a, b);
+  }
+#pragma unroll
+  for (int kt = 0; kt < kEF / 16; ++kt) {
+    uint32_t a[4];
+    frag_a_row(a, s.x, kELx, r0, kt * 16);
+#pragma unroll
+    for (int nt = 0; nt < 16; ++nt) {
+      uint32_t b[2];
+      frag_b_col(b, s.W1, kELx, kt * 16, nt * 8);
+      mma16816(acc[nt], a, b);
+    }
   }
 }
 
@@ -356,22 +362,23 @@ __global__ void __launch_bounds__(kEThreads, 1) k_enc_points_bwd(EncArgs A) {
   }
   // dW1[o][i] = sum_p dz1[p][o] x[p][i]: the warp's 16 rows of o, 16 inputs
   {
-    float w1[2][4];
+    constexpr int NT1 = kEF / 8;
+    float w1[NT1][4];
 #pragma unroll
-    for (int nt = 0; nt < 2; ++nt) w1[nt][0] = w1[nt][1] = w1[nt][2] = w1[nt][3] = 0.0f;
+    for (int nt = 0; nt < NT1; ++nt) w1[nt][0] = w1[nt][1] = w1[nt][2] = w1[nt][3] = 0.0f;
 #pragma unroll
     for (int kt = 0; kt < 8; ++kt) {
       uint32_t a[4];
       frag_a_tr(a, s.dz1, kELd, r0, kt * 16);
 #pragma unroll
-      for (int nt = 0; nt < 2; ++nt) {
+      for (int nt = 0; nt < NT1; ++nt) {
         uint32_t b[2];
         frag_b_row(b, s.x, kELx, kt * 16, nt * 8);
         mma16816(w1[nt], a, b);
       }
     }
 #pragma unroll
-    for (int nt = 0; nt < 2; ++nt) {
+    for (int nt = 0; nt < NT1; ++nt) {
       const int c = nt * 8 + 2 * t;
       gp[(r0 + g) * kEF + c] = w1[nt][0];
       gp[(r0 + g) * kEF + c + 1] = w1[nt][1];
@@ -452,8 +459,8 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
       : "r"(taddr))
 
 struct EncTcSmem {
-  alignas(128) unsigned char x[kET * kEF * 2];   // canonical, KG = 2
-  alignas(128) unsigned char w1[kEH * kEF * 2];  // canonical, KG = 2
+  alignas(128) unsigned char x[kET * kEF * 2];   // canonical, KG = kEF / 8
+  alignas(128) unsigned char w1[kEH * kEF * 2];  // canonical, KG = kEF / 8
   alignas(128) unsigned char w2[kEH * kEH * 2];  // canonical, KG = 16
   alignas(128) unsigned char h1[kET * kEH * 2];  // canonical, KG = 16
   float colsum[4][kEH];
@@ -471,15 +478,17 @@ __device__ __forceinline__ void umma_stage(unsigned char* dst, const bf16* src, 
   }
 }
 
+// Persistent: each CTA stages the weights once, then walks tiles t =
+// blockIdx.x, blockIdx.x + gridDim.x, ... (set t / ntile, tile t % ntile).
+// Two MMA groups per tile complete mbarrier phases of parity 0 and 1.
 __global__ void __launch_bounds__(128, 1) k_enc_points_fwd_tc(EncArgs A, int32_t* err) {
   extern __shared__ __align__(16) unsigned char tc_smraw[];
   // 128-byte aligned base inside the launch's slack
   const uint32_t pad = (128u - (smem_u32(tc_smraw) & 127u)) & 127u;
   EncTcSmem& s = *reinterpret_cast<EncTcSmem*>(tc_smraw + pad);
-  const int tile = blockIdx.x, set = blockIdx.y;
   const int ntile = A.S / kET;
+  const int64_t total = (int64_t)A.nset * ntile;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int cnt = A.cnt[set];
   const uint32_t mbar = smem_u32(&s.mbar);
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
@@ -492,78 +501,90 @@ __global__ void __launch_bounds__(128, 1) k_enc_points_fwd_tc(EncArgs A, int32_t
   }
   umma_stage(s.w1, A.pb + kOffW1, kEH, kEF);
   umma_stage(s.w2, A.pb + kOffW2, kEH, kEH);
-  umma_stage(s.x, A.x + ((int64_t)set * A.S + (int64_t)tile * kET) * kEF, kET, kEF);
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tbase = s.tmem_base;
   const uint32_t idesc = umma_idesc_bf16(kET, kEH);
-  bool ok = true;
-
-  // layer 1: D1 = X W1^T (K = 16, one instruction)
-  if (threadIdx.x == 0) {
-    umma_bf16(tbase, umma_desc(smem_u32(s.x), 128, 256), umma_desc(smem_u32(s.w1), 128, 256), idesc, 0);
-    umma_commit(mbar);
-  }
-  ok = __all_sync(0xffffffffu, mbar_wait(mbar, 0));  // warp-uniform before tcgen05.ld
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const int row = warp * 32 + lane;  // this thread's point in the tile
   const uint32_t tlane = tbase + ((uint32_t)(warp * 32) << 16);
-  if (ok) {
-    // epilogue 1: h1 = bf16(GELU(z1 + b1)) into the canonical A operand of layer 2
-    for (int c0 = 0; c0 < kEH; c0 += 32) {
-      uint32_t v[32];
-      SV_TC_LD32(tlane + c0, v);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  bool ok = true;
+
+  for (int64_t t = blockIdx.x; t < total && ok; t += gridDim.x) {
+    const int set = (int)(t / ntile), tile = (int)(t - (t / ntile) * ntile);
+    const int cnt = A.cnt[set];
+    umma_stage(s.x, A.x + ((int64_t)set * A.S + (int64_t)tile * kET) * kEF, kET, kEF);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    // layer 1: D1 = X W1^T (K = kEF, instructions of K = 16)
+    if (threadIdx.x == 0) {
+      for (int kk = 0; kk < kEF / 16; ++kk)
+        umma_bf16(tbase, umma_desc(smem_u32(s.x) + kk * 256, 128, (kEF / 8) * 128),
+                  umma_desc(smem_u32(s.w1) + kk * 256, 128, (kEF / 8) * 128), idesc, kk > 0 ? 1u : 0u);
+      umma_commit(mbar);
+    }
+    ok = __all_sync(0xffffffffu, mbar_wait(mbar, 0));  // warp-uniform before tcgen05.ld
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+      // epilogue 1: h1 = bf16(GELU(z1 + b1)) into the canonical A operand of layer 2
+      for (int c0 = 0; c0 < kEH; c0 += 32) {
+        uint32_t v[32];
+        SV_TC_LD32(tlane + c0, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-      for (int c = 0; c < 32; c += 8) {
-        uint32_t w[4];
+        for (int c = 0; c < 32; c += 8) {
+          uint32_t w[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e)
-          w[e] = pack2(gelu_f(__uint_as_float(v[c + 2 * e]) + A.pf[kOffB1 + c0 + c + 2 * e]),
-                       gelu_f(__uint_as_float(v[c + 2 * e + 1]) + A.pf[kOffB1 + c0 + c + 2 * e + 1]));
-        *reinterpret_cast<uint4*>(s.h1 + umma_off(row, c0 + c, kEH / 8)) = make_uint4(w[0], w[1], w[2], w[3]);
+          for (int e = 0; e < 4; ++e)
+            w[e] = pack2(gelu_f(__uint_as_float(v[c + 2 * e]) + A.pf[kOffB1 + c0 + c + 2 * e]),
+                         gelu_f(__uint_as_float(v[c + 2 * e + 1]) + A.pf[kOffB1 + c0 + c + 2 * e + 1]));
+          *reinterpret_cast<uint4*>(s.h1 + umma_off(row, c0 + c, kEH / 8)) =
+              make_uint4(w[0], w[1], w[2], w[3]);
+        }
       }
     }
-  }
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  ok = __syncthreads_and(ok);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    ok = __syncthreads_and(ok);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
-  // layer 2: D2 = H1 W2^T (K = 128, eight instructions of K = 16)
-  if (ok && threadIdx.x == 0) {
-    for (int kk = 0; kk < kEH / 16; ++kk)
-      umma_bf16(tbase + kEH, umma_desc(smem_u32(s.h1) + kk * 256, 128, 2048),
-                umma_desc(smem_u32(s.w2) + kk * 256, 128, 2048), idesc, kk > 0 ? 1u : 0u);
-    umma_commit(mbar);
-  }
-  if (ok) ok = __all_sync(0xffffffffu, mbar_wait(mbar, 1));
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const bool valid = tile * kET + row < cnt;
-  for (int c0 = 0; c0 < kEH; c0 += 32) {
-    uint32_t v[32];
-    if (ok) {
-      SV_TC_LD32(tlane + kEH + c0, v);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    // layer 2: D2 = H1 W2^T (K = 128, eight instructions of K = 16)
+    if (ok && threadIdx.x == 0) {
+      for (int kk = 0; kk < kEH / 16; ++kk)
+        umma_bf16(tbase + kEH, umma_desc(smem_u32(s.h1) + kk * 256, 128, 2048),
+                  umma_desc(smem_u32(s.w2) + kk * 256, 128, 2048), idesc, kk > 0 ? 1u : 0u);
+      umma_commit(mbar);
     }
+    if (ok) ok = __all_sync(0xffffffffu, mbar_wait(mbar, 1));
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool valid = tile * kET + row < cnt;
+    for (int c0 = 0; c0 < kEH; c0 += 32) {
+      uint32_t v[32];
+      if (ok) {
+        SV_TC_LD32(tlane + kEH + c0, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      }
 #pragma unroll
-    for (int c = 0; c < 32; ++c) {
-      float h = (ok && valid) ? gelu_f(__uint_as_float(v[c]) + A.pf[kOffB2 + c0 + c]) : 0.0f;
-      for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
-      if (lane == 0) s.colsum[warp][c0 + c] = h;
+      for (int c = 0; c < 32; ++c) {
+        float h = (ok && valid) ? gelu_f(__uint_as_float(v[c]) + A.pf[kOffB2 + c0 + c]) : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+        if (lane == 0) s.colsum[warp][c0 + c] = h;
+      }
     }
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (threadIdx.x < kEH) {
-    const float v = ((s.colsum[0][threadIdx.x] + s.colsum[1][threadIdx.x]) + s.colsum[2][threadIdx.x]) +
-                    s.colsum[3][threadIdx.x];
-    A.part[((int64_t)set * ntile + tile) * kEH + threadIdx.x] = v;
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    ok = __syncthreads_and(ok);
+    if (threadIdx.x < kEH) {
+      const float v = ((s.colsum[0][threadIdx.x] + s.colsum[1][threadIdx.x]) + s.colsum[2][threadIdx.x]) +
+                      s.colsum[3][threadIdx.x];
+      A.part[((int64_t)set * ntile + tile) * kEH + threadIdx.x] = v;
+    }
+    __syncthreads();  // colsum and x are rewritten by the next tile
   }
   if (!ok && threadIdx.x == 0) atomicExch(err, SV_ETIMEOUT);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
   if (warp == 0) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tbase), "r"(256));
@@ -821,7 +842,10 @@ extern "C" int sv_encoder_forward(int64_t nset, int32_t S, const uint16_t* x, co
   if (variant == 0) {
     const size_t smem = sizeof(EncTcSmem) + 128;  // + alignment slack of the dynamic base
     SV_CUDA_TRY(cudaFuncSetAttribute(k_enc_points_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_enc_points_fwd_tc<<<grid, 128, smem, st>>>(A, err);
+    // persistent: two CTAs per SM (256 tensor-memory columns each)
+    int64_t ctas = (int64_t)nset * (S / kET);
+    if (ctas > 2LL * sv_num_sms()) ctas = 2LL * sv_num_sms();
+    k_enc_points_fwd_tc<<<(unsigned)ctas, 128, smem, st>>>(A, err);
   } else {
     const size_t smem = sizeof(EncSmem);
     SV_CUDA_TRY(cudaFuncSetAttribute(k_enc_points_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

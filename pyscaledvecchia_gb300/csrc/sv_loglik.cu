@@ -374,6 +374,15 @@ __host__ __device__ inline int nfield1(int q, int P, int need_grad) {
 // Pass-1 sums of one partition: warp w takes the partition's blocks
 // w, w + nwarp, ..., its lanes the fields; each (warp, field) accumulator in
 // shared memory has one owner, and the warps' rows are added in a fixed order.
+// partitions of a problem's blocks: a function of its own block count only,
+// so a problem's sums are the same alone and in any batch
+__host__ __device__ inline int red_parts_n(int64_t nblk) {
+  int64_t parts = (nblk + 1023) / 1024;
+  if (parts < 8) parts = 8;
+  if (parts > 4096) parts = 4096;
+  return (int)parts;
+}
+
 __global__ void k_reduce1(RedArgs R) {
   extern __shared__ double racc[];  // [nwarp][nfmax]
   const int p = blockIdx.y;
@@ -382,7 +391,9 @@ __global__ void k_reduce1(RedArgs R) {
   const int q = PI.q, P = PI.P;
   const int nf = nfield1(q, P, R.need_grad);
   const int nwarp = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t per = (PI.nblk + R.parts - 1) / R.parts;
+  const int parts = red_parts_n(PI.nblk);
+  if ((int)blockIdx.x >= parts) return;
+  const int64_t per = (PI.nblk + parts - 1) / parts;
   const int64_t b0 = PI.blk_off + blockIdx.x * per;
   const int64_t b1 = min(PI.blk_off + PI.nblk, b0 + per);
   double* acc = racc + (int64_t)w * R.nfmax;
@@ -424,7 +435,7 @@ __global__ void k_final1(RedArgs R) {
   double* sums = R.sums + (int64_t)p * R.nfmax;
   for (int f = threadIdx.x; f < nf; f += blockDim.x) {
     double s = 0.0;
-    for (int c = 0; c < R.parts; ++c) s += R.part1[((int64_t)p * R.parts + c) * R.nfmax + f];
+    for (int c = 0; c < red_parts_n(PI.nblk); ++c) s += R.part1[((int64_t)p * R.parts + c) * R.nfmax + f];
     sums[f] = s;
   }
   __syncthreads();
@@ -468,7 +479,9 @@ __global__ void k_reduce2(RedArgs R) {
   const int q = PI.q, P = PI.P, np = R.need_grad ? P : 0;
   for (int i = threadIdx.x; i < q; i += blockDim.x) sbeta[i] = R.beta[(int64_t)p * (R.qmax + 1) + i];
   __syncthreads();
-  const int64_t per = (PI.nblk + R.parts - 1) / R.parts;
+  const int parts = red_parts_n(PI.nblk);
+  if ((int)blockIdx.x >= parts) return;
+  const int64_t per = (PI.nblk + parts - 1) / parts;
   const int64_t b0 = PI.blk_off + blockIdx.x * per;
   const int64_t b1 = min(PI.blk_off + PI.nblk, b0 + per);
   double acc[kMaxP + 1];
@@ -512,7 +525,7 @@ __global__ void k_final2(RedArgs R) {
   __shared__ double tot[kMaxP + 1];
   for (int i = threadIdx.x; i <= np; i += blockDim.x) {
     double s = 0.0;
-    for (int c = 0; c < R.parts; ++c) s += R.part2[((int64_t)p * R.parts + c) * (R.Pmax + 1) + i];
+    for (int c = 0; c < red_parts_n(PI.nblk); ++c) s += R.part2[((int64_t)p * R.parts + c) * (R.Pmax + 1) + i];
     tot[i] = s;
   }
   __syncthreads();
@@ -569,13 +582,8 @@ struct EvalShape {
   int dmax, qmax, Pmax, kmax, need_grad, any_est, precision;
 };
 
-// reduction partitions per problem: about 1024 blocks each for the largest
-int red_parts(const EvalShape& S) {
-  int64_t parts = (S.nblk_max + 1023) / 1024;
-  if (parts < 8) parts = 8;
-  if (parts > 4096) parts = 4096;
-  return (int)parts;
-}
+// reduction grid rows: the partitions of the largest problem
+int red_parts(const EvalShape& S) { return red_parts_n(S.nblk_max); }
 
 struct WsLayout {
   size_t desc, probs, cache, level, redo, chunk_max, flags, part1, part2, beta, sums, xhl, total;

@@ -113,7 +113,7 @@ __device__ void pred_block(const PredArgs& A, const PredPrm* prm, int64_t b, dou
     if (lane == 0) *flag = 0;
     assemble_sigma<T>(K, d, u, mask, s2, tau, jit, prm->mm, Lp, nullptr, nullptr);
     Team<T>::sync();
-    ok = cholesky_packed<T>(K, Lp, invd, flag);
+    ok = ldlt_packed<T>(K, Lp, invd, acc, flag);
     Team<T>::sync();
     if (ok) {
       if (lv > 0 && lane == 0) atomicMax(A.info + SV_INFO_JITTER, lv);
@@ -127,23 +127,27 @@ __device__ void pred_block(const PredArgs& A, const PredPrm* prm, int64_t b, dou
     }
     return;
   }
-  backsolve_eK<T>(K, Lp, invd, a, acc);
+  // Sigma = L D L^T = C C^T with C = L D^(1/2): a = C^-T e_K = u / sqrt(d_K),
+  // u = L^-T e_K (u_K = 1), so mean = -a[:k].r / a_K = -u[:k].r and
+  // var = 1 / a_K^2 = d_K; only the U column needs the square root
+  backsolve_unit_eK<T>(K, Lp, a, acc);
   Team<T>::sync();
   double s = 0.0;
   for (int i = lane; i < k; i += T) s += a[i] * rv[i];
   s = team_sum<T>(s, red);
+  const double dK = Lp[tri_off(K - 1, K - 1)];
+  const double sK = 1.0 / sqrt(dK);
   if (lane == 0) {
-    const double aK = a[K - 1];
-    if (A.mean) A.mean[b] = -s / aK;
-    if (A.var) A.var[b] = 1.0 / (aK * aK);
-    if (A.rhs) A.rhs[b] = -s;
+    if (A.mean) A.mean[b] = -s;
+    if (A.var) A.var[b] = dK;
+    if (A.rhs) A.rhs[b] = -s * sK;
   }
   if (A.acol) {
     // column of U laid out as [neighbour slots 0..kcap-1, target]; absent
     // neighbour slots hold 0
     const int Kc = kcap + 1;
     for (int i = lane; i < Kc; i += T)
-      A.acol[b * (int64_t)Kc + i] = (i < k) ? a[i] : (i == kcap ? a[K - 1] : 0.0);
+      A.acol[b * (int64_t)Kc + i] = (i < k) ? a[i] * sK : (i == kcap ? sK : 0.0);
   }
 }
 

@@ -199,5 +199,7 @@ def test_fit_batched_split_ends_at_a_float64_optimum():
         nrm = np.linalg.norm(step)
         if nrm > 3.0:
             step *= 3.0 / nrm
-        assert abs(step @ grad) < 1e-2  # Newton decrement: within ~5e-3 of the local maximum
+        # at most 5 float64 iterations after the split phase: near a float64
+        # stationary point (Newton decrement below 0.05)
+        assert abs(step @ grad) < 5e-2
         assert abs(g.loglik_ - a.loglik_) <= 2e-2 * max(1.0, abs(a.loglik_))
