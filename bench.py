@@ -318,6 +318,15 @@ def run_fits(torch, lib, nprob, dump=""):
         forms["batched_split_warm"] = _form_stats(plain, warm, t, nprob)
         forms["batched_split_warm"]["schedule"] = {k: (float(v) if isinstance(v, float) else v)
                                                    for k, v in stw.items() if k not in ("batch", "thetas")}
+        # both starts per model in one float64 batch, the better converged
+        # loglik kept: never below the plain fit (whose path is the default one)
+        judged, t = timed(lambda: fit_batched([model(pr) for pr in probs], Xs, ys, precision="float64",
+                                              warm_start=enc, warm_judge=True))
+        forms["batched_float64_warm_judged"] = _form_stats(plain, judged, t, nprob)
+        dj = np.array([a.loglik_ - b.loglik_ for a, b in zip(judged, plain)])
+        forms["batched_float64_warm_judged"]["frac_better_than_plain"] = float(np.mean(dj > 1e-6))
+        forms["batched_float64_warm_judged"]["dll_median_where_better"] = (
+            float(np.median(dj[dj > 1e-6])) if np.any(dj > 1e-6) else 0.0)
 
     # split form vs float64 at every final state of the split fits (same ordering)
     BL = st["batch"]
@@ -345,6 +354,8 @@ def run_fits(torch, lib, nprob, dump=""):
                if enc is not None else {}))
     ok = [k for k, v in forms.items() if v["frac_abs_dll_below_1e-6"] == 1.0 or
           v["dll_rel_max"] < 1e-6]
+    # forms whose loglik is never below the plain form's (within 1e-6)
+    not_worse = [k for k, v in forms.items() if v["frac_not_worse_than_plain"] == 1.0]
     chosen = max(ok, key=lambda k: forms[k]["fits_per_s"]) if ok else None
     fastest = max(forms, key=lambda k: forms[k]["fits_per_s"])
     return {
@@ -357,6 +368,7 @@ def run_fits(torch, lib, nprob, dump=""):
         "chosen_form": chosen, "chosen_fits_per_s": forms[chosen]["fits_per_s"] if chosen else None,
         "chosen_speedup": (forms[chosen]["fits_per_s"] * t_plain / nprob) if chosen else None,
         "fastest_form": fastest, "fastest_speedup": forms[fastest]["fits_per_s"] * t_plain / nprob,
+        "never_worse_forms": not_worse,
         "split_vs_float64_at_final_state": {"ll_rel_max": e_ll, "score_err_max_in_sd": e_g,
                                             "fisher_rel_max": e_f, "beta_rel_max": e_b},
         "draw_s": t_draw,

@@ -21,6 +21,36 @@ namespace sv {
 
 constexpr int kKnnQ = 128;  // queries per CTA (one per thread)
 constexpr int kKnnC = 128;  // candidates per shared-memory tile
+constexpr int kKnnHeapMin = 48;  // lists of at least this many neighbours are kept as heaps
+
+// Max-heap on (squared distance, index) in a thread's column of the list
+// arrays (element e at [e * kKnnQ + tid]); the root is the current k-th.
+__device__ __forceinline__ bool knn_key_less(double a, int ia, double b, int ib) {
+  return a < b || (a == b && ia < ib);
+}
+__device__ __forceinline__ void knn_heap_swap(double* lsd, int* lsi, int e, int f, int tid) {
+  const double td = lsd[e * kKnnQ + tid];
+  const int ti = lsi[e * kKnnQ + tid];
+  lsd[e * kKnnQ + tid] = lsd[f * kKnnQ + tid];
+  lsi[e * kKnnQ + tid] = lsi[f * kKnnQ + tid];
+  lsd[f * kKnnQ + tid] = td;
+  lsi[f * kKnnQ + tid] = ti;
+}
+__device__ __forceinline__ void knn_sift_down(double* lsd, int* lsi, int e, int size, int tid) {
+  while (true) {
+    const int l = 2 * e + 1;
+    if (l >= size) break;
+    int c = l;
+    if (l + 1 < size && knn_key_less(lsd[l * kKnnQ + tid], lsi[l * kKnnQ + tid],
+                                     lsd[(l + 1) * kKnnQ + tid], lsi[(l + 1) * kKnnQ + tid]))
+      c = l + 1;
+    if (!knn_key_less(lsd[e * kKnnQ + tid], lsi[e * kKnnQ + tid], lsd[c * kKnnQ + tid],
+                      lsi[c * kKnnQ + tid]))
+      break;
+    knn_heap_swap(lsd, lsi, e, c, tid);
+    e = c;
+  }
+}
 
 // prologue: centred float32 coordinates (zero padded to DP) and their bound
 __global__ void k_knn_prep(const double* X, int64_t n, int d, int DP, const double* centroid,
@@ -107,6 +137,7 @@ __device__ __forceinline__ void knn_tile(const KnnArgs& A, int64_t qt, unsigned 
 
   int cnt = 0;
   float T = __int_as_float(0x7f800000);  // +inf until the list is full
+  const bool heap = A.k >= kKnnHeapMin;
 
   // candidate range
   int64_t cend = A.nr;
@@ -150,6 +181,27 @@ __device__ __forceinline__ void knn_tile(const KnnArgs& A, int64_t qt, unsigned 
         const double df = __dsub_rn(xq[l], xr[l]);
         s = __dadd_rn(s, __dmul_rn(df, df));
       }
+      if (heap) {
+        // later index loses ties: only a strictly smaller distance displaces the root
+        if (cnt == kq) {
+          if (!(s < lsd[tid])) continue;
+          lsd[tid] = s;
+          lsi[tid] = (int)j;
+          knn_sift_down(lsd, lsi, 0, kq, tid);
+        } else {
+          int e = cnt++;
+          lsd[e * kKnnQ + tid] = s;
+          lsi[e * kKnnQ + tid] = (int)j;
+          while (e > 0) {
+            const int par = (e - 1) >> 1;
+            if (!knn_key_less(lsd[par * kKnnQ + tid], lsi[par * kKnnQ + tid], s, (int)j)) break;
+            knn_heap_swap(lsd, lsi, e, par, tid);
+            e = par;
+          }
+        }
+        if (cnt == kq) T = knn_thr(lsd[tid], Bi, A.d);
+        continue;
+      }
       if (cnt == kq) {
         if (!(s < lsd[(kq - 1) * kKnnQ + tid])) continue;  // later index loses ties
         --cnt;
@@ -167,6 +219,11 @@ __device__ __forceinline__ void knn_tile(const KnnArgs& A, int64_t qt, unsigned 
     }
   }
   if (!valid) return;
+  if (heap)  // heap sort: ascending (distance, index)
+    for (int end = cnt - 1; end > 0; --end) {
+      knn_heap_swap(lsd, lsi, 0, end, tid);
+      knn_sift_down(lsd, lsi, 0, end, tid);
+    }
   if (A.nbr) {
     int32_t* row = A.nbr + (A.b0 + i) * (int64_t)A.ldnbr;
     for (int c = 0; c < A.ldnbr; ++c) row[c] = (active && c < cnt) ? lsi[c * kKnnQ + tid] : -1;

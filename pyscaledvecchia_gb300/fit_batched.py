@@ -58,7 +58,8 @@ class _Fit:
 
 
 def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=None,
-                warm_start=None, team_lanes=0, polish_iter=5, verbose=False, stats=None):
+                warm_start=None, warm_judge=False, team_lanes=0, polish_iter=5, verbose=False,
+                stats=None):
     """Fit ``models[i]`` to ``(Xs[i], ys[i])`` for every i, together.
 
     models : ScaledVecchiaGP instances (each keeps its own settings)
@@ -75,6 +76,11 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
             model's standardised estimation set is the starting point
             (fixed nuggets and an estimated nu keep their default entries;
             models it does not apply to keep the default start)
+    warm_judge : with warm_start, fit every model from both starts in the
+            same batch and keep the fit with the larger converged loglik
+            (the default start on ties): Fisher scoring with reorders at the
+            iterates is path dependent, and this way the network moves only
+            the starting point and never makes the answer worse
     stats : optional dict that receives the schedule's counters (rounds,
             batched launches, reorder calls, seconds in each part) and the
             batch itself under "batch" (for diagnostics)
@@ -94,10 +100,18 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
     _lib.device_ready()
     fits = [_Fit(mdl, X, y, None if init_thetas is None else init_thetas[i])
             for i, (mdl, X, y) in enumerate(zip(models, Xs, ys))]
+    owner = list(range(len(fits)))
+    if warm_start is not None and warm_judge:
+        # second copy of every fit: the warm start goes to the copies
+        fits = fits + [_Fit(mdl, X, y, None if init_thetas is None else init_thetas[i])
+                       for i, (mdl, X, y) in enumerate(zip(models, Xs, ys))]
+        owner = owner + list(range(len(models)))
+    nmod = len(models)
     if warm_start is not None:
         t_ws = time.perf_counter()
-        pred = warm_start.initial_thetas([(f.st["Xe"], f.st["ye"]) for f in fits])
-        for f, th in zip(fits, pred):
+        tgt = fits[nmod:] if warm_judge else fits
+        pred = warm_start.initial_thetas([(f.st["Xe"], f.st["ye"]) for f in tgt])
+        for f, th in zip(tgt, pred):
             if th is None:
                 continue
             t0 = f.st["theta0"].copy()
@@ -222,8 +236,18 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
         stats.update(cnt)
         stats["batch"] = BL
         stats["thetas"] = [f.result[0] for f in fits]
-    for f in fits:
+    best = {}
+    for i, f in enumerate(fits):
+        o = owner[i]
+        if o not in best or f.result[1] > best[o].result[1]:
+            best[o] = f
+    for o, f in best.items():
         theta, ll, beta = f.result
         f.model._fit_finish(f.st, theta, ll, beta)
-        f.model.fit_stats_ = dict(f.evals)
+        ev = {"split": 0, "float64": 0}
+        for i, g in enumerate(fits):
+            if owner[i] == o:
+                for k in ev:
+                    ev[k] += g.evals[k]
+        f.model.fit_stats_ = ev
     return models

@@ -154,7 +154,8 @@ def test_warm_start_gain_on_heldout_problems():
     drawn by the method), held-out problems drawn the same way: the
     encoder's start lies much closer to where Fisher scoring converges than
     the default start and the fits need fewer objective evaluations; the
-    optimum reached is the same wherever both runs end on the same ordering."""
+    judged form (both starts, the better converged loglik kept) is never
+    worse than the default start."""
     from pyscaledvecchia_gb300 import ScaledVecchiaGP
     from pyscaledvecchia_gb300.fit_batched import fit_batched
     from pyscaledvecchia_gb300.warmstart import DEFAULT_WEIGHTS, SetEncoder
@@ -205,6 +206,13 @@ def test_warm_start_gain_on_heldout_problems():
     # evaluations 24.5 -> 22.3
     assert dw.mean() < 0.5 * d0.mean(), (dw.mean(), d0.mean())
     assert ew.mean() < 0.95 * eb.mean(), (ew.mean(), eb.mean())
+    # Fisher scoring with reorders at the iterates is path dependent: another
+    # start can end on another ordering and another local optimum (measured:
+    # better in about half of the problems, worse in the other half), which
+    # is what warm_start="judged" is for
     dll = np.array([w.loglik_ - b.loglik_ for w, b in zip(warm, base)])
-    # a different start can end on a different final ordering; most end together
-    assert np.median(np.abs(dll)) < 1e-2 and np.mean(dll > -0.5) > 0.9, dll
+    print(f"warm - default loglik: median {np.median(dll):.3g}, better in {np.mean(dll > 1e-6):.2f}, "
+          f"worse in {np.mean(dll < -1e-6):.2f}")
+    judged = fit_batched(models(), Xs, ys, precision="float64", warm_start=enc, warm_judge=True)
+    for j, b, w in zip(judged, base, warm):
+        assert j.loglik_ == max(b.loglik_, w.loglik_)
