@@ -464,6 +464,7 @@ struct EncTcSmem {
   alignas(128) unsigned char w2[kEH * kEH * 2];  // canonical, KG = 16
   alignas(128) unsigned char h1[kET * kEH * 2];  // canonical, KG = 16
   float colsum[4][kEH];
+  float tr[4][32][33];  // per-warp 32 x 32 transpose buffer of the pooling epilogue
   uint64_t mbar;
   uint32_t tmem_base;
 };
@@ -566,12 +567,17 @@ __global__ void __launch_bounds__(128, 1) k_enc_points_fwd_tc(EncArgs A, int32_t
         SV_TC_LD32(tlane + kEH + c0, v);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       }
+      // column sums over the warp's 32 rows: transpose through shared memory,
+      // then lane c adds up column c0 + c
 #pragma unroll
-      for (int c = 0; c < 32; ++c) {
-        float h = (ok && valid) ? gelu_f(__uint_as_float(v[c]) + A.pf[kOffB2 + c0 + c]) : 0.0f;
-        for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
-        if (lane == 0) s.colsum[warp][c0 + c] = h;
-      }
+      for (int c = 0; c < 32; ++c)
+        s.tr[warp][c][lane] = (ok && valid) ? gelu_f(__uint_as_float(v[c]) + A.pf[kOffB2 + c0 + c]) : 0.0f;
+      __syncwarp();
+      float h = 0.0f;
+#pragma unroll
+      for (int r = 0; r < 32; ++r) h += s.tr[warp][lane][r];
+      s.colsum[warp][c0 + lane] = h;
+      __syncwarp();
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     ok = __syncthreads_and(ok);
