@@ -54,8 +54,9 @@ def pack_groups(groups, n=None):
             nbr[o:o + c, :k] = nb
         gid[o:o + c] = g
         o += c
+    # padding is -1, so plain extrema check every entry
     if n is not None and B and (rowb.min() < 0 or rowb.max() >= n or
-                                (kmax and (nbr[nbr >= 0].max(initial=0) >= n))):
+                                (kmax and (nbr.max() >= n or nbr.min() < -1))):
         raise ValueError("conditioning sets reference rows outside the data")
     big = (kb + 1) > _WARP_K
     if big.any() and not np.all(np.diff(big.astype(np.int8)) >= 0):
@@ -78,12 +79,15 @@ def chunk_ids(gid, group_k, group_len, Pc):
         ids_per_group.append(ids)
     if gid.shape[0] == 0:
         return np.zeros(0, dtype=np.int32)
+    flat = np.concatenate(ids_per_group)
+    if np.all(np.diff(gid) >= 0):
+        # groups in order (no warp/CTA regrouping): block b is the flat entry b
+        return flat.astype(np.int32)
     # rank of each block inside its group (the stable warp/CTA split keeps it)
     sort_idx = np.argsort(gid, kind="stable")
     first = np.searchsorted(gid[sort_idx], np.arange(len(group_k)))
     rank = np.empty(gid.shape[0], dtype=np.int64)
     rank[sort_idx] = np.arange(gid.shape[0]) - first[gid[sort_idx]]
-    flat = np.concatenate(ids_per_group)
     offs = np.concatenate([[0], np.cumsum(group_len)])[:-1].astype(np.int64)
     return flat[offs[gid] + rank].astype(np.int32)
 
