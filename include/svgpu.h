@@ -95,7 +95,9 @@ typedef struct sv_reorder_prob {
   int64_t x_off, y_off, z_off;     /* destination rows (maximin order)       */
   int64_t blk_off;                 /* likelihood block of row 0              */
   int64_t first;                   /* first row of the ordering (ordering.py:72) */
-  int32_t d, q, m, pad;
+  int32_t d, q, m;
+  int32_t flags;                   /* bit 0: resolve every maximin step from the
+                                      exact square roots (same result; a test aid) */
 } sv_reorder_prob;
 
 typedef struct sv_reorder_desc {

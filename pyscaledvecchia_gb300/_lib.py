@@ -55,7 +55,7 @@ class ReorderProb(ctypes.Structure):
     """Mirror of sv_reorder_prob (include/svgpu.h)."""
     _fields_ = [("n", c_i64), ("xe_off", c_i64), ("ye_off", c_i64), ("ze_off", c_i64),
                 ("x_off", c_i64), ("y_off", c_i64), ("z_off", c_i64), ("blk_off", c_i64),
-                ("first", c_i64), ("d", c_i32), ("q", c_i32), ("m", c_i32), ("pad", c_i32)]
+                ("first", c_i64), ("d", c_i32), ("q", c_i32), ("m", c_i32), ("flags", c_i32)]
 
 
 class ReorderDesc(ctypes.Structure):

@@ -12,12 +12,25 @@
 //           (the _nn_groups layout, ordering.py:119-127, with row i = block i).
 //
 // Maximin runs one thread-block cluster per problem.  The cluster's CTAs
-// split the problem's points; each keeps, in shared memory, the float64
-// distances, float32 skip thresholds and float32 coordinates centred on the
-// first row, and makes every update decision exactly as the single-problem
-// kernel (sv_maximin.cu) does: float32 screening with a rigorous bound, the
-// float64 distance in IEEE sequential arithmetic wherever the bound cannot
-// exclude an update.  Per step the CTAs' candidates (distance bits, index)
+// split the problem's points; each keeps, in shared memory, the squared
+// float64 distances, float32 skip thresholds, exact coordinates and float32
+// coordinates centred on the first row.  Every decision is the reference's:
+//  * screening: a rigorous float32 bound skips a point only when the
+//    reference would not update it;
+//  * update: the squared distance s_new is computed in IEEE sequential
+//    float64 exactly as ordering.py:52-57 does before its square root; the
+//    point is updated when s_new < s_stored (bit compare).  With a correctly
+//    rounded, monotone sqrt this keeps fl(sqrt(s_stored)) equal to the
+//    reference's stored distance at every step: the reference updates only
+//    when fl(sqrt(s_new)) < fl(sqrt(s_stored)), which implies s_new <
+//    s_stored; an update here that the reference skips has
+//    fl(sqrt(s_new)) == fl(sqrt(s_stored)) and leaves the root unchanged.
+//    No square root is taken on this path;
+//  * argmax: candidates compare squared bits, then indices.  Distinct squares
+//    can round to the same root only within a few ulps, so whenever a loser
+//    within 4 ulps of the winner has a smaller index, the step resolves its
+//    winner again from the exact roots of every point within 4 ulps (one
+//    more cluster exchange; rare).  Per step the CTAs' candidates (distance bits, index)
 // meet through distributed shared memory after one hardware cluster barrier
 // (double-buffered by step parity), so there is no spin-wait at all.
 // Problems are grouped by cluster size (1, 2, 4 or 8 CTAs, the smallest
@@ -35,8 +48,9 @@ namespace cg = cooperative_groups;
 namespace sv {
 
 constexpr int kMcThreads = 512;
-constexpr int kMcStaticSmem =
-    64 * 8 * 2 + 64 * 4 + 4 + 2 * 8 * (kMcThreads / 32) + 4 * 8 + 2 * 64 * 8 + 8 + 64;
+// static shared memory of k_maximin_cluster (3.7 KB), rounded up: the
+// capacity of a cluster is computed from what is left of 227 KB
+constexpr int kMcStaticSmem = 4096;
 constexpr int kMcMaxCluster = 16;
 
 struct RoProb {
@@ -56,6 +70,28 @@ __device__ __forceinline__ void cand_better(long long ob, long long oi, long lon
     bb = ob;
     bi = oi;
   }
+}
+
+// merge of (squared-distance bits, index, near-tie flag) candidates: larger
+// bits win, then the smaller index; a loser within 4 ulps below the winner
+// with a smaller index may share the winner's square root
+__device__ __forceinline__ void cand_merge(long long ob, long long oi, int of, long long& bb,
+                                           long long& bi, int& bf) {
+  const bool ow = ob > bb || (ob == bb && oi < bi);
+  const long long wb = ow ? ob : bb, wi = ow ? oi : bi;
+  const long long lb = ow ? bb : ob, li = ow ? bi : oi;
+  int f = of | bf;
+  if (lb >= 0 && wb - lb <= 4 && li < wi) f = 1;
+  bb = wb;
+  bi = wi;
+  bf = f;
+}
+
+// float32 screening threshold from a squared distance: an upper bound of
+// (fl(sqrt(s)) (1 + (d+4) 2^-53) + B_p) (1 + 2^-40), d <= 64
+__device__ __forceinline__ float thr_sq(double s, float Bp) {
+  const float r = __fsqrt_ru(__double2float_ru(s));  // >= sqrt(s)
+  return __fmul_ru(__fadd_ru(r, Bp), 1.0f + 0x1p-20f);
 }
 
 // (1+2^-24)^(d+2) (1+2^-20) as a float32 rounded up
@@ -146,9 +182,15 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
   __shared__ float vj[64];
   __shared__ float Bj_f;
   __shared__ long long red_bits[kMcThreads / 32], red_idx[kMcThreads / 32];
+  __shared__ int red_flag[kMcThreads / 32];
   __shared__ long long cand_bits[2], cand_idx[2];
+  __shared__ int cand_flag[2];
   __shared__ double cand_x[2][64];  // the CTA candidate's exact coordinates
+  __shared__ long long res_bits[2], res_idx[2];  // exact-root resolution
+  __shared__ double res_x[2][64];
   __shared__ long long s_pivot;
+  __shared__ int s_flag;
+  const bool force_roots = (P.pad & 1) != 0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarp = blockDim.x >> 5;
   const float growth = mc_growth(d);
@@ -181,8 +223,9 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
     const float bj = Bj_f;
     long long best_bits = -1LL;  // below every non-negative double
     long long best_idx = 0x7fffffffffffffffLL;
+    int best_flag = 0;
     for (int p = threadIdx.x; p < S; p += blockDim.x) {
-      double dp = dist[p];
+      double dp = dist[p];  // squared distance
       if (__double_as_longlong(dp) < 0) continue;  // already ordered (ordering.py:50-51)
       const long long gp = p0 + p;
       if (gp == j) {
@@ -197,42 +240,43 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
       const float tb = __fadd_ru(thr[p], bj);
       const float bound = __fmul_ru(__fmul_ru(tb, tb), growth);
       if (!(s32 >= bound)) {
-        // possible update: decide exactly (ordering.py:52-57)
-        const double dj = __dsqrt_rn(sqdist_exact(xs + (int64_t)p * d, xj, d));
-        if (dj < dp) {
-          dp = dj;
-          dist[p] = dj;
-          thr[p] = thr_base(dj, (double)Bp[p], d);
+        // possible update: the reference's squared distance (ordering.py:52-57)
+        const double sn = sqdist_exact(xs + (int64_t)p * d, xj, d);
+        if (__double_as_longlong(sn) < __double_as_longlong(dp)) {
+          dp = sn;
+          dist[p] = sn;
+          thr[p] = thr_sq(sn, Bp[p]);
         }
       }
       const long long bits = __double_as_longlong(dp);
-      if (bits > best_bits && bits <= 0x7ff0000000000000LL) {
-        best_bits = bits;
-        best_idx = gp;
-      }
+      if (bits <= 0x7ff0000000000000LL) cand_merge(bits, gp, 0, best_bits, best_idx, best_flag);
     }
-    // larger distance wins, then the smaller index (np.argmax's first maximum)
     for (int o = 16; o > 0; o >>= 1)
-      cand_better(__shfl_xor_sync(0xffffffffu, best_bits, o), __shfl_xor_sync(0xffffffffu, best_idx, o),
-                  best_bits, best_idx);
+      cand_merge(__shfl_xor_sync(0xffffffffu, best_bits, o), __shfl_xor_sync(0xffffffffu, best_idx, o),
+                 __shfl_xor_sync(0xffffffffu, best_flag, o), best_bits, best_idx, best_flag);
     if (lane == 0) {
       red_bits[warp] = best_bits;
       red_idx[warp] = best_idx;
+      red_flag[warp] = best_flag;
     }
     __syncthreads();
     const int par = (int)(t & 1);
     long long bb = -1LL, bi = 0x7fffffffffffffffLL;
+    int bf = 0;
     if (warp == 0) {
       if (lane < nwarp) {
         bb = red_bits[lane];
         bi = red_idx[lane];
+        bf = red_flag[lane];
       }
       for (int o = 16; o > 0; o >>= 1)
-        cand_better(__shfl_xor_sync(0xffffffffu, bb, o), __shfl_xor_sync(0xffffffffu, bi, o), bb, bi);
+        cand_merge(__shfl_xor_sync(0xffffffffu, bb, o), __shfl_xor_sync(0xffffffffu, bi, o),
+                   __shfl_xor_sync(0xffffffffu, bf, o), bb, bi, bf);
       if (C > 1) {
         if (lane == 0) {
           cand_bits[par] = bb;
           cand_idx[par] = bi;
+          cand_flag[par] = bf;
         }
         if (bi != 0x7fffffffffffffffLL)
           for (int l = lane; l < d; l += 32) cand_x[par][l] = xs[(bi - p0) * d + l];
@@ -246,22 +290,104 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
       if (warp == 0) {
         bb = -1LL;
         bi = 0x7fffffffffffffffLL;
+        bf = 0;
         if (lane < C) {
           bb = cluster.map_shared_rank(cand_bits, lane)[par];
           bi = cluster.map_shared_rank(cand_idx, lane)[par];
+          bf = cluster.map_shared_rank(cand_flag, lane)[par];
         }
         for (int o = 16; o > 0; o >>= 1)
-          cand_better(__shfl_xor_sync(0xffffffffu, bb, o), __shfl_xor_sync(0xffffffffu, bi, o), bb, bi);
+          cand_merge(__shfl_xor_sync(0xffffffffu, bb, o), __shfl_xor_sync(0xffffffffu, bi, o),
+                     __shfl_xor_sync(0xffffffffu, bf, o), bb, bi, bf);
       }
+    }
+    if (threadIdx.x == 0) {
+      s_pivot = bi;
+      s_flag = (bf || force_roots) && bi != 0x7fffffffffffffffLL;
+      red_bits[0] = bb;  // the winner's squared bits for the resolution below
+    }
+    __syncthreads();
+    const double* src = nullptr;  // the winner's exact row (warp 0)
+    if (s_flag) {
+      // exact-root resolution among the points within 4 ulps of the winner
+      const long long wb = red_bits[0];
+      long long rb = -1LL, ri = 0x7fffffffffffffffLL;
+      for (int p = threadIdx.x; p < S; p += blockDim.x) {
+        const long long bits = __double_as_longlong(dist[p]);
+        if (bits < 0 || bits > wb || bits < wb - 4) continue;
+        const long long rbits = __double_as_longlong(__dsqrt_rn(dist[p]));
+        if (rbits > rb || (rbits == rb && p0 + p < ri)) {
+          rb = rbits;
+          ri = p0 + p;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long ob = __shfl_xor_sync(0xffffffffu, rb, o), oi = __shfl_xor_sync(0xffffffffu, ri, o);
+        if (ob > rb || (ob == rb && oi < ri)) {
+          rb = ob;
+          ri = oi;
+        }
+      }
+      __syncthreads();  // red_bits[0] has been read by every thread
+      if (lane == 0) {
+        red_bits[warp] = rb;
+        red_idx[warp] = ri;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        rb = -1LL;
+        ri = 0x7fffffffffffffffLL;
+        if (lane < nwarp) {
+          rb = red_bits[lane];
+          ri = red_idx[lane];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          const long long ob = __shfl_xor_sync(0xffffffffu, rb, o), oi = __shfl_xor_sync(0xffffffffu, ri, o);
+          if (ob > rb || (ob == rb && oi < ri)) {
+            rb = ob;
+            ri = oi;
+          }
+        }
+        if (C > 1) {
+          if (lane == 0) {
+            res_bits[par] = rb;
+            res_idx[par] = ri;
+          }
+          if (ri != 0x7fffffffffffffffLL)
+            for (int l = lane; l < d; l += 32) res_x[par][l] = xs[(ri - p0) * d + l];
+        }
+      }
+      if (C > 1) {
+        cluster.sync();
+        if (warp == 0) {
+          rb = -1LL;
+          ri = 0x7fffffffffffffffLL;
+          if (lane < C) {
+            rb = cluster.map_shared_rank(res_bits, lane)[par];
+            ri = cluster.map_shared_rank(res_idx, lane)[par];
+          }
+          for (int o = 16; o > 0; o >>= 1) {
+            const long long ob = __shfl_xor_sync(0xffffffffu, rb, o), oi = __shfl_xor_sync(0xffffffffu, ri, o);
+            if (ob > rb || (ob == rb && oi < ri)) {
+              rb = ob;
+              ri = oi;
+            }
+          }
+        }
+      }
+      if (warp == 0) {
+        bi = ri;
+        const int owner = (int)(bi / per);
+        src = (C == 1 || owner == r) ? xs + (bi - p0) * d : cluster.map_shared_rank(&res_x[par][0], owner);
+      }
+    } else if (warp == 0 && bi != 0x7fffffffffffffffLL) {
+      const int owner = (int)(bi / per);
+      src = (C == 1 || owner == r) ? xs + (bi - p0) * d : cluster.map_shared_rank(&cand_x[par][0], owner);
     }
     if (warp == 0) {
       if (lane == 0) s_pivot = bi;
       if (bi != 0x7fffffffffffffffLL) {
         if (r == 0 && lane == 0) order[t + 1] = bi;
-        // the winner's exact row: from this CTA's points, or published by its owner
-        const int owner = (int)(bi / per);
-        const double* src = (C == 1 || owner == r) ? xs + (bi - p0) * d
-                                                   : cluster.map_shared_rank(&cand_x[par][0], owner);
         mc_pivot_from(src, d, cen, xj, vj, &Bj_f);
       } else if (r == 0 && lane == 0) {
         // no finite candidate left (NaN inputs): report and stop
@@ -409,6 +535,7 @@ static int ro_plan(const sv_reorder_desc* D, const sv_reorder_prob* hp, RoPlan& 
     R.d = U.d;
     R.q = U.q;
     R.m = U.m;
+    R.pad = U.flags & 1;  // bit 0: resolve every maximin step from exact roots
     R.DP = knn_pad_dim(U.d);
     R.C = mc_cluster_size(U.n, U.d, maxsm);
     if (R.C == 0) return SV_EINVAL;
@@ -418,7 +545,6 @@ static int ro_plan(const sv_reorder_desc* D, const sv_reorder_prob* hp, RoPlan& 
     L.nv += U.n * R.DP;
     R.row_off = L.nrows;
     L.nrows += U.n;
-    R.pad = 0;
     KnnBatchProb& K = L.kprobs[i];
     K.xs_off = R.xs_off + U.n * U.d;
     K.v_off = R.v_off;

@@ -136,7 +136,7 @@ class DeviceProblem:
             n += 1 + (1 if warp else 0) + (1 if cta else 0)
         if split and warp:
             n += 1  # float64 re-evaluation of flagged blocks
-        return n + 4
+        return n + 2 + 4  # status/parameter set-up, then the four reduction kernels
 
     def chunk_tensor(self, Pc):
         if Pc not in self._chunks:
