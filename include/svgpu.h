@@ -96,8 +96,10 @@ typedef struct sv_reorder_prob {
   int64_t blk_off;                 /* likelihood block of row 0              */
   int64_t first;                   /* first row of the ordering (ordering.py:72) */
   int32_t d, q, m;
-  int32_t flags;                   /* bit 0: resolve every maximin step from the
-                                      exact square roots (same result; a test aid) */
+  int32_t flags;                   /* test aids, same orders by other routes: bit 0
+                                      ranks every maximin pivot choice by exact
+                                      roots, bit 1 takes one pivot per pass by a
+                                      full scan */
 } sv_reorder_prob;
 
 typedef struct sv_reorder_desc {

@@ -294,13 +294,14 @@ class BatchedLikelihood:
             self._max_rows[d] = int(self.lib.sv_maximin_cluster_max_rows(d))
         return int(self.n[i]) <= self._max_rows[d]
 
-    def reorder(self, ids, thetas, return_orders=False, exact_roots=False):
+    def reorder(self, ids, thetas, return_orders=False, maximin_flags=0):
         """Rebuild the Vecchia structure of problems ``ids`` at their
         parameters (gp.py:182-191) on the device: scaled inputs, maximin
         order, reordered X/y/Z and neighbour columns.  ``thetas[j]`` belongs
         to ``ids[j]``.  Returns the orders (list of int64 arrays) on request.
-        exact_roots resolves every maximin step from the exact square roots
-        (the result is the same; it exercises that path in tests)."""
+        maximin_flags are test aids that give the same orders by other
+        routes: 1 ranks every choice of pivot by exact square roots, 2 takes
+        one pivot per pass by a full scan of the problem's points."""
         lib, torch = self.lib, self.torch
         ids = [int(i) for i in ids]
         if not ids:
@@ -320,7 +321,7 @@ class BatchedLikelihood:
             P.n, P.xe_off, P.ye_off, P.ze_off = int(self.n[i]), int(self.x_off[i]), int(self.y_off[i]), int(self.z_off[i])
             P.x_off, P.y_off, P.z_off = int(self.x_off[i]), int(self.y_off[i]), int(self.z_off[i])
             P.blk_off, P.first = int(self.blk_off[i]), first
-            P.d, P.q, P.m, P.flags = d, int(self.q[i]), int(self.m[i]), int(bool(exact_roots))
+            P.d, P.q, P.m, P.flags = d, int(self.q[i]), int(self.m[i]), int(maximin_flags) & 3
         D = _lib.ReorderDesc()
         D.nprob, D.dmax, D.ldnbr = len(ids), self.dmax, self.ldnbr
         nbytes = int(lib.sv_reorder_batched_workspace_bytes(D, ctypes.cast(probs, ctypes.c_void_p)))

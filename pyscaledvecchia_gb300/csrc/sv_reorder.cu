@@ -26,14 +26,12 @@
 //    s_stored; an update here that the reference skips has
 //    fl(sqrt(s_new)) == fl(sqrt(s_stored)) and leaves the root unchanged.
 //    No square root is taken on this path;
-//  * argmax: candidates compare squared bits, then indices.  Distinct squares
-//    can round to the same root only within a few ulps, so whenever a loser
-//    within 4 ulps of the winner has a smaller index, the step resolves its
-//    winner again from the exact roots of every point within 4 ulps (one
-//    more cluster exchange; rare).  Per step the CTAs' candidates (distance bits, index)
-// meet through distributed shared memory after one hardware cluster barrier
-// (double-buffered by step parity), so there is no spin-wait at all.
-// Problems are grouped by cluster size (1, 2, 4 or 8 CTAs, the smallest
+//  * argmax: many pivots per pass, each provably the reference's next choice
+//    (the comment above k_maximin_cluster gives the argument); candidate
+//    lists meet through distributed shared memory after one hardware cluster
+//    barrier per pass (double-buffered by pass parity), so there is no
+//    spin-wait at all.
+// Problems are grouped by cluster size (1, 2, 4, 8 or 16 CTAs, the smallest
 // whose shared memory holds the problem), one launch per group, largest
 // problems first.
 #include <cooperative_groups.h>
@@ -48,43 +46,94 @@ namespace cg = cooperative_groups;
 namespace sv {
 
 constexpr int kMcThreads = 512;
-// static shared memory of k_maximin_cluster (3.7 KB), rounded up: the
+constexpr int kMcWarps = kMcThreads / 32;
+constexpr int kMcU = 31;      // candidates per pass: lanes 0..30 of the merged list
+constexpr int kMcSlots = 32;  // candidate slots; slot 31 holds a pivot found by a full scan
+constexpr int kMcNone = 0x7fffffff;
+// static shared memory of k_maximin_cluster (about 1.3 KB), rounded up: the
 // capacity of a cluster is computed from what is left of 227 KB
 constexpr int kMcStaticSmem = 4096;
 constexpr int kMcMaxCluster = 16;
+// work area: the warps' candidate lists (bits + index) or the pair distances
+constexpr int kMcWorkBytes = ((kMcU * kMcU * 8 > kMcWarps * 32 * 12 ? kMcU * kMcU * 8 : kMcWarps * 32 * 12) + 15) & ~15;
 
 struct RoProb {
   int64_t n, xe_off, ye_off, ze_off, x_off, y_off, z_off, blk_off, first;
   int64_t xs_off;   // doubles: this call's scaled rows (and their maximin-order copy)
   int64_t v_off;    // floats: centred float32 rows [n][DP]
   int64_t row_off;  // rows: order, B
-  int32_t d, q, m, DP, C, pad;
+  int32_t d, q, m, DP, C, flags;
 };
 
 // per-point shared memory of the cluster maximin: dist f64, exact coordinates
 // f64[d], thr f32, B f32, float32 centred coordinates f32[d]
 __host__ __device__ inline int64_t mc_point_bytes(int d) { return 16 + 12 * (int64_t)d; }
+// per-CTA shared memory before the points: candidate slots (exact and float32
+// coordinates, squared bits, index, bound) and the work area
+__host__ __device__ inline int64_t mc_fixed_bytes(int d) {
+  return (int64_t)kMcSlots * (12 * d + 16) + kMcWorkBytes;
+}
 
-__device__ __forceinline__ void cand_better(long long ob, long long oi, long long& bb, long long& bi) {
-  if (ob > bb || (ob == bb && oi < bi)) {
-    bb = ob;
-    bi = oi;
+// candidate order: larger squared-distance bits first, then the smaller index
+__device__ __forceinline__ bool mc_greater(long long ab, int ai, long long bb, int bi) {
+  return ab > bb || (ab == bb && ai < bi);
+}
+
+// bitonic sort of one key per lane, descending in mc_greater order
+__device__ __forceinline__ void mc_warp_sort(long long& b, int& i) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const long long ob = __shfl_xor_sync(0xffffffffu, b, j);
+      const int oi = __shfl_xor_sync(0xffffffffu, i, j);
+      const bool take_greater = ((lane & k) == 0) == ((lane & j) == 0);
+      if (mc_greater(ob, oi, b, i) == take_greater) {
+        b = ob;
+        i = oi;
+      }
+    }
+}
+
+// top 32 of two descending lists (own keys and (ob, oi), in lane order),
+// descending; every key left out is below the 32nd key kept
+__device__ __forceinline__ void mc_warp_merge(long long& b, int& i, long long ob, int oi) {
+  const int lane = threadIdx.x & 31;
+  const long long rb = __shfl_sync(0xffffffffu, ob, 31 - lane);
+  const int ri = __shfl_sync(0xffffffffu, oi, 31 - lane);
+  if (mc_greater(rb, ri, b, i)) {
+    b = rb;
+    i = ri;
+  }
+#pragma unroll
+  for (int j = 16; j > 0; j >>= 1) {
+    const long long xb = __shfl_xor_sync(0xffffffffu, b, j);
+    const int xi = __shfl_xor_sync(0xffffffffu, i, j);
+    if (mc_greater(xb, xi, b, i) == ((lane & j) == 0)) {
+      b = xb;
+      i = xi;
+    }
   }
 }
 
-// merge of (squared-distance bits, index, near-tie flag) candidates: larger
-// bits win, then the smaller index; a loser within 4 ulps below the winner
-// with a smaller index may share the winner's square root
-__device__ __forceinline__ void cand_merge(long long ob, long long oi, int of, long long& bb,
-                                           long long& bi, int& bf) {
-  const bool ow = ob > bb || (ob == bb && oi < bi);
-  const long long wb = ow ? ob : bb, wi = ow ? oi : bi;
-  const long long lb = ow ? bb : ob, li = ow ? bi : oi;
-  int f = of | bf;
-  if (lb >= 0 && wb - lb <= 4 && li < wi) f = 1;
-  bb = wb;
-  bi = wi;
-  bf = f;
+// largest key of the warp, in every lane
+__device__ __forceinline__ void mc_warp_max(long long& b, int& i) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long ob = __shfl_xor_sync(0xffffffffu, b, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, i, o);
+    if (mc_greater(ob, oi, b, i)) {
+      b = ob;
+      i = oi;
+    }
+  }
+}
+
+__device__ __forceinline__ long long mc_warp_max_bits(long long b) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+  return b;
 }
 
 // float32 screening threshold from a squared distance: an upper bound of
@@ -92,6 +141,14 @@ __device__ __forceinline__ void cand_merge(long long ob, long long oi, int of, l
 __device__ __forceinline__ float thr_sq(double s, float Bp) {
   const float r = __fsqrt_ru(__double2float_ru(s));  // >= sqrt(s)
   return __fmul_ru(__fadd_ru(r, Bp), 1.0f + 0x1p-20f);
+}
+
+// float32 screen: false only when the pivot cannot lower the stored distance
+// (s32 = float32 squared distance of the centred images, th = the point's
+// threshold, Bj = the pivot's rounding bound)
+__device__ __forceinline__ bool mc_may_update(float s32, float th, float Bj, float growth) {
+  const float tb = __fadd_ru(th, Bj);
+  return !(s32 >= __fmul_ru(__fmul_ru(tb, tb), growth));
 }
 
 // (1+2^-24)^(d+2) (1+2^-20) as a float32 rounded up
@@ -122,43 +179,68 @@ __global__ void k_ro_scale(const RoProb* probs, const double* ranges, int dmax, 
     Xs[P.xs_off + e] = __ddiv_rn(Xe[P.xe_off + e], r[e % d]);
 }
 
-// warp 0: exact pivot row, its float32 image and rounding bound
-__device__ __forceinline__ void mc_load_pivot(const double* X, long long j, int d, const double* cen,
-                                              double* xj, float* vj, float* Bj) {
-  const int lane = threadIdx.x & 31;
-  double e2 = 0.0;
-  for (int l = lane; l < d; l += 32) {
-    const double x = X[j * d + l];
-    const double c = x - cen[l];
-    xj[l] = x;
-    vj[l] = __double2float_rn(c);
-    e2 += c * c;
-  }
-  for (int o = 16; o > 0; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
-  if (lane == 0) *Bj = __double2float_ru(1.01 * 0x1p-24 * sqrt(e2));
+// shared-memory layout of one CTA of the cluster maximin (identical in every
+// CTA of a cluster, so remote reads use the same offsets)
+struct McSmem {
+  double* Ux;      // [32][d] exact coordinates of the candidate slots
+  float* Uv;       // [32][d] their centred float32 images
+  long long* Ub;   // [32] squared-distance bits at the start of the selection
+  int* Ui;         // [32] row index
+  float* UB;       // [32] float32 rounding bound of the image
+  double* pairS;   // [31][31] exact squared distances between candidates (work area)
+  long long* wlb;  // [warps][32] candidate lists (work area)
+  int* wli;
+  double* dist;    // [Sc] squared distance to the ordered set; -1 once ordered
+  double* xs;      // [Sc][d] exact coordinates
+  float* thr;      // [Sc] float32 screening threshold
+  float* Bp;       // [Sc] float32 rounding bound of the image
+  float* v;        // [d][Sc] centred float32 images
+};
+
+__device__ __forceinline__ McSmem mc_layout(unsigned char* base, int d, int Sc) {
+  McSmem L;
+  L.Ux = (double*)base;
+  L.Uv = (float*)(base + (size_t)kMcSlots * 8 * d);
+  L.Ub = (long long*)(base + (size_t)kMcSlots * 12 * d);
+  L.Ui = (int*)(L.Ub + kMcSlots);
+  L.UB = (float*)(L.Ui + kMcSlots);
+  unsigned char* work = base + (size_t)kMcSlots * (12 * d + 16);
+  L.pairS = (double*)work;
+  L.wlb = (long long*)work;
+  L.wli = (int*)(work + kMcWarps * 32 * 8);
+  unsigned char* pts = work + kMcWorkBytes;
+  L.dist = (double*)pts;
+  L.xs = L.dist + Sc;
+  L.thr = (float*)(L.xs + (size_t)Sc * d);
+  L.Bp = L.thr + Sc;
+  L.v = L.Bp + Sc;
+  return L;
 }
 
-// warp 0: pivot row from a row of d doubles (shared or distributed shared memory)
-__device__ __forceinline__ void mc_pivot_from(const double* src, int d, const double* cen, double* xj,
-                                              float* vj, float* Bj) {
-  const int lane = threadIdx.x & 31;
-  double e2 = 0.0;
-  for (int l = lane; l < d; l += 32) {
-    const double x = src[l];
-    const double c = x - cen[l];
-    xj[l] = x;
-    vj[l] = __double2float_rn(c);
-    e2 += c * c;
-  }
-  for (int o = 16; o > 0; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
-  if (lane == 0) *Bj = __double2float_ru(1.01 * 0x1p-24 * sqrt(e2));
-}
-
+// Cluster maximin in passes.  A pass applies a batch of pivots, in order, to
+// every unordered point (the reference's update, ordering.py:49-58, once per
+// pivot), then chooses the next batch:
+//  * the cluster's 31 largest keys (squared bits, then index) form the
+//    candidate set U, and R bounds the squared bits of every other point
+//    (the 32nd key and every thread's third-largest key);
+//  * the exact squared distances between candidates (float32-screened) give
+//    each candidate's value after any pivots taken from U;
+//  * repeatedly the largest surviving candidate is the reference's next
+//    pivot (ordering.py:42-47: largest root, then smallest index) as long as
+//    its squared bits exceed R by more than 4 ulps: distinct squares with
+//    equal roots lie within 3 ulps, so every point outside U then has a
+//    smaller root.  Candidates within 4 ulps of the largest are ranked by
+//    their exact roots;
+//  * if not even the first choice is certain (many near-equal distances, as
+//    on a lattice), every point within 4 ulps of the largest square is ranked
+//    by its exact root across the cluster and one pivot is taken.
+// flags bit 0 ranks every choice by exact roots, bit 1 takes one pivot per
+// pass by the full scan; both give the same order (test aids).
 __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* probs,
                                                                 const int32_t* plist,
                                                                 const double* Xs, int64_t* ord,
                                                                 int32_t* info) {
-  extern __shared__ unsigned char smraw[];
+  extern __shared__ __align__(16) unsigned char smraw[];
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();
   const int r = (int)cluster.block_rank();
@@ -168,235 +250,378 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
   const int d = P.d;
   const double* X = Xs + P.xs_off;
   int64_t* order = ord + P.row_off;
-  const int64_t per = (n + C - 1) / C;
-  const int64_t p0 = (int64_t)r * per;
-  const int64_t p1 = min(n, p0 + per);
-  const int S = (int)max((int64_t)0, p1 - p0);
-  const int Sc = (int)per;
-  double* dist = (double*)smraw;
-  double* xs = dist + Sc;  // exact coordinates of the CTA's points, row-major
-  float* thr = (float*)(xs + (int64_t)Sc * d);
-  float* Bp = thr + Sc;
-  float* v = Bp + Sc;
-  __shared__ double xj[64], cen[64];
-  __shared__ float vj[64];
-  __shared__ float Bj_f;
-  __shared__ long long red_bits[kMcThreads / 32], red_idx[kMcThreads / 32];
-  __shared__ int red_flag[kMcThreads / 32];
-  __shared__ long long cand_bits[2], cand_idx[2];
-  __shared__ int cand_flag[2];
-  __shared__ double cand_x[2][64];  // the CTA candidate's exact coordinates
-  __shared__ long long res_bits[2], res_idx[2];  // exact-root resolution
-  __shared__ double res_x[2][64];
-  __shared__ long long s_pivot;
-  __shared__ int s_flag;
-  const bool force_roots = (P.pad & 1) != 0;
+  const int per = (int)((n + C - 1) / C);
+  const int p0 = r * per;
+  const int S = (int)max((int64_t)0, min(n, (int64_t)p0 + per) - p0);
+  const int Sc = per;
+  const McSmem M = mc_layout(smraw, d, Sc);
+  __shared__ double cen[64];
+  __shared__ long long cl_b[2][32], cl_Kb[2];
+  __shared__ int cl_i[2][32], cl_Ki[2];
+  __shared__ long long w_Kb[kMcWarps];
+  __shared__ int w_Ki[kMcWarps];
+  __shared__ int piv_slot[kMcSlots];
+  __shared__ int s_k, s_tie, s_err, s_Ki;
+  __shared__ long long s_Kb, s_top;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarp = blockDim.x >> 5;
   const float growth = mc_growth(d);
+  const bool roots_always = (P.flags & 1) != 0;
+  const bool scan_always = (P.flags & 2) != 0;
+
+  // the rows of another CTA of the cluster (or this one)
+  auto owner_of = [&](int idx) { return idx / per; };
+  auto rows_of = [&](int owner) -> McSmem {
+    if (C == 1 || owner == r) return M;
+    McSmem O = M;
+    O.xs = cluster.map_shared_rank(M.xs, owner);
+    O.v = cluster.map_shared_rank(M.v, owner);
+    O.Bp = cluster.map_shared_rank(M.Bp, owner);
+    return O;
+  };
+  // candidate slot u <- row idx (warp-cooperative over the coordinates)
+  auto fetch_slot = [&](int u, int idx, int t0, int tstep) {
+    const int owner = owner_of(idx), loc = idx - owner * per;
+    const McSmem O = rows_of(owner);
+    for (int l = t0; l < d; l += tstep) {
+      M.Ux[u * d + l] = O.xs[(size_t)loc * d + l];
+      M.Uv[u * d + l] = O.v[(size_t)l * Sc + loc];
+    }
+    if (t0 == 0) {
+      M.UB[u] = O.Bp[loc];
+      M.Ui[u] = idx;
+    }
+  };
 
   // centre: the first row (any shift serves the float32 screen)
   for (int l = threadIdx.x; l < d; l += blockDim.x) cen[l] = X[P.first * d + l];
   __syncthreads();
-  for (int e = threadIdx.x; e < S * d; e += blockDim.x) xs[e] = X[p0 * d + e];
+  for (int e = threadIdx.x; e < S * d; e += blockDim.x) M.xs[e] = X[(size_t)p0 * d + e];
   for (int p = threadIdx.x; p < S; p += blockDim.x) {
-    const double* xp = X + (p0 + p) * d;
+    const double* xp = X + (size_t)(p0 + p) * d;
     double e2 = 0.0;
     for (int l = 0; l < d; ++l) {
       const double c = xp[l] - cen[l];
-      v[l * Sc + p] = __double2float_rn(c);
+      M.v[(size_t)l * Sc + p] = __double2float_rn(c);
       e2 += c * c;
     }
-    Bp[p] = __double2float_ru(1.01 * 0x1p-24 * sqrt(e2));
-    dist[p] = __longlong_as_double(0x7ff0000000000000LL);  // +inf: first pass is exact
-    thr[p] = __int_as_float(0x7f800000);
+    M.Bp[p] = __double2float_ru(1.01 * 0x1p-24 * sqrt(e2));
+    M.dist[p] = __longlong_as_double(0x7ff0000000000000LL);  // +inf: the first pass is exact
+    M.thr[p] = __int_as_float(0x7f800000);
   }
+  if (C > 1)
+    cluster.sync();  // every CTA's rows are in place before the first remote read
+  else
+    __syncthreads();
+  // the first pivot: row `first` (ordering.py:38-39) in slot 31
+  if (warp == 0) fetch_slot(kMcU, (int)P.first, lane, 32);
   if (threadIdx.x == 0) {
-    s_pivot = P.first;
+    piv_slot[0] = kMcU;
+    s_k = 1;
+    s_err = 0;
+    s_tie = 0;
     if (r == 0) order[0] = P.first;
   }
-  if (warp == 0) mc_load_pivot(X, P.first, d, cen, xj, vj, &Bj_f);
   __syncthreads();
 
-  for (int64_t t = 0; t + 1 < n; ++t) {
-    const long long j = s_pivot;
-    const float bj = Bj_f;
-    long long best_bits = -1LL;  // below every non-negative double
-    long long best_idx = 0x7fffffffffffffffLL;
-    int best_flag = 0;
-    for (int p = threadIdx.x; p < S; p += blockDim.x) {
-      double dp = dist[p];  // squared distance
-      if (__double_as_longlong(dp) < 0) continue;  // already ordered (ordering.py:50-51)
-      const long long gp = p0 + p;
-      if (gp == j) {
-        dist[p] = -1.0;  // ordering.py:58
-        continue;
-      }
-      float s32 = 0.0f;
-      for (int l = 0; l < d; ++l) {
-        const float df = __fsub_rn(v[l * Sc + p], vj[l]);
-        s32 = __fmaf_rn(df, df, s32);
-      }
-      const float tb = __fadd_ru(thr[p], bj);
-      const float bound = __fmul_ru(__fmul_ru(tb, tb), growth);
-      if (!(s32 >= bound)) {
-        // possible update: the reference's squared distance (ordering.py:52-57)
-        const double sn = sqdist_exact(xs + (int64_t)p * d, xj, d);
-        if (__double_as_longlong(sn) < __double_as_longlong(dp)) {
-          dp = sn;
-          dist[p] = sn;
-          thr[p] = thr_sq(sn, Bp[p]);
-        }
-      }
-      const long long bits = __double_as_longlong(dp);
-      if (bits <= 0x7ff0000000000000LL) cand_merge(bits, gp, 0, best_bits, best_idx, best_flag);
-    }
-    for (int o = 16; o > 0; o >>= 1)
-      cand_merge(__shfl_xor_sync(0xffffffffu, best_bits, o), __shfl_xor_sync(0xffffffffu, best_idx, o),
-                 __shfl_xor_sync(0xffffffffu, best_flag, o), best_bits, best_idx, best_flag);
+  // Candidate lists: from every thread's three largest keys (b1 > b2 > b3),
+  // the cluster's 32 largest keys land in slots 0..31 (bits Ub, index Ui) and
+  // (Kb, Ki) is the largest key that may belong to a point outside slots
+  // 0..30: the 32nd key or a thread's third.  The same in every CTA.
+  int par = 0;  // parity of the list buffers, flipped per collection
+  auto collect = [&](long long b1, int i1, long long b2, int i2, long long b3, int i3,
+                     long long& Kb, int& Ki) {
+    mc_warp_sort(b1, i1);
+    mc_warp_sort(b2, i2);
+    mc_warp_merge(b1, i1, b2, i2);
+    mc_warp_max(b3, i3);
+    M.wlb[warp * 32 + lane] = b1;
+    M.wli[warp * 32 + lane] = i1;
     if (lane == 0) {
-      red_bits[warp] = best_bits;
-      red_idx[warp] = best_idx;
-      red_flag[warp] = best_flag;
+      w_Kb[warp] = b3;
+      w_Ki[warp] = i3;
     }
     __syncthreads();
-    const int par = (int)(t & 1);
-    long long bb = -1LL, bi = 0x7fffffffffffffffLL;
-    int bf = 0;
+    // the CTA's list: a tree over the warps
+    for (int s = nwarp >> 1; s >= 1; s >>= 1) {
+      if (warp < s) {
+        mc_warp_merge(b1, i1, M.wlb[(warp + s) * 32 + lane], M.wli[(warp + s) * 32 + lane]);
+        if (s > 1) {
+          M.wlb[warp * 32 + lane] = b1;
+          M.wli[warp * 32 + lane] = i1;
+        }
+      }
+      if (s > 1) __syncthreads();
+    }
+    long long kb = -1LL;
+    int ki = kMcNone;
     if (warp == 0) {
       if (lane < nwarp) {
-        bb = red_bits[lane];
-        bi = red_idx[lane];
-        bf = red_flag[lane];
+        kb = w_Kb[lane];
+        ki = w_Ki[lane];
       }
-      for (int o = 16; o > 0; o >>= 1)
-        cand_merge(__shfl_xor_sync(0xffffffffu, bb, o), __shfl_xor_sync(0xffffffffu, bi, o),
-                   __shfl_xor_sync(0xffffffffu, bf, o), bb, bi, bf);
+      mc_warp_max(kb, ki);
       if (C > 1) {
+        cl_b[par][lane] = b1;
+        cl_i[par][lane] = i1;
         if (lane == 0) {
-          cand_bits[par] = bb;
-          cand_idx[par] = bi;
-          cand_flag[par] = bf;
+          cl_Kb[par] = kb;
+          cl_Ki[par] = ki;
         }
-        if (bi != 0x7fffffffffffffffLL)
-          for (int l = lane; l < d; l += 32) cand_x[par][l] = xs[(bi - p0) * d + l];
       }
     }
     if (C > 1) {
-      // every CTA's candidate of this step is visible after the barrier; the
-      // slots of step t are rewritten at t + 2, after the next barrier, which
-      // no CTA passes before all have read them
+      // the cluster's list: every CTA merges all lists (the same keys, so the
+      // same result everywhere).  A buffer is rewritten two collections on,
+      // after the next cluster barrier, which no CTA passes before all have
+      // read it.
       cluster.sync();
-      if (warp == 0) {
-        bb = -1LL;
-        bi = 0x7fffffffffffffffLL;
-        bf = 0;
-        if (lane < C) {
-          bb = cluster.map_shared_rank(cand_bits, lane)[par];
-          bi = cluster.map_shared_rank(cand_idx, lane)[par];
-          bf = cluster.map_shared_rank(cand_flag, lane)[par];
-        }
-        for (int o = 16; o > 0; o >>= 1)
-          cand_merge(__shfl_xor_sync(0xffffffffu, bb, o), __shfl_xor_sync(0xffffffffu, bi, o),
-                     __shfl_xor_sync(0xffffffffu, bf, o), bb, bi, bf);
-      }
-    }
-    if (threadIdx.x == 0) {
-      s_pivot = bi;
-      s_flag = (bf || force_roots) && bi != 0x7fffffffffffffffLL;
-      red_bits[0] = bb;  // the winner's squared bits for the resolution below
-    }
-    __syncthreads();
-    const double* src = nullptr;  // the winner's exact row (warp 0)
-    if (s_flag) {
-      // exact-root resolution among the points within 4 ulps of the winner
-      const long long wb = red_bits[0];
-      long long rb = -1LL, ri = 0x7fffffffffffffffLL;
-      for (int p = threadIdx.x; p < S; p += blockDim.x) {
-        const long long bits = __double_as_longlong(dist[p]);
-        if (bits < 0 || bits > wb || bits < wb - 4) continue;
-        const long long rbits = __double_as_longlong(__dsqrt_rn(dist[p]));
-        if (rbits > rb || (rbits == rb && p0 + p < ri)) {
-          rb = rbits;
-          ri = p0 + p;
-        }
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        const long long ob = __shfl_xor_sync(0xffffffffu, rb, o), oi = __shfl_xor_sync(0xffffffffu, ri, o);
-        if (ob > rb || (ob == rb && oi < ri)) {
-          rb = ob;
-          ri = oi;
-        }
-      }
-      __syncthreads();  // red_bits[0] has been read by every thread
-      if (lane == 0) {
-        red_bits[warp] = rb;
-        red_idx[warp] = ri;
-      }
-      __syncthreads();
-      if (warp == 0) {
-        rb = -1LL;
-        ri = 0x7fffffffffffffffLL;
-        if (lane < nwarp) {
-          rb = red_bits[lane];
-          ri = red_idx[lane];
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-          const long long ob = __shfl_xor_sync(0xffffffffu, rb, o), oi = __shfl_xor_sync(0xffffffffu, ri, o);
-          if (ob > rb || (ob == rb && oi < ri)) {
-            rb = ob;
-            ri = oi;
+      if (warp == 0)
+        for (int c = 0; c < C; ++c) {
+          if (c == r) continue;
+          mc_warp_merge(b1, i1, cluster.map_shared_rank(&cl_b[par][0], c)[lane],
+                        cluster.map_shared_rank(&cl_i[par][0], c)[lane]);
+          const long long ob = *cluster.map_shared_rank(&cl_Kb[par], c);
+          const int oi = *cluster.map_shared_rank(&cl_Ki[par], c);
+          if (mc_greater(ob, oi, kb, ki)) {
+            kb = ob;
+            ki = oi;
           }
         }
-        if (C > 1) {
-          if (lane == 0) {
-            res_bits[par] = rb;
-            res_idx[par] = ri;
-          }
-          if (ri != 0x7fffffffffffffffLL)
-            for (int l = lane; l < d; l += 32) res_x[par][l] = xs[(ri - p0) * d + l];
-        }
-      }
-      if (C > 1) {
-        cluster.sync();
-        if (warp == 0) {
-          rb = -1LL;
-          ri = 0x7fffffffffffffffLL;
-          if (lane < C) {
-            rb = cluster.map_shared_rank(res_bits, lane)[par];
-            ri = cluster.map_shared_rank(res_idx, lane)[par];
-          }
-          for (int o = 16; o > 0; o >>= 1) {
-            const long long ob = __shfl_xor_sync(0xffffffffu, rb, o), oi = __shfl_xor_sync(0xffffffffu, ri, o);
-            if (ob > rb || (ob == rb && oi < ri)) {
-              rb = ob;
-              ri = oi;
-            }
-          }
-        }
-      }
-      if (warp == 0) {
-        bi = ri;
-        const int owner = (int)(bi / per);
-        src = (C == 1 || owner == r) ? xs + (bi - p0) * d : cluster.map_shared_rank(&res_x[par][0], owner);
-      }
-    } else if (warp == 0 && bi != 0x7fffffffffffffffLL) {
-      const int owner = (int)(bi / per);
-      src = (C == 1 || owner == r) ? xs + (bi - p0) * d : cluster.map_shared_rank(&cand_x[par][0], owner);
     }
     if (warp == 0) {
-      if (lane == 0) s_pivot = bi;
-      if (bi != 0x7fffffffffffffffLL) {
-        if (r == 0 && lane == 0) order[t + 1] = bi;
-        mc_pivot_from(src, d, cen, xj, vj, &Bj_f);
-      } else if (r == 0 && lane == 0) {
-        // no finite candidate left (NaN inputs): report and stop
-        set_error(info + 4 * pid + SV_INFO_STATUS, SV_EINVAL);
-        info[4 * pid + SV_INFO_BLOCK] = (int)t;
+      const long long b32 = __shfl_sync(0xffffffffu, b1, 31);
+      const int i32 = __shfl_sync(0xffffffffu, i1, 31);
+      if (mc_greater(b32, i32, kb, ki)) {
+        kb = b32;
+        ki = i32;
+      }
+      M.Ub[lane] = b1;  // slot 31 is rewritten before any use
+      M.Ui[lane] = i1;
+      if (lane == 0) {
+        s_Kb = kb;
+        s_Ki = ki;
       }
     }
     __syncthreads();
-    if (s_pivot == 0x7fffffffffffffffLL) break;  // the same value in every CTA
+    Kb = s_Kb;
+    Ki = s_Ki;
+    par ^= 1;
+  };
+  // the candidates' rows, then their pairwise exact squared distances
+  // (float32-screened: +inf where neither can lower the other)
+  auto fetch_pairs = [&]() {
+    for (int e = threadIdx.x; e < kMcU * d; e += blockDim.x) {
+      const int u = e / d, l = e - u * d;
+      if (M.Ub[u] < 0) continue;
+      const int idx = M.Ui[u];
+      const int owner = owner_of(idx), loc = idx - owner * per;
+      const McSmem O = rows_of(owner);
+      M.Ux[u * d + l] = O.xs[(size_t)loc * d + l];
+      M.Uv[u * d + l] = O.v[(size_t)l * Sc + loc];
+      if (l == 0) M.UB[u] = O.Bp[loc];
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < kMcU * kMcU; t += blockDim.x) {
+      const int a = t / kMcU, b = t - a * kMcU;
+      if (a >= b || M.Ub[a] < 0 || M.Ub[b] < 0) continue;
+      float s32 = 0.0f;
+      for (int l = 0; l < d; ++l) {
+        const float df = __fsub_rn(M.Uv[a * d + l], M.Uv[b * d + l]);
+        s32 = __fmaf_rn(df, df, s32);
+      }
+      const float ta = thr_sq(__longlong_as_double(M.Ub[a]), M.UB[a]);
+      const float tb = thr_sq(__longlong_as_double(M.Ub[b]), M.UB[b]);
+      double sp = __longlong_as_double(0x7ff0000000000000LL);  // cannot update
+      if (mc_may_update(s32, ta, M.UB[b], growth) || mc_may_update(s32, tb, M.UB[a], growth))
+        sp = sqdist_exact(M.Ux + a * d, M.Ux + b * d, d);  // (x_a - x_b)^2 = (x_b - x_a)^2
+      M.pairS[a * kMcU + b] = sp;
+      M.pairS[b * kMcU + a] = sp;
+    }
+    __syncthreads();
+  };
+  auto insert3 = [](long long b, int i, long long& b1, int& i1, long long& b2, int& i2, long long& b3,
+                    int& i3) {
+    if (mc_greater(b, i, b1, i1)) {
+      b3 = b2;
+      i3 = i2;
+      b2 = b1;
+      i2 = i1;
+      b1 = b;
+      i1 = i;
+    } else if (mc_greater(b, i, b2, i2)) {
+      b3 = b2;
+      i3 = i2;
+      b2 = b;
+      i2 = i;
+    } else if (mc_greater(b, i, b3, i3)) {
+      b3 = b;
+      i3 = i;
+    }
+  };
+
+  int64_t nsel = 1;
+  while (nsel < n) {
+    // 1. apply the pivots to this CTA's points; keep each thread's three
+    //    largest keys
+    const int k = s_k;
+    long long b1 = -1, b2 = -1, b3 = -1;
+    int i1 = kMcNone, i2 = kMcNone, i3 = kMcNone;
+    for (int p = threadIdx.x; p < S; p += blockDim.x) {
+      double dp = M.dist[p];
+      if (__double_as_longlong(dp) < 0) continue;  // ordered (ordering.py:50-51)
+      const int gp = p0 + p;
+      float th = M.thr[p];
+      bool changed = false;
+      for (int t = 0; t < k; ++t) {
+        const int u = piv_slot[t];
+        if (M.Ui[u] == gp) {
+          dp = -1.0;  // ordering.py:58
+          changed = true;
+          break;
+        }
+        const float* vu = M.Uv + u * d;
+        float s32 = 0.0f;
+        for (int l = 0; l < d; ++l) {
+          const float df = __fsub_rn(M.v[(size_t)l * Sc + p], vu[l]);
+          s32 = __fmaf_rn(df, df, s32);
+        }
+        if (mc_may_update(s32, th, M.UB[u], growth)) {
+          // the reference's squared distance (ordering.py:52-57)
+          const double sn = sqdist_exact(M.xs + (size_t)p * d, M.Ux + u * d, d);
+          if (__double_as_longlong(sn) < __double_as_longlong(dp)) {
+            dp = sn;
+            th = thr_sq(sn, M.Bp[p]);
+            changed = true;
+          }
+        }
+      }
+      if (changed) {
+        M.dist[p] = dp;
+        M.thr[p] = th;
+      }
+      const long long b = __double_as_longlong(dp);
+      if (b < 0 || b >= 0x7ff0000000000000LL) continue;  // ordered, or not finite
+      insert3(b, gp, b1, i1, b2, i2, b3, i3);
+    }
+    // 2. candidates U = slots 0..30; R bounds every other point's bits
+    long long R;
+    int Ri;
+    collect(b1, i1, b2, i2, b3, i3, R, Ri);
+    fetch_pairs();
+    // 3. pivots from the candidates (warp 0, one candidate per lane)
+    if (warp == 0) {
+      long long sb = lane < kMcU ? M.Ub[lane] : -1LL;
+      const int si = lane < kMcU ? M.Ui[lane] : kMcNone;
+      bool alive = sb >= 0;
+      long long top = sb;  // lane 0: the largest square
+      top = __shfl_sync(0xffffffffu, top, 0);
+      int kk = 0;
+      while (!scan_always && kk < kMcU && nsel + kk < n) {
+        long long mb = alive ? sb : -1LL;
+        int mi = alive ? si : kMcNone;
+        mc_warp_max(mb, mi);
+        if (mb < 0 || !(R < 0 || mb > R + 4)) break;  // none left, or not certain
+        const unsigned nearm = __ballot_sync(0xffffffffu, alive && sb >= mb - 4 && si < mi);
+        if (nearm || roots_always) {
+          // equal roots: the smaller index (ordering.py:45 keeps the first maximum)
+          long long rb = -1LL;
+          int ri = kMcNone;
+          if (alive && sb >= mb - 4) {
+            rb = __double_as_longlong(__dsqrt_rn(__longlong_as_double(sb)));
+            ri = si;
+          }
+          mc_warp_max(rb, ri);
+          mi = ri;
+        }
+        const int ws = __ffs(__ballot_sync(0xffffffffu, alive && si == mi)) - 1;
+        if (lane == 0) piv_slot[kk] = ws;
+        if (lane == ws) alive = false;
+        if (alive) {
+          const long long sn = __double_as_longlong(M.pairS[lane * kMcU + ws]);
+          if (sn < sb) sb = sn;
+        }
+        ++kk;
+      }
+      if (lane == 0) {
+        s_k = kk;
+        s_tie = kk == 0;
+        s_top = top;
+        if (r == 0)
+          for (int t = 0; t < kk; ++t) order[nsel + t] = M.Ui[piv_slot[t]];
+      }
+    }
+    __syncthreads();
+    if (s_tie) {
+      // 4. tie pass: no choice was certain, so many squares lie within 4 ulps
+      //    of the largest, top.  The largest root is fl(sqrt(top)); the points
+      //    with that root, T, are the reference's next choices in index order
+      //    (ordering.py:45) while they keep it.  Slots 0..30 take the 31
+      //    smallest indices of T; any other member of T has an index >= the
+      //    bound Ki.
+      const long long top = s_top;
+      if (top < 0) {
+        // no finite candidate left (NaN inputs): report and stop
+        if (threadIdx.x == 0) {
+          s_err = 1;
+          if (r == 0) {
+            set_error(info + 4 * pid + SV_INFO_STATUS, SV_EINVAL);
+            info[4 * pid + SV_INFO_BLOCK] = (int)nsel;
+          }
+        }
+      } else {
+        const long long rmax = __double_as_longlong(__dsqrt_rn(__longlong_as_double(top)));
+        b1 = b2 = b3 = -1;
+        i1 = i2 = i3 = kMcNone;
+        for (int p = threadIdx.x; p < S; p += blockDim.x) {
+          const double dp = M.dist[p];
+          const long long bits = __double_as_longlong(dp);
+          if (bits < 0 || bits > top || bits < top - 4) continue;
+          if (__double_as_longlong(__dsqrt_rn(dp)) != rmax) continue;
+          // key: the smaller index first; the low 3 bits carry top - bits
+          insert3(((1LL << 40) - (p0 + p)) * 8 + (top - bits), p0 + p, b1, i1, b2, i2, b3, i3);
+        }
+        long long Kb;
+        int Ki;
+        collect(b1, i1, b2, i2, b3, i3, Kb, Ki);
+        const int bound = Kb >= 0 ? Ki : kMcNone;
+        // the slots' squares from their keys
+        if (threadIdx.x < kMcU && M.Ub[threadIdx.x] >= 0) M.Ub[threadIdx.x] = top - (M.Ub[threadIdx.x] & 7);
+        __syncthreads();
+        fetch_pairs();
+        if (warp == 0) {
+          long long sb = lane < kMcU ? M.Ub[lane] : -1LL;
+          const int si = lane < kMcU ? M.Ui[lane] : kMcNone;
+          bool alive = sb >= 0, tied = alive;
+          int kk = 0;
+          while (kk < kMcU && nsel + kk < n) {
+            int mi = alive && tied ? si : kMcNone;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mi = min(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+            if (mi == kMcNone || mi >= bound) break;
+            const int ws = __ffs(__ballot_sync(0xffffffffu, alive && si == mi)) - 1;
+            if (lane == 0) piv_slot[kk] = ws;
+            if (lane == ws) alive = false;
+            if (alive) {
+              const double sn = M.pairS[lane * kMcU + ws];
+              if (__double_as_longlong(sn) < sb) {
+                sb = __double_as_longlong(sn);
+                if (tied) tied = __double_as_longlong(__dsqrt_rn(sn)) == rmax;
+              }
+            }
+            ++kk;
+          }
+          if (lane == 0) {
+            s_k = kk;
+            if (r == 0)
+              for (int t = 0; t < kk; ++t) order[nsel + t] = M.Ui[piv_slot[t]];
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (s_err) break;  // the same value in every CTA
+    nsel += s_k;
   }
   // keep this CTA's shared memory alive until every remote read is done
   if (C > 1) cluster.sync();
@@ -490,7 +715,7 @@ static int mc_max_cluster() {
 
 // cluster size for n rows of dimension d: 1, 2, 4, 8 (or 16), or 0 when none fits
 static int mc_cluster_size(int64_t n, int d, int maxsm) {
-  const int64_t budget = (int64_t)maxsm - kMcStaticSmem;
+  const int64_t budget = (int64_t)maxsm - kMcStaticSmem - mc_fixed_bytes(d);
   const int cmax = mc_max_cluster();
   for (int C = 1; C <= cmax; C *= 2) {
     const int64_t per = (n + C - 1) / C;
@@ -535,7 +760,7 @@ static int ro_plan(const sv_reorder_desc* D, const sv_reorder_prob* hp, RoPlan& 
     R.d = U.d;
     R.q = U.q;
     R.m = U.m;
-    R.pad = U.flags & 1;  // bit 0: resolve every maximin step from exact roots
+    R.flags = U.flags & 3;  // maximin test aids: exact roots always (1), full scans (2)
     R.DP = knn_pad_dim(U.d);
     R.C = mc_cluster_size(U.n, U.d, maxsm);
     if (R.C == 0) return SV_EINVAL;
@@ -564,7 +789,8 @@ static int ro_plan(const sv_reorder_desc* D, const sv_reorder_prob* hp, RoPlan& 
     if (R.n < 1) continue;
     const int g = R.C == 1 ? 0 : R.C == 2 ? 1 : R.C == 4 ? 2 : R.C == 8 ? 3 : 4;
     L.plist[g].push_back(i);
-    const size_t sm = (size_t)((R.n + R.C - 1) / R.C) * (size_t)mc_point_bytes(R.d);
+    const size_t sm = (size_t)((R.n + R.C - 1) / R.C) * (size_t)mc_point_bytes(R.d) +
+                      (size_t)mc_fixed_bytes(R.d);
     L.smem[g] = std::max(L.smem[g], sm);
     if (R.m < 1 || R.n < 2) continue;
     int gi = 0;
@@ -639,14 +865,14 @@ int maximin_cluster_single(const double* X, int64_t n, int d, int64_t first, int
   h.p.d = d;
   h.p.C = C;
   SV_CUDA_TRY(cudaMemcpyAsync(ws, &h, sizeof(h), cudaMemcpyHostToDevice, st));
-  const size_t smem = (size_t)((n + C - 1) / C) * (size_t)mc_point_bytes(d);
+  const size_t smem = (size_t)((n + C - 1) / C) * (size_t)mc_point_bytes(d) + (size_t)mc_fixed_bytes(d);
   return launch_maximin_cluster(C, smem, 1, (const RoProb*)ws, (const int32_t*)(ws + sizeof(RoProb)),
                                 X, order, info, st);
 }
 
 int64_t maximin_cluster_max_rows(int d) {
   if (d < 1 || d > 64) return 0;
-  const int64_t budget = (int64_t)ro_max_smem() - kMcStaticSmem;
+  const int64_t budget = (int64_t)ro_max_smem() - kMcStaticSmem - mc_fixed_bytes(d);
   return (int64_t)mc_max_cluster() * (budget / mc_point_bytes(d));
 }
 

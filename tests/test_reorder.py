@@ -72,17 +72,19 @@ def test_batched_reorder_matches_single_problem_path():
         np.testing.assert_array_equal(got, want)
 
 
-def test_exact_root_resolution_gives_the_same_orders():
-    """Resolving every maximin step from the exact square roots (the path
-    the kernel takes when two candidates' squared distances lie within a few
-    ulps) gives the same orders as the squared-distance comparisons."""
+@pytest.mark.parametrize("flags", [1, 2])
+def test_other_maximin_routes_give_the_same_orders(flags):
+    """Ranking every pivot choice by exact square roots (the route taken when
+    candidates' squared distances lie within a few ulps) and taking one pivot
+    per pass by a full scan (the route taken when no batch of pivots is
+    certain) give the same orders as the default passes."""
     from pyscaledvecchia_gb300.batched import BatchedLikelihood
     probs, raw, thetas = _problems()
     BL = BatchedLikelihood(probs)
     BL.set_sources([r[0] for r in raw], [r[1] for r in raw], [r[2] for r in raw], [r[3] for r in raw])
     ids = list(range(len(probs)))
     a = BL.reorder(ids, thetas, return_orders=True)
-    b = BL.reorder(ids, thetas, return_orders=True, exact_roots=True)
+    b = BL.reorder(ids, thetas, return_orders=True, maximin_flags=flags)
     for i, (x, y) in enumerate(zip(a, b)):
         np.testing.assert_array_equal(x, y)
         order, _ = _expected(*raw[i], thetas[i])
@@ -91,7 +93,7 @@ def test_exact_root_resolution_gives_the_same_orders():
 
 def test_lattice_ties_through_the_cluster_kernel(oracle):
     """Exact ties (a lattice) and duplicates through the cluster maximin,
-    plain and with exact-root resolution, against the oracle."""
+    by every route, against the oracle."""
     from pyscaledvecchia_gb300.batched import BatchedLikelihood, BatchProblem, ordered_groups
     g = np.arange(30, dtype=float)
     X = np.array([[a, b] for a in g for b in g])
@@ -100,8 +102,8 @@ def test_lattice_ties_through_the_cluster_kernel(oracle):
     BL = BatchedLikelihood([BatchProblem(X, np.zeros(n), None, ordered_groups(n, 5))])
     BL.set_sources([X], [np.zeros(n)], [None], [5])
     ref = oracle.maximin_order(X)
-    for exact in (False, True):
-        o = BL.reorder([0], [np.zeros(4)], return_orders=True, exact_roots=exact)[0]
+    for flags in (0, 1, 2):
+        o = BL.reorder([0], [np.zeros(4)], return_orders=True, maximin_flags=flags)[0]
         np.testing.assert_array_equal(o, ref)
 
 
