@@ -68,10 +68,12 @@ struct RoProb {
 // per-point shared memory of the cluster maximin: dist f64, exact coordinates
 // f64[d], thr f32, B f32, float32 centred coordinates f32[d]
 __host__ __device__ inline int64_t mc_point_bytes(int d) { return 16 + 12 * (int64_t)d; }
+// width of the pivot images held in registers (zero padded)
+__host__ __device__ inline int mc_dv(int d) { return d <= 4 ? 4 : d <= 8 ? 8 : d <= 16 ? 16 : d <= 32 ? 32 : 64; }
 // per-CTA shared memory before the points: candidate slots (exact and float32
-// coordinates, squared bits, index, bound) and the work area
+// coordinates, squared bits, index, bound), the pivot images and the work area
 __host__ __device__ inline int64_t mc_fixed_bytes(int d) {
-  return (int64_t)kMcSlots * (12 * d + 16) + kMcWorkBytes;
+  return (int64_t)kMcSlots * (12 * d + 16) + (int64_t)kMcSlots * 4 * mc_dv(d) + kMcWorkBytes;
 }
 
 // candidate order: larger squared-distance bits first, then the smaller index
@@ -79,19 +81,26 @@ __device__ __forceinline__ bool mc_greater(long long ab, int ai, long long bb, i
   return ab > bb || (ab == bb && ai < bi);
 }
 
-// bitonic sort of one key per lane, descending in mc_greater order
-__device__ __forceinline__ void mc_warp_sort(long long& b, int& i) {
+// two bitonic sorts of one key per lane, descending in mc_greater order, at
+// once (independent chains, one latency)
+__device__ __forceinline__ void mc_warp_sort2(long long& b, int& i, long long& c, int& j) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int k = 2; k <= 32; k <<= 1)
 #pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      const long long ob = __shfl_xor_sync(0xffffffffu, b, j);
-      const int oi = __shfl_xor_sync(0xffffffffu, i, j);
-      const bool take_greater = ((lane & k) == 0) == ((lane & j) == 0);
+    for (int s = k >> 1; s > 0; s >>= 1) {
+      const long long ob = __shfl_xor_sync(0xffffffffu, b, s);
+      const int oi = __shfl_xor_sync(0xffffffffu, i, s);
+      const long long oc = __shfl_xor_sync(0xffffffffu, c, s);
+      const int oj = __shfl_xor_sync(0xffffffffu, j, s);
+      const bool take_greater = ((lane & k) == 0) == ((lane & s) == 0);
       if (mc_greater(ob, oi, b, i) == take_greater) {
         b = ob;
         i = oi;
+      }
+      if (mc_greater(oc, oj, c, j) == take_greater) {
+        c = oc;
+        j = oj;
       }
     }
 }
@@ -151,6 +160,14 @@ __device__ __forceinline__ bool mc_may_update(float s32, float th, float Bj, flo
   return !(s32 >= __fmul_ru(__fmul_ru(tb, tb), growth));
 }
 
+// upper bound of the exact squared distance (ordering.py:52-57) between two
+// rows from their images' float32 squared distance s32 and rounding bounds
+// Ba, Bb: (sqrt(s32 growth^2) + Ba + Bb)^2 (1 + 2^-20), rounded up
+__device__ __forceinline__ float mc_sq_upper(float s32, float Ba, float Bb, float growth) {
+  const float t = __fadd_ru(__fadd_ru(__fsqrt_ru(__fmul_ru(__fmul_ru(s32, growth), growth)), Ba), Bb);
+  return __fmul_ru(__fmul_ru(t, t), 1.0f + 0x1p-20f);
+}
+
 // (1+2^-24)^(d+2) (1+2^-20) as a float32 rounded up
 __device__ __forceinline__ float mc_growth(int d) {
   double g = 1.0;
@@ -187,6 +204,7 @@ struct McSmem {
   long long* Ub;   // [32] squared-distance bits at the start of the selection
   int* Ui;         // [32] row index
   float* UB;       // [32] float32 rounding bound of the image
+  float* Pv;       // [32][DV] images of this pass's pivots, zero padded to DV
   double* pairS;   // [31][31] exact squared distances between candidates (work area)
   long long* wlb;  // [warps][32] candidate lists (work area)
   int* wli;
@@ -204,7 +222,8 @@ __device__ __forceinline__ McSmem mc_layout(unsigned char* base, int d, int Sc) 
   L.Ub = (long long*)(base + (size_t)kMcSlots * 12 * d);
   L.Ui = (int*)(L.Ub + kMcSlots);
   L.UB = (float*)(L.Ui + kMcSlots);
-  unsigned char* work = base + (size_t)kMcSlots * (12 * d + 16);
+  L.Pv = (float*)(base + (size_t)kMcSlots * (12 * d + 16));
+  unsigned char* work = (unsigned char*)(L.Pv + kMcSlots * mc_dv(d));
   L.pairS = (double*)work;
   L.wlb = (long long*)work;
   L.wli = (int*)(work + kMcWarps * 32 * 8);
@@ -215,6 +234,189 @@ __device__ __forceinline__ McSmem mc_layout(unsigned char* base, int d, int Sc) 
   L.Bp = L.thr + Sc;
   L.v = L.Bp + Sc;
   return L;
+}
+
+// keep the three largest keys b1 > b2 > b3 (mc_greater order)
+__device__ __forceinline__ void mc_insert3(long long b, int i, long long& b1, int& i1, long long& b2,
+                                           int& i2, long long& b3, int& i3) {
+  if (mc_greater(b, i, b1, i1)) {
+    b3 = b2;
+    i3 = i2;
+    b2 = b1;
+    i2 = i1;
+    b1 = b;
+    i1 = i;
+  } else if (mc_greater(b, i, b2, i2)) {
+    b3 = b2;
+    i3 = i2;
+    b2 = b;
+    i2 = i;
+  } else if (mc_greater(b, i, b3, i3)) {
+    b3 = b;
+    i3 = i;
+  }
+}
+
+// exact squared distances (ordering.py:52-57) of the pivots in `mask`, in
+// pivot order, lower point p's distance; its threshold follows
+__device__ __forceinline__ void mc_exact(const McSmem& M, const int* Ps, int p, int d, unsigned mask) {
+  const double* xp = M.xs + (size_t)p * d;
+  double dp = M.dist[p];
+  const long long b0 = __double_as_longlong(dp);
+  do {
+    const int t = __ffs(mask) - 1;
+    mask &= mask - 1;
+    const double sn = sqdist_exact(xp, M.Ux + Ps[t] * d, d);
+    if (__double_as_longlong(sn) < __double_as_longlong(dp)) dp = sn;
+  } while (mask);
+  if (__double_as_longlong(dp) != b0) {
+    M.dist[p] = dp;
+    M.thr[p] = thr_sq(dp, M.Bp[p]);
+  }
+}
+
+// float32 squared distance of a register image to pivot image t
+template <int DV>
+__device__ __forceinline__ float mc_s32(const float (&vp)[DV], const float4* pv) {
+  float s32 = 0.0f;
+#pragma unroll
+  for (int q = 0; q < DV / 4; ++q) {
+    const float4 f = pv[q];
+    float df = __fsub_rn(vp[4 * q], f.x);
+    s32 = __fmaf_rn(df, df, s32);
+    df = __fsub_rn(vp[4 * q + 1], f.y);
+    s32 = __fmaf_rn(df, df, s32);
+    df = __fsub_rn(vp[4 * q + 2], f.z);
+    s32 = __fmaf_rn(df, df, s32);
+    df = __fsub_rn(vp[4 * q + 3], f.w);
+    s32 = __fmaf_rn(df, df, s32);
+  }
+  return s32;
+}
+
+// queue of (point, pivot mask) for the exact distances, in the work area
+constexpr int kMcQueue = kMcWorkBytes / 8;
+
+// after the screen of point p: ordered if it is a pivot of this pass
+// (ordering.py:58); else the pivots in `mask` go to the queue (processed by
+// dense warps: a float64 warp instruction costs the same with one lane
+// active as with 32), or are applied here when the queue is full
+__device__ __forceinline__ void mc_screened(const McSmem& M, const int* Ps, int* qn, int p, int d,
+                                            bool hit, unsigned mask) {
+  if (hit) {
+    M.dist[p] = -1.0;
+    mask = 0;
+  }
+  const unsigned act = __activemask();
+  const unsigned want = __ballot_sync(act, mask != 0);
+  if (!want) return;
+  const int leader = __ffs(want) - 1;
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(qn, __popc(want));
+  base = __shfl_sync(act, base, leader);
+  if (mask) {
+    const int slot = base + __popc(want & ((1u << lane) - 1));
+    if (slot < kMcQueue) {
+      int2* q = reinterpret_cast<int2*>(M.pairS);
+      q[slot] = make_int2(p, (int)mask);
+    } else {
+      mc_exact(M, Ps, p, d, mask);
+    }
+  }
+}
+
+// This pass's pivots (table entries t < k: row Pi, bound PB, image Pv, slot
+// Ps of the exact coordinates) applied to the CTA's points, then each
+// thread's three largest keys.  For every point the float32 screen runs over
+// all pivots first, with the threshold of the pass start (an upper bound of
+// every later one, so a pivot it skips cannot update); the exact squared
+// distances of the pivots left then update in pivot order, as the reference
+// applies them (ordering.py:49-58).  DV: the image width held in registers
+// (0: read from shared memory, any d); up to 16, two points share each
+// read of a pivot image.
+template <int DV>
+__device__ __forceinline__ void mc_apply(const McSmem& M, const int* Pi, const float* PB,
+                                         const int* Ps, int* qn, int k, int S, int Sc, int d,
+                                         int p0, float growth, long long& b1, int& i1,
+                                         long long& b2, int& i2, long long& b3, int& i3) {
+  if constexpr (DV > 0 && DV <= 16) {
+    const int T = blockDim.x;
+    for (int p = threadIdx.x; p < S; p += 2 * T) {
+      const int q = p + T;
+      const bool liveA = __double_as_longlong(M.dist[p]) >= 0;
+      const bool liveB = q < S && __double_as_longlong(M.dist[q]) >= 0;
+      if (!liveA && !liveB) continue;  // ordered (ordering.py:50-51)
+      const float thA = M.thr[p], thB = liveB ? M.thr[q] : 0.0f;
+      float va[DV], vb[DV];
+#pragma unroll
+      for (int l = 0; l < DV; ++l) {
+        va[l] = l < d ? M.v[(size_t)l * Sc + p] : 0.0f;
+        vb[l] = l < d && liveB ? M.v[(size_t)l * Sc + q] : 0.0f;
+      }
+      unsigned mA = 0, mB = 0;
+      bool hA = false, hB = false;
+#pragma unroll 2
+      for (int t = 0; t < k; ++t) {
+        const float4* pv = reinterpret_cast<const float4*>(M.Pv + t * DV);
+        const float sA = mc_s32<DV>(va, pv), sB = mc_s32<DV>(vb, pv);
+        const int pi = Pi[t];
+        const float pb = PB[t];
+        hA = hA || pi == p0 + p;
+        hB = hB || pi == p0 + q;
+        if (mc_may_update(sA, thA, pb, growth)) mA |= 1u << t;
+        if (mc_may_update(sB, thB, pb, growth)) mB |= 1u << t;
+      }
+      mc_screened(M, Ps, qn, p, d, hA, liveA ? mA : 0u);
+      if (liveB) mc_screened(M, Ps, qn, q, d, hB, mB);
+    }
+  } else {
+    constexpr int W = DV > 0 ? DV : 64;
+    for (int p = threadIdx.x; p < S; p += blockDim.x) {
+      if (__double_as_longlong(M.dist[p]) < 0) continue;  // ordered (ordering.py:50-51)
+      const float th = M.thr[p];
+      unsigned mask = 0;
+      bool hit = false;
+      if constexpr (DV > 0) {
+        float vp[DV];
+#pragma unroll
+        for (int l = 0; l < DV; ++l) vp[l] = l < d ? M.v[(size_t)l * Sc + p] : 0.0f;
+#pragma unroll 2
+        for (int t = 0; t < k; ++t) {
+          const float s32 = mc_s32<DV>(vp, reinterpret_cast<const float4*>(M.Pv + t * DV));
+          hit = hit || Pi[t] == p0 + p;
+          if (mc_may_update(s32, th, PB[t], growth)) mask |= 1u << t;
+        }
+      } else {
+        for (int t = 0; t < k; ++t) {
+          const float* pv = M.Pv + t * W;
+          float s32 = 0.0f;
+          for (int l = 0; l < d; ++l) {
+            const float df = __fsub_rn(M.v[(size_t)l * Sc + p], pv[l]);
+            s32 = __fmaf_rn(df, df, s32);
+          }
+          hit = hit || Pi[t] == p0 + p;
+          if (mc_may_update(s32, th, PB[t], growth)) mask |= 1u << t;
+        }
+      }
+      mc_screened(M, Ps, qn, p, d, hit, mask);
+    }
+  }
+  __syncthreads();
+  // the queued exact distances, densely
+  const int nq = min(*qn, kMcQueue);
+  const int2* q = reinterpret_cast<const int2*>(M.pairS);
+  for (int e = threadIdx.x; e < nq; e += blockDim.x) {
+    const int2 E = q[e];
+    mc_exact(M, Ps, E.x, d, (unsigned)E.y);
+  }
+  __syncthreads();
+  // each thread's three largest keys, its points in index order
+  for (int p = threadIdx.x; p < S; p += blockDim.x) {
+    const long long b = __double_as_longlong(M.dist[p]);
+    if (b < 0 || b >= 0x7ff0000000000000LL) continue;  // ordered, or not finite
+    mc_insert3(b, p0 + p, b1, i1, b2, i2, b3, i3);
+  }
 }
 
 // Cluster maximin in passes.  A pass applies a batch of pivots, in order, to
@@ -232,11 +434,11 @@ __device__ __forceinline__ McSmem mc_layout(unsigned char* base, int d, int Sc) 
 //    smaller root.  Candidates within 4 ulps of the largest are ranked by
 //    their exact roots;
 //  * if not even the first choice is certain (many near-equal distances, as
-//    on a lattice), every point within 4 ulps of the largest square is ranked
-//    by its exact root across the cluster and one pivot is taken.
-// flags bit 0 ranks every choice by exact roots, bit 1 takes one pivot per
-// pass by the full scan; both give the same order (test aids).
-__global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* probs,
+//    on a lattice), a tie pass takes the points whose root equals the largest
+//    root, in index order.
+// flags bit 0 ranks every choice by exact roots, bit 1 runs a tie pass every
+// time; both give the same order (test aids).
+__global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb* probs,
                                                                 const int32_t* plist,
                                                                 const double* Xs, int64_t* ord,
                                                                 int32_t* info) {
@@ -248,6 +450,7 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
   const RoProb& P = probs[pid];
   const int64_t n = P.n;
   const int d = P.d;
+  const int DV = mc_dv(d);
   const double* X = Xs + P.xs_off;
   int64_t* order = ord + P.row_off;
   const int per = (int)((n + C - 1) / C);
@@ -260,8 +463,9 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
   __shared__ int cl_i[2][32], cl_Ki[2];
   __shared__ long long w_Kb[kMcWarps];
   __shared__ int w_Ki[kMcWarps];
-  __shared__ int piv_slot[kMcSlots];
-  __shared__ int s_k, s_tie, s_err, s_Ki;
+  __shared__ int piv_slot[kMcSlots], P_i[kMcSlots], P_s[kMcSlots];
+  __shared__ float P_B[kMcSlots], Uthr[kMcSlots];
+  __shared__ int s_k, s_tie, s_err, s_Ki, s_qn;
   __shared__ long long s_Kb, s_top;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarp = blockDim.x >> 5;
@@ -279,18 +483,21 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
     O.Bp = cluster.map_shared_rank(M.Bp, owner);
     return O;
   };
-  // candidate slot u <- row idx (warp-cooperative over the coordinates)
-  auto fetch_slot = [&](int u, int idx, int t0, int tstep) {
-    const int owner = owner_of(idx), loc = idx - owner * per;
-    const McSmem O = rows_of(owner);
-    for (int l = t0; l < d; l += tstep) {
-      M.Ux[u * d + l] = O.xs[(size_t)loc * d + l];
-      M.Uv[u * d + l] = O.v[(size_t)l * Sc + loc];
+  // warp 0: the pivot table from slots piv_slot[0..kk)
+  auto build_pivots = [&](int kk) {
+    __syncwarp();
+    for (int e = lane; e < kk * DV; e += 32) {
+      const int t = e / DV, l = e - t * DV;
+      M.Pv[e] = l < d ? M.Uv[piv_slot[t] * d + l] : 0.0f;
     }
-    if (t0 == 0) {
-      M.UB[u] = O.Bp[loc];
-      M.Ui[u] = idx;
+    if (lane < kk) {
+      const int u = piv_slot[lane];
+      P_i[lane] = M.Ui[u];
+      P_B[lane] = M.UB[u];
+      P_s[lane] = u;
     }
+    if (lane == 0) s_qn = 0;
+    __syncwarp();
   };
 
   // centre: the first row (any shift serves the float32 screen)
@@ -314,13 +521,24 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
   else
     __syncthreads();
   // the first pivot: row `first` (ordering.py:38-39) in slot 31
-  if (warp == 0) fetch_slot(kMcU, (int)P.first, lane, 32);
-  if (threadIdx.x == 0) {
-    piv_slot[0] = kMcU;
-    s_k = 1;
-    s_err = 0;
-    s_tie = 0;
-    if (r == 0) order[0] = P.first;
+  if (warp == 0) {
+    const int idx = (int)P.first;
+    const int owner = owner_of(idx), loc = idx - owner * per;
+    const McSmem O = rows_of(owner);
+    for (int l = lane; l < d; l += 32) {
+      M.Ux[kMcU * d + l] = O.xs[(size_t)loc * d + l];
+      M.Uv[kMcU * d + l] = O.v[(size_t)l * Sc + loc];
+    }
+    if (lane == 0) {
+      M.UB[kMcU] = O.Bp[loc];
+      M.Ui[kMcU] = idx;
+      piv_slot[0] = kMcU;
+      s_k = 1;
+      s_err = 0;
+      s_tie = 0;
+      if (r == 0) order[0] = P.first;
+    }
+    build_pivots(1);
   }
   __syncthreads();
 
@@ -331,8 +549,7 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
   int par = 0;  // parity of the list buffers, flipped per collection
   auto collect = [&](long long b1, int i1, long long b2, int i2, long long b3, int i3,
                      long long& Kb, int& Ki) {
-    mc_warp_sort(b1, i1);
-    mc_warp_sort(b2, i2);
+    mc_warp_sort2(b1, i1, b2, i2);
     mc_warp_merge(b1, i1, b2, i2);
     mc_warp_max(b3, i3);
     M.wlb[warp * 32 + lane] = b1;
@@ -342,17 +559,20 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
       w_Ki[warp] = i3;
     }
     __syncthreads();
-    // the CTA's list: a tree over the warps
-    for (int s = nwarp >> 1; s >= 1; s >>= 1) {
-      if (warp < s) {
-        mc_warp_merge(b1, i1, M.wlb[(warp + s) * 32 + lane], M.wli[(warp + s) * 32 + lane]);
-        if (s > 1) {
-          M.wlb[warp * 32 + lane] = b1;
-          M.wli[warp * 32 + lane] = i1;
+    // a tree over the lists wlb[0..m): warp w < s merges list w + s
+    auto tree = [&](int m) {
+      for (int s = m >> 1; s >= 1; s >>= 1) {
+        if (warp < s) {
+          mc_warp_merge(b1, i1, M.wlb[(warp + s) * 32 + lane], M.wli[(warp + s) * 32 + lane]);
+          if (s > 1) {
+            M.wlb[warp * 32 + lane] = b1;
+            M.wli[warp * 32 + lane] = i1;
+          }
         }
+        if (s > 1) __syncthreads();
       }
-      if (s > 1) __syncthreads();
-    }
+    };
+    tree(nwarp);
     long long kb = -1LL;
     int ki = kMcNone;
     if (warp == 0) {
@@ -376,18 +596,24 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
       // after the next cluster barrier, which no CTA passes before all have
       // read it.
       cluster.sync();
-      if (warp == 0)
-        for (int c = 0; c < C; ++c) {
-          if (c == r) continue;
-          mc_warp_merge(b1, i1, cluster.map_shared_rank(&cl_b[par][0], c)[lane],
-                        cluster.map_shared_rank(&cl_i[par][0], c)[lane]);
-          const long long ob = *cluster.map_shared_rank(&cl_Kb[par], c);
-          const int oi = *cluster.map_shared_rank(&cl_Ki[par], c);
-          if (mc_greater(ob, oi, kb, ki)) {
-            kb = ob;
-            ki = oi;
-          }
+      if (warp < C) {
+        // warp c brings the list of CTA c (one remote round trip for all)
+        b1 = cluster.map_shared_rank(&cl_b[par][0], warp)[lane];
+        i1 = cluster.map_shared_rank(&cl_i[par][0], warp)[lane];
+        M.wlb[warp * 32 + lane] = b1;
+        M.wli[warp * 32 + lane] = i1;
+      }
+      if (warp == 0) {
+        kb = -1LL;
+        ki = kMcNone;
+        if (lane < C) {
+          kb = *cluster.map_shared_rank(&cl_Kb[par], lane);
+          ki = *cluster.map_shared_rank(&cl_Ki[par], lane);
         }
+        mc_warp_max(kb, ki);
+      }
+      __syncthreads();
+      tree(C);
     }
     if (warp == 0) {
       const long long b32 = __shfl_sync(0xffffffffu, b1, 31);
@@ -410,7 +636,7 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
   };
   // the candidates' rows, then their pairwise exact squared distances
   // (float32-screened: +inf where neither can lower the other)
-  auto fetch_pairs = [&]() {
+  auto fetch_pairs = [&](double Rv) {
     for (int e = threadIdx.x; e < kMcU * d; e += blockDim.x) {
       const int u = e / d, l = e - u * d;
       if (M.Ub[u] < 0) continue;
@@ -419,7 +645,11 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
       const McSmem O = rows_of(owner);
       M.Ux[u * d + l] = O.xs[(size_t)loc * d + l];
       M.Uv[u * d + l] = O.v[(size_t)l * Sc + loc];
-      if (l == 0) M.UB[u] = O.Bp[loc];
+      if (l == 0) {
+        const float B = O.Bp[loc];
+        M.UB[u] = B;
+        Uthr[u] = thr_sq(__longlong_as_double(M.Ub[u]), B);
+      }
     }
     __syncthreads();
     for (int t = threadIdx.x; t < kMcU * kMcU; t += blockDim.x) {
@@ -430,34 +660,17 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
         const float df = __fsub_rn(M.Uv[a * d + l], M.Uv[b * d + l]);
         s32 = __fmaf_rn(df, df, s32);
       }
-      const float ta = thr_sq(__longlong_as_double(M.Ub[a]), M.UB[a]);
-      const float tb = thr_sq(__longlong_as_double(M.Ub[b]), M.UB[b]);
       double sp = __longlong_as_double(0x7ff0000000000000LL);  // cannot update
-      if (mc_may_update(s32, ta, M.UB[b], growth) || mc_may_update(s32, tb, M.UB[a], growth))
-        sp = sqdist_exact(M.Ux + a * d, M.Ux + b * d, d);  // (x_a - x_b)^2 = (x_b - x_a)^2
+      if (mc_may_update(s32, Uthr[a], M.UB[b], growth) || mc_may_update(s32, Uthr[b], M.UB[a], growth)) {
+        if (Rv >= 0.0 && (double)mc_sq_upper(s32, M.UB[a], M.UB[b], growth) < Rv)
+          sp = -1.0;  // either, once the other is a pivot, falls below R: out of this pass
+        else
+          sp = sqdist_exact(M.Ux + a * d, M.Ux + b * d, d);  // (x_a - x_b)^2 = (x_b - x_a)^2
+      }
       M.pairS[a * kMcU + b] = sp;
       M.pairS[b * kMcU + a] = sp;
     }
     __syncthreads();
-  };
-  auto insert3 = [](long long b, int i, long long& b1, int& i1, long long& b2, int& i2, long long& b3,
-                    int& i3) {
-    if (mc_greater(b, i, b1, i1)) {
-      b3 = b2;
-      i3 = i2;
-      b2 = b1;
-      i2 = i1;
-      b1 = b;
-      i1 = i;
-    } else if (mc_greater(b, i, b2, i2)) {
-      b3 = b2;
-      i3 = i2;
-      b2 = b;
-      i2 = i;
-    } else if (mc_greater(b, i, b3, i3)) {
-      b3 = b;
-      i3 = i;
-    }
   };
 
   int64_t nsel = 1;
@@ -467,61 +680,71 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
     const int k = s_k;
     long long b1 = -1, b2 = -1, b3 = -1;
     int i1 = kMcNone, i2 = kMcNone, i3 = kMcNone;
-    for (int p = threadIdx.x; p < S; p += blockDim.x) {
-      double dp = M.dist[p];
-      if (__double_as_longlong(dp) < 0) continue;  // ordered (ordering.py:50-51)
-      const int gp = p0 + p;
-      float th = M.thr[p];
-      bool changed = false;
-      for (int t = 0; t < k; ++t) {
-        const int u = piv_slot[t];
-        if (M.Ui[u] == gp) {
-          dp = -1.0;  // ordering.py:58
-          changed = true;
-          break;
-        }
-        const float* vu = M.Uv + u * d;
-        float s32 = 0.0f;
-        for (int l = 0; l < d; ++l) {
-          const float df = __fsub_rn(M.v[(size_t)l * Sc + p], vu[l]);
-          s32 = __fmaf_rn(df, df, s32);
-        }
-        if (mc_may_update(s32, th, M.UB[u], growth)) {
-          // the reference's squared distance (ordering.py:52-57)
-          const double sn = sqdist_exact(M.xs + (size_t)p * d, M.Ux + u * d, d);
-          if (__double_as_longlong(sn) < __double_as_longlong(dp)) {
-            dp = sn;
-            th = thr_sq(sn, M.Bp[p]);
-            changed = true;
-          }
-        }
-      }
-      if (changed) {
-        M.dist[p] = dp;
-        M.thr[p] = th;
-      }
-      const long long b = __double_as_longlong(dp);
-      if (b < 0 || b >= 0x7ff0000000000000LL) continue;  // ordered, or not finite
-      insert3(b, gp, b1, i1, b2, i2, b3, i3);
+    switch (DV) {
+      case 4:
+        mc_apply<4>(M, P_i, P_B, P_s, &s_qn, k, S, Sc, d, p0, growth, b1, i1, b2, i2, b3, i3);
+        break;
+      case 8:
+        mc_apply<8>(M, P_i, P_B, P_s, &s_qn, k, S, Sc, d, p0, growth, b1, i1, b2, i2, b3, i3);
+        break;
+      case 16:
+        mc_apply<16>(M, P_i, P_B, P_s, &s_qn, k, S, Sc, d, p0, growth, b1, i1, b2, i2, b3, i3);
+        break;
+      case 32:
+        mc_apply<32>(M, P_i, P_B, P_s, &s_qn, k, S, Sc, d, p0, growth, b1, i1, b2, i2, b3, i3);
+        break;
+      default:
+        mc_apply<0>(M, P_i, P_B, P_s, &s_qn, k, S, Sc, d, p0, growth, b1, i1, b2, i2, b3, i3);
     }
     // 2. candidates U = slots 0..30; R bounds every other point's bits
     long long R;
     int Ri;
     collect(b1, i1, b2, i2, b3, i3, R, Ri);
-    fetch_pairs();
+    fetch_pairs(R >= 0 ? __longlong_as_double(R) : -1.0);
     // 3. pivots from the candidates (warp 0, one candidate per lane)
     if (warp == 0) {
       long long sb = lane < kMcU ? M.Ub[lane] : -1LL;
       const int si = lane < kMcU ? M.Ui[lane] : kMcNone;
       bool alive = sb >= 0;
-      long long top = sb;  // lane 0: the largest square
-      top = __shfl_sync(0xffffffffu, top, 0);
+      const long long top = __shfl_sync(0xffffffffu, sb, 0);  // the largest square
       int kk = 0;
+      if (!scan_always && !roots_always) {
+        // the leading run of slots that are certain in list order: each is
+        // above R + 4 ulps, more than 4 ulps above the next slot (no equal
+        // root below it) and not lowered by a slot before it
+        bool red = false;
+        for (int i = 0; i < lane && i < kMcU; ++i)
+          red = red || __double_as_longlong(M.pairS[lane * kMcU + i]) < sb;  // (knock-outs are < 0)
+        const long long nb = __shfl_down_sync(0xffffffffu, sb, 1);
+        const bool near = lane + 1 < kMcU && nb >= 0 && nb >= sb - 4;
+        const bool bad = lane >= kMcU || !alive || red || near || !(R < 0 || sb > R + 4);
+        const int m = (int)min((int64_t)(__ffs(__ballot_sync(0xffffffffu, bad)) - 1), n - nsel);
+        if (m > 0) {
+          if (lane < m) {
+            piv_slot[lane] = lane;
+            alive = false;
+          }
+          for (int i = 0; alive && i < m; ++i) {
+            const long long sn = __double_as_longlong(M.pairS[lane * kMcU + i]);
+            if (sn < 0)
+              alive = false;  // below R: cannot be chosen in this pass
+            else if (sn < sb)
+              sb = sn;
+          }
+          kk = m;
+        }
+      }
       while (!scan_always && kk < kMcU && nsel + kk < n) {
-        long long mb = alive ? sb : -1LL;
-        int mi = alive ? si : kMcNone;
-        mc_warp_max(mb, mi);
-        if (mb < 0 || !(R < 0 || mb > R + 4)) break;  // none left, or not certain
+        // the largest key among the survivors: high word, low word, index
+        const unsigned hi = alive ? (unsigned)((unsigned long long)sb >> 32) + 1u : 0u;
+        const unsigned mh = __reduce_max_sync(0xffffffffu, hi);
+        if (mh == 0) break;  // none left
+        const unsigned lo = alive && hi == mh ? (unsigned)sb : 0u;
+        const unsigned ml = __reduce_max_sync(0xffffffffu, lo);
+        const long long mb = ((long long)(mh - 1u) << 32) | (long long)ml;
+        if (!(R < 0 || mb > R + 4)) break;  // not certain
+        const bool is_max = alive && hi == mh && (unsigned)sb == ml;
+        int mi = (int)__reduce_min_sync(0xffffffffu, is_max ? (unsigned)si : (unsigned)kMcNone);
         const unsigned nearm = __ballot_sync(0xffffffffu, alive && sb >= mb - 4 && si < mi);
         if (nearm || roots_always) {
           // equal roots: the smaller index (ordering.py:45 keeps the first maximum)
@@ -539,16 +762,20 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
         if (lane == ws) alive = false;
         if (alive) {
           const long long sn = __double_as_longlong(M.pairS[lane * kMcU + ws]);
-          if (sn < sb) sb = sn;
+          if (sn < 0)
+            alive = false;  // below R after this pivot: cannot be chosen in this pass
+          else if (sn < sb)
+            sb = sn;
         }
         ++kk;
       }
+      build_pivots(kk);
       if (lane == 0) {
         s_k = kk;
         s_tie = kk == 0;
         s_top = top;
         if (r == 0)
-          for (int t = 0; t < kk; ++t) order[nsel + t] = M.Ui[piv_slot[t]];
+          for (int t = 0; t < kk; ++t) order[nsel + t] = P_i[t];
       }
     }
     __syncthreads();
@@ -579,7 +806,7 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
           if (bits < 0 || bits > top || bits < top - 4) continue;
           if (__double_as_longlong(__dsqrt_rn(dp)) != rmax) continue;
           // key: the smaller index first; the low 3 bits carry top - bits
-          insert3(((1LL << 40) - (p0 + p)) * 8 + (top - bits), p0 + p, b1, i1, b2, i2, b3, i3);
+          mc_insert3(((1LL << 40) - (p0 + p)) * 8 + (top - bits), p0 + p, b1, i1, b2, i2, b3, i3);
         }
         long long Kb;
         int Ki;
@@ -588,16 +815,14 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
         // the slots' squares from their keys
         if (threadIdx.x < kMcU && M.Ub[threadIdx.x] >= 0) M.Ub[threadIdx.x] = top - (M.Ub[threadIdx.x] & 7);
         __syncthreads();
-        fetch_pairs();
+        fetch_pairs(-1.0);
         if (warp == 0) {
           long long sb = lane < kMcU ? M.Ub[lane] : -1LL;
           const int si = lane < kMcU ? M.Ui[lane] : kMcNone;
           bool alive = sb >= 0, tied = alive;
           int kk = 0;
           while (kk < kMcU && nsel + kk < n) {
-            int mi = alive && tied ? si : kMcNone;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) mi = min(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+            const int mi = (int)__reduce_min_sync(0xffffffffu, alive && tied ? (unsigned)si : (unsigned)kMcNone);
             if (mi == kMcNone || mi >= bound) break;
             const int ws = __ffs(__ballot_sync(0xffffffffu, alive && si == mi)) - 1;
             if (lane == 0) piv_slot[kk] = ws;
@@ -611,10 +836,11 @@ __global__ void __launch_bounds__(kMcThreads) k_maximin_cluster(const RoProb* pr
             }
             ++kk;
           }
+          build_pivots(kk);
           if (lane == 0) {
             s_k = kk;
             if (r == 0)
-              for (int t = 0; t < kk; ++t) order[nsel + t] = M.Ui[piv_slot[t]];
+              for (int t = 0; t < kk; ++t) order[nsel + t] = P_i[t];
           }
         }
       }
