@@ -58,6 +58,15 @@ int sv_last_cuda_error(void);
 size_t sv_maximin_workspace_bytes(int64_t n, int32_t d);
 int sv_maximin_order(const double* X, int64_t n, int32_t d, int64_t first, int64_t* order,
                      int32_t* info, void* workspace, size_t workspace_bytes, sv_stream_t stream);
+/* The same with test aids that give the same order by other routes: bit 0
+ * ranks every pivot choice by exact roots, bit 1 takes pivots by the tie
+ * pass only, bit 2 runs the grid form even when one cluster would hold X. */
+int sv_maximin_order_flags(const double* X, int64_t n, int32_t d, int64_t first, int64_t* order,
+                           int32_t* info, void* workspace, size_t workspace_bytes, int32_t flags,
+                           sv_stream_t stream);
+/* largest n sv_maximin_order accepts for dimension d (rows held in the
+ * shared memory of all SMs); SV_EINVAL above it */
+int64_t sv_maximin_max_rows(int32_t d);
 
 /* Ordered nearest neighbours: replaces ordering.py:76-116 (find_ordered_nn).
  * nn is (n, m+1) int64: column 0 = row index, columns 1..min(i,m) the nearest

@@ -65,9 +65,11 @@ struct RoProb {
   int32_t d, q, m, DP, C, flags;
 };
 
-// per-point shared memory of the cluster maximin: dist f64, exact coordinates
-// f64[d], thr f32, B f32, float32 centred coordinates f32[d]
-__host__ __device__ inline int64_t mc_point_bytes(int d) { return 16 + 12 * (int64_t)d; }
+// per-point shared memory of the pass maximin: dist f64, exact coordinates
+// f64[d] (cluster form only), thr f32, B f32, float32 centred coordinates f32[d]
+__host__ __device__ inline int64_t mc_point_bytes(int d, bool grid = false) {
+  return 16 + (grid ? 4 : 12) * (int64_t)d;
+}
 // width of the pivot images held in registers (zero padded)
 __host__ __device__ inline int mc_dv(int d) { return d <= 4 ? 4 : d <= 8 ? 8 : d <= 16 ? 16 : d <= 32 ? 32 : 64; }
 // per-CTA shared memory before the points: candidate slots (exact and float32
@@ -168,6 +170,14 @@ __device__ __forceinline__ float mc_sq_upper(float s32, float Ba, float Bb, floa
   return __fmul_ru(__fmul_ru(t, t), 1.0f + 0x1p-20f);
 }
 
+// rounding bound of a float32 image v = fl32(c) of a centred row c:
+// ||c - v|| <= 2^-24 (1 + 2^-23) ||v||, formed with upward rounding
+__device__ __forceinline__ float mc_img_bound(const float* v, int d) {
+  float e2 = 0.0f;
+  for (int l = 0; l < d; ++l) e2 = __fmaf_ru(v[l], v[l], e2);
+  return __fmul_ru(__fsqrt_ru(e2), 1.01f * 0x1p-24f);
+}
+
 // (1+2^-24)^(d+2) (1+2^-20) as a float32 rounded up
 __device__ __forceinline__ float mc_growth(int d) {
   double g = 1.0;
@@ -209,13 +219,15 @@ struct McSmem {
   long long* wlb;  // [warps][32] candidate lists (work area)
   int* wli;
   double* dist;    // [Sc] squared distance to the ordered set; -1 once ordered
-  double* xs;      // [Sc][d] exact coordinates
+  const double* xs;  // [Sc][d] exact coordinates (shared memory, or the rows in global memory)
   float* thr;      // [Sc] float32 screening threshold
   float* Bp;       // [Sc] float32 rounding bound of the image
   float* v;        // [d][Sc] centred float32 images
 };
 
-__device__ __forceinline__ McSmem mc_layout(unsigned char* base, int d, int Sc) {
+// xg: the CTA's exact rows in global memory (grid form), or null to keep
+// them in shared memory (cluster form)
+__device__ __forceinline__ McSmem mc_layout(unsigned char* base, int d, int Sc, const double* xg) {
   McSmem L;
   L.Ux = (double*)base;
   L.Uv = (float*)(base + (size_t)kMcSlots * 8 * d);
@@ -229,8 +241,8 @@ __device__ __forceinline__ McSmem mc_layout(unsigned char* base, int d, int Sc) 
   L.wli = (int*)(work + kMcWarps * 32 * 8);
   unsigned char* pts = work + kMcWorkBytes;
   L.dist = (double*)pts;
-  L.xs = L.dist + Sc;
-  L.thr = (float*)(L.xs + (size_t)Sc * d);
+  L.xs = xg ? xg : L.dist + Sc;
+  L.thr = (float*)(L.dist + Sc + (xg ? 0 : (size_t)Sc * d));
   L.Bp = L.thr + Sc;
   L.v = L.Bp + Sc;
   return L;
@@ -419,10 +431,27 @@ __device__ __forceinline__ void mc_apply(const McSmem& M, const int* Pi, const f
   }
 }
 
-// Cluster maximin in passes.  A pass applies a batch of pivots, in order, to
-// every unordered point (the reference's update, ordering.py:49-58, once per
+// One problem of the pass maximin.
+struct McRun {
+  const double* X;     // the problem's rows (scaled), n x d
+  int64_t n;
+  int64_t first;       // the first row of the order (ordering.py:72)
+  int64_t* order;
+  int32_t* info;       // the problem's 4 status words
+  int32_t d, flags;
+  // grid form: candidate lists of every CTA [2][G][32], their bounds [2][G],
+  // and the monotone arrival counter of the grid barrier
+  long long* gl_b;
+  int* gl_i;
+  long long* gl_Kb;
+  int* gl_Ki;
+  unsigned* arrive;
+};
+
+// Maximin in passes.  A pass applies a batch of pivots, in order, to every
+// unordered point (the reference's update, ordering.py:49-58, once per
 // pivot), then chooses the next batch:
-//  * the cluster's 31 largest keys (squared bits, then index) form the
+//  * the 31 largest keys (squared bits, then index) of all CTAs form the
 //    candidate set U, and R bounds the squared bits of every other point
 //    (the 32nd key and every thread's third-largest key);
 //  * the exact squared distances between candidates (float32-screened) give
@@ -436,28 +465,25 @@ __device__ __forceinline__ void mc_apply(const McSmem& M, const int* Pi, const f
 //  * if not even the first choice is certain (many near-equal distances, as
 //    on a lattice), a tie pass takes the points whose root equals the largest
 //    root, in index order.
-// flags bit 0 ranks every choice by exact roots, bit 1 runs a tie pass every
-// time; both give the same order (test aids).
-__global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb* probs,
-                                                                const int32_t* plist,
-                                                                const double* Xs, int64_t* ord,
-                                                                int32_t* info) {
+// The CTAs' lists meet through a hardware cluster barrier and distributed
+// shared memory (cluster form, kGrid false), or through global memory and a
+// grid barrier with bounded waits (grid form: one CTA per SM of a
+// cooperative launch, exact rows read from global memory).  flags bit 0
+// ranks every choice by exact roots, bit 1 runs a tie pass every time; both
+// give the same order (test aids).
+template <bool kGrid>
+__device__ __forceinline__ void mc_run(const McRun& Q, int C, int r) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  cg::cluster_group cluster = cg::this_cluster();
-  const int C = (int)cluster.num_blocks();
-  const int r = (int)cluster.block_rank();
-  const int pid = plist[blockIdx.x / C];
-  const RoProb& P = probs[pid];
-  const int64_t n = P.n;
-  const int d = P.d;
+  const int64_t n = Q.n;
+  const int d = Q.d;
   const int DV = mc_dv(d);
-  const double* X = Xs + P.xs_off;
-  int64_t* order = ord + P.row_off;
+  const double* X = Q.X;
+  int64_t* order = Q.order;
   const int per = (int)((n + C - 1) / C);
   const int p0 = r * per;
   const int S = (int)max((int64_t)0, min(n, (int64_t)p0 + per) - p0);
   const int Sc = per;
-  const McSmem M = mc_layout(smraw, d, Sc);
+  const McSmem M = mc_layout(smraw, d, Sc, kGrid ? X + (size_t)p0 * d : nullptr);
   __shared__ double cen[64];
   __shared__ long long cl_b[2][32], cl_Kb[2];
   __shared__ int cl_i[2][32], cl_Ki[2];
@@ -465,23 +491,60 @@ __global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb*
   __shared__ int w_Ki[kMcWarps];
   __shared__ int piv_slot[kMcSlots], P_i[kMcSlots], P_s[kMcSlots];
   __shared__ float P_B[kMcSlots], Uthr[kMcSlots];
-  __shared__ int s_k, s_tie, s_err, s_Ki, s_qn;
+  __shared__ int s_k, s_tie, s_err, s_Ki, s_qn, s_abort;
+  __shared__ unsigned s_epoch;
   __shared__ long long s_Kb, s_top;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarp = blockDim.x >> 5;
   const float growth = mc_growth(d);
-  const bool roots_always = (P.flags & 1) != 0;
-  const bool scan_always = (P.flags & 2) != 0;
+  const bool roots_always = (Q.flags & 1) != 0;
+  const bool scan_always = (Q.flags & 2) != 0;
 
-  // the rows of another CTA of the cluster (or this one)
-  auto owner_of = [&](int idx) { return idx / per; };
-  auto rows_of = [&](int owner) -> McSmem {
-    if (C == 1 || owner == r) return M;
-    McSmem O = M;
-    O.xs = cluster.map_shared_rank(M.xs, owner);
-    O.v = cluster.map_shared_rank(M.v, owner);
-    O.Bp = cluster.map_shared_rank(M.Bp, owner);
-    return O;
+  // all CTAs of the problem: the hardware cluster barrier, or the grid
+  // barrier (monotone arrival counter, bounded wait); false once a wait gave up
+  auto all_sync = [&]() -> bool {
+    if constexpr (kGrid) {
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(Q.arrive, 1u);
+        const unsigned target = (unsigned)C * ++s_epoch;
+        unsigned it = 0;
+        while (ld_acquire_u32(Q.arrive) < target) {
+          if (++it > (SV_SPIN_LIMIT >> 4)) {
+            set_error(Q.info + SV_INFO_STATUS, SV_ETIMEOUT);
+            s_abort = 1;
+            break;
+          }
+        }
+        __threadfence();
+      }
+      __syncthreads();
+      return s_abort == 0;
+    } else {
+      if (C > 1)
+        cg::this_cluster().sync();
+      else
+        __syncthreads();
+      return true;
+    }
+  };
+  // element l of row idx: exact coordinate and float32 image
+  auto row_elem = [&](int idx, int l, double& x, float& vv) {
+    if constexpr (kGrid) {
+      x = X[(size_t)idx * d + l];
+      vv = __double2float_rn(x - cen[l]);
+    } else {
+      const int owner = idx / per, loc = idx - owner * per;
+      const double* xs = M.xs;
+      const float* v = M.v;
+      if (C > 1 && owner != r) {
+        xs = cg::this_cluster().map_shared_rank(M.xs, owner);
+        v = cg::this_cluster().map_shared_rank(M.v, owner);
+      }
+      x = xs[(size_t)loc * d + l];
+      vv = v[(size_t)l * Sc + loc];
+    }
   };
   // warp 0: the pivot table from slots piv_slot[0..kk)
   auto build_pivots = [&](int kk) {
@@ -501,9 +564,14 @@ __global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb*
   };
 
   // centre: the first row (any shift serves the float32 screen)
-  for (int l = threadIdx.x; l < d; l += blockDim.x) cen[l] = X[P.first * d + l];
+  for (int l = threadIdx.x; l < d; l += blockDim.x) cen[l] = X[Q.first * d + l];
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    s_epoch = 0;
+  }
   __syncthreads();
-  for (int e = threadIdx.x; e < S * d; e += blockDim.x) M.xs[e] = X[(size_t)p0 * d + e];
+  if constexpr (!kGrid)
+    for (int e = threadIdx.x; e < S * d; e += blockDim.x) const_cast<double*>(M.xs)[e] = X[(size_t)p0 * d + e];
   for (int p = threadIdx.x; p < S; p += blockDim.x) {
     const double* xp = X + (size_t)(p0 + p) * d;
     double e2 = 0.0;
@@ -516,39 +584,34 @@ __global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb*
     M.dist[p] = __longlong_as_double(0x7ff0000000000000LL);  // +inf: the first pass is exact
     M.thr[p] = __int_as_float(0x7f800000);
   }
-  if (C > 1)
-    cluster.sync();  // every CTA's rows are in place before the first remote read
-  else
-    __syncthreads();
+  // every CTA's rows are in place before the first remote read
+  if (!all_sync()) return;
   // the first pivot: row `first` (ordering.py:38-39) in slot 31
   if (warp == 0) {
-    const int idx = (int)P.first;
-    const int owner = owner_of(idx), loc = idx - owner * per;
-    const McSmem O = rows_of(owner);
-    for (int l = lane; l < d; l += 32) {
-      M.Ux[kMcU * d + l] = O.xs[(size_t)loc * d + l];
-      M.Uv[kMcU * d + l] = O.v[(size_t)l * Sc + loc];
-    }
+    const int idx = (int)Q.first;
+    for (int l = lane; l < d; l += 32) row_elem(idx, l, M.Ux[kMcU * d + l], M.Uv[kMcU * d + l]);
+    __syncwarp();
     if (lane == 0) {
-      M.UB[kMcU] = O.Bp[loc];
+      M.UB[kMcU] = mc_img_bound(M.Uv + kMcU * d, d);
       M.Ui[kMcU] = idx;
       piv_slot[0] = kMcU;
       s_k = 1;
       s_err = 0;
       s_tie = 0;
-      if (r == 0) order[0] = P.first;
+      if (r == 0) order[0] = Q.first;
     }
     build_pivots(1);
   }
   __syncthreads();
 
   // Candidate lists: from every thread's three largest keys (b1 > b2 > b3),
-  // the cluster's 32 largest keys land in slots 0..31 (bits Ub, index Ui) and
-  // (Kb, Ki) is the largest key that may belong to a point outside slots
+  // the 32 largest keys of all CTAs land in slots 0..31 (bits Ub, index Ui)
+  // and (Kb, Ki) is the largest key that may belong to a point outside slots
   // 0..30: the 32nd key or a thread's third.  The same in every CTA.
+  // False once a grid wait gave up.
   int par = 0;  // parity of the list buffers, flipped per collection
   auto collect = [&](long long b1, int i1, long long b2, int i2, long long b3, int i3,
-                     long long& Kb, int& Ki) {
+                     long long& Kb, int& Ki) -> bool {
     mc_warp_sort2(b1, i1, b2, i2);
     mc_warp_merge(b1, i1, b2, i2);
     mc_warp_max(b3, i3);
@@ -559,9 +622,9 @@ __global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb*
       w_Ki[warp] = i3;
     }
     __syncthreads();
-    // a tree over the lists wlb[0..m): warp w < s merges list w + s
-    auto tree = [&](int m) {
-      for (int s = m >> 1; s >= 1; s >>= 1) {
+    // a tree over the lists wlb[0..nwarp): warp w < s merges list w + s
+    auto tree = [&]() {
+      for (int s = nwarp >> 1; s >= 1; s >>= 1) {
         if (warp < s) {
           mc_warp_merge(b1, i1, M.wlb[(warp + s) * 32 + lane], M.wli[(warp + s) * 32 + lane]);
           if (s > 1) {
@@ -572,7 +635,7 @@ __global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb*
         if (s > 1) __syncthreads();
       }
     };
-    tree(nwarp);
+    tree();
     long long kb = -1LL;
     int ki = kMcNone;
     if (warp == 0) {
@@ -581,39 +644,84 @@ __global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb*
         ki = w_Ki[lane];
       }
       mc_warp_max(kb, ki);
-      if (C > 1) {
-        cl_b[par][lane] = b1;
-        cl_i[par][lane] = i1;
-        if (lane == 0) {
-          cl_Kb[par] = kb;
-          cl_Ki[par] = ki;
-        }
-      }
     }
     if (C > 1) {
-      // the cluster's list: every CTA merges all lists (the same keys, so the
-      // same result everywhere).  A buffer is rewritten two collections on,
-      // after the next cluster barrier, which no CTA passes before all have
-      // read it.
-      cluster.sync();
-      if (warp < C) {
-        // warp c brings the list of CTA c (one remote round trip for all)
-        b1 = cluster.map_shared_rank(&cl_b[par][0], warp)[lane];
-        i1 = cluster.map_shared_rank(&cl_i[par][0], warp)[lane];
-        M.wlb[warp * 32 + lane] = b1;
-        M.wli[warp * 32 + lane] = i1;
-      }
-      if (warp == 0) {
-        kb = -1LL;
-        ki = kMcNone;
-        if (lane < C) {
-          kb = *cluster.map_shared_rank(&cl_Kb[par], lane);
-          ki = *cluster.map_shared_rank(&cl_Ki[par], lane);
+      // every CTA merges all lists (the same keys, so the same result
+      // everywhere).  A buffer is rewritten two collections on, after the
+      // next barrier, which no CTA passes before all have read it.
+      if constexpr (kGrid) {
+        if (warp == 0) {
+          Q.gl_b[((size_t)par * C + r) * 32 + lane] = b1;
+          Q.gl_i[((size_t)par * C + r) * 32 + lane] = i1;
+          if (lane == 0) {
+            Q.gl_Kb[par * C + r] = kb;
+            Q.gl_Ki[par * C + r] = ki;
+          }
         }
-        mc_warp_max(kb, ki);
+        if (!all_sync()) return false;
+        // warp w merges the lists of CTAs w, w + nwarp, ... (next one in flight)
+        b1 = -1LL;
+        i1 = kMcNone;
+        long long nb = -1LL;
+        int ni = kMcNone;
+        if (warp < C) {
+          nb = __ldcg(Q.gl_b + ((size_t)par * C + warp) * 32 + lane);
+          ni = __ldcg(Q.gl_i + ((size_t)par * C + warp) * 32 + lane);
+        }
+        for (int c = warp; c < C; c += nwarp) {
+          const long long ob = nb;
+          const int oi = ni;
+          if (c + nwarp < C) {
+            nb = __ldcg(Q.gl_b + ((size_t)par * C + c + nwarp) * 32 + lane);
+            ni = __ldcg(Q.gl_i + ((size_t)par * C + c + nwarp) * 32 + lane);
+          }
+          mc_warp_merge(b1, i1, ob, oi);
+        }
+        if (warp == 0) {
+          kb = -1LL;
+          ki = kMcNone;
+          for (int c = lane; c < C; c += 32) {
+            const long long ob = __ldcg(Q.gl_Kb + par * C + c);
+            const int oi = __ldcg(Q.gl_Ki + par * C + c);
+            if (mc_greater(ob, oi, kb, ki)) {
+              kb = ob;
+              ki = oi;
+            }
+          }
+          mc_warp_max(kb, ki);
+        }
+      } else {
+        cg::cluster_group cluster = cg::this_cluster();
+        if (warp == 0) {
+          cl_b[par][lane] = b1;
+          cl_i[par][lane] = i1;
+          if (lane == 0) {
+            cl_Kb[par] = kb;
+            cl_Ki[par] = ki;
+          }
+        }
+        cluster.sync();
+        b1 = -1LL;
+        i1 = kMcNone;
+        if (warp < C) {
+          // warp c brings the list of CTA c (one remote round trip for all)
+          b1 = cluster.map_shared_rank(&cl_b[par][0], warp)[lane];
+          i1 = cluster.map_shared_rank(&cl_i[par][0], warp)[lane];
+        }
+        if (warp == 0) {
+          kb = -1LL;
+          ki = kMcNone;
+          if (lane < C) {
+            kb = *cluster.map_shared_rank(&cl_Kb[par], lane);
+            ki = *cluster.map_shared_rank(&cl_Ki[par], lane);
+          }
+          mc_warp_max(kb, ki);
+        }
       }
+      M.wlb[warp * 32 + lane] = b1;
+      M.wli[warp * 32 + lane] = i1;
       __syncthreads();
-      tree(C);
+      tree();
     }
     if (warp == 0) {
       const long long b32 = __shfl_sync(0xffffffffu, b1, 31);
@@ -633,23 +741,22 @@ __global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb*
     Kb = s_Kb;
     Ki = s_Ki;
     par ^= 1;
+    return true;
   };
   // the candidates' rows, then their pairwise exact squared distances
-  // (float32-screened: +inf where neither can lower the other)
+  // (float32-screened: +inf where neither can lower the other; -1 where a
+  // float32 upper bound already puts either below R once the other is a pivot)
   auto fetch_pairs = [&](double Rv) {
     for (int e = threadIdx.x; e < kMcU * d; e += blockDim.x) {
       const int u = e / d, l = e - u * d;
-      if (M.Ub[u] < 0) continue;
-      const int idx = M.Ui[u];
-      const int owner = owner_of(idx), loc = idx - owner * per;
-      const McSmem O = rows_of(owner);
-      M.Ux[u * d + l] = O.xs[(size_t)loc * d + l];
-      M.Uv[u * d + l] = O.v[(size_t)l * Sc + loc];
-      if (l == 0) {
-        const float B = O.Bp[loc];
-        M.UB[u] = B;
-        Uthr[u] = thr_sq(__longlong_as_double(M.Ub[u]), B);
-      }
+      if (M.Ub[u] >= 0) row_elem(M.Ui[u], l, M.Ux[u * d + l], M.Uv[u * d + l]);
+    }
+    __syncthreads();
+    if (threadIdx.x < kMcU && M.Ub[threadIdx.x] >= 0) {
+      const int u = threadIdx.x;
+      const float B = mc_img_bound(M.Uv + u * d, d);
+      M.UB[u] = B;
+      Uthr[u] = thr_sq(__longlong_as_double(M.Ub[u]), B);
     }
     __syncthreads();
     for (int t = threadIdx.x; t < kMcU * kMcU; t += blockDim.x) {
@@ -699,7 +806,7 @@ __global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb*
     // 2. candidates U = slots 0..30; R bounds every other point's bits
     long long R;
     int Ri;
-    collect(b1, i1, b2, i2, b3, i3, R, Ri);
+    if (!collect(b1, i1, b2, i2, b3, i3, R, Ri)) return;  // a grid wait gave up
     fetch_pairs(R >= 0 ? __longlong_as_double(R) : -1.0);
     // 3. pivots from the candidates (warp 0, one candidate per lane)
     if (warp == 0) {
@@ -792,8 +899,8 @@ __global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb*
         if (threadIdx.x == 0) {
           s_err = 1;
           if (r == 0) {
-            set_error(info + 4 * pid + SV_INFO_STATUS, SV_EINVAL);
-            info[4 * pid + SV_INFO_BLOCK] = (int)nsel;
+            set_error(Q.info + SV_INFO_STATUS, SV_EINVAL);
+            Q.info[SV_INFO_BLOCK] = (int)nsel;
           }
         }
       } else {
@@ -810,7 +917,7 @@ __global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb*
         }
         long long Kb;
         int Ki;
-        collect(b1, i1, b2, i2, b3, i3, Kb, Ki);
+        if (!collect(b1, i1, b2, i2, b3, i3, Kb, Ki)) return;
         const int bound = Kb >= 0 ? Ki : kMcNone;
         // the slots' squares from their keys
         if (threadIdx.x < kMcU && M.Ub[threadIdx.x] >= 0) M.Ub[threadIdx.x] = top - (M.Ub[threadIdx.x] & 7);
@@ -850,8 +957,35 @@ __global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb*
     nsel += s_k;
   }
   // keep this CTA's shared memory alive until every remote read is done
-  if (C > 1) cluster.sync();
+  if constexpr (!kGrid)
+    if (C > 1) cg::this_cluster().sync();
 }
+
+__global__ void __launch_bounds__(kMcThreads, 1) k_maximin_cluster(const RoProb* probs,
+                                                                   const int32_t* plist,
+                                                                   const double* Xs, int64_t* ord,
+                                                                   int32_t* info) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int pid = plist[blockIdx.x / C];
+  const RoProb& P = probs[pid];
+  McRun Q = {};
+  Q.X = Xs + P.xs_off;
+  Q.n = P.n;
+  Q.first = P.first;
+  Q.order = ord + P.row_off;
+  Q.info = info + 4 * pid;
+  Q.d = P.d;
+  Q.flags = P.flags;
+  mc_run<false>(Q, C, (int)cluster.block_rank());
+}
+
+// grid form: one problem over a cooperative grid (one CTA per SM)
+__global__ void __launch_bounds__(kMcThreads, 1) k_maximin_grid(McRun Q) {
+  mc_run<true>(Q, (int)gridDim.x, (int)blockIdx.x);
+}
+
+
 
 // X, y, Z <- rows of X_e, y_e, Z_e in maximin order; Xso <- Xs in that order;
 // grid row = problem
@@ -1078,7 +1212,7 @@ static int launch_maximin_cluster(int C, size_t smem, unsigned nclusters, const 
 // One problem through the cluster kernel (sv_maximin_order for n that fits
 // one cluster).  ws: 256 bytes of device scratch.
 int maximin_cluster_single(const double* X, int64_t n, int d, int64_t first, int64_t* order,
-                           int32_t* info, char* ws, cudaStream_t st) {
+                           int32_t* info, char* ws, int flags, cudaStream_t st) {
   const int C = mc_cluster_size(n, d, ro_max_smem());
   if (C == 0) return SV_EINVAL;
   struct {
@@ -1090,10 +1224,70 @@ int maximin_cluster_single(const double* X, int64_t n, int d, int64_t first, int
   h.p.first = first;
   h.p.d = d;
   h.p.C = C;
+  h.p.flags = flags & 3;
   SV_CUDA_TRY(cudaMemcpyAsync(ws, &h, sizeof(h), cudaMemcpyHostToDevice, st));
   const size_t smem = (size_t)((n + C - 1) / C) * (size_t)mc_point_bytes(d) + (size_t)mc_fixed_bytes(d);
   return launch_maximin_cluster(C, smem, 1, (const RoProb*)ws, (const int32_t*)(ws + sizeof(RoProb)),
                                 X, order, info, st);
+}
+
+// grid form: CTAs (one per SM at most, >= 64 rows each) and rows per CTA
+static int mg_plan(int64_t n, int d, int& G, int& per, size_t& smem) {
+  const int nsm = sv_num_sms();
+  const int64_t budget = (int64_t)ro_max_smem() - kMcStaticSmem - mc_fixed_bytes(d);
+  G = (int)std::min<int64_t>(nsm, std::max<int64_t>(1, (n + 63) / 64));
+  per = (int)((n + G - 1) / G);
+  if ((int64_t)per * mc_point_bytes(d, true) > budget) return SV_EINVAL;
+  smem = (size_t)per * (size_t)mc_point_bytes(d, true) + (size_t)mc_fixed_bytes(d);
+  return SV_OK;
+}
+
+size_t maximin_grid_workspace_bytes() {
+  const size_t g2 = 2 * (size_t)sv_num_sms();
+  return ro_align(g2 * 32 * 8) + ro_align(g2 * 32 * 4) + ro_align(g2 * 8) + ro_align(g2 * 4) + 256;
+}
+
+int64_t maximin_grid_max_rows(int d) {
+  if (d < 1 || d > 64) return 0;
+  const int64_t budget = (int64_t)ro_max_smem() - kMcStaticSmem - mc_fixed_bytes(d);
+  return (int64_t)sv_num_sms() * (budget / mc_point_bytes(d, true));
+}
+
+// One problem through the grid form (a cooperative launch, one CTA per SM).
+int maximin_grid_single(const double* X, int64_t n, int d, int64_t first, int64_t* order,
+                        int32_t* info, char* ws, size_t ws_bytes, int flags, cudaStream_t st) {
+  int G = 0, per = 0;
+  size_t smem = 0;
+  if (mg_plan(n, d, G, per, smem) != SV_OK) return SV_EINVAL;
+  if (ws_bytes < maximin_grid_workspace_bytes()) return SV_ENOSPC;
+  SV_CUDA_TRY(cudaFuncSetAttribute(k_maximin_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int active = 0;
+  SV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&active, k_maximin_grid, kMcThreads, smem));
+  if (active < 1 || G > active * sv_num_sms()) return SV_EINVAL;
+  const size_t g2 = 2 * (size_t)sv_num_sms();
+  McRun Q = {};
+  Q.X = X;
+  Q.n = n;
+  Q.first = first;
+  Q.order = order;
+  Q.info = info;
+  Q.d = d;
+  Q.flags = flags & 3;
+  size_t off = 0;
+  Q.gl_b = (long long*)(ws + off);
+  off += ro_align(g2 * 32 * 8);
+  Q.gl_i = (int*)(ws + off);
+  off += ro_align(g2 * 32 * 4);
+  Q.gl_Kb = (long long*)(ws + off);
+  off += ro_align(g2 * 8);
+  Q.gl_Ki = (int*)(ws + off);
+  off += ro_align(g2 * 4);
+  Q.arrive = (unsigned*)(ws + off);
+  SV_CUDA_TRY(cudaMemsetAsync(Q.arrive, 0, sizeof(unsigned), st));
+  void* args[] = {&Q};
+  SV_CUDA_TRY(cudaLaunchCooperativeKernel((void*)k_maximin_grid, dim3((unsigned)G), dim3(kMcThreads), args,
+                                          smem, st));
+  return SV_OK;
 }
 
 int64_t maximin_cluster_max_rows(int d) {

@@ -25,9 +25,14 @@ int launch_knn_batched(int DP, const KnnBatchProb* probs, const int2* tiles, int
                        int kcap, cudaStream_t st);
 
 // single-problem maximin through the cluster kernel (n <= maximin_cluster_max_rows(d));
-// ws: 256 bytes of device scratch
+// ws: 256 bytes of device scratch; flags: the test aids of sv_reorder_prob
 int maximin_cluster_single(const double* X, int64_t n, int d, int64_t first, int64_t* order,
-                           int32_t* info, char* ws, cudaStream_t st);
+                           int32_t* info, char* ws, int flags, cudaStream_t st);
 int64_t maximin_cluster_max_rows(int d);
+// single-problem maximin through the grid form (n <= maximin_grid_max_rows(d))
+int maximin_grid_single(const double* X, int64_t n, int d, int64_t first, int64_t* order,
+                        int32_t* info, char* ws, size_t ws_bytes, int flags, cudaStream_t st);
+size_t maximin_grid_workspace_bytes();
+int64_t maximin_grid_max_rows(int d);
 
 }  // namespace sv

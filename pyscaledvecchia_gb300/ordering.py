@@ -22,15 +22,21 @@ from . import _lib
 __all__ = ["maximin_order", "find_ordered_nn"]
 
 
-def maximin_order_device(torch, Xd, first: int):
-    """Maximin permutation of the rows of a device (n, d) float64 tensor."""
+def maximin_order_device(torch, Xd, first: int, flags: int = 0):
+    """Maximin permutation of the rows of a device (n, d) float64 tensor.
+    ``flags`` (test aids, same order): 1 ranks every pivot choice by exact
+    roots, 2 takes pivots by tie passes only, 4 forces the grid form."""
     lib = _lib.load_library()
     n, d = Xd.shape
     order = torch.empty(n, dtype=torch.int64, device="cuda")
     info = _lib.new_info(torch)
     ws = _lib.workspace(torch, lib.sv_maximin_workspace_bytes(n, d))
-    rc = lib.sv_maximin_order(_lib.ptr(Xd), n, d, int(first), _lib.ptr(order), _lib.ptr(info),
-                              _lib.ptr(ws), ws.numel(), _lib.stream_handle(torch))
+    if flags:
+        rc = lib.sv_maximin_order_flags(_lib.ptr(Xd), n, d, int(first), _lib.ptr(order), _lib.ptr(info),
+                                        _lib.ptr(ws), ws.numel(), int(flags), _lib.stream_handle(torch))
+    else:
+        rc = lib.sv_maximin_order(_lib.ptr(Xd), n, d, int(first), _lib.ptr(order), _lib.ptr(info),
+                                  _lib.ptr(ws), ws.numel(), _lib.stream_handle(torch))
     _lib.check(lib, rc, "sv_maximin_order")
     return order, info
 

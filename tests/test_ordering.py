@@ -95,6 +95,42 @@ def test_maximin_ties_and_duplicates(oracle):
     np.testing.assert_array_equal(_sv().maximin_order(X), oracle.maximin_order(X))
 
 
+def _maximin_routed(X, flags):
+    import torch
+    from pyscaledvecchia_gb300 import _lib
+    from pyscaledvecchia_gb300.ordering import maximin_order_device
+    lib, _ = _lib.device_ready()
+    first = int(np.argmin(((X - X.mean(0)) ** 2).sum(1)))
+    o, info = maximin_order_device(torch, _lib.to_dev(torch, X, np.float64), first, flags)
+    _lib.check_info(lib, info.cpu().numpy(), "sv_maximin_order")
+    return o.cpu().numpy()
+
+
+@pytest.mark.parametrize("flags", [4, 5, 6, 1, 2])
+def test_maximin_routes_vs_oracle(oracle, flags):
+    """The grid form (flag 4: lists through global memory behind a grid
+    barrier, one CTA per SM from 9,728 rows) and the exact-root and tie-pass
+    routes (flags 1, 2) give the reference's order on random rows, a lattice
+    with duplicates and rows on a coarse grid of values."""
+    rng = np.random.default_rng(11)
+    g = np.arange(30, dtype=float)
+    lattice = np.array([[a, b] for a in g for b in g])
+    cases = [rng.random((12000, 4)) / np.exp(rng.uniform(-1, 1, 4)),
+             np.vstack([lattice, lattice[::9]]) / 7.0,
+             np.round(rng.random((2500, 3)) * 12) / 3.0,
+             rng.random((700, 64))]
+    for X in cases:
+        np.testing.assert_array_equal(_maximin_routed(X, flags), oracle.maximin_order(X))
+
+
+def test_maximin_grid_form_limits():
+    from pyscaledvecchia_gb300 import _lib
+    lib, _ = _lib.device_ready()
+    for d in (2, 10, 64):
+        assert lib.sv_maximin_max_rows(d) > lib.sv_maximin_cluster_max_rows(d)
+    assert lib.sv_maximin_max_rows(10) > 500_000
+
+
 @pytest.mark.parametrize("n,d,m,start", [(20000, 10, 30, 0), (5000, 3, 140, 0),
                                          (4000, 6, 25, 1500), (3000, 2, 8, 0)])
 def test_ordered_knn_exact_vs_oracle(oracle, n, d, m, start):
