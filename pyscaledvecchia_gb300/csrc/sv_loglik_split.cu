@@ -107,6 +107,44 @@ __device__ __forceinline__ double pivot_rcp(double dkk) {
   return 1.0 / dkk;
 }
 
+// Rows i of the float32 right-hand sides dSigma_l a for l = 1..d:
+//   R(1 + l, i) = -s2 sum_{j != i} g_ij a_j (u_il - u_jl)^2,
+// one pass over the neighbours j with row i's coordinates, the squared
+// differences and the d sums in registers (DR >= d, zero padded); the same
+// roundings in the same order as a pass per l.
+template <int DR>
+__device__ __forceinline__ void split_dsig_row(int i, int K, int d, int code, float s2f,
+                                               const float* u, const float* a32, double* R) {
+  float ui[DR], S[DR];
+#pragma unroll
+  for (int l = 0; l < DR; ++l) {
+    ui[l] = l < d ? u[i * d + l] : 0.0f;
+    S[l] = 0.0f;
+  }
+  for (int j = 0; j < K; ++j) {
+    if (j == i) continue;  // g_ii a_i (u_i - u_i)^2 adds exactly nothing
+    const float* uj = u + j * d;
+    float sq[DR];
+    float r2 = 0.0f;
+#pragma unroll
+    for (int l = 0; l < DR; ++l)
+      if (l < d) {
+        const float df = ui[l] - uj[l];
+        r2 = fmaf(df, df, r2);
+        sq[l] = df * df;
+      }
+    float M, g;
+    matern_closed_f32(code, sqrtf(r2), M, g);
+    const float c = g * a32[j];
+#pragma unroll
+    for (int l = 0; l < DR; ++l)
+      if (l < d) S[l] = fmaf(c, sq[l], S[l]);
+  }
+#pragma unroll
+  for (int l = 0; l < DR; ++l)
+    if (l < d) R[(1 + l) * 33 + i] = (double)(-s2f * S[l]);
+}
+
 // L is stored packed by columns with capacity 32: entry (i, j), i >= j, at
 // cstart(j) + i - j.  Column walks (scaling, trailing updates, forward
 // solves) then touch consecutive words, free of bank conflicts.
@@ -372,6 +410,16 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       // p = 0: Sigma (un-jittered) a = L_KK e_K - jit a
       for (int i = tl; i < K; i += G) R[i] = ((i == k) ? lKK : 0.0) - jit * a[i];
       // p = 1..d (float32): -s2 sum_j g_ij a_j (u_il - u_jl)^2
+      if (d <= 12) {
+        for (int i = tl; i < K; i += G) {
+          if (d <= 4)
+            split_dsig_row<4>(i, K, d, code, s2f, u, a32, R);
+          else if (d <= 8)
+            split_dsig_row<8>(i, K, d, code, s2f, u, a32, R);
+          else
+            split_dsig_row<12>(i, K, d, code, s2f, u, a32, R);
+        }
+      } else
       for (int i = tl; i < K; i += G) {
         float cj[32];
 #pragma unroll
