@@ -118,18 +118,17 @@ __device__ __forceinline__ void split_dsig_row(int i, int K, int d, int code, fl
   float ui[DR], S[DR];
 #pragma unroll
   for (int l = 0; l < DR; ++l) {
-    ui[l] = l < d ? u[i * d + l] : 0.0f;
+    ui[l] = l < d ? u[l * 32 + i] : 0.0f;
     S[l] = 0.0f;
   }
   for (int j = 0; j < K; ++j) {
     if (j == i) continue;  // g_ii a_i (u_i - u_i)^2 adds exactly nothing
-    const float* uj = u + j * d;
     float sq[DR];
     float r2 = 0.0f;
 #pragma unroll
     for (int l = 0; l < DR; ++l)
       if (l < d) {
-        const float df = ui[l] - uj[l];
+        const float df = ui[l] - u[l * 32 + j];
         r2 = fmaf(df, df, r2);
         sq[l] = df * df;
       }
@@ -150,6 +149,52 @@ __device__ __forceinline__ void split_dsig_row(int i, int K, int d, int code, fl
 // solves) then touch consecutive words, free of bank conflicts.
 __device__ __forceinline__ int cstart(int j) { return j * 32 - (j * (j - 1)) / 2; }
 __device__ __forceinline__ int cm(int i, int j) { return cstart(j) + (i - j); }
+
+// Entries (h, j < h) and (K-1-h, j < K-1-h) of Sigma below the diagonal,
+// s2 (1 - D(r_ij)), and both diagonal entries dj; u is [d][32] (row i at
+// column i), the current row's coordinates are held in registers (DR >= d,
+// 0: read from shared memory).  The same value per entry as any other
+// traversal.
+template <int DR>
+__device__ __forceinline__ void split_sigma_rows(int h, int K, int d, int code, double s2, double dj,
+                                                 const float* u, double* Lp) {
+  const int ib = K - 1 - h;            // >= h
+  const int na = ib == h ? 0 : h;      // entries of row h when it is a row of its own
+  constexpr int W = DR > 0 ? DR : 1;
+  float ur[W];
+  int i = na > 0 ? h : ib;
+  if constexpr (DR > 0) {
+#pragma unroll
+    for (int l = 0; l < DR; ++l) ur[l] = l < d ? u[l * 32 + i] : 0.0f;
+  }
+  for (int s = 0; s < na + ib; ++s) {
+    if (s == na && na > 0) {
+      i = ib;
+      if constexpr (DR > 0) {
+#pragma unroll
+        for (int l = 0; l < DR; ++l) ur[l] = l < d ? u[l * 32 + i] : 0.0f;
+      }
+    }
+    const int j = s < na ? s : s - na;
+    float r2 = 0.0f;
+    if constexpr (DR > 0) {
+#pragma unroll
+      for (int l = 0; l < DR; ++l)
+        if (l < d) {
+          const float df = ur[l] - u[l * 32 + j];
+          r2 = fmaf(df, df, r2);
+        }
+    } else {
+      for (int l = 0; l < d; ++l) {
+        const float df = u[l * 32 + i] - u[l * 32 + j];
+        r2 = fmaf(df, df, r2);
+      }
+    }
+    Lp[cm(i, j)] = fma(-s2, (double)matern_deficit_f32(code, sqrtf(r2)), s2);
+  }
+  Lp[cm(h, h)] = dj;
+  if (ib != h) Lp[cm(ib, ib)] = dj;
+}
 
 template <int G>
 __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, int wpc) {
@@ -208,7 +253,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         const int i = t / d, l = t - (t / d) * d;
         const float2 v = XH[(int64_t)idx[i] * d + l];
         const float2 w = xs[l];
-        u[t] = (v.x - w.x) + (v.y - w.y);
+        u[l * 32 + i] = (v.x - w.x) + (v.y - w.y);
       }
       if (A.need_grad)
         for (int i = tl; i < K; i += G) {
@@ -230,23 +275,18 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       if (need) {
         jit = (lv > 0) ? jitter_pow10(lv) * diag : 0.0;  // 10^p * mean(diag)
         rho_bits = dbits(A.rho_min * (diag + jit));
-        const int npair = K * (K + 1) / 2;
-        for (int t = tl; t < npair; t += G) {
-          int i, j;
-          tri_index(t, i, j);
-          double v;
-          if (i == j) {
-            v = diag + jit;
-          } else {
-            float r2 = 0.0f;
-            for (int l = 0; l < d; ++l) {
-              const float df = u[i * d + l] - u[j * d + l];
-              r2 = fmaf(df, df, r2);
-            }
-            // s2 (1 - D): the deficit carries the information of close pairs
-            v = fma(-s2, (double)matern_deficit_f32(code, sqrtf(r2)), s2);
-          }
-          Lp[cm(i, j)] = v;
+        // lane h takes rows h and K-1-h (K-1 entries below the diagonal
+        // between them); s2 (1 - D): the deficit carries the information of
+        // close pairs
+        for (int h = tl; 2 * h < K; h += G) {
+          if (d <= 4)
+            split_sigma_rows<4>(h, K, d, code, s2, diag + jit, u, Lp);
+          else if (d <= 8)
+            split_sigma_rows<8>(h, K, d, code, s2, diag + jit, u, Lp);
+          else if (d <= 12)
+            split_sigma_rows<12>(h, K, d, code, s2, diag + jit, u, Lp);
+          else
+            split_sigma_rows<0>(h, K, d, code, s2, diag + jit, u, Lp);
         }
         if (tl == 0) *tflag = 0;
       }
@@ -428,7 +468,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
           if (j < K && j != i) {
             float r2 = 0.0f;
             for (int l = 0; l < d; ++l) {
-              const float df = u[i * d + l] - u[j * d + l];
+              const float df = u[l * 32 + i] - u[l * 32 + j];
               r2 = fmaf(df, df, r2);
             }
             float M, g;
@@ -438,12 +478,12 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
           cj[j] = c;
         }
         for (int l = 0; l < d; ++l) {
-          const float uil = u[i * d + l];
+          const float uil = u[l * 32 + i];
           float s = 0.0f;
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             if (j < K) {
-              const float df = uil - u[j * d + l];
+              const float df = uil - u[l * 32 + j];
               s = fmaf(cj[j], df * df, s);
             }
           }
