@@ -144,6 +144,20 @@ __device__ __forceinline__ void split_dsig_row(int i, int K, int d, int code, fl
     if (l < d) R[(1 + l) * 33 + i] = (double)(-s2f * S[l]);
 }
 
+// pivot kk of the team's factorisation: LAPACK's criterion (a pivot that is
+// not > 0, i.e. negative, zero or NaN, fails: flag[0]), the conditioning
+// test against rho_min (flag[1]) and the reciprocal
+__device__ __forceinline__ void split_pivot(double dkk, int kk, long long rho_bits, double* invd,
+                                            volatile int* flag) {
+  const long long bd = dbits(dkk);
+  if (bd <= 0 || bd >= kBitsInf) {
+    flag[0] = 1;
+  } else {
+    if (bd < rho_bits) flag[1] = 1;
+    invd[kk] = pivot_rcp(dkk);
+  }
+}
+
 // L is stored packed by columns with capacity 32: entry (i, j), i >= j, at
 // cstart(j) + i - j.  Column walks (scaling, trailing updates, forward
 // solves) then touch consecutive words, free of bank conflicts.
@@ -269,7 +283,6 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     bool done = !active, failed = false;
     double jit = 0.0;
     long long rho_bits = 0;
-    bool ill = false;  // a pivot ratio L_kk^2 / Sigma_kk fell below rho_min (team lane 0)
     while (__any_sync(full, !done)) {
       const bool need = !done;
       if (need) {
@@ -288,26 +301,19 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
           else
             split_sigma_rows<0>(h, K, d, code, s2, diag + jit, u, Lp);
         }
-        if (tl == 0) *tflag = 0;
+        if (tl == 0) {
+          tflag[0] = 0;  // a pivot failed
+          tflag[1] = 0;  // a pivot ratio L_kk^2 / Sigma_kk fell below rho_min
+        }
       }
       __syncwarp();
+      if (need && tl == 0) split_pivot(Lp[cm(0, 0)], 0, rho_bits, invd, tflag);
+      __syncwarp();
       // right-looking LDL^T by columns, warp-uniform step loop; acc holds the
-      // unscaled pivot column of the current step
+      // unscaled pivot column of the current step.  The lane that updates
+      // (kk+1, kk+1) takes the next pivot's reciprocal at once (look-ahead).
       for (int kk = 0; kk < Kw; ++kk) {
-        const bool go = need && kk < K;
-        if (go && tl == 0 && *tflag == 0) {
-          const double dkk = Lp[cm(kk, kk)];
-          const long long bd = dbits(dkk);
-          // LAPACK criterion: a pivot that is not > 0 (negative, zero or NaN) fails
-          if (bd <= 0 || bd >= kBitsInf) {
-            *tflag = 1;
-          } else {
-            ill = ill || (bd < rho_bits);
-            invd[kk] = pivot_rcp(dkk);
-          }
-        }
-        __syncwarp();
-        const bool go2 = go && *tflag == 0;
+        const bool go2 = need && kk < K && tflag[0] == 0;
         if (go2) {
           const double inv = invd[kk];
           double* colk = Lp + cstart(kk) - kk;  // colk[i] = L(i, kk)
@@ -352,16 +358,20 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
                 }
 #pragma unroll
               for (int u4 = 0; u4 < kSplitU; ++u4)
-                if (t + u4 * G < cnt) Lp[cm(ii[u4], jj[u4])] = fma(-lik[u4], ajk[u4], aij[u4]);
+                if (t + u4 * G < cnt) {
+                  const double nv = fma(-lik[u4], ajk[u4], aij[u4]);
+                  Lp[cm(ii[u4], jj[u4])] = nv;
+                  if (ii[u4] == kk + 1 && jj[u4] == kk + 1) split_pivot(nv, kk + 1, rho_bits, invd, tflag);
+                }
             }
           }
         }
         __syncwarp();
       }
       if (need) {
-        if (*tflag == 0) {
+        if (tflag[0] == 0) {
           done = true;
-        } else if (ill = false, ++lv > 9) {
+        } else if (++lv > 9) {
           done = true;
           failed = true;
         }
@@ -386,7 +396,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         A.flags[0] = 1;
       }
       // ill-conditioned blocks lose too much to float32 assembly: redo in float64
-      const bool again = ill;
+      const bool again = tflag[1] != 0;
       A.redo[b] = again ? 1 : 0;
       if (again) atomicAdd(info + SV_INFO_AUX, 1);
     }
