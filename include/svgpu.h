@@ -144,7 +144,7 @@ typedef struct sv_loglik_desc {
   int32_t precision;    /* 0 = float64 throughout; 1 = split: float32 assembly, */
                         /*   dSigma.a and Gram products, float64 factorisation */
                         /*   and solves (closed-form nu, k+1 <= 32 blocks)     */
-  int32_t team_lanes;   /* split form: lanes per block (4, 8, 16, 32; 0 = 8)   */
+  int32_t team_lanes;   /* split form: lanes per block (4, 8, 16, 32; 0 = 16)  */
   double split_rho_min; /* split form: blocks whose smallest pivot ratio      */
                         /*   L_kk^2 / Sigma_kk is below this (0 = 1e-4) are    */
                         /*   re-evaluated in float64; info[SV_INFO_AUX] counts */

@@ -731,7 +731,9 @@ int run_eval(const EvalCall& C, cudaStream_t st) {
   // split form: closed-form nu for every problem and at most 32 right-hand
   // sides (d + q <= 29); anything else runs the float64 kernels
   const bool split = S.precision == 1 && !S.any_est && A.NRmax <= 32;
-  const int lanes = C.team_lanes > 0 ? C.team_lanes : 8;
+  // 16 lanes per block is the fastest team width measured for every K from 6
+  // to 31 (d = 3 and 10); 8 and 32 trail by up to 37 % and 12 %
+  const int lanes = C.team_lanes > 0 ? C.team_lanes : 16;
   if (split && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32) return SV_EINVAL;
 
   auto warp_pass = [&](LikArgs B) -> int {
