@@ -162,6 +162,21 @@ typedef struct sv_loglik_desc {
  *   chunk : device int32[nblk] chunk ids (desc->chunked) or NULL
  *   out   : device float64[1 + P + P*P + q] = ll, grad, fish (row-major), beta
  *   info  : device int32[4] (SV_INFO_*) */
+/* The block table of sv_vecchia_loglik from the groups of _nn_groups
+ * (ordering.py:119-127), packed on the device: group g's rows (device int64,
+ * count of them) with k neighbour rows each (device int64, count x k
+ * row-major) become blocks out_off .. out_off+count-1: rowb = row, kb = k,
+ * nbr = the neighbours then -1 up to ldnbr.  An index outside [0, n) sets
+ * *bad (device int32, cleared first) and is written as 0. */
+typedef struct sv_pack_group {
+  const int64_t* rows;
+  const int64_t* nb;
+  int64_t count, out_off;
+  int32_t k, pad;
+} sv_pack_group;
+int sv_pack_blocks(const sv_pack_group* groups, int32_t ngroups, int64_t n, int32_t ldnbr,
+                   int32_t* rowb, int32_t* kb, int32_t* nbr, int32_t* bad, sv_stream_t stream);
+
 size_t sv_loglik_workspace_bytes(const sv_loglik_desc* desc);
 int sv_vecchia_loglik(const sv_loglik_desc* desc, const double* theta, const double* X,
                       const double* y, const double* Z, const int32_t* rowb, const int32_t* kb,

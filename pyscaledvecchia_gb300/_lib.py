@@ -58,6 +58,12 @@ class ReorderProb(ctypes.Structure):
                 ("first", c_i64), ("d", c_i32), ("q", c_i32), ("m", c_i32), ("flags", c_i32)]
 
 
+class PackGroup(ctypes.Structure):
+    """Mirror of sv_pack_group (include/svgpu.h)."""
+    _fields_ = [("rows", c_vp), ("nb", c_vp), ("count", c_i64), ("out_off", c_i64),
+                ("k", c_i32), ("pad", c_i32)]
+
+
 class ReorderDesc(ctypes.Structure):
     """Mirror of sv_reorder_desc (include/svgpu.h)."""
     _fields_ = [("nprob", c_i64), ("dmax", c_i32), ("ldnbr", c_i32)]
@@ -86,6 +92,7 @@ SIGNATURES = {
     "sv_reorder_batched_workspace_bytes": (c_sz, [ctypes.POINTER(ReorderDesc), c_vp]),
     "sv_reorder_batched": (c_i32, [ctypes.POINTER(ReorderDesc), c_vp, c_vp] + [c_vp] * 10 + [c_sz, c_vp]),
     "sv_loglik_workspace_bytes": (c_sz, [ctypes.POINTER(LoglikDesc)]),
+    "sv_pack_blocks": (c_i32, [c_vp, c_i32, c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "sv_vecchia_loglik": (c_i32, [ctypes.POINTER(LoglikDesc), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
                                   c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "sv_loglik_batched_workspace_bytes": (c_sz, [ctypes.POINTER(BatchDesc)]),

@@ -15,6 +15,8 @@ libsvgpu.so (sv_vecchia_loglik); the host only packs the conditioning sets.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 
 from . import _lib
@@ -109,19 +111,70 @@ class DeviceProblem:
         self.X = _lib.to_dev(torch, Xo, np.float64)
         self.y = _lib.to_dev(torch, yo, np.float64)
         self.Z = _lib.to_dev(torch, np.asarray(Zo, dtype=np.float64), np.float64) if self.has_Z else None
-        rowb, kb, nbr, gid, gk, gl = pack_groups(groups, self.n)
-        self.nblk = rowb.shape[0]
-        self.kmax = int(kb.max()) if self.nblk else 0
-        self.nblk_warp = int(np.sum(kb + 1 <= _WARP_K))
-        self.rowb = _lib.to_dev(torch, rowb, np.int32)
-        self.kb = _lib.to_dev(torch, kb, np.int32)
-        self.nbr = _lib.to_dev(torch, nbr, np.int32)
-        self.ldnbr = nbr.shape[1]
-        self._gid, self._gk, self._gl = gid, gk, gl
+        self._pack_on_device(groups)
         self._chunks = {}
         self._ws = None
         self.out = None
         self.info = _lib.new_info(torch)
+
+    def _pack_on_device(self, groups):
+        """The block table of ``pack_groups`` built on the device (sv_pack_blocks)
+        from the groups' own arrays: warp-sized groups first, group order kept;
+        a row or neighbour index outside the data raises ValueError."""
+        torch, lib = self.torch, self.lib
+        rows_l, nb_l = [], []
+        for rows, nb in groups:
+            rows = np.ascontiguousarray(rows, dtype=np.int64).reshape(-1)
+            nb = np.ascontiguousarray(nb, dtype=np.int64).reshape(rows.shape[0], -1)
+            rows_l.append(rows)
+            nb_l.append(nb)
+        gk = [nb.shape[1] for nb in nb_l]
+        gl = [r.shape[0] for r in rows_l]
+        order = [g for g in range(len(gk)) if gk[g] + 1 <= _WARP_K] + \
+                [g for g in range(len(gk)) if gk[g] + 1 > _WARP_K]
+        B = int(sum(gl))
+        kmax = max(gk) if gk else 0
+        self.nblk = B
+        self.kmax = kmax if B else 0
+        self.nblk_warp = int(sum(gl[g] for g in range(len(gk)) if gk[g] + 1 <= _WARP_K))
+        self.ldnbr = max(kmax, 1)
+        self.rowb = torch.empty(max(B, 1), dtype=torch.int32, device="cuda")[:B]
+        self.kb = torch.empty(max(B, 1), dtype=torch.int32, device="cuda")[:B]
+        self.nbr = torch.empty((max(B, 1), self.ldnbr), dtype=torch.int32, device="cuda")[:B]
+        self._gid = np.repeat(np.asarray(order, dtype=np.int32),
+                              np.asarray([gl[g] for g in order], dtype=np.int64))
+        self._gk, self._gl = gk, gl
+        if B == 0:
+            return
+        # small groups travel in one copy, large ones in their own
+        small = [g for g in order if gl[g] * max(gk[g], 1) < 65536]
+        dev = {}
+        if small:
+            flat = np.concatenate([np.concatenate([rows_l[g], nb_l[g].reshape(-1)]) for g in small])
+            fd = _lib.to_dev(torch, flat, np.int64)
+            o = 0
+            for g in small:
+                c, k = gl[g], gk[g]
+                dev[g] = (fd[o:o + c], fd[o + c:o + c + c * k])
+                o += c + c * k
+        for g in order:
+            if g not in dev:
+                dev[g] = (_lib.to_dev(torch, rows_l[g], np.int64), _lib.to_dev(torch, nb_l[g], np.int64))
+        desc = (_lib.PackGroup * len(order))()
+        o = 0
+        for j, g in enumerate(order):
+            r_d, nb_d = dev[g]
+            desc[j].rows = r_d.data_ptr() if gl[g] else None
+            desc[j].nb = nb_d.data_ptr() if gl[g] * gk[g] else None
+            desc[j].count, desc[j].out_off, desc[j].k = gl[g], o, gk[g]
+            o += gl[g]
+        bad = torch.empty(1, dtype=torch.int32, device="cuda")
+        rc = lib.sv_pack_blocks(ctypes.cast(desc, ctypes.c_void_p), len(order), self.n, self.ldnbr,
+                                _lib.ptr(self.rowb), _lib.ptr(self.kb), _lib.ptr(self.nbr), _lib.ptr(bad),
+                                _lib.stream_handle(torch))
+        _lib.check(lib, rc, "sv_pack_blocks")
+        if int(bad.item()):  # waits for the copies and the packing
+            raise ValueError("conditioning sets reference rows outside the data")
 
     def kernel_launches(self, precision="float64", chunked=True, estimate_nu=False, nu=2.5):
         """Number of library kernels one evaluation launches."""

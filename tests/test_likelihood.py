@@ -232,3 +232,45 @@ def test_bad_nu_raises():
     nn = sv.find_ordered_nn(X, 3)
     with pytest.raises(ValueError):
         sv.vecchia_profile_loglik(np.zeros(4), X, np.zeros(10), None, _nn_groups(nn, 3), -1.0)
+
+
+def test_bad_conditioning_sets_raise(problem):
+    """Rows or neighbours outside the data raise ValueError (checked while the
+    block table is packed on the device, before any kernel reads them)."""
+    sv, _, _, _ = _sv()
+    X, y, theta = problem
+    n, d = X.shape
+    order, groups = _prep(X, theta, 8, d)
+    Xo, yo, Z = X[order], y[order], np.ones((n, 1))
+    for bad_value in (n, n + 7, -2, -1):
+        bad = [(np.asarray(r).copy(), np.asarray(nb).copy()) for r, nb in groups]
+        rows, nb = bad[-1]
+        nb[len(rows) // 2, 0] = bad_value
+        with pytest.raises(ValueError):
+            sv.vecchia_profile_loglik(theta, Xo, yo, Z, bad, 2.5)
+    bad = [(np.asarray(r).copy(), np.asarray(nb).copy()) for r, nb in groups]
+    bad[-1][0][3] = n
+    with pytest.raises(ValueError):
+        sv.vecchia_profile_loglik(theta, Xo, yo, Z, bad, 2.5)
+    # the good sets still evaluate afterwards
+    assert np.isfinite(sv.vecchia_profile_loglik(theta, Xo, yo, Z, groups, 2.5)[0])
+
+
+def test_group_order_and_large_blocks_pack_like_the_host(oracle):
+    """Conditioning sets given in any group order, with blocks beyond a warp
+    (k + 1 > 32), give the oracle's values through the device-packed table."""
+    sv, _, _, _nn_groups = _sv()
+    rng = np.random.default_rng(21)
+    n, d, m = 1500, 3, 40
+    X = rng.random((n, d))
+    y = rng.standard_normal(n)
+    Z = np.ones((n, 1))
+    nn = sv.find_ordered_nn(X, m)
+    groups = _nn_groups(nn, m)
+    theta = np.array([0.1, math.log(0.3), math.log(0.2), math.log(0.4), math.log(0.01)])
+    ref = oracle.vecchia_loglik(theta, X, y, Z, groups, 2.5)
+    shuffled = [groups[i] for i in rng.permutation(len(groups))]
+    for gs in (groups, shuffled):
+        ll, g, F, beta = sv.vecchia_profile_loglik(theta, X, y, Z, gs, 2.5)
+        assert abs(ll - ref[0]) <= 1e-9 * abs(ref[0])
+        np.testing.assert_allclose(g, ref[1], rtol=1e-8, atol=1e-8 * np.abs(ref[1]).max())
