@@ -655,7 +655,9 @@ struct EvalCall {
 int launch_warp_kernel(LikArgs A, cudaStream_t st) {
   const int nsm = sv_num_sms();
   const size_t team = sizeof(double) * team_smem_doubles(32, A.dmax, A.NRmax, A.need_grad, A.any_estimate_nu);
-  int wpc = 8;
+  // as many warps (teams) per CTA as shared memory holds: the float64 pipe
+  // needs every resident warp it can get to cover its latency
+  int wpc = 16;
   while (wpc > 1 && wpc * team > (size_t)max_smem_optin()) --wpc;
   const size_t smem = wpc * team;
   if (smem > (size_t)max_smem_optin()) return SV_EINVAL;
