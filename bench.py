@@ -95,10 +95,22 @@ class Clocks:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={q}",
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "25"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
+
+    def wait_first(self, timeout=5.0):
+        """Block until nvidia-smi has written its first sample (it takes a
+        while to start), so that the samples cover the whole timed region."""
+        t0 = time.perf_counter()
+        while self.p is not None and time.perf_counter() - t0 < timeout:
+            try:
+                if os.path.getsize(self.f.name) > 0:
+                    return
+            except OSError:
+                return
+            time.sleep(0.01)
 
     def stop(self):
         if self.p is None:
@@ -513,6 +525,7 @@ def main():
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks = Clocks(local)
+    clocks.wait_first()
     step_ms = time_form("split", best_lanes, args.steps, args.warmup)
     clk = clocks.stop()
     t_step = float(np.mean(step_ms)) * 1e-3
