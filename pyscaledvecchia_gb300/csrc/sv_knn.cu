@@ -101,6 +101,7 @@ struct KnnArgs {
   int32_t* nbr;        // ordered, block form: neighbour columns of blocks b0 + i
   int64_t b0;
   int ldnbr;
+  int wq_cap, wq_sort;  // large k: superset capacity and sort width per warp
 };
 
 __device__ __forceinline__ float knn_thr(double s64k, float Bi, int d) {
@@ -246,6 +247,275 @@ __global__ void __launch_bounds__(kKnnQ) k_knn(KnnArgs A) {
   knn_tile<DP>(A, qt, smraw);
 }
 
+// ---------------------------------------------------------------------------
+// Large k (kKnnHeapMin <= k <= kWqMaxK, DP <= 16): one warp per query.
+// The warps of a CTA (up to 8 queries) stream the same candidate tiles.  A
+// candidate's exact key (the float64 squared distance of the reference, IEEE
+// sequential) is bracketed by float32 bounds on its root,
+//   lo = sqrt(s32 / g) - B_q - B_c  <=  sqrt(key) (1 -+ tiny)  <=  hi = sqrt(s32 g) + B_q + B_c,
+// (s32 the float32 squared distance of the centred images, g the growth
+// factor of the screen above).  Each warp keeps in shared memory a superset
+// of its query's k nearest: every candidate whose lo does not exceed tau, the
+// k-th smallest hi kept so far (raised by 2^-20 for the root's rounding); no
+// candidate outside it can reach the k nearest.  When the buffer fills it is
+// filtered against the new tau, and if ties keep it full the exact keys of
+// its entries decide (sorted by (key, index), the first k kept).  At the end
+// the exact keys of the superset are sorted by (key, index): the reference's
+// k nearest in order.  float64 work is dense (one entry per lane) and limited
+// to about k entries per query.
+constexpr int kWqC = 256;      // candidates per tile
+constexpr int kWqMaxK = 1024;  // largest k of this path
+
+// superset capacity (k + 160 rounded to 32, at least 384) and sort width
+// (the power of two above it) per warp
+__host__ __device__ inline int wq_cap(int k) { return max(384, ((k + 160 + 31) / 32) * 32); }
+__host__ __device__ inline int wq_sort(int cap) {
+  int s = 32;
+  while (s < cap) s <<= 1;
+  return s;
+}
+
+struct WqSmem {
+  float* tv;      // [kWqC][DP] candidate images
+  float* tB;      // [kWqC] their bounds
+  float* bh;      // [warps][cap] hi of the superset entries
+  float* bl;      // [warps][cap] lo
+  int* bi;        // [warps][cap] index
+  double* bs;     // [warps][sort width] exact keys while sorting
+  int* bsi;       // [warps][sort width] their indices
+};
+
+__host__ __device__ inline size_t wq_smem_bytes(int DP, int warps, int cap, int sortw) {
+  return (size_t)kWqC * DP * 4 + (size_t)kWqC * 4 + (size_t)warps * ((size_t)cap * 12 + (size_t)sortw * 12);
+}
+
+// k-th smallest (k >= 1) of the n non-negative floats x[0..n) (warp):
+// radix search on the bit patterns, which order like the values
+__device__ __forceinline__ float wq_kth(const float* x, int n, int k) {
+  const int lane = threadIdx.x & 31;
+  unsigned res = 0;
+  for (int b = 30; b >= 0; --b) {
+    const unsigned trial = res | (1u << b);
+    int c = 0;
+    for (int e = lane; e < n; e += 32) c += __float_as_uint(x[e]) < trial;
+    c = __reduce_add_sync(0xffffffffu, c);
+    if (c < k) res = trial;  // fewer than k lie below: the k-th is >= trial
+  }
+  return __uint_as_float(res);
+}
+
+// exact keys of the n entries, sorted by (key, index); returns them in
+// S.bs/S.bsi[0..n) of this warp (warp-collective)
+__device__ __forceinline__ void wq_exact_sort(const WqSmem& S, int w, int n, const double* xq,
+                                              const double* Xr, int d, int cap, int sortw) {
+  const int lane = threadIdx.x & 31;
+  double* bs = S.bs + (size_t)w * sortw;
+  int* bsi = S.bsi + (size_t)w * sortw;
+  const int* bi = S.bi + (size_t)w * cap;
+  int np = 32;
+  while (np < n) np <<= 1;
+  for (int e = lane; e < np; e += 32) {
+    if (e < n) {
+      const int j = bi[e];
+      const double* xr = Xr + (size_t)j * d;
+      double s = 0.0;
+      for (int l = 0; l < d; ++l) {
+        const double df = __dsub_rn(xq[l], xr[l]);
+        s = __dadd_rn(s, __dmul_rn(df, df));
+      }
+      bs[e] = s;
+      bsi[e] = j;
+    } else {
+      bs[e] = __longlong_as_double(0x7ff0000000000000LL);
+      bsi[e] = 0x7fffffff;
+    }
+  }
+  __syncwarp();
+  // bitonic sort, ascending in (key, index)
+  for (int k = 2; k <= np; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = lane; t < np / 2; t += 32) {
+        const int lo = 2 * t - (t & (j - 1));  // index with bit j clear
+        const int hi = lo + j;
+        const bool up = (lo & k) == 0;
+        const double a = bs[lo], b = bs[hi];
+        const int ia = bsi[lo], ib = bsi[hi];
+        const bool agt = a > b || (a == b && ia > ib);
+        if (agt == up) {
+          bs[lo] = b;
+          bs[hi] = a;
+          bsi[lo] = ib;
+          bsi[hi] = ia;
+        }
+      }
+      __syncwarp();
+    }
+}
+
+template <int DP>
+__global__ void __launch_bounds__(256) k_knn_wq(KnnArgs A) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int nw = blockDim.x >> 5;
+  const int cap = A.wq_cap, sortw = A.wq_sort;
+  WqSmem S;
+  S.tv = (float*)smraw;
+  S.tB = S.tv + (size_t)kWqC * DP;
+  S.bh = S.tB + kWqC;
+  S.bl = S.bh + (size_t)nw * cap;
+  S.bi = (int*)(S.bl + (size_t)nw * cap);
+  S.bs = (double*)(S.bi + (size_t)nw * cap);  // 8-byte aligned: cap is a multiple of 32
+  S.bsi = (int*)(S.bs + (size_t)nw * sortw);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* bh = S.bh + (size_t)w * cap;
+  float* bl = S.bl + (size_t)w * cap;
+  int* bi = S.bi + (size_t)w * cap;
+  const int64_t ntile = (A.nq + nw - 1) / nw;
+  // ordered searches: largest rows first (their work grows with the row index)
+  const int64_t qt = A.ordered ? (ntile - 1 - blockIdx.x) : blockIdx.x;
+  const int64_t i = qt * nw + w;
+  const bool valid = i < A.nq;
+  int kq = A.k;
+  if (A.ordered) kq = (int)min((int64_t)A.m, i);
+  bool active = valid && kq > 0;
+  if (A.ordered && i < A.start) active = false;
+
+  float qv[DP];
+  float Bi = 0.0f;
+#pragma unroll
+  for (int l = 0; l < DP; ++l) qv[l] = valid ? A.vq[i * DP + l] : 0.0f;
+  if (valid) Bi = A.Bq[i];
+  const double* xq = A.Xq + (valid ? i : 0) * A.d;
+  int cnt = 0;
+  float Tq = __int_as_float(0x7f800000);  // tau' + B_q: +inf until a filter
+  const float g = A.growth;
+
+  // filter the superset against tau (the kq-th smallest hi); if ties keep it
+  // nearly full, keep the kq first by exact (key, index)
+  auto compact = [&]() {
+    const float tau = wq_kth(bh, cnt, kq);
+    const float taum = __fmul_ru(tau, 1.0f + 0x1p-20f);
+    int nc = 0;
+    for (int e0 = 0; e0 < cnt; e0 += 32) {
+      const int e = e0 + lane;
+      float h = 0.0f, l = 0.0f;
+      int ix = 0;
+      bool keep = false;
+      if (e < cnt) {
+        h = bh[e];
+        l = bl[e];
+        ix = bi[e];
+        keep = !(l > taum);
+      }
+      const unsigned km = __ballot_sync(0xffffffffu, keep);
+      __syncwarp();
+      if (keep) {
+        const int p = nc + __popc(km & ((1u << lane) - 1));
+        bh[p] = h;
+        bl[p] = l;
+        bi[p] = ix;
+      }
+      nc += __popc(km);
+      __syncwarp();
+    }
+    cnt = nc;
+    Tq = __fadd_ru(taum, Bi);
+    if (cnt > cap - 2 * 32) {
+      wq_exact_sort(S, w, cnt, xq, A.Xr, A.d, cap, sortw);
+      const double* bs = S.bs + (size_t)w * sortw;
+      const int* bsi = S.bsi + (size_t)w * sortw;
+      for (int e = lane; e < kq; e += 32) {
+        const double r = sqrt(bs[e]);
+        bh[e] = __double2float_ru(r * (1.0 + 0x1p-40));
+        bl[e] = __double2float_rd(r * (1.0 - 0x1p-40));
+        bi[e] = bsi[e];
+      }
+      __syncwarp();
+      cnt = kq;
+      const float tau2 = bh[kq - 1];  // the kq-th exact root, rounded up
+      Tq = __fadd_ru(__fmul_ru(tau2, 1.0f + 0x1p-20f), Bi);
+    }
+  };
+
+  int64_t cend = A.nr;
+  if (A.ordered) cend = min(A.nq, (qt + 1) * nw);  // rows < last query of the tile
+  for (int64_t c0 = 0; c0 < cend; c0 += kWqC) {
+    __syncthreads();
+    const int nc = (int)min((int64_t)kWqC, cend - c0);
+    for (int e = threadIdx.x; e < nc * DP; e += blockDim.x) S.tv[e] = A.vr[c0 * DP + e];
+    for (int e = threadIdx.x; e < nc; e += blockDim.x) S.tB[e] = A.Br[c0 + e];
+    __syncthreads();
+    if (!active) continue;
+    int cmax = nc;
+    if (A.ordered) {
+      const int64_t lim = i - c0;  // candidates j < i
+      if (lim <= 0) continue;
+      if (lim < cmax) cmax = (int)lim;
+    }
+    for (int cc0 = 0; cc0 < cmax; cc0 += 32) {
+      const int cc = cc0 + lane;
+      float s32 = 0.0f, Bc = 0.0f;
+      const bool in = cc < cmax;
+      if (in) {
+        const float* tv = S.tv + cc * DP;
+#pragma unroll
+        for (int l = 0; l < DP; l += 4) {
+          const float4 t4 = *reinterpret_cast<const float4*>(tv + l);
+          float df = __fsub_rn(qv[l], t4.x);
+          s32 = __fmaf_rn(df, df, s32);
+          df = __fsub_rn(qv[l + 1], t4.y);
+          s32 = __fmaf_rn(df, df, s32);
+          df = __fsub_rn(qv[l + 2], t4.z);
+          s32 = __fmaf_rn(df, df, s32);
+          df = __fsub_rn(qv[l + 3], t4.w);
+          s32 = __fmaf_rn(df, df, s32);
+        }
+        Bc = S.tB[cc];
+      }
+      // keep unless lo > tau': sqrt(s32 / g) > Tq + B_c
+      auto keep_of = [&]() {
+        if (!in) return false;
+        const float tb = __fadd_ru(Tq, Bc);
+        return !(s32 > __fmul_ru(__fmul_ru(tb, tb), g));
+      };
+      bool keep = keep_of();
+      unsigned km = __ballot_sync(0xffffffffu, keep);
+      if (!km) continue;
+      if (cnt + __popc(km) > cap) {
+        compact();
+        keep = keep_of();
+        km = __ballot_sync(0xffffffffu, keep);
+      }
+      if (keep) {
+        const int p = cnt + __popc(km & ((1u << lane) - 1));
+        const float bsum = __fadd_ru(Bi, Bc);
+        bh[p] = __fadd_ru(__fsqrt_ru(__fmul_ru(s32, g)), bsum);
+        bl[p] = __fsub_rd(__fsqrt_rd(__fdiv_rd(s32, g)), bsum);
+        bi[p] = (int)(c0 + cc);
+      }
+      cnt += __popc(km);
+      __syncwarp();
+    }
+  }
+  if (!valid) return;
+  int nout = 0;
+  if (active && cnt > 0) {
+    wq_exact_sort(S, w, cnt, xq, A.Xr, A.d, cap, sortw);
+    nout = min(cnt, kq);
+  }
+  const int* bsi = S.bsi + (size_t)w * sortw;
+  if (A.nbr) {
+    int32_t* row = A.nbr + (A.b0 + i) * (int64_t)A.ldnbr;
+    for (int c = lane; c < A.ldnbr; c += 32) row[c] = c < nout ? bsi[c] : -1;
+  } else if (A.ordered) {
+    int64_t* row = A.out + i * (int64_t)(A.m + 1);
+    if (lane == 0) row[0] = i;
+    for (int c = lane; c < A.m; c += 32) row[1 + c] = c < nout ? (int64_t)bsi[c] : -1;
+  } else {
+    int64_t* row = A.out + i * (int64_t)A.k;
+    for (int c = lane; c < A.k; c += 32) row[c] = c < nout ? (int64_t)bsi[c] : -1;
+  }
+}
+
 static int pad_dim(int d) {
   if (d <= 4) return 4;
   if (d <= 8) return 8;
@@ -266,7 +536,53 @@ static float growth_factor(int DP) {
   return gf;
 }
 
+static int knn_max_smem() {
+  int dev = 0, maxsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return maxsm;
+}
+
+// whether k takes the warp-per-query path, with its warps per CTA and shared memory
+static bool wq_plan(int k, int DP, int* warps, size_t* smem) {
+  if (k < kKnnHeapMin || k > kWqMaxK || DP > 16) return false;
+  const int cap = wq_cap(k), sw = wq_sort(cap);
+  int w = 8;
+  while (w > 1 && wq_smem_bytes(DP, w, cap, sw) > (size_t)knn_max_smem()) --w;
+  if (wq_smem_bytes(DP, w, cap, sw) > (size_t)knn_max_smem()) return false;
+  if (warps) *warps = w;
+  if (smem) *smem = wq_smem_bytes(DP, w, cap, sw);
+  return true;
+}
+
 static int launch_knn(const KnnArgs& A, int DP, int64_t grid, size_t smem, cudaStream_t st) {
+  if (wq_plan(A.k, DP, nullptr, nullptr)) {
+    // large k: one warp per query, as many warps per CTA (up to 8) as fit
+    KnnArgs W = A;
+    int warps = 0;
+    size_t wsm = 0;
+    wq_plan(A.k, DP, &warps, &wsm);
+    W.wq_cap = wq_cap(A.k);
+    W.wq_sort = wq_sort(W.wq_cap);
+    const int64_t wgrid = (A.nq + warps - 1) / warps;
+    switch (DP) {
+#define SV_WQ_CASE(V)                                                                          \
+  case V:                                                                                      \
+    SV_CUDA_TRY(cudaFuncSetAttribute(k_knn_wq<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     (int)wsm));                                               \
+    k_knn_wq<V><<<(unsigned)wgrid, warps * 32, wsm, st>>>(W);                                 \
+    break;
+      SV_WQ_CASE(4)
+      SV_WQ_CASE(8)
+      SV_WQ_CASE(12)
+      SV_WQ_CASE(16)
+#undef SV_WQ_CASE
+      default:
+        return SV_EINVAL;
+    }
+    SV_CUDA_TRY(cudaGetLastError());
+    return SV_OK;
+  }
   switch (DP) {
 #define SV_KNN_CASE(V)                                                                          \
   case V:                                                                                       \
@@ -377,6 +693,7 @@ extern "C" size_t sv_knn_query_workspace_bytes(int64_t nref, int64_t nq, int32_t
 static int knn_smem_ok(int DP, int k, size_t* smem) {
   *smem = sizeof(float) * (size_t)kKnnC * DP + sizeof(float) * kKnnC +
           (sizeof(double) + sizeof(int)) * (size_t)k * kKnnQ;
+  if (wq_plan(k, DP, nullptr, smem)) return 1;
   int dev = 0, maxsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);

@@ -154,6 +154,26 @@ def test_knn_query_exact_vs_oracle(oracle):
     np.testing.assert_array_equal(nb.cpu().numpy(), oracle.knn_query(Xr, Xq, 140))
 
 
+@pytest.mark.parametrize("k", [48, 140, 300])
+def test_large_k_lattice_ties_and_duplicates(oracle, k):
+    """Large k (one warp per query, a float32-bounded superset settled by
+    exact keys): lattice rows with exact ties and duplicated rows, ordered
+    and query searches, against the oracle."""
+    from pyscaledvecchia_gb300 import _lib
+    from pyscaledvecchia_gb300.ordering import knn_query_device
+    lib, torch = _lib.device_ready()
+    g = np.arange(11, dtype=float)
+    X = np.array([[a, b, c] for a in g for b in g for c in g]) / 3.0
+    X = np.vstack([X, X[::5]])
+    rng = np.random.default_rng(1)
+    X = X[rng.permutation(len(X))]
+    np.testing.assert_array_equal(_sv().find_ordered_nn(X, k, start=200), oracle.ordered_nn(X, k, 200))
+    Xq = np.vstack([X[:300], rng.uniform(-0.5, 4.0, (300, 3))])
+    nb, info = knn_query_device(torch, _lib.to_dev(torch, X, np.float64), _lib.to_dev(torch, Xq, np.float64), k)
+    _lib.check_info(lib, info.cpu().numpy(), "knn")
+    np.testing.assert_array_equal(nb.cpu().numpy(), oracle.knn_query(X, Xq, k))
+
+
 def test_knn_lattice_ties(oracle):
     g = np.arange(12, dtype=float)
     X = np.array([[a, b, c] for a in g for b in g for c in g])
