@@ -165,13 +165,18 @@ __global__ void k_pred_warp(PredArgs A) {
   }
 }
 
-__global__ void k_pred_cta(PredArgs A) {
+// threads of the CTA that owns one large prediction block: two CTAs of a
+// 141-point block fill an SM's shared memory, so 8 warps each keep 16 warps
+// resident to cover the float64 latency
+constexpr int kPredCta = 256;
+
+__global__ void __launch_bounds__(kPredCta) k_pred_cta(PredArgs A) {
   extern __shared__ double smem[];
   PredPrm* prm = (PredPrm*)smem;
   pred_params(A, prm);
   double* sm = smem + (sizeof(PredPrm) + 7) / 8;
   for (int64_t b = blockIdx.x; b < A.nblk; b += gridDim.x) {
-    pred_block<128>(A, prm, b, sm);
+    pred_block<kPredCta>(A, prm, b, sm);
     __syncthreads();
   }
 }
@@ -295,7 +300,7 @@ extern "C" int sv_predict_blocks(const sv_pred_desc* D, const double* theta, con
     SV_CUDA_TRY(cudaFuncSetAttribute(k_pred_cta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int64_t grid = D->nblk;
     if (grid > 16LL * nsm) grid = 16LL * nsm;
-    k_pred_cta<<<(unsigned)grid, 128, smem, st>>>(A);
+    k_pred_cta<<<(unsigned)grid, kPredCta, smem, st>>>(A);
   }
   SV_CUDA_TRY(cudaGetLastError());
   return SV_OK;
