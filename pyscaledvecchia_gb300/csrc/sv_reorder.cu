@@ -1092,6 +1092,7 @@ struct RoPlan {
   std::vector<int2> tiles[8];      // kNN tiles per padded dimension
   int DPs[8] = {4, 8, 12, 16, 24, 32, 48, 64};
   int kcap[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int trows[8] = {128, 128, 128, 128, 128, 128, 128, 128};  // kNN tile heights
   int64_t nrows = 0, nxs = 0, nv = 0;
   // workspace layout
   size_t o_probs, o_kprobs, o_plist[5], o_tiles[8], o_ranges, o_xs, o_v, o_b, o_ord, total, staged;
@@ -1156,7 +1157,17 @@ static int ro_plan(const sv_reorder_desc* D, const sv_reorder_prob* hp, RoPlan& 
     int gi = 0;
     while (L.DPs[gi] != R.DP) ++gi;
     L.kcap[gi] = std::max(L.kcap[gi], R.m);
-    const int64_t nt = (R.n + 127) / 128;
+  }
+  // kNN tiles (largest problems and, within one, the last rows first), of the
+  // height the search of each padded dimension takes
+  for (int g = 0; g < 8; ++g)
+    L.trows[g] = L.kcap[g] > 0 ? knn_batched_tile_rows(L.DPs[g], L.kcap[g]) : 128;
+  for (int32_t i : byn) {
+    const RoProb& R = L.probs[i];
+    if (R.n < 1 || R.m < 1 || R.n < 2) continue;
+    int gi = 0;
+    while (L.DPs[gi] != R.DP) ++gi;
+    const int64_t nt = (R.n + L.trows[gi] - 1) / L.trows[gi];
     for (int64_t t = nt - 1; t >= 0; --t) L.tiles[gi].push_back(make_int2(i, (int)t));
   }
   // workspace: staged tables first, then the arrays

@@ -18,6 +18,10 @@ struct KnnBatchProb {
 // padded dimension of the float32 screening rows (4, 8, 12, 16, 24, 32, 48, 64)
 int knn_pad_dim(int d);
 
+// rows per query tile of the batched ordered kNN for padded dimension DP and
+// largest neighbour count kcap (the tile table must be built with it)
+int knn_batched_tile_rows(int DP, int kcap);
+
 // ordered kNN of every (problem, query tile) entry of tiles (one CTA each);
 // all problems of the launch share DP; kcap >= every m
 int launch_knn_batched(int DP, const KnnBatchProb* probs, const int2* tiles, int64_t ntiles,
