@@ -397,26 +397,45 @@ __global__ void k_reduce1(RedArgs R) {
   const int64_t b0 = PI.blk_off + blockIdx.x * per;
   const int64_t b1 = min(PI.blk_off + PI.nblk, b0 + per);
   double* acc = racc + (int64_t)w * R.nfmax;
-  for (int f = lane; f < nf; f += 32) acc[f] = 0.0;
   const int foff = 3 + 2 * q + P * (2 + q);
-  for (int64_t b = b0 + w; b < b1; b += nwarp) {
-    const double* c = R.cache + b * R.CS;
-    for (int f = lane; f < nf; f += 32) {
-      double v;
-      if (f == 0) {
-        v = log(c[0]);
-      } else if (f < 1 + q) {
-        v = c[2 + (f - 1)] * c[1];
-      } else if (f < 1 + q + q * q) {
-        const int e = f - 1 - q;
-        const int i = e / q, jj = e - (e / q) * q;
-        v = c[2 + i] * c[2 + jj];
-      } else {
-        v = c[foff + (f - 1 - q - q * q)];
+  // the (warp, field) sums, one owner lane each: fields lane + 32 r < 128 in
+  // registers a[r], the rest (large d) in shared memory
+  constexpr int kFr = 4;
+  double a[kFr];
+#pragma unroll
+  for (int r = 0; r < kFr; ++r) a[r] = 0.0;
+  for (int f = lane + 32 * kFr; f < nf; f += 32) acc[f] = 0.0;
+  auto field = [&](const double* c, int f, double lgj) -> double {
+    if (f == 0) return lgj;
+    if (f < 1 + q) return c[2 + (f - 1)] * c[1];
+    if (f < 1 + q + q * q) {
+      const int e = f - 1 - q;
+      const int i = e / q, jj = e - (e / q) * q;
+      return c[2 + i] * c[2 + jj];
+    }
+    return c[foff + (f - 1 - q - q * q)];
+  };
+  for (int64_t base = b0 + w; base < b1; base += 32 * (int64_t)nwarp) {
+    // log L_KK of the warp's next 32 blocks, one per lane (a float64 warp
+    // instruction costs the same with one lane as with 32)
+    const int64_t bl = base + (int64_t)lane * nwarp;
+    const double lg = bl < b1 ? log(R.cache[bl * R.CS]) : 0.0;
+    for (int j = 0; j < 32; ++j) {
+      const int64_t b = base + (int64_t)j * nwarp;
+      if (b >= b1) break;
+      const double lgj = __shfl_sync(0xffffffffu, lg, j);
+      const double* c = R.cache + b * R.CS;
+#pragma unroll
+      for (int r = 0; r < kFr; ++r) {
+        const int f = lane + 32 * r;
+        if (f < nf) a[r] += field(c, f, lgj);
       }
-      acc[f] += v;
+      for (int f = lane + 32 * kFr; f < nf; f += 32) acc[f] += field(c, f, lgj);
     }
   }
+#pragma unroll
+  for (int r = 0; r < kFr; ++r)
+    if (lane + 32 * r < nf) acc[lane + 32 * r] = a[r];
   __syncthreads();
   double* part = R.part1 + ((int64_t)p * R.parts + blockIdx.x) * R.nfmax;
   for (int f = threadIdx.x; f < nf; f += blockDim.x) {
