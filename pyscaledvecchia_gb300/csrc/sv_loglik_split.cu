@@ -509,41 +509,18 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     // W = D^(-1/2) L^-1 dSigma a.  Without jitter Sigma a = L_KK e_K, whose
     // solution is sqrt(d_K) e_K, so that column is left out of the solve.
     const int c0 = (jit == 0.0) ? 1 : 0;
-    for (int i = 0; i < Kw - 1; ++i) {
-      if (ok && i < K - 1) {
-        const int m = K - i - 1;
-        const int cnt = m * (NR - c0);
-        if (tl < cnt) {
+    // columns c0 + tl, c0 + tl + G, ... per lane: every element sees the
+    // steps in order, with no warp synchronisation between steps
+    if (ok)
+      for (int c = c0 + tl; c < NR; c += G) {
+        double* col = R + c * 33;
+        for (int i = 0; i < K - 1; ++i) {
+          const double ri = col[i];
           const double* coli = Lp + cstart(i) - i;  // coli[j] = L(j, i)
-          int c = c0 + tl / m, r = tl - (tl / m) * m;
-          for (int t = tl; t < cnt; t += kSplitU * G) {
-            int cc[kSplitU], jj[kSplitU];
-#pragma unroll
-            for (int u4 = 0; u4 < kSplitU; ++u4) {
-              cc[u4] = c;
-              jj[u4] = i + 1 + r;
-              r += G;
-              while (r >= m) {
-                r -= m;
-                ++c;
-              }
-            }
-            double lji[kSplitU], rci[kSplitU], rcj[kSplitU];
-#pragma unroll
-            for (int u4 = 0; u4 < kSplitU; ++u4)
-              if (t + u4 * G < cnt) {
-                lji[u4] = coli[jj[u4]];
-                rci[u4] = R[cc[u4] * 33 + i];
-                rcj[u4] = R[cc[u4] * 33 + jj[u4]];
-              }
-#pragma unroll
-            for (int u4 = 0; u4 < kSplitU; ++u4)
-              if (t + u4 * G < cnt) R[cc[u4] * 33 + jj[u4]] = fma(-lji[u4], rci[u4], rcj[u4]);
-          }
+          for (int j = i + 1; j < K; ++j) col[j] = fma(-coli[j], ri, col[j]);
         }
       }
-      __syncwarp();
-    }
+    __syncwarp();
     if (ok) {
       if (c0 == 1)
         for (int i = tl; i < K; i += G) R[i] = (i == k) ? lKK : 0.0;
