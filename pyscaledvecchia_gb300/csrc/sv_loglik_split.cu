@@ -30,6 +30,8 @@ constexpr int kSplitMaxThreads = 512;
 // independent elements per lane per round of the factorisation update and the
 // multi-column forward solve (instruction-level parallelism per lane)
 constexpr int kSplitU = 4;
+// elements per round of the two-column trailing update (two FMAs each)
+constexpr int kSplitU2 = 2;
 
 __device__ __forceinline__ void matern_closed_f32(int code, float r, float& M, float& g) {
   if (code == 0) {
@@ -218,16 +220,19 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tm = lane / G, tl = lane - (lane / G) * G;
   const int dmax = A.dmax;
-  const int64_t slot = split_slot_doubles(dmax, A.NRmax);
+  // at least one R column: column 0 of R and a are the factorisation's scratch
+  const int nrs = A.NRmax > 0 ? A.NRmax : 1;
+  const int64_t slot = split_slot_doubles(dmax, nrs);
   double* Lp = smem + (int64_t)(warp * NB + tm) * slot;
   double* R = Lp + 528;  // NR columns, stride 33
-  double* a = R + 33 * A.NRmax;
+  double* a = R + 33 * nrs;
   double* invd = a + 32;
   float* a32 = (float*)(invd + 32);
   float* u = a32 + 32;
   int* idx = (int*)(u + 32 * dmax);
   volatile int* tflag = idx + 32;
   double* acc = R;            // column 0 of R is scratch during the a solve
+  double* acc2 = a;           // second unscaled column of the two-column factorisation step
   float* R32 = (float*)Lp;    // float32 copy of R once L is no longer needed
 
   const int64_t nb = A.b1 - A.b0;
@@ -309,37 +314,58 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       __syncwarp();
       if (need && tl == 0) split_pivot(Lp[cm(0, 0)], 0, rho_bits, invd, tflag);
       __syncwarp();
-      // right-looking LDL^T by columns, warp-uniform step loop; acc holds the
-      // unscaled pivot column of the current step.  The lane that updates
-      // (kk+1, kk+1) takes the next pivot's reciprocal at once (look-ahead).
-      for (int kk = 0; kk < Kw; ++kk) {
-        const bool go2 = need && kk < K && tflag[0] == 0;
-        if (go2) {
+      // right-looking LDL^T, two columns per step (warp-uniform loop):
+      //  1. column kk scaled by 1/d_kk, its unscaled values in acc;
+      //  2. column kk+1 takes step kk's update, its pivot follows at once;
+      //  3. column kk+1 scaled, its unscaled values in acc2;
+      //  4. every trailing element (j >= kk+2) takes both updates in one visit,
+      //     fma(-l(i,kk+1) a(j,kk+1), fma(-l(i,kk) a(j,kk), A(i,j))), the same two
+      //     roundings in the same order as two single steps; the lane that
+      //     updates (kk+2, kk+2) takes that pivot's reciprocal (look-ahead).
+      // A failed pivot stops the attempt (it is redone with jitter).
+      for (int kk = 0; kk < Kw; kk += 2) {
+        const bool go = need && kk < K && tflag[0] == 0;
+        double* colk1 = Lp + cstart(kk) - kk;            // colk1[i] = L(i, kk)
+        double* colk2 = Lp + cstart(kk + 1) - (kk + 1);  // colk2[i] = L(i, kk+1)
+        if (go) {
           const double inv = invd[kk];
-          double* colk = Lp + cstart(kk) - kk;  // colk[i] = L(i, kk)
           for (int i = kk + 1 + tl; i < K; i += G) {
-            const double v = colk[i];
+            const double v = colk1[i];
             acc[i] = v;
-            colk[i] = v * inv;
+            colk1[i] = v * inv;
           }
         }
         __syncwarp();
+        const bool two = go && kk + 1 < K;
+        if (two) {
+          const double a1 = acc[kk + 1];
+          for (int i = kk + 1 + tl; i < K; i += G) {
+            const double v = fma(-colk1[i], a1, colk2[i]);
+            colk2[i] = v;
+            acc2[i] = v;
+            if (i == kk + 1) split_pivot(v, kk + 1, rho_bits, invd, tflag);
+          }
+        }
+        __syncwarp();
+        const bool go2 = two && tflag[0] == 0;
         if (go2) {
-          const int m = K - kk - 1;
+          const double inv = invd[kk + 1];
+          for (int i = kk + 2 + tl; i < K; i += G) colk2[i] = acc2[i] * inv;
+        }
+        __syncwarp();
+        if (go2) {
+          const int m = K - kk - 2;
           const int cnt = m * (m + 1) / 2;
           if (tl < cnt) {
-            const double* colk = Lp + cstart(kk) - kk;
-            int j = kk + 1, rem = tl;
+            int j = kk + 2, rem = tl;
             while (rem >= K - j) {
               rem -= K - j;
               ++j;
             }
-            // kSplitU (4) independent elements per round keep several float64 FMAs
-            // in flight per lane:  A(i, j) -= l(i, k) * A(j, k)
-            for (int t = tl; t < cnt; t += kSplitU * G) {
-              int jj[kSplitU], ii[kSplitU];
+            for (int t = tl; t < cnt; t += kSplitU2 * G) {
+              int jj[kSplitU2], ii[kSplitU2];
 #pragma unroll
-              for (int u4 = 0; u4 < kSplitU; ++u4) {
+              for (int u4 = 0; u4 < kSplitU2; ++u4) {
                 jj[u4] = j;
                 ii[u4] = j + rem;
                 rem += G;
@@ -348,20 +374,22 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
                   ++j;
                 }
               }
-              double lik[kSplitU], ajk[kSplitU], aij[kSplitU];
+              double l1[kSplitU2], l2[kSplitU2], a1[kSplitU2], a2[kSplitU2], aij[kSplitU2];
 #pragma unroll
-              for (int u4 = 0; u4 < kSplitU; ++u4)
+              for (int u4 = 0; u4 < kSplitU2; ++u4)
                 if (t + u4 * G < cnt) {
-                  lik[u4] = colk[ii[u4]];
-                  ajk[u4] = acc[jj[u4]];
+                  l1[u4] = colk1[ii[u4]];
+                  l2[u4] = colk2[ii[u4]];
+                  a1[u4] = acc[jj[u4]];
+                  a2[u4] = acc2[jj[u4]];
                   aij[u4] = Lp[cm(ii[u4], jj[u4])];
                 }
 #pragma unroll
-              for (int u4 = 0; u4 < kSplitU; ++u4)
+              for (int u4 = 0; u4 < kSplitU2; ++u4)
                 if (t + u4 * G < cnt) {
-                  const double nv = fma(-lik[u4], ajk[u4], aij[u4]);
+                  const double nv = fma(-l2[u4], a2[u4], fma(-l1[u4], a1[u4], aij[u4]));
                   Lp[cm(ii[u4], jj[u4])] = nv;
-                  if (ii[u4] == kk + 1 && jj[u4] == kk + 1) split_pivot(nv, kk + 1, rho_bits, invd, tflag);
+                  if (ii[u4] == kk + 2 && jj[u4] == kk + 2) split_pivot(nv, kk + 2, rho_bits, invd, tflag);
                 }
             }
           }
@@ -609,7 +637,8 @@ int launch_block_split(const LikArgs& A, int lanes, cudaStream_t st) {
   int dev = 0, maxsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const size_t per_warp = sizeof(double) * (size_t)split_slot_doubles(A.dmax, A.NRmax) * (32 / lanes);
+  const size_t per_warp =
+      sizeof(double) * (size_t)split_slot_doubles(A.dmax, A.NRmax > 0 ? A.NRmax : 1) * (32 / lanes);
   int wpc = kSplitMaxThreads / 32;
   while (wpc > 1 && wpc * per_warp > (size_t)maxsm) --wpc;
   const size_t smem = wpc * per_warp;
