@@ -30,8 +30,11 @@ constexpr int kSplitMaxThreads = 512;
 // independent elements per lane per round of the factorisation update and the
 // multi-column forward solve (instruction-level parallelism per lane)
 constexpr int kSplitU = 4;
-// elements per round of the two-column trailing update (two FMAs each)
-constexpr int kSplitU2 = 2;
+// columns per factorisation step (panel width) and trailing elements per
+// round of a step (kSplitW FMAs each): measured at C2, widths 2, 3, 4, 6, 8
+// took 9.31, 9.18, 9.05, 9.11, 9.16 ms
+constexpr int kSplitW = 4;
+constexpr int kSplitU2 = 1;
 
 __device__ __forceinline__ void matern_closed_f32(int code, float r, float& M, float& g) {
   if (code == 0) {
@@ -220,8 +223,9 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tm = lane / G, tl = lane - (lane / G) * G;
   const int dmax = A.dmax;
-  // at least one R column: column 0 of R and a are the factorisation's scratch
-  const int nrs = A.NRmax > 0 ? A.NRmax : 1;
+  // at least kSplitW - 1 R columns: R's first columns and a are the
+  // factorisation's scratch
+  const int nrs = A.NRmax > kSplitW - 1 ? A.NRmax : kSplitW - 1;
   const int64_t slot = split_slot_doubles(dmax, nrs);
   double* Lp = smem + (int64_t)(warp * NB + tm) * slot;
   double* R = Lp + 528;  // NR columns, stride 33
@@ -232,7 +236,10 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
   int* idx = (int*)(u + 32 * dmax);
   volatile int* tflag = idx + 32;
   double* acc = R;            // column 0 of R is scratch during the a solve
-  double* acc2 = a;           // second unscaled column of the two-column factorisation step
+  // unscaled columns of a factorisation step: R's first columns, then a
+  double* accs[kSplitW];
+#pragma unroll
+  for (int p = 0; p < kSplitW; ++p) accs[p] = p < kSplitW - 1 ? R + 33 * p : a;
   float* R32 = (float*)Lp;    // float32 copy of R once L is no longer needed
 
   const int64_t nb = A.b1 - A.b0;
@@ -314,50 +321,52 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       __syncwarp();
       if (need && tl == 0) split_pivot(Lp[cm(0, 0)], 0, rho_bits, invd, tflag);
       __syncwarp();
-      // right-looking LDL^T, two columns per step (warp-uniform loop):
-      //  1. column kk scaled by 1/d_kk, its unscaled values in acc;
-      //  2. column kk+1 takes step kk's update, its pivot follows at once;
-      //  3. column kk+1 scaled, its unscaled values in acc2;
-      //  4. every trailing element (j >= kk+2) takes both updates in one visit,
-      //     fma(-l(i,kk+1) a(j,kk+1), fma(-l(i,kk) a(j,kk), A(i,j))), the same two
-      //     roundings in the same order as two single steps; the lane that
-      //     updates (kk+2, kk+2) takes that pivot's reciprocal (look-ahead).
+      // right-looking LDL^T, kSplitW columns (a panel) per step, warp-uniform
+      // loop.  Panel column c = kk + p takes the steps kk .. c-1 in order (its
+      // pivot follows at once), then is scaled by 1/d_c, its unscaled values
+      // in accs[p]; every trailing element (j >= kk + kSplitW) then takes all
+      // kSplitW updates in one visit, fma(-l(i,s) a(j,s), .) for s = kk, kk+1,
+      // ...: the same roundings in the same order as single steps.  The lane
+      // that updates (kk+W, kk+W) takes that pivot's reciprocal (look-ahead).
       // A failed pivot stops the attempt (it is redone with jitter).
-      for (int kk = 0; kk < Kw; kk += 2) {
-        const bool go = need && kk < K && tflag[0] == 0;
-        double* colk1 = Lp + cstart(kk) - kk;            // colk1[i] = L(i, kk)
-        double* colk2 = Lp + cstart(kk + 1) - (kk + 1);  // colk2[i] = L(i, kk+1)
+      auto colp = [&](int c) { return Lp + cstart(c) - c; };  // colp(c)[i] = L(i, c)
+      for (int kk = 0; kk < Kw; kk += kSplitW) {
+        bool go = need && kk < K && tflag[0] == 0;
+#pragma unroll
+        for (int p = 0; p < kSplitW; ++p) {
+          const int c = kk + p;
+          if (p > 0) {
+            if (go && c < K) {
+              double* colc = colp(c);
+              for (int i = c + tl; i < K; i += G) {
+                double v = colc[i];
+#pragma unroll
+                for (int s2 = 0; s2 < p; ++s2) v = fma(-colp(kk + s2)[i], accs[s2][c], v);
+                colc[i] = v;
+                accs[p][i] = v;
+                if (i == c) split_pivot(v, c, rho_bits, invd, tflag);
+              }
+            }
+            __syncwarp();
+            go = go && tflag[0] == 0;
+          }
+          if (go && c < K) {
+            double* colc = colp(c);
+            const double inv = invd[c];
+            for (int i = c + 1 + tl; i < K; i += G) {
+              const double v = p == 0 ? colc[i] : accs[p][i];
+              if (p == 0) accs[0][i] = v;
+              colc[i] = v * inv;
+            }
+          }
+          __syncwarp();
+        }
         if (go) {
-          const double inv = invd[kk];
-          for (int i = kk + 1 + tl; i < K; i += G) {
-            const double v = colk1[i];
-            acc[i] = v;
-            colk1[i] = v * inv;
-          }
-        }
-        __syncwarp();
-        const bool two = go && kk + 1 < K;
-        if (two) {
-          const double a1 = acc[kk + 1];
-          for (int i = kk + 1 + tl; i < K; i += G) {
-            const double v = fma(-colk1[i], a1, colk2[i]);
-            colk2[i] = v;
-            acc2[i] = v;
-            if (i == kk + 1) split_pivot(v, kk + 1, rho_bits, invd, tflag);
-          }
-        }
-        __syncwarp();
-        const bool go2 = two && tflag[0] == 0;
-        if (go2) {
-          const double inv = invd[kk + 1];
-          for (int i = kk + 2 + tl; i < K; i += G) colk2[i] = acc2[i] * inv;
-        }
-        __syncwarp();
-        if (go2) {
-          const int m = K - kk - 2;
-          const int cnt = m * (m + 1) / 2;
+          const int j0 = kk + kSplitW;
+          const int m = K - j0;
+          const int cnt = m > 0 ? m * (m + 1) / 2 : 0;
           if (tl < cnt) {
-            int j = kk + 2, rem = tl;
+            int j = j0, rem = tl;
             while (rem >= K - j) {
               rem -= K - j;
               ++j;
@@ -374,22 +383,22 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
                   ++j;
                 }
               }
-              double l1[kSplitU2], l2[kSplitU2], a1[kSplitU2], a2[kSplitU2], aij[kSplitU2];
+              double nv[kSplitU2];
+#pragma unroll
+              for (int u4 = 0; u4 < kSplitU2; ++u4)
+                if (t + u4 * G < cnt) nv[u4] = Lp[cm(ii[u4], jj[u4])];
+#pragma unroll
+              for (int s2 = 0; s2 < kSplitW; ++s2) {
+                const double* cs = colp(kk + s2);
+#pragma unroll
+                for (int u4 = 0; u4 < kSplitU2; ++u4)
+                  if (t + u4 * G < cnt) nv[u4] = fma(-cs[ii[u4]], accs[s2][jj[u4]], nv[u4]);
+              }
 #pragma unroll
               for (int u4 = 0; u4 < kSplitU2; ++u4)
                 if (t + u4 * G < cnt) {
-                  l1[u4] = colk1[ii[u4]];
-                  l2[u4] = colk2[ii[u4]];
-                  a1[u4] = acc[jj[u4]];
-                  a2[u4] = acc2[jj[u4]];
-                  aij[u4] = Lp[cm(ii[u4], jj[u4])];
-                }
-#pragma unroll
-              for (int u4 = 0; u4 < kSplitU2; ++u4)
-                if (t + u4 * G < cnt) {
-                  const double nv = fma(-l2[u4], a2[u4], fma(-l1[u4], a1[u4], aij[u4]));
-                  Lp[cm(ii[u4], jj[u4])] = nv;
-                  if (ii[u4] == kk + 2 && jj[u4] == kk + 2) split_pivot(nv, kk + 2, rho_bits, invd, tflag);
+                  Lp[cm(ii[u4], jj[u4])] = nv[u4];
+                  if (ii[u4] == j0 && jj[u4] == j0) split_pivot(nv[u4], j0, rho_bits, invd, tflag);
                 }
             }
           }
@@ -638,7 +647,8 @@ int launch_block_split(const LikArgs& A, int lanes, cudaStream_t st) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t per_warp =
-      sizeof(double) * (size_t)split_slot_doubles(A.dmax, A.NRmax > 0 ? A.NRmax : 1) * (32 / lanes);
+      sizeof(double) * (size_t)split_slot_doubles(A.dmax, A.NRmax > kSplitW - 1 ? A.NRmax : kSplitW - 1) *
+      (32 / lanes);
   int wpc = kSplitMaxThreads / 32;
   while (wpc > 1 && wpc * per_warp > (size_t)maxsm) --wpc;
   const size_t smem = wpc * per_warp;
