@@ -34,6 +34,8 @@ constexpr int kSplitU = 4;
 // round of a step (kSplitW FMAs each): measured at C2, widths 2, 3, 4, 6, 8
 // took 9.31, 9.18, 9.05, 9.11, 9.16 ms
 constexpr int kSplitW = 4;
+// steps per pass of the forward solves
+constexpr int kSplitWF = 4;
 constexpr int kSplitU2 = 1;
 
 __device__ __forceinline__ void matern_closed_f32(int code, float r, float& M, float& g) {
@@ -546,15 +548,32 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     // W = D^(-1/2) L^-1 dSigma a.  Without jitter Sigma a = L_KK e_K, whose
     // solution is sqrt(d_K) e_K, so that column is left out of the solve.
     const int c0 = (jit == 0.0) ? 1 : 0;
-    // columns c0 + tl, c0 + tl + G, ... per lane: every element sees the
-    // steps in order, with no warp synchronisation between steps
+    // columns c0 + tl, c0 + tl + G, ... per lane, with no warp
+    // synchronisation between steps; kSplitWF steps per pass: the panel's
+    // own rows are finished in order, then every later row takes the
+    // panel's updates in one visit (each element sees the steps in order)
     if (ok)
       for (int c = c0 + tl; c < NR; c += G) {
         double* col = R + c * 33;
-        for (int i = 0; i < K - 1; ++i) {
-          const double ri = col[i];
-          const double* coli = Lp + cstart(i) - i;  // coli[j] = L(j, i)
-          for (int j = i + 1; j < K; ++j) col[j] = fma(-coli[j], ri, col[j]);
+        for (int i = 0; i < K - 1; i += kSplitWF) {
+          const int ns = min(kSplitWF, K - 1 - i);  // steps i .. i+ns-1
+          double r[kSplitWF];
+#pragma unroll
+          for (int s2 = 0; s2 < kSplitWF; ++s2)
+            if (s2 < ns) {
+              double v = col[i + s2];
+#pragma unroll
+              for (int t2 = 0; t2 < s2; ++t2) v = fma(-Lp[cm(i + s2, i + t2)], r[t2], v);
+              r[s2] = v;
+              col[i + s2] = v;
+            }
+          for (int j = i + ns; j < K; ++j) {
+            double v = col[j];
+#pragma unroll
+            for (int t2 = 0; t2 < kSplitWF; ++t2)
+              if (t2 < ns) v = fma(-Lp[cm(j, i + t2)], r[t2], v);
+            col[j] = v;
+          }
         }
       }
     __syncwarp();
