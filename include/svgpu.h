@@ -177,6 +177,16 @@ typedef struct sv_pack_group {
 int sv_pack_blocks(const sv_pack_group* groups, int32_t ngroups, int64_t n, int32_t ldnbr,
                    int32_t* rowb, int32_t* kb, int32_t* nbr, int32_t* bad, sv_stream_t stream);
 
+/* Jitter-sharing chunk of every block (the chunks of _covariance.py:255-259
+ * that likelihood.py:114 factorises together): block r of a group, at
+ * out_off + r in the block table, gets chunk base + r / step, where step is
+ * _chunks' row count and base the chunks of the groups before it. */
+typedef struct sv_chunk_group {
+  int64_t count, out_off;
+  int32_t base, step;
+} sv_chunk_group;
+int sv_chunk_ids(const sv_chunk_group* groups, int32_t ngroups, int32_t* ids, sv_stream_t stream);
+
 size_t sv_loglik_workspace_bytes(const sv_loglik_desc* desc);
 int sv_vecchia_loglik(const sv_loglik_desc* desc, const double* theta, const double* X,
                       const double* y, const double* Z, const int32_t* rowb, const int32_t* kb,

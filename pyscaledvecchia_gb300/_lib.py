@@ -64,6 +64,11 @@ class PackGroup(ctypes.Structure):
                 ("k", c_i32), ("pad", c_i32)]
 
 
+class ChunkGroup(ctypes.Structure):
+    """Mirror of sv_chunk_group (include/svgpu.h)."""
+    _fields_ = [("count", c_i64), ("out_off", c_i64), ("base", c_i32), ("step", c_i32)]
+
+
 class ReorderDesc(ctypes.Structure):
     """Mirror of sv_reorder_desc (include/svgpu.h)."""
     _fields_ = [("nprob", c_i64), ("dmax", c_i32), ("ldnbr", c_i32)]
@@ -93,6 +98,7 @@ SIGNATURES = {
     "sv_reorder_batched": (c_i32, [ctypes.POINTER(ReorderDesc), c_vp, c_vp] + [c_vp] * 10 + [c_sz, c_vp]),
     "sv_loglik_workspace_bytes": (c_sz, [ctypes.POINTER(LoglikDesc)]),
     "sv_pack_blocks": (c_i32, [c_vp, c_i32, c_i64, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "sv_chunk_ids": (c_i32, [c_vp, c_i32, c_vp, c_vp]),
     "sv_vecchia_loglik": (c_i32, [ctypes.POINTER(LoglikDesc), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
                                   c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "sv_loglik_batched_workspace_bytes": (c_sz, [ctypes.POINTER(BatchDesc)]),
@@ -169,12 +175,11 @@ def stream_handle(torch):
 
 
 def to_dev(torch, arr, dtype):
-    """numpy -> device tensor (contiguous)."""
+    """numpy -> device tensor (contiguous).  A plain copy from pageable
+    memory: over the GB300's chip-to-chip link it takes half the time of a
+    copy staged through pinned memory (48 MB: 0.29 ms against 0.57 ms)."""
     a = np.ascontiguousarray(arr, dtype=dtype)
-    t = torch.from_numpy(a)
-    if a.size:
-        t = t.pin_memory() if a.nbytes >= (1 << 20) else t
-    return t.to("cuda", non_blocking=True)
+    return torch.from_numpy(a).to("cuda")
 
 
 def ptr(t):

@@ -144,6 +144,7 @@ class DeviceProblem:
         self._gid = np.repeat(np.asarray(order, dtype=np.int32),
                               np.asarray([gl[g] for g in order], dtype=np.int64))
         self._gk, self._gl = gk, gl
+        self._goff = [0] * len(gk)  # first block of each group in the packed table
         if B == 0:
             return
         # small groups travel in one copy, large ones in their own
@@ -163,6 +164,7 @@ class DeviceProblem:
         desc = (_lib.PackGroup * len(order))()
         o = 0
         for j, g in enumerate(order):
+            self._goff[g] = o
             r_d, nb_d = dev[g]
             desc[j].rows = r_d.data_ptr() if gl[g] else None
             desc[j].nb = nb_d.data_ptr() if gl[g] * gk[g] else None
@@ -192,9 +194,24 @@ class DeviceProblem:
         return n + 2 + 4  # status/parameter set-up, then the four reduction kernels
 
     def chunk_tensor(self, Pc):
+        """Chunk of every block (chunk_ids), computed on the device from the
+        groups' sizes and _chunks' row counts (sv_chunk_ids)."""
         if Pc not in self._chunks:
-            ids = chunk_ids(self._gid, self._gk, self._gl, Pc)
-            self._chunks[Pc] = _lib.to_dev(self.torch, ids, np.int32)
+            torch, lib = self.torch, self.lib
+            G = len(self._gk)
+            desc = (_lib.ChunkGroup * max(G, 1))()
+            base = 0
+            for g in range(G):
+                k, ln = self._gk[g], self._gl[g]
+                step = max(1, 4_000_000 // max(1, (k + 1) * (k + 1) * max(Pc, 1)))  # _chunks
+                desc[g].count, desc[g].out_off = ln, self._goff[g]
+                desc[g].base, desc[g].step = base, step
+                base += (ln + step - 1) // step
+            ids = torch.empty(max(self.nblk, 1), dtype=torch.int32, device="cuda")[:self.nblk]
+            rc = lib.sv_chunk_ids(ctypes.cast(desc, ctypes.c_void_p), G, _lib.ptr(ids),
+                                  _lib.stream_handle(torch))
+            _lib.check(lib, rc, "sv_chunk_ids")
+            self._chunks[Pc] = ids
         return self._chunks[Pc]
 
     def launch(self, theta_dev, P, nu, estimate_nu, need_grad, var_penalty, log_var_target,

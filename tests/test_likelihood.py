@@ -274,3 +274,22 @@ def test_group_order_and_large_blocks_pack_like_the_host(oracle):
         ll, g, F, beta = sv.vecchia_profile_loglik(theta, X, y, Z, gs, 2.5)
         assert abs(ll - ref[0]) <= 1e-9 * abs(ref[0])
         np.testing.assert_allclose(g, ref[1], rtol=1e-8, atol=1e-8 * np.abs(ref[1]).max())
+
+
+def test_device_chunk_ids_match_the_host_rule():
+    """Chunk ids computed on the device (sv_chunk_ids) equal the host rule
+    (chunk_ids: _chunks per group, groups numbered in their own order), for
+    groups in order, shuffled, and with blocks beyond a warp moved last."""
+    sv, _, _, _nn_groups = _sv()
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem, chunk_ids
+    rng = np.random.default_rng(5)
+    for n, d, m in ((3000, 3, 20), (2500, 2, 45)):
+        X = rng.random((n, d))
+        groups = _nn_groups(sv.find_ordered_nn(X, m), m)
+        for gs in (groups, [groups[i] for i in rng.permutation(len(groups))]):
+            prob = DeviceProblem(X, rng.standard_normal(n), None, gs)
+            for Pc in (1, d + 2):
+                got = prob.chunk_tensor(Pc).cpu().numpy()
+                want = chunk_ids(prob._gid, prob._gk, prob._gl, Pc)
+                np.testing.assert_array_equal(got, want)
+
