@@ -2,27 +2,34 @@
 // evaluation (blocks with K = k+1 <= 32, closed-form nu).
 //
 // Same per-block record as the float64 kernels (likelihood.py:111-144 of the
-// reference), computed with float64 only where conditioning needs it:
-//   float32 : centred scaled coordinates, distances, the correlation
-//             deficit 1 - M (accurate for close pairs) and g, the
-//             products dSigma_l a (K^2 d), the Fisher / score Gram products;
-//   float64 : the diagonal s2(1+tau) (+ jitter), the Cholesky factorisation,
-//             a = L^-T e_K, the forward solves W = L^-1 [dSigma a], L^-1 y,
-//             L^-1 Z, log L_KK and everything reduced afterwards.
-// On GB300 a float64 instruction costs 1/66 of the FP32 rate and a masked
-// lane costs as much as an active one, so a block is owned by a team of G
-// lanes and a warp holds 32/G blocks: the serial part of each factorisation
-// step is shared by 32/G blocks.  The factorisation is LDL^T (unit lower L,
-// D = diag(d_k)), which needs one reciprocal per step (an FP32 seed and one
-// float64 Newton step) and no square roots; the Cholesky factor is
+// reference), computed with float64 precision only where conditioning needs
+// it:
+//   float32      : centred scaled coordinates, distances, the correlation
+//                  deficit 1 - M (accurate for close pairs) and g, the
+//                  products dSigma_l a (K^2 d), the Fisher / score Gram
+//                  products;
+//   double-float : (pairs of float32, about 46 bits; sv_df64.cuh) the entries
+//                  s2 (1 - D) and the diagonal s2 (1 + tau) (+ jitter), the
+//                  LDL^T factorisation, a = L^-T e_K, the forward solves
+//                  W = L^-1 [dSigma a], L^-1 y, L^-1 Z and the GLS sums;
+//   float64      : the record and everything reduced afterwards.
+// On GB300 a float64 instruction occupies the float64 pipe for about 64
+// scheduler cycles, a float32 instruction for one: a double-float update
+// v - l a takes about 12 float32 instructions, several times less than the
+// float64 FMA it replaces, with errors (2^-46 relative) far below the float32
+// assembly's.  A block is owned by a team of G lanes and a warp holds 32/G
+// blocks.  The factorisation is LDL^T (unit lower L, D = diag(d_k)), which
+// needs one reciprocal per step and no square roots; the Cholesky factor is
 // C = L D^(1/2), so a = C^-T e_K = L^-T e_K / sqrt(d_K), W = D^(-1/2) L^-1 V
 // (unit forward solves, the D^(-1/2) weights applied in the float32 Gram)
-// and L_KK = sqrt(d_K) (one float64 square root per block).
+// and L_KK = sqrt(d_K).  Blocks whose scale or data leave float32's exponent
+// range are left to the float64 pass.
 //
 // Warp-uniform outer loops (up to the warp's largest K) with team-local
 // predication keep every __syncwarp reached by all lanes when the blocks of a
 // warp differ in size.
 #include "sv_loglik.cuh"
+#include "sv_df64.cuh"
 
 namespace sv {
 
@@ -95,23 +102,16 @@ __device__ __forceinline__ float matern_deficit_f32(int code, float r) {
   return e * fmaf(c * c, 1.0f / 6.0f, exp_tail(c, 3));
 }
 
-// Order tests on the bit patterns of positive doubles (integer pipe, not the
-// slow float64 pipe): for x, y >= 0, x < y <=> bits(x) < bits(y).
+// Order tests on the bit patterns of positive numbers (integer pipe): for
+// x, y >= 0, x < y <=> bits(x) < bits(y).
 __device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
 constexpr long long kBitsTiny = 0x39B4484BFEEBC2A0LL;  // 1e-30
 constexpr long long kBitsHuge = 0x46293E5939A08CEALL;  // 1e30
-constexpr long long kBitsInf = 0x7FF0000000000000LL;
+constexpr int kFBitsInf = 0x7F800000;
 
-// float64 reciprocal of a pivot from the float32 reciprocal refined by one
-// Newton step y <- y + y (1 - d y): relative error about 2^-44, far below the
-// float32 assembly error of the split form; a chain of two float64 FMAs.
-__device__ __forceinline__ double pivot_rcp(double dkk) {
-  const long long bd = dbits(dkk);
-  if (bd > kBitsTiny && bd < kBitsHuge) {
-    const double y = (double)(1.0f / (float)dkk);
-    return fma(y, fma(-dkk, y, 1.0), y);
-  }
-  return 1.0 / dkk;
+// |x| < 1e30 for a float64 x (bit test; NaN fails)
+__device__ __forceinline__ bool in_f32_range(double x) {
+  return (dbits(x) & 0x7FFFFFFFFFFFFFFFLL) < kBitsHuge;
 }
 
 // Rows i of the float32 right-hand sides dSigma_l a for l = 1..d:
@@ -121,7 +121,7 @@ __device__ __forceinline__ double pivot_rcp(double dkk) {
 // roundings in the same order as a pass per l.
 template <int DR>
 __device__ __forceinline__ void split_dsig_row(int i, int K, int d, int code, float s2f,
-                                               const float* u, const float* a32, double* R) {
+                                               const float* u, const float* a32, dfv* R) {
   float ui[DR], S[DR];
 #pragma unroll
   for (int l = 0; l < DR; ++l) {
@@ -148,20 +148,21 @@ __device__ __forceinline__ void split_dsig_row(int i, int K, int d, int code, fl
   }
 #pragma unroll
   for (int l = 0; l < DR; ++l)
-    if (l < d) R[(1 + l) * 33 + i] = (double)(-s2f * S[l]);
+    if (l < d) R[(1 + l) * 33 + i] = df_make(-s2f * S[l], 0.0f);
 }
 
 // pivot kk of the team's factorisation: LAPACK's criterion (a pivot that is
 // not > 0, i.e. negative, zero or NaN, fails: flag[0]), the conditioning
-// test against rho_min (flag[1]) and the reciprocal
-__device__ __forceinline__ void split_pivot(double dkk, int kk, long long rho_bits, double* invd,
+// test against rho_min (flag[1]; rho_bits = bits of the float32 threshold)
+// and the reciprocal.  A normalised pair has the sign of its hi part.
+__device__ __forceinline__ void split_pivot(dfv dkk, int kk, int rho_bits, dfv* invd,
                                             volatile int* flag) {
-  const long long bd = dbits(dkk);
-  if (bd <= 0 || bd >= kBitsInf) {
+  const int bd = __float_as_int(dkk.hi);
+  if (bd <= 0 || bd >= kFBitsInf) {
     flag[0] = 1;
   } else {
     if (bd < rho_bits) flag[1] = 1;
-    invd[kk] = pivot_rcp(dkk);
+    invd[kk] = df_rcp(dkk);
   }
 }
 
@@ -177,8 +178,8 @@ __device__ __forceinline__ int cm(int i, int j) { return cstart(j) + (i - j); }
 // 0: read from shared memory).  The same value per entry as any other
 // traversal.
 template <int DR>
-__device__ __forceinline__ void split_sigma_rows(int h, int K, int d, int code, double s2, double dj,
-                                                 const float* u, double* Lp) {
+__device__ __forceinline__ void split_sigma_rows(int h, int K, int d, int code, dfv s2, dfv dj,
+                                                 const float* u, dfv* Lp) {
   const int ib = K - 1 - h;            // >= h
   const int na = ib == h ? 0 : h;      // entries of row h when it is a row of its own
   constexpr int W = DR > 0 ? DR : 1;
@@ -211,7 +212,7 @@ __device__ __forceinline__ void split_sigma_rows(int h, int K, int d, int code, 
         r2 = fmaf(df, df, r2);
       }
     }
-    Lp[cm(i, j)] = fma(-s2, (double)matern_deficit_f32(code, sqrtf(r2)), s2);
+    Lp[cm(i, j)] = df_scaled_deficit(s2, matern_deficit_f32(code, sqrtf(r2)));
   }
   Lp[cm(h, h)] = dj;
   if (ib != h) Lp[cm(ib, ib)] = dj;
@@ -224,25 +225,28 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
   const unsigned full = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tm = lane / G, tl = lane - (lane / G) * G;
+  const unsigned tmask = (G == 32 ? full : ((1u << G) - 1u)) << (tm * G);
   const int dmax = A.dmax;
   // at least kSplitW - 1 R columns: R's first columns and a are the
   // factorisation's scratch
   const int nrs = A.NRmax > kSplitW - 1 ? A.NRmax : kSplitW - 1;
   const int64_t slot = split_slot_doubles(dmax, nrs);
-  double* Lp = smem + (int64_t)(warp * NB + tm) * slot;
-  double* R = Lp + 528;  // NR columns, stride 33
-  double* a = R + 33 * nrs;
-  double* invd = a + 32;
+  dfv* Lp = (dfv*)(smem + (int64_t)(warp * NB + tm) * slot);
+  dfv* R = Lp + 528;  // NR columns, stride 33
+  dfv* a = R + 33 * nrs;
+  dfv* invd = a + 32;
   float* a32 = (float*)(invd + 32);
   float* u = a32 + 32;
   int* idx = (int*)(u + 32 * dmax);
   volatile int* tflag = idx + 32;
-  double* acc = R;            // column 0 of R is scratch during the a solve
+  dfv* acc = R;               // column 0 of R is scratch during the a solve
   // unscaled columns of a factorisation step: R's first columns, then a
-  double* accs[kSplitW];
+  dfv* accs[kSplitW];
 #pragma unroll
   for (int p = 0; p < kSplitW; ++p) accs[p] = p < kSplitW - 1 ? R + 33 * p : a;
   float* R32 = (float*)Lp;    // float32 copy of R once L is no longer needed
+  double* wkd = (double*)a;   // float64 last rows of the solutions, for the record
+  const dfv dzero = df_make(0.0f, 0.0f);
 
   const int64_t nb = A.b1 - A.b0;
   const int64_t stride = (int64_t)gridDim.x * wpc * NB;
@@ -264,15 +268,20 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     const float s2f = (float)s2;
     const int code = PI.closed;
     const double diag = s2 * (1.0 + tau);
+    const dfv s2d = df_from_double(s2);
     const double* Y = A.y + PI.y_off;
     const double* Zm = A.Z + PI.z_off;
     const float2* XH = A.xhl + PI.x_off;
     int32_t* info = A.info + 4 * pid;
+    // scale inside [1e-30, 1e30] and data below 1e30 in magnitude keep every
+    // pair inside float32's exponent range; other blocks go to the float64 pass
+    bool range_ok = dbits(diag) > kBitsTiny && dbits(diag) < kBitsHuge;
 
     // ---- gather: neighbours first, self last; coordinates centred on self
     if (active)
       for (int i = tl; i < K; i += G) idx[i] = (i < k) ? A.nbr[b * A.ldnbr + i] : A.rowb[b];
     __syncwarp();
+    bool data_ok = true;
     if (active) {
       // centred scaled coordinates from the (hi, lo) float32 pairs: the
       // difference keeps ~24 bits relative to itself, however close the points
@@ -283,37 +292,44 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         const float2 w = xs[l];
         u[l * 32 + i] = (v.x - w.x) + (v.y - w.y);
       }
-      if (A.need_grad)
-        for (int i = tl; i < K; i += G) {
-          R[P * 33 + i] = Y[idx[i]];
-          for (int c = 0; c < q; ++c) R[(P + 1 + c) * 33 + i] = Zm[(int64_t)idx[i] * q + c];
+      for (int i = tl; i < K; i += G) {
+        const double yv = Y[idx[i]];
+        data_ok = data_ok && in_f32_range(yv);
+        if (A.need_grad) R[P * 33 + i] = df_from_double(yv);
+        for (int c = 0; c < q; ++c) {
+          const double zv = Zm[(int64_t)idx[i] * q + c];
+          data_ok = data_ok && in_f32_range(zv);
+          if (A.need_grad) R[(P + 1 + c) * 33 + i] = df_from_double(zv);
         }
+      }
     }
+    range_ok = range_ok && (__ballot_sync(full, !data_ok) & tmask) == 0;
     __syncwarp();
 
-    // ---- Sigma (float32 deficit, float64 entries) and Cholesky with the
+    // ---- Sigma (float32 deficit, double-float entries) and LDL^T with the
     //      jitter ladder of _covariance.py:235-252
     int lv = (active && A.fixup) ? A.chunk_max[A.chunk[b]] : 0;
-    bool done = !active, failed = false;
+    bool done = !active || !range_ok, failed = active && !range_ok;
     double jit = 0.0;
-    long long rho_bits = 0;
+    int rho_bits = 0;
     while (__any_sync(full, !done)) {
       const bool need = !done;
       if (need) {
         jit = (lv > 0) ? jitter_pow10(lv) * diag : 0.0;  // 10^p * mean(diag)
-        rho_bits = dbits(A.rho_min * (diag + jit));
+        rho_bits = __float_as_int((float)(A.rho_min * (diag + jit)));
+        const dfv dj = df_from_double(diag + jit);
         // lane h takes rows h and K-1-h (K-1 entries below the diagonal
         // between them); s2 (1 - D): the deficit carries the information of
         // close pairs
         for (int h = tl; 2 * h < K; h += G) {
           if (d <= 4)
-            split_sigma_rows<4>(h, K, d, code, s2, diag + jit, u, Lp);
+            split_sigma_rows<4>(h, K, d, code, s2d, dj, u, Lp);
           else if (d <= 8)
-            split_sigma_rows<8>(h, K, d, code, s2, diag + jit, u, Lp);
+            split_sigma_rows<8>(h, K, d, code, s2d, dj, u, Lp);
           else if (d <= 12)
-            split_sigma_rows<12>(h, K, d, code, s2, diag + jit, u, Lp);
+            split_sigma_rows<12>(h, K, d, code, s2d, dj, u, Lp);
           else
-            split_sigma_rows<0>(h, K, d, code, s2, diag + jit, u, Lp);
+            split_sigma_rows<0>(h, K, d, code, s2d, dj, u, Lp);
         }
         if (tl == 0) {
           tflag[0] = 0;  // a pivot failed
@@ -327,10 +343,11 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       // loop.  Panel column c = kk + p takes the steps kk .. c-1 in order (its
       // pivot follows at once), then is scaled by 1/d_c, its unscaled values
       // in accs[p]; every trailing element (j >= kk + kSplitW) then takes all
-      // kSplitW updates in one visit, fma(-l(i,s) a(j,s), .) for s = kk, kk+1,
-      // ...: the same roundings in the same order as single steps.  The lane
-      // that updates (kk+W, kk+W) takes that pivot's reciprocal (look-ahead).
-      // A failed pivot stops the attempt (it is redone with jitter).
+      // kSplitW updates in one visit, l(i,s) a(j,s) for s = kk, kk+1, ... in
+      // order, in a double-float accumulator normalised once per visit.  The
+      // lane that updates (kk+W, kk+W) takes that pivot's reciprocal
+      // (look-ahead).  A failed pivot stops the attempt (it is redone with
+      // jitter).
       auto colp = [&](int c) { return Lp + cstart(c) - c; };  // colp(c)[i] = L(i, c)
       for (int kk = 0; kk < Kw; kk += kSplitW) {
         bool go = need && kk < K && tflag[0] == 0;
@@ -339,11 +356,13 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
           const int c = kk + p;
           if (p > 0) {
             if (go && c < K) {
-              double* colc = colp(c);
+              dfv* colc = colp(c);
               for (int i = c + tl; i < K; i += G) {
-                double v = colc[i];
+                const dfv v0 = colc[i];
+                float s = v0.hi, t = v0.lo;
 #pragma unroll
-                for (int s2 = 0; s2 < p; ++s2) v = fma(-colp(kk + s2)[i], accs[s2][c], v);
+                for (int s2 = 0; s2 < p; ++s2) df_fms_acc(s, t, colp(kk + s2)[i], accs[s2][c]);
+                const dfv v = df_norm(s, t);
                 colc[i] = v;
                 accs[p][i] = v;
                 if (i == c) split_pivot(v, c, rho_bits, invd, tflag);
@@ -353,12 +372,12 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
             go = go && tflag[0] == 0;
           }
           if (go && c < K) {
-            double* colc = colp(c);
-            const double inv = invd[c];
+            dfv* colc = colp(c);
+            const dfv inv = invd[c];
             for (int i = c + 1 + tl; i < K; i += G) {
-              const double v = p == 0 ? colc[i] : accs[p][i];
+              const dfv v = p == 0 ? colc[i] : accs[p][i];
               if (p == 0) accs[0][i] = v;
-              colc[i] = v * inv;
+              colc[i] = df_mul(v, inv);
             }
           }
           __syncwarp();
@@ -385,22 +404,27 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
                   ++j;
                 }
               }
-              double nv[kSplitU2];
+              float sv[kSplitU2], tv[kSplitU2];
 #pragma unroll
               for (int u4 = 0; u4 < kSplitU2; ++u4)
-                if (t + u4 * G < cnt) nv[u4] = Lp[cm(ii[u4], jj[u4])];
+                if (t + u4 * G < cnt) {
+                  const dfv v0 = Lp[cm(ii[u4], jj[u4])];
+                  sv[u4] = v0.hi;
+                  tv[u4] = v0.lo;
+                }
 #pragma unroll
               for (int s2 = 0; s2 < kSplitW; ++s2) {
-                const double* cs = colp(kk + s2);
+                const dfv* cs = colp(kk + s2);
 #pragma unroll
                 for (int u4 = 0; u4 < kSplitU2; ++u4)
-                  if (t + u4 * G < cnt) nv[u4] = fma(-cs[ii[u4]], accs[s2][jj[u4]], nv[u4]);
+                  if (t + u4 * G < cnt) df_fms_acc(sv[u4], tv[u4], cs[ii[u4]], accs[s2][jj[u4]]);
               }
 #pragma unroll
               for (int u4 = 0; u4 < kSplitU2; ++u4)
                 if (t + u4 * G < cnt) {
-                  Lp[cm(ii[u4], jj[u4])] = nv[u4];
-                  if (ii[u4] == j0 && jj[u4] == j0) split_pivot(nv[u4], j0, rho_bits, invd, tflag);
+                  const dfv nv = df_norm(sv[u4], tv[u4]);
+                  Lp[cm(ii[u4], jj[u4])] = nv;
+                  if (ii[u4] == j0 && jj[u4] == j0) split_pivot(nv, j0, rho_bits, invd, tflag);
                 }
             }
           }
@@ -420,8 +444,9 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
 
     double* rec = A.cache + b * (int64_t)A.CS;
     if (failed) {
-      // not positive definite even with jitter after float32 assembly: the
-      // float64 pass decides (and reports a failure if it fails as well)
+      // not positive definite even with jitter after float32 assembly, or
+      // outside float32's range: the float64 pass decides (and reports a
+      // failure if it fails as well)
       if (tl == 0) {
         A.level[b] = 0;
         A.redo[b] = 1;
@@ -441,46 +466,54 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     }
     const bool ok = active && !failed;
 
-    // ---- a = C^-T e_K = L^-T e_K / sqrt(d_K)  (float64, unit back substitution)
-    double lKK = 0.0, sK = 0.0;  // L_KK = sqrt(d_K) and its reciprocal
+    // ---- a = C^-T e_K = L^-T e_K / sqrt(d_K)  (unit back substitution)
+    dfv lKKd = dzero, sKd = dzero;  // L_KK = sqrt(d_K) and its reciprocal
     if (ok) {
-      lKK = sqrt(Lp[cm(k, k)]);
-      sK = 1.0 / lKK;
-      if (tl == 0) rec[0] = lKK;  // L_KK; the log is taken in the reduction
-      for (int i = tl; i < K; i += G) acc[i] = (i == k) ? 1.0 : 0.0;
+      lKKd = df_sqrt(Lp[cm(k, k)]);
+      sKd = df_rcp(lKKd);
+      if (tl == 0) rec[0] = df_to_double(lKKd);  // L_KK; the log is taken in the reduction
+      for (int i = tl; i < K; i += G) acc[i] = (i == k) ? df_make(1.0f, 0.0f) : dzero;
     }
     __syncwarp();
     for (int i = Kw - 1; i >= 0; --i) {
       if (ok && i < K) {
-        const double ai = acc[i];
-        for (int j = tl; j < i; j += G) acc[j] -= Lp[cm(i, j)] * ai;
+        const dfv ai = acc[i];
+        for (int j = tl; j < i; j += G) acc[j] = df_fms(acc[j], Lp[cm(i, j)], ai);
       }
       __syncwarp();
     }
     if (ok)
       for (int i = tl; i < K; i += G) {
-        const double ai = acc[i] * sK;
+        const dfv ai = df_mul(acc[i], sKd);
         a[i] = ai;
-        a32[i] = (float)ai;
+        a32[i] = ai.hi;
       }
     __syncwarp();
 
-    // ---- GLS parts (float64 team sums)
+    // ---- GLS parts a'y, a'Z (double-float team sums of unnormalised pairs)
     {
-      double vy = 0.0;
-      if (ok)
-        for (int i = tl; i < K; i += G) vy += a[i] * Y[idx[i]];
-      for (int o = G / 2; o > 0; o >>= 1) vy += __shfl_xor_sync(full, vy, o);
-      if (ok && tl == 0) rec[1] = vy;
+      const int qw = __reduce_max_sync(full, active ? q : 0);
       // teams of one warp may belong to problems with different q: the
       // shuffles run to the warp's largest q
-      const int qw = __reduce_max_sync(full, active ? q : 0);
-      for (int c = 0; c < qw; ++c) {
-        double vz = 0.0;
-        if (ok && c < q)
-          for (int i = tl; i < K; i += G) vz += a[i] * Zm[(int64_t)idx[i] * q + c];
-        for (int o = G / 2; o > 0; o >>= 1) vz += __shfl_xor_sync(full, vz, o);
-        if (ok && c < q && tl == 0) rec[2 + c] = vz;
+      for (int c = 0; c <= qw; ++c) {
+        float s = 0.0f, t = 0.0f;
+        if (ok && c <= q)
+          for (int i = tl; i < K; i += G) {
+            dfv v;
+            if (A.need_grad)
+              v = R[(P + c) * 33 + i];
+            else
+              v = df_from_double(c == 0 ? Y[idx[i]] : Zm[(int64_t)idx[i] * q + (c - 1)]);
+            df_fms_acc(s, t, a[i], df_make(-v.hi, -v.lo));
+          }
+        for (int o = G / 2; o > 0; o >>= 1) {
+          const float so = __shfl_xor_sync(full, s, o), to = __shfl_xor_sync(full, t, o);
+          float s3, e;
+          two_sum(s, so, s3, e);
+          s = s3;
+          t = df_addf(t, df_addf(to, e));
+        }
+        if (ok && c <= q && tl == 0) rec[1 + c] = (double)s + (double)t;
       }
     }
     if (!A.need_grad) {
@@ -497,7 +530,11 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     // ---- right-hand sides dSigma_p a
     if (ok) {
       // p = 0: Sigma (un-jittered) a = L_KK e_K - jit a
-      for (int i = tl; i < K; i += G) R[i] = ((i == k) ? lKK : 0.0) - jit * a[i];
+      const dfv jitd = df_from_double(jit);
+      for (int i = tl; i < K; i += G) {
+        const dfv e = (i == k) ? lKKd : dzero;
+        R[i] = jit == 0.0 ? e : df_fms(e, jitd, a[i]);
+      }
       // p = 1..d (float32): -s2 sum_j g_ij a_j (u_il - u_jl)^2
       if (d <= 12) {
         for (int i = tl; i < K; i += G) {
@@ -536,52 +573,61 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
               s = fmaf(cj[j], df * df, s);
             }
           }
-          R[(1 + l) * 33 + i] = (double)(-s2f * s);
+          R[(1 + l) * 33 + i] = df_make(-s2f * s, 0.0f);
         }
       }
       // nugget row: dSigma_tau = s2 tau I
-      for (int i = tl; i < K; i += G) R[(P - 1) * 33 + i] = s2 * tau * a[i];
+      const dfv s2taud = df_from_double(s2 * tau);
+      for (int i = tl; i < K; i += G) R[(P - 1) * 33 + i] = df_mul(s2taud, a[i]);
     }
     __syncwarp();
 
-    // ---- forward solves (float64) with the unit factor: L^-1 [dSigma a, y, Z];
-    // W = D^(-1/2) L^-1 dSigma a.  Without jitter Sigma a = L_KK e_K, whose
-    // solution is sqrt(d_K) e_K, so that column is left out of the solve.
+    // ---- forward solves (double-float) with the unit factor:
+    // L^-1 [dSigma a, y, Z]; W = D^(-1/2) L^-1 dSigma a.  Without jitter
+    // Sigma a = L_KK e_K, whose solution is sqrt(d_K) e_K, so that column is
+    // left out of the solve.
     const int c0 = (jit == 0.0) ? 1 : 0;
     // columns c0 + tl, c0 + tl + G, ... per lane, with no warp
     // synchronisation between steps; kSplitWF steps per pass: the panel's
-    // own rows are finished in order, then every later row takes the
-    // panel's updates in one visit (each element sees the steps in order)
+    // own rows are finished in order (and normalised), then every later row
+    // takes the panel's updates in one visit, stored as an unnormalised
+    // accumulator until its own step
     if (ok)
       for (int c = c0 + tl; c < NR; c += G) {
-        double* col = R + c * 33;
+        dfv* col = R + c * 33;
         for (int i = 0; i < K - 1; i += kSplitWF) {
           const int ns = min(kSplitWF, K - 1 - i);  // steps i .. i+ns-1
-          double r[kSplitWF];
+          dfv r[kSplitWF];
 #pragma unroll
           for (int s2 = 0; s2 < kSplitWF; ++s2)
             if (s2 < ns) {
-              double v = col[i + s2];
+              const dfv v0 = col[i + s2];
+              float s = v0.hi, t = v0.lo;
 #pragma unroll
-              for (int t2 = 0; t2 < s2; ++t2) v = fma(-Lp[cm(i + s2, i + t2)], r[t2], v);
-              r[s2] = v;
-              col[i + s2] = v;
+              for (int t2 = 0; t2 < s2; ++t2) df_fms_acc(s, t, Lp[cm(i + s2, i + t2)], r[t2]);
+              r[s2] = df_norm(s, t);
+              col[i + s2] = r[s2];
             }
           for (int j = i + ns; j < K; ++j) {
-            double v = col[j];
+            const dfv v0 = col[j];
+            float s = v0.hi, t = v0.lo;
 #pragma unroll
             for (int t2 = 0; t2 < kSplitWF; ++t2)
-              if (t2 < ns) v = fma(-Lp[cm(j, i + t2)], r[t2], v);
-            col[j] = v;
+              if (t2 < ns) df_fms_acc(s, t, Lp[cm(j, i + t2)], r[t2]);
+            col[j] = df_make(s, t);
           }
         }
+        col[K - 1] = df_norm(col[K - 1].hi, col[K - 1].lo);
       }
     __syncwarp();
     if (ok) {
       if (c0 == 1)
-        for (int i = tl; i < K; i += G) R[i] = (i == k) ? lKK : 0.0;
+        for (int i = tl; i < K; i += G) R[i] = (i == k) ? lKKd : dzero;
       // a32 is free now: it takes the float32 weights d_j^(-1/2)
-      for (int j = tl; j < K; j += G) a32[j] = sqrtf((float)invd[j]);
+      for (int j = tl; j < K; j += G) a32[j] = sqrtf(invd[j].hi);
+      // a is free: the last rows of the solutions times 1 / L_KK, in float64
+      for (int c = tl; c < NR; c += G)
+        wkd[c] = df_to_double(df_mul((c == 0 && c0 == 1) ? lKKd : R[c * 33 + k], sKd));
     }
     __syncwarp();
 
@@ -590,7 +636,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     if (ok) {
       for (int e = tl; e < NR * 33; e += G) {
         const int c = e / 33, j = e - (e / 33) * 33;
-        R32[e] = (j < K) ? (float)R[c * 33 + j] * a32[j] : 0.0f;
+        R32[e] = (j < K) ? R[c * 33 + j].hi * a32[j] : 0.0f;
       }
     }
     __syncwarp();
@@ -599,8 +645,8 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       double* wzy = wK + P;
       double* wzZ = wzy + P;
       double* F = wzZ + P * q;
-      for (int c = tl; c < 1 + q; c += G) rec[2 + q + c] = R[(P + c) * 33 + k] * sK;
-      for (int p = tl; p < P; p += G) wK[p] = R[p * 33 + k] * sK;
+      for (int c = tl; c < 1 + q; c += G) rec[2 + q + c] = wkd[P + c];
+      for (int p = tl; p < P; p += G) wK[p] = wkd[p];
       const int nf = P * (P + 1) / 2;
       const int ntot = nf + P * (1 + q);
       for (int t = tl; t < ntot; t += G) {
@@ -617,7 +663,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         float sacc = 0.0f;
         for (int i = 0; i < K; ++i) sacc = fmaf(r1[i], r2[i], sacc);
         if (t < nf) {
-          F[t] = 0.5 * (2.0 * (double)sacc - (R[c1 * 33 + k] * sK) * (R[c2 * 33 + k] * sK));
+          F[t] = fma(-0.5 * wkd[c1], wkd[c2], (double)sacc);
         } else {
           const int s3 = t - nf;
           const int p = s3 / (1 + q);
