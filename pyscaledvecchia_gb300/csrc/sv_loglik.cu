@@ -740,6 +740,7 @@ int run_eval(const EvalCall& C, cudaStream_t st) {
   A.redo_mode = 0;
   A.rho_min = C.rho_min > 0.0 ? C.rho_min : 1e-4;
   A.xhl = (float2*)(ws + W.xhl);
+  A.kcap = S.kmax + 1 < 32 ? (S.kmax + 1 > 0 ? S.kmax + 1 : 1) : 32;
 
   k_info_init<<<(int)((S.nprob + 255) / 256), 256, 0, st>>>(C.info, (int)S.nprob);
   SV_CUDA_TRY(cudaGetLastError());

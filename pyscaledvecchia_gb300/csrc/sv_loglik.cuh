@@ -51,6 +51,7 @@ struct LikArgs {
   int redo_mode;          // float64 kernel: only blocks flagged by the split kernel
   double rho_min;
   float2* xhl;            // split form: x / lambda as float32 (hi, lo) pairs
+  int kcap;               // split form: largest K of the launch (<= 32)
 };
 
 // block id of the t-th entry handled by a launch
@@ -87,8 +88,18 @@ __host__ __device__ inline int record_stride(int q, int P, int need_grad) {
 // a as float32 (16) | coordinates float32 (16 d) | indices + flags (18);
 // the stride is kept = 8 (mod 16) doubles so that two 8-lane teams in a
 // half-warp fall on disjoint banks
-__host__ __device__ inline int split_slot_doubles(int d, int NR) {
-  int s = 528 + 33 * NR + 64 + 16 + 16 * d + 18;
+// split kernel: L's packed capacity for blocks of up to kc points (the
+// launch's largest K), at least the float32 copy of R that reuses it
+__host__ __device__ inline int split_lp_cap(int kc, int NR) {
+  const int tri = kc * (kc + 1) / 2, r32 = (33 * NR + 1) / 2;
+  const int c = tri > r32 ? tri : r32;
+  return c + (c & 1);
+}
+
+// split kernel team slot (8-byte words): L (packed, pivot reciprocals on
+// the diagonal), R (NR columns of 33), a, a32, u (d x 32 floats), idx, flags
+__host__ __device__ inline int split_slot_doubles(int d, int NR, int kc) {
+  int s = split_lp_cap(kc, NR) + 33 * NR + 32 + 16 + 16 * d + 18;
   s += ((8 - s % 16) + 16) % 16;
   return s;
 }

@@ -34,15 +34,15 @@
 namespace sv {
 
 constexpr int kSplitMaxThreads = 512;
-// independent elements per lane per round of the factorisation update and the
-// multi-column forward solve (instruction-level parallelism per lane)
-constexpr int kSplitU = 4;
-// columns per factorisation step (panel width) and trailing elements per
-// round of a step (kSplitW FMAs each): measured at C2, widths 2, 3, 4, 6, 8
-// took 9.31, 9.18, 9.05, 9.11, 9.16 ms
-constexpr int kSplitW = 4;
-// steps per pass of the forward solves
-constexpr int kSplitWF = 4;
+// Panel widths, measured at n = 200k, d = 10, m = 30 (ms per evaluation):
+// columns per factorisation step (kSplitW) and steps per forward-solve pass
+// (kSplitWF) 4/4 6.71, 6/4 6.54, 4/8 6.54, 6/8 6.42, 8/8 6.38; two later rows
+// per iteration of a forward-solve pass (kSplitJU, independent double-float
+// chains) 8/8 6.29, 8/12 6.27, 6/6 6.32; two trailing elements per lane per
+// factorisation round (kSplitU2) 7.24 against 6.71.
+constexpr int kSplitW = 8;
+constexpr int kSplitWF = 8;
+constexpr int kSplitJU = 2;
 constexpr int kSplitU2 = 1;
 
 __device__ __forceinline__ void matern_closed_f32(int code, float r, float& M, float& g) {
@@ -151,26 +151,27 @@ __device__ __forceinline__ void split_dsig_row(int i, int K, int d, int code, fl
     if (l < d) R[(1 + l) * 33 + i] = df_make(-s2f * S[l], 0.0f);
 }
 
-// pivot kk of the team's factorisation: LAPACK's criterion (a pivot that is
+// a pivot of the team's factorisation: LAPACK's criterion (a pivot that is
 // not > 0, i.e. negative, zero or NaN, fails: flag[0]), the conditioning
 // test against rho_min (flag[1]; rho_bits = bits of the float32 threshold)
-// and the reciprocal.  A normalised pair has the sign of its hi part.
-__device__ __forceinline__ void split_pivot(dfv dkk, int kk, int rho_bits, dfv* invd,
-                                            volatile int* flag) {
+// and the reciprocal, which takes the pivot's place on L's diagonal.  A
+// normalised pair has the sign of its hi part.
+__device__ __forceinline__ void split_pivot(dfv dkk, dfv* diag, int rho_bits, volatile int* flag) {
   const int bd = __float_as_int(dkk.hi);
   if (bd <= 0 || bd >= kFBitsInf) {
     flag[0] = 1;
   } else {
     if (bd < rho_bits) flag[1] = 1;
-    invd[kk] = df_rcp(dkk);
+    *diag = df_rcp(dkk);
   }
 }
 
-// L is stored packed by columns with capacity 32: entry (i, j), i >= j, at
-// cstart(j) + i - j.  Column walks (scaling, trailing updates, forward
-// solves) then touch consecutive words, free of bank conflicts.
-__device__ __forceinline__ int cstart(int j) { return j * 32 - (j * (j - 1)) / 2; }
-__device__ __forceinline__ int cm(int i, int j) { return cstart(j) + (i - j); }
+// L is stored packed by columns with capacity kc (the launch's largest K):
+// entry (i, j), i >= j, at cstart(j) + i - j.  Column walks (scaling,
+// trailing updates, forward solves) then touch consecutive words, free of
+// bank conflicts.  Once factored, the diagonal holds the pivots' reciprocals.
+__device__ __forceinline__ int cstart(int j, int kc) { return j * kc - (j * (j - 1)) / 2; }
+__device__ __forceinline__ int cm(int i, int j, int kc) { return cstart(j, kc) + (i - j); }
 
 // Entries (h, j < h) and (K-1-h, j < K-1-h) of Sigma below the diagonal,
 // s2 (1 - D(r_ij)), and both diagonal entries dj; u is [d][32] (row i at
@@ -179,7 +180,7 @@ __device__ __forceinline__ int cm(int i, int j) { return cstart(j) + (i - j); }
 // traversal.
 template <int DR>
 __device__ __forceinline__ void split_sigma_rows(int h, int K, int d, int code, dfv s2, dfv dj,
-                                                 const float* u, dfv* Lp) {
+                                                 const float* u, dfv* Lp, int kc) {
   const int ib = K - 1 - h;            // >= h
   const int na = ib == h ? 0 : h;      // entries of row h when it is a row of its own
   constexpr int W = DR > 0 ? DR : 1;
@@ -212,10 +213,10 @@ __device__ __forceinline__ void split_sigma_rows(int h, int K, int d, int code, 
         r2 = fmaf(df, df, r2);
       }
     }
-    Lp[cm(i, j)] = df_scaled_deficit(s2, matern_deficit_f32(code, sqrtf(r2)));
+    Lp[cm(i, j, kc)] = df_scaled_deficit(s2, matern_deficit_f32(code, sqrtf(r2)));
   }
-  Lp[cm(h, h)] = dj;
-  if (ib != h) Lp[cm(ib, ib)] = dj;
+  Lp[cm(h, h, kc)] = dj;
+  if (ib != h) Lp[cm(ib, ib, kc)] = dj;
 }
 
 template <int G>
@@ -230,12 +231,13 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
   // at least kSplitW - 1 R columns: R's first columns and a are the
   // factorisation's scratch
   const int nrs = A.NRmax > kSplitW - 1 ? A.NRmax : kSplitW - 1;
-  const int64_t slot = split_slot_doubles(dmax, nrs);
+  const int kc = A.kcap;
+  const int64_t slot = split_slot_doubles(dmax, nrs, kc);
   dfv* Lp = (dfv*)(smem + (int64_t)(warp * NB + tm) * slot);
-  dfv* R = Lp + 528;  // NR columns, stride 33
+  dfv* R = Lp + split_lp_cap(kc, nrs);  // NR columns, stride 33
   dfv* a = R + 33 * nrs;
-  dfv* invd = a + 32;
-  float* a32 = (float*)(invd + 32);
+  float* a32 = (float*)(a + 32);
+  auto cm = [kc](int i, int j) { return sv::cm(i, j, kc); };
   float* u = a32 + 32;
   int* idx = (int*)(u + 32 * dmax);
   volatile int* tflag = idx + 32;
@@ -292,15 +294,12 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         const float2 w = xs[l];
         u[l * 32 + i] = (v.x - w.x) + (v.y - w.y);
       }
+      // y and Z enter R after the factorisation, whose scratch columns
+      // may cover theirs (measured: no faster when loaded here where they
+      // do not); here only their range is checked
       for (int i = tl; i < K; i += G) {
-        const double yv = Y[idx[i]];
-        data_ok = data_ok && in_f32_range(yv);
-        if (A.need_grad) R[P * 33 + i] = df_from_double(yv);
-        for (int c = 0; c < q; ++c) {
-          const double zv = Zm[(int64_t)idx[i] * q + c];
-          data_ok = data_ok && in_f32_range(zv);
-          if (A.need_grad) R[(P + 1 + c) * 33 + i] = df_from_double(zv);
-        }
+        data_ok = data_ok && in_f32_range(Y[idx[i]]);
+        for (int c = 0; c < q; ++c) data_ok = data_ok && in_f32_range(Zm[(int64_t)idx[i] * q + c]);
       }
     }
     range_ok = range_ok && (__ballot_sync(full, !data_ok) & tmask) == 0;
@@ -323,13 +322,13 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         // close pairs
         for (int h = tl; 2 * h < K; h += G) {
           if (d <= 4)
-            split_sigma_rows<4>(h, K, d, code, s2d, dj, u, Lp);
+            split_sigma_rows<4>(h, K, d, code, s2d, dj, u, Lp, kc);
           else if (d <= 8)
-            split_sigma_rows<8>(h, K, d, code, s2d, dj, u, Lp);
+            split_sigma_rows<8>(h, K, d, code, s2d, dj, u, Lp, kc);
           else if (d <= 12)
-            split_sigma_rows<12>(h, K, d, code, s2d, dj, u, Lp);
+            split_sigma_rows<12>(h, K, d, code, s2d, dj, u, Lp, kc);
           else
-            split_sigma_rows<0>(h, K, d, code, s2d, dj, u, Lp);
+            split_sigma_rows<0>(h, K, d, code, s2d, dj, u, Lp, kc);
         }
         if (tl == 0) {
           tflag[0] = 0;  // a pivot failed
@@ -337,18 +336,19 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         }
       }
       __syncwarp();
-      if (need && tl == 0) split_pivot(Lp[cm(0, 0)], 0, rho_bits, invd, tflag);
+      if (need && tl == 0) split_pivot(Lp[0], Lp, rho_bits, tflag);
       __syncwarp();
       // right-looking LDL^T, kSplitW columns (a panel) per step, warp-uniform
       // loop.  Panel column c = kk + p takes the steps kk .. c-1 in order (its
       // pivot follows at once), then is scaled by 1/d_c, its unscaled values
       // in accs[p]; every trailing element (j >= kk + kSplitW) then takes all
       // kSplitW updates in one visit, l(i,s) a(j,s) for s = kk, kk+1, ... in
-      // order, in a double-float accumulator normalised once per visit.  The
+      // order, kept as an unnormalised double-float accumulator (normalised
+      // where it becomes a multiplier, a pivot or a square root).  The
       // lane that updates (kk+W, kk+W) takes that pivot's reciprocal
       // (look-ahead).  A failed pivot stops the attempt (it is redone with
       // jitter).
-      auto colp = [&](int c) { return Lp + cstart(c) - c; };  // colp(c)[i] = L(i, c)
+      auto colp = [&](int c) { return Lp + cstart(c, kc) - c; };  // colp(c)[i] = L(i, c)
       for (int kk = 0; kk < Kw; kk += kSplitW) {
         bool go = need && kk < K && tflag[0] == 0;
 #pragma unroll
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
                 const dfv v = df_norm(s, t);
                 colc[i] = v;
                 accs[p][i] = v;
-                if (i == c) split_pivot(v, c, rho_bits, invd, tflag);
+                if (i == c) split_pivot(v, colc + c, rho_bits, tflag);
               }
             }
             __syncwarp();
@@ -373,9 +373,9 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
           }
           if (go && c < K) {
             dfv* colc = colp(c);
-            const dfv inv = invd[c];
+            const dfv inv = colc[c];
             for (int i = c + 1 + tl; i < K; i += G) {
-              const dfv v = p == 0 ? colc[i] : accs[p][i];
+              const dfv v = p == 0 ? df_norm(colc[i].hi, colc[i].lo) : accs[p][i];
               if (p == 0) accs[0][i] = v;
               colc[i] = df_mul(v, inv);
             }
@@ -422,9 +422,9 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
 #pragma unroll
               for (int u4 = 0; u4 < kSplitU2; ++u4)
                 if (t + u4 * G < cnt) {
-                  const dfv nv = df_norm(sv[u4], tv[u4]);
-                  Lp[cm(ii[u4], jj[u4])] = nv;
-                  if (ii[u4] == j0 && jj[u4] == j0) split_pivot(nv, j0, rho_bits, invd, tflag);
+                  Lp[cm(ii[u4], jj[u4])] = df_make(sv[u4], tv[u4]);
+                  if (ii[u4] == j0 && jj[u4] == j0)
+                    split_pivot(df_norm(sv[u4], tv[u4]), Lp + cm(j0, j0), rho_bits, tflag);
                 }
             }
           }
@@ -469,8 +469,8 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     // ---- a = C^-T e_K = L^-T e_K / sqrt(d_K)  (unit back substitution)
     dfv lKKd = dzero, sKd = dzero;  // L_KK = sqrt(d_K) and its reciprocal
     if (ok) {
-      lKKd = df_sqrt(Lp[cm(k, k)]);
-      sKd = df_rcp(lKKd);
+      sKd = df_sqrt(Lp[cm(k, k)]);  // the diagonal holds 1 / d_K
+      lKKd = df_rcp(sKd);
       if (tl == 0) rec[0] = df_to_double(lKKd);  // L_KK; the log is taken in the reduction
       for (int i = tl; i < K; i += G) acc[i] = (i == k) ? df_make(1.0f, 0.0f) : dzero;
     }
@@ -490,7 +490,8 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       }
     __syncwarp();
 
-    // ---- GLS parts a'y, a'Z (double-float team sums of unnormalised pairs)
+    // ---- GLS parts a'y, a'Z (double-float team sums of unnormalised pairs);
+    //      y and Z also take their columns of R for the forward solves
     {
       const int qw = __reduce_max_sync(full, active ? q : 0);
       // teams of one warp may belong to problems with different q: the
@@ -499,11 +500,8 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         float s = 0.0f, t = 0.0f;
         if (ok && c <= q)
           for (int i = tl; i < K; i += G) {
-            dfv v;
-            if (A.need_grad)
-              v = R[(P + c) * 33 + i];
-            else
-              v = df_from_double(c == 0 ? Y[idx[i]] : Zm[(int64_t)idx[i] * q + (c - 1)]);
+            const dfv v = df_from_double(c == 0 ? Y[idx[i]] : Zm[(int64_t)idx[i] * q + (c - 1)]);
+            if (A.need_grad) R[(P + c) * 33 + i] = v;
             df_fms_acc(s, t, a[i], df_make(-v.hi, -v.lo));
           }
         for (int o = G / 2; o > 0; o >>= 1) {
@@ -608,6 +606,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
               r[s2] = df_norm(s, t);
               col[i + s2] = r[s2];
             }
+#pragma unroll kSplitJU
           for (int j = i + ns; j < K; ++j) {
             const dfv v0 = col[j];
             float s = v0.hi, t = v0.lo;
@@ -624,7 +623,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       if (c0 == 1)
         for (int i = tl; i < K; i += G) R[i] = (i == k) ? lKKd : dzero;
       // a32 is free now: it takes the float32 weights d_j^(-1/2)
-      for (int j = tl; j < K; j += G) a32[j] = sqrtf(invd[j].hi);
+      for (int j = tl; j < K; j += G) a32[j] = sqrtf(Lp[cm(j, j)].hi);
       // a is free: the last rows of the solutions times 1 / L_KK, in float64
       for (int c = tl; c < NR; c += G)
         wkd[c] = df_to_double(df_mul((c == 0 && c0 == 1) ? lKKd : R[c * 33 + k], sKd));
@@ -712,7 +711,7 @@ int launch_block_split(const LikArgs& A, int lanes, cudaStream_t st) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t per_warp =
-      sizeof(double) * (size_t)split_slot_doubles(A.dmax, A.NRmax > kSplitW - 1 ? A.NRmax : kSplitW - 1) *
+      sizeof(double) * (size_t)split_slot_doubles(A.dmax, A.NRmax > kSplitW - 1 ? A.NRmax : kSplitW - 1, A.kcap) *
       (32 / lanes);
   int wpc = kSplitMaxThreads / 32;
   while (wpc > 1 && wpc * per_warp > (size_t)maxsm) --wpc;

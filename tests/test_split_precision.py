@@ -1,5 +1,6 @@
 """Split-precision likelihood (float32 assembly / dSigma.a / Gram products,
-float64 Cholesky, solves, log-determinants) against the float64 form.
+double-float LDL^T, solves and GLS sums, float64 records and reductions)
+against the float64 form.
 
 Blocks whose smallest pivot ratio L_kk^2 / Sigma_kk is below 1e-4 are
 re-evaluated in float64, so the float32 assembly error stays bounded on
@@ -60,3 +61,30 @@ def test_split_other_closed_forms(nu):
     b = prob.evaluate(theta, nu, precision="split")
     assert abs(a[0] - b[0]) <= 5e-6 * abs(a[0])
     assert np.abs(a[1] - b[1]).max() <= 1e-3 * np.abs(a[1]).max()
+
+
+@pytest.mark.parametrize("what", ["y", "s2"])
+def test_split_out_of_float32_range_goes_to_float64(what):
+    """Data above 1e30 in magnitude, or a scale outside [1e-30, 1e30], leave
+    float32's exponent range: those blocks are evaluated by the float64 pass,
+    so the result is the float64 form's."""
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    from pyscaledvecchia_gb300.ordering import _nn_groups, find_ordered_nn, maximin_order
+    rng = np.random.default_rng(11)
+    n, d, m = 2000, 3, 15
+    X = rng.random((n, d))
+    theta = np.array([0.0, -1.0, -0.5, 0.2, math.log(1e-3)])
+    y = rng.standard_normal(n)
+    if what == "y":
+        y = y * 1e31
+    else:
+        theta[0] = math.log(1e31)
+    order = maximin_order(X / np.exp(theta[1:1 + d]))
+    nn = find_ordered_nn((X / np.exp(theta[1:1 + d]))[order], m)
+    prob = DeviceProblem(X[order], y[order], np.ones((n, 1)), _nn_groups(nn, m))
+    a = prob.evaluate(theta, 2.5)
+    b = prob.evaluate(theta, 2.5, precision="split")
+    assert np.isfinite(b[0])
+    assert abs(a[0] - b[0]) <= 1e-12 * abs(a[0])
+    np.testing.assert_allclose(b[1], a[1], rtol=1e-10, atol=1e-10 * np.abs(a[1]).max())
+    np.testing.assert_allclose(b[2], a[2], rtol=1e-10, atol=1e-10 * np.abs(a[2]).max())
