@@ -41,6 +41,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Vecchia fits/s, chosen vs plain form on GB300 at |dloglik|<1e-6; blocks/s"
+# float32 instructions per double-float multiply-add of the split kernel
+# (df_fms_acc in pyscaledvecchia_gb300/csrc/sv_df64.cuh: 1 MUL, 3 FMA, 8 ADD)
+DF_OPS = 12
+# DRAM bytes (read + write) per block of one k_block_split<16> launch at the
+# default size, from the ncu capture summarised in
+# profiles/k_block_split16_n200k_traffic.md (None: not captured)
+SPLIT_TRAFFIC_PER_BLOCK = None
 
 
 def parse():
@@ -143,19 +150,24 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def measured_peak_fp64(lib, torch):
+def measured_peak(lib, torch, probe="fp64"):
+    """TFLOP/s of the float64 (probe="fp64") or float32 ("fp32") FMA probe:
+    8 independent FMA chains in each of sv_fp64_probe_threads() threads,
+    best of three timed launches after a warm-up."""
     from pyscaledvecchia_gb300 import _lib
     nthr = int(lib.sv_fp64_probe_threads())
-    out = torch.empty(nthr, dtype=torch.float64, device="cuda")
-    iters = 4096
+    dt = torch.float64 if probe == "fp64" else torch.float32
+    fn = lib.sv_fp64_fma_probe if probe == "fp64" else lib.sv_fp32_fma_probe
+    out = torch.empty(nthr, dtype=dt, device="cuda")
+    iters = 4096 if probe == "fp64" else 65536
     st = _lib.stream_handle(torch)
-    lib.sv_fp64_fma_probe(_lib.ptr(out), iters, st)
+    fn(_lib.ptr(out), iters, st)
     torch.cuda.synchronize()
     best = 0.0
     for _ in range(3):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        lib.sv_fp64_fma_probe(_lib.ptr(out), iters, st)
+        fn(_lib.ptr(out), iters, st)
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
@@ -557,13 +569,18 @@ def main():
         torch.distributed.destroy_process_group()
         return
 
-    peak = measured_peak_fp64(lib, torch)
+    peak = measured_peak(lib, torch, "fp64")
+    peak32 = measured_peak(lib, torch, "fp32")
+    # the split kernel computes its float64-grade work (factorisation and
+    # solves) in double-float on the FP32 pipe: one multiply-add (2 float64
+    # flops) takes DF_OPS float32 instructions (1 MUL, 3 FMA, 8 ADD)
+    peak_df = peak32 / DF_OPS
     achieved = flops / t_step / 1e12
     line = {
         "metric": METRIC, "value": value, "unit": "blocks/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 assembly/Gram + f64 factorisation (split form)",
+        "dtype": "f32 assembly/Gram + double-float (f32 pair) LDL^T/solves + f64 records (split form)",
         "data": "synthetic (seeded; y = Vecchia draw on the GPU)",
         "config": {"workload": f"loglik+score+Fisher, n={n}, d={d}, m={m}, nu={nu}, "
                                "split-precision form",
@@ -573,10 +590,15 @@ def main():
         "e2e": {"value": world * n / t_e2e, "unit": "blocks/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches_per_step * args.steps),
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "basis": "K^3/3 + (P+2)K^2 float64 flops per block (Cholesky, a, W, z); "
-                              "peak = float64 FMA probe measured in this run"},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_df, "unit": "TFLOP/s",
+                     "frac": achieved / peak_df, "traffic": (None if SPLIT_TRAFFIC_PER_BLOCK is None
+                                                  else SPLIT_TRAFFIC_PER_BLOCK * n),
+                     "basis": "achieved = K^3/3 + (P+2)K^2 float64-grade flops per block "
+                              "(LDL^T, a, W, z), computed in double-float; peak = the FP32 FMA "
+                              f"probe measured in this run ({peak32:.1f} TFLOP/s) / {DF_OPS} "
+                              "float32 instructions per double-float multiply-add; traffic = "
+                              "DRAM bytes per block of an ncu capture at this size x blocks",
+                     "fp64_pipe_peak": peak, "fp64_pipe_frac": achieved / peak},
         "clocks": clk,
         "extra": {"ll_split": res[0], "ll_float64": res64[0], "ll_e2e": ll_e2e,
                   "rel_dll_split_vs_float64": abs(res[0] - res64[0]) / abs(res64[0]),

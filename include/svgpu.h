@@ -396,6 +396,11 @@ int sv_joint_solve(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr, const 
 int64_t sv_fp64_probe_threads(void);
 int sv_fp64_fma_probe(double* out, int32_t iters, sv_stream_t stream);
 
+/* No reference counterpart: the same probe with float32 FMAs (one float per
+ * thread, sv_fp64_probe_threads() threads), the FP32-pipe peak that the
+ * split kernel's double-float arithmetic is measured against. */
+int sv_fp32_fma_probe(float* out, int32_t iters, sv_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -126,6 +126,7 @@ SIGNATURES = {
     "sv_joint_solve_workspace_bytes": (c_sz, [c_i64]),
     "sv_fp64_probe_threads": (c_i64, []),
     "sv_fp64_fma_probe": (c_i32, [c_vp, c_i32, c_vp]),
+    "sv_fp32_fma_probe": (c_i32, [c_vp, c_i32, c_vp]),
     "sv_joint_solve": (c_i32, [c_i64, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp,
                                c_vp, c_sz, c_vp]),
 }

@@ -88,9 +88,35 @@ __global__ void k_fp64_probe(double* out, int iters) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 }
 
+// 8 independent float32 FMA chains per thread (peak-rate measurement of the
+// FP32 pipe, which carries the split kernel's double-float arithmetic)
+__global__ void k_fp32_probe(float* out, int iters) {
+  float a0 = threadIdx.x * 1e-3f, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5,
+        a6 = a0 + 6, a7 = a0 + 7;
+  const float s = 0.999999f;
+  for (int i = 0; i < iters; ++i) {
+    a0 = __fmaf_rn(a0, s, 1e-9f);
+    a1 = __fmaf_rn(a1, s, 1e-9f);
+    a2 = __fmaf_rn(a2, s, 1e-9f);
+    a3 = __fmaf_rn(a3, s, 1e-9f);
+    a4 = __fmaf_rn(a4, s, 1e-9f);
+    a5 = __fmaf_rn(a5, s, 1e-9f);
+    a6 = __fmaf_rn(a6, s, 1e-9f);
+    a7 = __fmaf_rn(a7, s, 1e-9f);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
 }  // namespace sv
 
 extern "C" int64_t sv_fp64_probe_threads(void) { return 8LL * sv_num_sms() * 256; }
+
+extern "C" int sv_fp32_fma_probe(float* out, int32_t iters, sv_stream_t stream) {
+  if (!out || iters < 1) return SV_EINVAL;
+  sv::k_fp32_probe<<<8 * sv_num_sms(), 256, 0, (cudaStream_t)stream>>>(out, iters);
+  SV_CUDA_TRY(cudaGetLastError());
+  return SV_OK;
+}
 
 extern "C" int sv_fp64_fma_probe(double* out, int32_t iters, sv_stream_t stream) {
   if (!out || iters < 1) return SV_EINVAL;

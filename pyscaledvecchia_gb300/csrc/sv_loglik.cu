@@ -305,6 +305,7 @@ __device__ __forceinline__ bool block_selected(const LikArgs& A, int64_t b, int 
 
 __global__ void k_block_warp(LikArgs A) {
   extern __shared__ double smem[];
+  if (!pass_has_work(A)) return;
   const int64_t per_team = team_smem_doubles(32, A.dmax, A.NRmax, A.need_grad, A.any_estimate_nu);
   const int w = threadIdx.x >> 5;
   double* sm = smem + w * per_team;
@@ -324,6 +325,7 @@ __global__ void k_block_warp(LikArgs A) {
 
 __global__ void k_block_cta(LikArgs A) {
   extern __shared__ double smem[];
+  if (!pass_has_work(A)) return;
   for (int64_t t = A.b0 + blockIdx.x; t < A.b1; t += gridDim.x) {
     const int64_t b = launch_block(A, t);
     if (A.probs[block_problem(A, b)].skip) continue;
@@ -420,17 +422,34 @@ __global__ void k_reduce1(RedArgs R) {
     // instruction costs the same with one lane as with 32)
     const int64_t bl = base + (int64_t)lane * nwarp;
     const double lg = bl < b1 ? log(R.cache[bl * R.CS]) : 0.0;
-    for (int j = 0; j < 32; ++j) {
-      const int64_t b = base + (int64_t)j * nwarp;
-      if (b >= b1) break;
-      const double lgj = __shfl_sync(0xffffffffu, lg, j);
-      const double* c = R.cache + b * R.CS;
+    const int nj = (int)min((int64_t)32, (b1 - base + nwarp - 1) / nwarp);
+    // kRb blocks' register fields are loaded before they are added (in
+    // block order, so the sums are those of one block at a time)
+    constexpr int kRb = 4;
+    for (int j0 = 0; j0 < nj; j0 += kRb) {
+      double v[kRb][kFr];
 #pragma unroll
-      for (int r = 0; r < kFr; ++r) {
-        const int f = lane + 32 * r;
-        if (f < nf) a[r] += field(c, f, lgj);
+      for (int u = 0; u < kRb; ++u) {
+        const int j = j0 + u < nj ? j0 + u : nj - 1;
+        const double lgj = __shfl_sync(0xffffffffu, lg, j);
+        const double* c = R.cache + (base + (int64_t)j * nwarp) * R.CS;
+#pragma unroll
+        for (int r = 0; r < kFr; ++r) {
+          const int f = lane + 32 * r;
+          v[u][r] = f < nf ? field(c, f, lgj) : 0.0;
+        }
       }
-      for (int f = lane + 32 * kFr; f < nf; f += 32) acc[f] += field(c, f, lgj);
+#pragma unroll
+      for (int u = 0; u < kRb; ++u) {
+        if (j0 + u >= nj) break;
+#pragma unroll
+        for (int r = 0; r < kFr; ++r)
+          if (lane + 32 * r < nf) a[r] += v[u][r];
+        const int j = j0 + u;
+        const double lgj = __shfl_sync(0xffffffffu, lg, j);
+        const double* c = R.cache + (base + (int64_t)j * nwarp) * R.CS;
+        for (int f = lane + 32 * kFr; f < nf; f += 32) acc[f] += field(c, f, lgj);
+      }
     }
   }
 #pragma unroll
@@ -452,9 +471,12 @@ __global__ void k_final1(RedArgs R) {
   const int q = PI.q, P = PI.P;
   const int nf = nfield1(q, P, R.need_grad);
   double* sums = R.sums + (int64_t)p * R.nfmax;
+  const int parts = red_parts_n(PI.nblk);
   for (int f = threadIdx.x; f < nf; f += blockDim.x) {
     double s = 0.0;
-    for (int c = 0; c < red_parts_n(PI.nblk); ++c) s += R.part1[((int64_t)p * R.parts + c) * R.nfmax + f];
+    const double* src = R.part1 + (int64_t)p * R.parts * R.nfmax + f;
+#pragma unroll 8
+    for (int c = 0; c < parts; ++c) s += src[(int64_t)c * R.nfmax];
     sums[f] = s;
   }
   __syncthreads();
@@ -542,9 +564,12 @@ __global__ void k_final2(RedArgs R) {
   if (PI.skip) return;
   const int P = PI.P, q = PI.q, np = R.need_grad ? P : 0;
   __shared__ double tot[kMaxP + 1];
+  const int parts = red_parts_n(PI.nblk);
   for (int i = threadIdx.x; i <= np; i += blockDim.x) {
     double s = 0.0;
-    for (int c = 0; c < red_parts_n(PI.nblk); ++c) s += R.part2[((int64_t)p * R.parts + c) * (R.Pmax + 1) + i];
+    const double* src = R.part2 + (int64_t)p * R.parts * (R.Pmax + 1) + i;
+#pragma unroll 8
+    for (int c = 0; c < parts; ++c) s += src[(int64_t)c * (R.Pmax + 1)];
     tot[i] = s;
   }
   __syncthreads();

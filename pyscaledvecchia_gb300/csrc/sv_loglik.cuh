@@ -42,7 +42,7 @@ struct LikArgs {
   int8_t* level;
   int8_t* redo;
   int32_t* chunk_max;
-  int32_t* flags;         // [0] = any block used jitter
+  int32_t* flags;         // [0] = any block used jitter, [1] = any block flagged for redo
   int32_t* info;          // 4 words per problem
   int64_t b0, b1;         // list range (indices into list, or block ids)
   int nprob, ldnbr, CS, kt, dmax, NRmax;  // kt = team block capacity (32 or kmax+1)
@@ -53,6 +53,15 @@ struct LikArgs {
   float2* xhl;            // split form: x / lambda as float32 (hi, lo) pairs
   int kcap;               // split form: largest K of the launch (<= 32)
 };
+
+// The chunk fix-up pass has work only when some block used jitter
+// (flags[0]); the float64 re-evaluation only when the split kernel flagged a
+// block (flags[1]).  Both flags are cleared at the start of an evaluation.
+__device__ __forceinline__ bool pass_has_work(const LikArgs& A) {
+  if (A.fixup && A.flags[0] == 0) return false;
+  if (A.redo_mode && A.flags[1] == 0) return false;
+  return true;
+}
 
 // block id of the t-th entry handled by a launch
 __device__ __forceinline__ int64_t launch_block(const LikArgs& A, int64_t t) {

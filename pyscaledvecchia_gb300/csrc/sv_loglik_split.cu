@@ -223,6 +223,7 @@ template <int G>
 __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, int wpc) {
   extern __shared__ double smem[];
   constexpr int NB = 32 / G;
+  if (!pass_has_work(A)) return;
   const unsigned full = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tm = lane / G, tl = lane - (lane / G) * G;
@@ -450,6 +451,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       if (tl == 0) {
         A.level[b] = 0;
         A.redo[b] = 1;
+        A.flags[1] = 1;
         atomicAdd(info + SV_INFO_AUX, 1);
       }
       for (int f = tl; f < A.CS; f += G) rec[f] = 0.0;
@@ -462,7 +464,10 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       // ill-conditioned blocks lose too much to float32 assembly: redo in float64
       const bool again = tflag[1] != 0;
       A.redo[b] = again ? 1 : 0;
-      if (again) atomicAdd(info + SV_INFO_AUX, 1);
+      if (again) {
+        A.flags[1] = 1;
+        atomicAdd(info + SV_INFO_AUX, 1);
+      }
     }
     const bool ok = active && !failed;
 
