@@ -61,6 +61,15 @@ __global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, in
     } else {
       I.tau = exp(th[1 + d]);
     }
+    {
+      const double dg = I.s2 * (1.0 + I.tau), s2t = I.s2 * I.tau;
+      I.s2_hi = (float)I.s2;
+      I.s2_lo = (float)(I.s2 - (double)I.s2_hi);
+      I.dg_hi = (float)dg;
+      I.dg_lo = (float)(dg - (double)I.dg_hi);
+      I.s2t_hi = (float)s2t;
+      I.s2t_lo = (float)(s2t - (double)I.s2t_hi);
+    }
     MaternMode mm;
     mm.closed = D.estimate_nu ? -1 : matern_closed_code(D.nu);
     I.closed = mm.closed;

@@ -23,6 +23,8 @@ struct ProbInfo {
   int32_t d, q, P, estimate_nu, closed, skip;
   double nu_fixed, var_penalty, log_var_target;
   double s2, tau;
+  // split form: s2, s2 (1 + tau) and s2 tau as float32 (hi, lo) pairs
+  float s2_hi, s2_lo, dg_hi, dg_lo, s2t_hi, s2t_lo;
   MaternMode mm;
   double invlam[kMaxD];
 };

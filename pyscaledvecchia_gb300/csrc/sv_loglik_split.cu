@@ -250,6 +250,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
   float* R32 = (float*)Lp;    // float32 copy of R once L is no longer needed
   double* wkd = (double*)a;   // float64 last rows of the solutions, for the record
   const dfv dzero = df_make(0.0f, 0.0f);
+  const float rhof = (float)A.rho_min;
 
   const int64_t nb = A.b1 - A.b0;
   const int64_t stride = (int64_t)gridDim.x * wpc * NB;
@@ -271,7 +272,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
     const float s2f = (float)s2;
     const int code = PI.closed;
     const double diag = s2 * (1.0 + tau);
-    const dfv s2d = df_from_double(s2);
+    const dfv s2d = df_make(PI.s2_hi, PI.s2_lo);
     const double* Y = A.y + PI.y_off;
     const double* Zm = A.Z + PI.z_off;
     const float2* XH = A.xhl + PI.x_off;
@@ -316,8 +317,14 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       const bool need = !done;
       if (need) {
         jit = (lv > 0) ? jitter_pow10(lv) * diag : 0.0;  // 10^p * mean(diag)
-        rho_bits = __float_as_int((float)(A.rho_min * (diag + jit)));
-        const dfv dj = df_from_double(diag + jit);
+        dfv dj;
+        if (lv > 0) {
+          rho_bits = __float_as_int((float)(A.rho_min * (diag + jit)));
+          dj = df_from_double(diag + jit);
+        } else {
+          rho_bits = __float_as_int(rhof * PI.dg_hi);
+          dj = df_make(PI.dg_hi, PI.dg_lo);
+        }
         // lane h takes rows h and K-1-h (K-1 entries below the diagonal
         // between them); s2 (1 - D): the deficit carries the information of
         // close pairs
@@ -580,7 +587,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         }
       }
       // nugget row: dSigma_tau = s2 tau I
-      const dfv s2taud = df_from_double(s2 * tau);
+      const dfv s2taud = df_make(PI.s2t_hi, PI.s2t_lo);
       for (int i = tl; i < K; i += G) R[(P - 1) * 33 + i] = df_mul(s2taud, a[i]);
     }
     __syncwarp();
