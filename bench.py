@@ -45,9 +45,11 @@ METRIC = "Vecchia fits/s, chosen vs plain form on GB300 at |dloglik|<1e-6; block
 # (df_fms_acc in pyscaledvecchia_gb300/csrc/sv_df64.cuh: 1 MUL, 3 FMA, 8 ADD)
 DF_OPS = 12
 # DRAM bytes (read + write) per block of one k_block_split<16> launch at the
-# default size, from the ncu capture summarised in
-# profiles/k_block_split16_n200k_traffic.md (None: not captured)
-SPLIT_TRAFFIC_PER_BLOCK = None
+# default size (n = 200,000; other sizes report no traffic: at 20,000 blocks
+# the records stay in L2), from the ncu capture summarised in
+# profiles/k_block_split16_n200k_traffic.md: (45.08 MB read + 134.42 MB
+# written) / 200,000 blocks
+SPLIT_TRAFFIC_PER_BLOCK = 897.5
 
 
 def parse():
@@ -591,8 +593,8 @@ def main():
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches_per_step * args.steps),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_df, "unit": "TFLOP/s",
-                     "frac": achieved / peak_df, "traffic": (None if SPLIT_TRAFFIC_PER_BLOCK is None
-                                                  else SPLIT_TRAFFIC_PER_BLOCK * n),
+                     "frac": achieved / peak_df,
+                     "traffic": SPLIT_TRAFFIC_PER_BLOCK * n if n == 200000 else None,
                      "basis": "achieved = K^3/3 + (P+2)K^2 float64-grade flops per block "
                               "(LDL^T, a, W, z), computed in double-float; peak = the FP32 FMA "
                               f"probe measured in this run ({peak32:.1f} TFLOP/s) / {DF_OPS} "
