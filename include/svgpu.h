@@ -142,8 +142,9 @@ typedef struct sv_loglik_desc {
   int32_t estimate_nu;  /* 1: theta = [log s2, log lam.., log nu, log tau]     */
   int32_t chunked;      /* 1: chunk[] gives the jitter-sharing chunk of a block */
   int32_t precision;    /* 0 = float64 throughout; 1 = split: float32 assembly, */
-                        /*   dSigma.a and Gram products, float64 factorisation */
-                        /*   and solves (closed-form nu, k+1 <= 32 blocks)     */
+                        /*   dSigma.a and Gram products, double-float (float32 */
+                        /*   pair) factorisation and solves, float64 records   */
+                        /*   (closed-form nu, k+1 <= 32 blocks)                */
   int32_t team_lanes;   /* split form: lanes per block (4, 8, 16, 32; 0 = 16)  */
   double split_rho_min; /* split form: blocks whose smallest pivot ratio      */
                         /*   L_kk^2 / Sigma_kk is below this (0 = 1e-4) are    */
@@ -163,11 +164,13 @@ typedef struct sv_loglik_desc {
  *   out   : device float64[1 + P + P*P + q] = ll, grad, fish (row-major), beta
  *   info  : device int32[4] (SV_INFO_*) */
 /* The block table of sv_vecchia_loglik from the groups of _nn_groups
- * (ordering.py:119-127), packed on the device: group g's rows (device int64,
- * count of them) with k neighbour rows each (device int64, count x k
- * row-major) become blocks out_off .. out_off+count-1: rowb = row, kb = k,
- * nbr = the neighbours then -1 up to ldnbr.  An index outside [0, n) sets
- * *bad (device int32, cleared first) and is written as 0. */
+ * (ordering.py:119-127), packed on the device: group g's rows (int64, count
+ * of them) with k neighbour rows each (int64, count x k row-major) become
+ * blocks out_off .. out_off+count-1: rowb = row, kb = k, nbr = the
+ * neighbours then -1 up to ldnbr.  An index outside [0, n) sets *bad (device
+ * int32, cleared first) and is written as 0.  rows and nb are device memory,
+ * or ordinary host memory when sv_device_reads_host_memory reports 1 (the
+ * caller keeps it alive until the stream has passed the packing). */
 typedef struct sv_pack_group {
   const int64_t* rows;
   const int64_t* nb;
@@ -393,6 +396,11 @@ int sv_joint_solve(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr, const 
  * chains of `iters` FMAs in each of sv_fp64_probe_threads() threads, one
  * double written per thread to out), used to state the float64 peak that the
  * block kernels are measured against. */
+/* No reference counterpart: *out = 1 when the current device reads ordinary
+ * (pageable) host memory coherently through the host's page tables (a
+ * Grace-Blackwell chip-to-chip link), else 0. */
+int sv_device_reads_host_memory(int32_t* out);
+
 int64_t sv_fp64_probe_threads(void);
 int sv_fp64_fma_probe(double* out, int32_t iters, sv_stream_t stream);
 

@@ -109,6 +109,16 @@ __global__ void k_fp32_probe(float* out, int iters) {
 
 }  // namespace sv
 
+extern "C" int sv_device_reads_host_memory(int32_t* out) {
+  if (!out) return SV_EINVAL;
+  int dev = 0, pageable = 0, host_tables = 0;
+  SV_CUDA_TRY(cudaGetDevice(&dev));
+  SV_CUDA_TRY(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
+  SV_CUDA_TRY(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+  *out = (pageable && host_tables) ? 1 : 0;
+  return SV_OK;
+}
+
 extern "C" int64_t sv_fp64_probe_threads(void) { return 8LL * sv_num_sms() * 256; }
 
 extern "C" int sv_fp32_fma_probe(float* out, int32_t iters, sv_stream_t stream) {

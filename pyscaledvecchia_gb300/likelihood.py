@@ -141,34 +141,41 @@ class DeviceProblem:
         self.rowb = torch.empty(max(B, 1), dtype=torch.int32, device="cuda")[:B]
         self.kb = torch.empty(max(B, 1), dtype=torch.int32, device="cuda")[:B]
         self.nbr = torch.empty((max(B, 1), self.ldnbr), dtype=torch.int32, device="cuda")[:B]
-        self._gid = np.repeat(np.asarray(order, dtype=np.int32),
-                              np.asarray([gl[g] for g in order], dtype=np.int64))
+        self._order = order
         self._gk, self._gl = gk, gl
         self._goff = [0] * len(gk)  # first block of each group in the packed table
         if B == 0:
             return
-        # small groups travel in one copy, large ones in their own
-        small = [g for g in order if gl[g] * max(gk[g], 1) < 65536]
-        dev = {}
-        if small:
-            flat = np.concatenate([np.concatenate([rows_l[g], nb_l[g].reshape(-1)]) for g in small])
-            fd = _lib.to_dev(torch, flat, np.int64)
-            o = 0
-            for g in small:
-                c, k = gl[g], gk[g]
-                dev[g] = (fd[o:o + c], fd[o + c:o + c + c * k])
-                o += c + c * k
-        for g in order:
-            if g not in dev:
-                dev[g] = (_lib.to_dev(torch, rows_l[g], np.int64), _lib.to_dev(torch, nb_l[g], np.int64))
         desc = (_lib.PackGroup * len(order))()
+        if _lib.device_reads_host_memory(lib):
+            # the packing kernel reads the groups' own arrays over the
+            # chip-to-chip link: no copies (the arrays outlive the wait below)
+            src = {g: (rows_l[g].ctypes.data, nb_l[g].ctypes.data) for g in order}
+        else:
+            # small groups travel in one copy, large ones in their own
+            small = [g for g in order if gl[g] * max(gk[g], 1) < 65536]
+            src, keep = {}, []
+            if small:
+                flat = np.concatenate([np.concatenate([rows_l[g], nb_l[g].reshape(-1)]) for g in small])
+                fd = _lib.to_dev(torch, flat, np.int64)
+                keep.append(fd)
+                base, o = fd.data_ptr(), 0
+                for g in small:
+                    c, k = gl[g], gk[g]
+                    src[g] = (base + 8 * o, base + 8 * (o + c))
+                    o += c + c * k
+            for g in order:
+                if g not in src:
+                    r_d, nb_d = _lib.to_dev(torch, rows_l[g], np.int64), _lib.to_dev(torch, nb_l[g], np.int64)
+                    keep += [r_d, nb_d]
+                    src[g] = (r_d.data_ptr(), nb_d.data_ptr())
         o = 0
         for j, g in enumerate(order):
             self._goff[g] = o
-            r_d, nb_d = dev[g]
-            desc[j].rows = r_d.data_ptr() if gl[g] else None
-            desc[j].nb = nb_d.data_ptr() if gl[g] * gk[g] else None
-            desc[j].count, desc[j].out_off, desc[j].k = gl[g], o, gk[g]
+            d = desc[j]
+            d.rows = src[g][0] if gl[g] else None
+            d.nb = src[g][1] if gl[g] * gk[g] else None
+            d.count, d.out_off, d.k = gl[g], o, gk[g]
             o += gl[g]
         bad = torch.empty(1, dtype=torch.int32, device="cuda")
         rc = lib.sv_pack_blocks(ctypes.cast(desc, ctypes.c_void_p), len(order), self.n, self.ldnbr,
@@ -177,6 +184,13 @@ class DeviceProblem:
         _lib.check(lib, rc, "sv_pack_blocks")
         if int(bad.item()):  # waits for the copies and the packing
             raise ValueError("conditioning sets reference rows outside the data")
+
+    @property
+    def _gid(self):
+        """Group of every packed block (host form, for checks of the device tables)."""
+        order = self._order
+        return np.repeat(np.asarray(order, dtype=np.int32),
+                         np.asarray([self._gl[g] for g in order], dtype=np.int64))
 
     def kernel_launches(self, precision="float64", chunked=True, estimate_nu=False, nu=2.5):
         """Number of library kernels one evaluation launches."""
@@ -219,9 +233,11 @@ class DeviceProblem:
         """Enqueue one evaluation; results land in self.out / self.info.
 
         precision "float64" is the reference's arithmetic; "split" computes
-        distances, Matern terms, dSigma.a and the Gram products in float32 and
-        keeps the factorisation, solves and log-determinants in float64
-        (closed-form nu; other cases fall back to float64 in the library)."""
+        distances, Matern terms, dSigma.a and the Gram products in float32,
+        the factorisation and solves in double-float (float32 pairs, about 46
+        bits) and the records and reductions in float64 (closed-form nu;
+        other cases, and blocks that are ill-conditioned or outside float32's
+        exponent range, are evaluated in float64 by the library)."""
         torch, lib = self.torch, self.lib
         D = _lib.LoglikDesc()
         D.n, D.nblk, D.nblk_warp = self.n, self.nblk, self.nblk_warp
@@ -285,7 +301,7 @@ def vecchia_profile_loglik(theta, Xo, yo, Zo, groups, nu, estimate_nu=False,
     nu : fixed Matern smoothness (ignored with ``estimate_nu``).
     precision (keyword only, not in the reference): "float64" (default, the
             reference's arithmetic) or "split" (float32 assembly and Gram
-            products, float64 factorisation; see DeviceProblem.launch).
+            products, double-float factorisation; see DeviceProblem.launch).
     Returns (ll, grad, fisher, beta); grad and fisher are None when
     ``need_grad`` is False.  Raises numpy.linalg.LinAlgError when a block
     cannot be factorised even with jitter.

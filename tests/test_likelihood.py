@@ -293,3 +293,28 @@ def test_device_chunk_ids_match_the_host_rule():
                 want = chunk_ids(prob._gid, prob._gk, prob._gl, Pc)
                 np.testing.assert_array_equal(got, want)
 
+
+
+def test_block_table_same_from_host_reads_and_copies(monkeypatch):
+    """The block table packed from the groups' NumPy arrays read in place
+    (where the device reads host memory) equals the one packed from device
+    copies, including ragged groups, k > 31 and a bad index."""
+    sv, _, _, _nn_groups = _sv()
+    from pyscaledvecchia_gb300 import _lib
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    rng = np.random.default_rng(9)
+    n, d, m = 4000, 3, 40
+    X = rng.random((n, d))
+    groups = _nn_groups(sv.find_ordered_nn(X, m), m)
+    y = rng.standard_normal(n)
+    tables = []
+    for direct in (True, False):
+        monkeypatch.setattr(_lib, "_HOST_READABLE", direct)
+        prob = DeviceProblem(X, y, None, groups)
+        tables.append([t.cpu().numpy() for t in (prob.rowb, prob.kb, prob.nbr)])
+        bad = [(g[0], g[1].copy()) for g in groups]
+        bad[-1][1][5, 3] = n + 7
+        with pytest.raises(ValueError):
+            DeviceProblem(X, y, None, bad)
+    for a, b in zip(*tables):
+        np.testing.assert_array_equal(a, b)
