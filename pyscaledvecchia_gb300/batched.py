@@ -137,6 +137,15 @@ class BatchedLikelihood:
         wlist = np.flatnonzero(~big).astype(np.int32)
         clist = np.flatnonzero(big).astype(np.int32)
         self.nwarp, self.ncta = wlist.shape[0], clist.shape[0]
+        if ("split" in self.precisions and self.team_lanes == 0 and self.nwarp > 0
+                and not self.any_est and self.Pmax + 1 + self.qmax <= 32):
+            # one team width per launch: the autotuner's choice for the
+            # problem with the most blocks of at most 32 points
+            from . import autotune
+            wp = bprob[wlist]
+            i = int(np.argmax(np.bincount(wp, minlength=self.nprob)))
+            Kw = int(kb[wlist][wp == i].max()) + 1
+            self.team_lanes = autotune.team_lanes(Kw, int(self.d[i]), int(self.q[i]), self.need_grad)
 
         xlen = np.array([a.shape[0] for a in xs], dtype=np.int64)
         self.x_off = np.concatenate([[0], np.cumsum(xlen)[:-1]]).astype(np.int64)

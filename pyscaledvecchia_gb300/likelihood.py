@@ -239,6 +239,10 @@ class DeviceProblem:
         other cases, and blocks that are ill-conditioned or outside float32's
         exponent range, are evaluated in float64 by the library)."""
         torch, lib = self.torch, self.lib
+        if (precision == "split" and not team_lanes and self.nblk_warp > 0 and not estimate_nu
+                and nu in (0.5, 1.5, 2.5) and self.d + 3 + self.q <= 32):
+            from . import autotune
+            team_lanes = autotune.team_lanes(min(self.kmax + 1, 32), self.d, self.q, need_grad)
         D = _lib.LoglikDesc()
         D.n, D.nblk, D.nblk_warp = self.n, self.nblk, self.nblk_warp
         D.d, D.q, D.ldnbr, D.kmax = self.d, self.q, self.ldnbr, self.kmax

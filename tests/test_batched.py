@@ -57,12 +57,12 @@ def _mixed_batch():
     return [_mk(**s) for s in specs]
 
 
-def _single(pr, th, precision="float64", need_grad=True):
+def _single(pr, th, precision="float64", need_grad=True, team_lanes=0):
     from pyscaledvecchia_gb300.likelihood import DeviceProblem
     dp = DeviceProblem(pr.Xo, pr.yo, pr.Zo, pr.groups)
     return dp.evaluate(th, pr.nu, estimate_nu=pr.estimate_nu, need_grad=need_grad,
                        var_penalty=pr.var_penalty, log_var_target=pr.log_var_target,
-                       precision=precision)
+                       precision=precision, team_lanes=team_lanes)
 
 
 def _assert_same(res, ref):
@@ -91,10 +91,13 @@ def test_batched_split_equals_single():
     from pyscaledvecchia_gb300.batched import BatchedLikelihood
     # closed-form nu, no estimated nu: the split kernels take every block <= 32
     items = [it for it in _mixed_batch() if not it[0].estimate_nu and it[0].nu in (0.5, 1.5, 2.5)]
-    BL = BatchedLikelihood([p for p, _ in items], precisions=("split",))
-    res = BL.evaluate([t for _, t in items])
-    for (pr, th), r in zip(items, res):
-        _assert_same(r, _single(pr, th, precision="split"))
+    # bit for bit at the same team width (the autotuner may pick another
+    # width per problem on its own)
+    for lanes in (8, 16):
+        BL = BatchedLikelihood([p for p, _ in items], precisions=("split",), team_lanes=lanes)
+        res = BL.evaluate([t for _, t in items])
+        for (pr, th), r in zip(items, res):
+            _assert_same(r, _single(pr, th, precision="split", team_lanes=lanes))
 
 
 def test_skipped_problems_keep_outputs_and_graph_replay():
