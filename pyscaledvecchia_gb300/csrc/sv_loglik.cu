@@ -112,6 +112,61 @@ __host__ __device__ inline int64_t team_smem_doubles(int kt, int d, int NR, int 
   return s;
 }
 
+// dSigma_l a for l = 1..d (_covariance.py:142-146), one warp per block, lane i
+// owning row i:  S_il = sum_{j != i} g_ij a_j (u_il - u_jl)^2.  Every unordered
+// pair is visited once: in round r lane i takes the pair (i, i + r mod K),
+// adds its own term and hands the squared differences to lane i + r by a
+// shuffle, which adds g_ij a_i times them (rounds 1 .. K/2; for even K the
+// pairs of round K/2 are met from both ends, each lane adding its own term).
+// Half the float64 work of a pass per (row, coordinate) over all partners;
+// the sums are those of the same terms in another (fixed) order.
+template <int DR>
+__device__ __forceinline__ void dsig_pairs_warp(int K, int d, const double* u, const double* Gp,
+                                                const double* a, double* R, int ldr, int lane) {
+  const unsigned full = 0xffffffffu;
+  const bool own = lane < K;
+  double ui[DR], S[DR];
+#pragma unroll
+  for (int l = 0; l < DR; ++l) {
+    ui[l] = (own && l < d) ? u[lane * d + l] : 0.0;
+    S[l] = 0.0;
+  }
+  auto g = [&](int i, int j) { return i >= j ? Gp[tri_off(i, j)] : Gp[tri_off(j, i)]; };
+  for (int r = 1; r <= K / 2; ++r) {
+    int j = lane + r;
+    if (j >= K) j -= K;
+    int src = lane - r;
+    if (src < 0) src += K;
+    const bool both = !((K & 1) == 0 && r == K / 2);
+    double cij = 0.0, cji = 0.0;
+    if (own) {
+      cij = g(lane, j) * a[j];
+      cji = g(lane, src) * a[src];
+    }
+    double sq[DR];
+#pragma unroll
+    for (int l = 0; l < DR; ++l) {
+      sq[l] = 0.0;
+      if (own && l < d) {
+        const double df = ui[l] - u[j * d + l];
+        sq[l] = df * df;
+        S[l] = fma(cij, sq[l], S[l]);
+      }
+    }
+    if (both) {
+#pragma unroll
+      for (int l = 0; l < DR; ++l)
+        if (l < d) {
+          const double rv = __shfl_sync(full, sq[l], src & 31);
+          if (own) S[l] = fma(cji, rv, S[l]);
+        }
+    }
+  }
+#pragma unroll
+  for (int l = 0; l < DR; ++l)
+    if (own && l < d) R[(1 + l) * ldr + lane] = S[l];
+}
+
 // One block, processed by a team (float64 throughout).  Writes the block's record.
 template <int T>
 __device__ void block_pass1(const LikArgs& A, int64_t b, double* sm) {
@@ -233,6 +288,19 @@ __device__ void block_pass1(const LikArgs& A, int64_t b, double* sm) {
   for (int i = lane; i < K; i += T)
     R[i] = ((i == K - 1) ? Lp[tri_off(K - 1, K - 1)] : 0.0) - jit_used * a[i];
   // p = 1..d: (dSigma_l a)_i = sum_j G_ij (u_il - u_jl)^2 a_j   (_covariance.py:142-146)
+  bool dsig_done = false;
+  if constexpr (T == 32) {
+    if (K <= 32 && d <= 12) {
+      if (d <= 4)
+        dsig_pairs_warp<4>(K, d, u, Gp, a, R, ldr, lane);
+      else if (d <= 8)
+        dsig_pairs_warp<8>(K, d, u, Gp, a, R, ldr, lane);
+      else
+        dsig_pairs_warp<12>(K, d, u, Gp, a, R, ldr, lane);
+      dsig_done = true;
+    }
+  }
+  if (!dsig_done)
   for (int t = lane; t < K * d; t += T) {
     const int i = t / d, l = t - (t / d) * d;
     const double uil = u[i * d + l];
