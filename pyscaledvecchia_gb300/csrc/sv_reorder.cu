@@ -37,6 +37,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "sv_reorder.cuh"
@@ -1301,6 +1302,54 @@ int maximin_grid_single(const double* X, int64_t n, int d, int64_t first, int64_
   return SV_OK;
 }
 
+// Helper streams for launches that do not depend on one another (the
+// maximin launches of the cluster sizes, the neighbour-search launches of the
+// dimension classes): each launch lasts as long as its largest problem, so
+// running them side by side costs the longest instead of the sum.  Created
+// once per device; every call forks them off its own stream with an event and
+// joins them back before the work that needs their results.  Calls from
+// several host threads at once may serialise on the helpers, never misorder.
+constexpr int kRoHelpers = 7;
+static cudaStream_t g_ro_helper[kRoHelpers];
+static int g_ro_helper_dev = -1;
+static std::mutex g_ro_mu;
+
+static int ro_helper_streams(cudaStream_t* out) {
+  std::lock_guard<std::mutex> lk(g_ro_mu);
+  int dev = 0;
+  SV_CUDA_TRY(cudaGetDevice(&dev));
+  if (g_ro_helper_dev != dev) {
+    for (int i = 0; i < kRoHelpers; ++i)
+      SV_CUDA_TRY(cudaStreamCreateWithFlags(&g_ro_helper[i], cudaStreamNonBlocking));
+    g_ro_helper_dev = dev;
+  }
+  for (int i = 0; i < kRoHelpers; ++i) out[i] = g_ro_helper[i];
+  return SV_OK;
+}
+
+// helpers hs[0 .. n-1] wait for the work enqueued on st so far
+static int ro_fork(cudaStream_t st, const cudaStream_t* hs, int n) {
+  if (n <= 0) return SV_OK;
+  cudaEvent_t e;
+  SV_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  SV_CUDA_TRY(cudaEventRecord(e, st));
+  for (int i = 0; i < n; ++i) SV_CUDA_TRY(cudaStreamWaitEvent(hs[i], e, 0));
+  SV_CUDA_TRY(cudaEventDestroy(e));
+  return SV_OK;
+}
+
+// st waits for the work enqueued on hs[0 .. n-1] so far
+static int ro_join(cudaStream_t st, const cudaStream_t* hs, int n) {
+  for (int i = 0; i < n; ++i) {
+    cudaEvent_t e;
+    SV_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    SV_CUDA_TRY(cudaEventRecord(e, hs[i]));
+    SV_CUDA_TRY(cudaStreamWaitEvent(st, e, 0));
+    SV_CUDA_TRY(cudaEventDestroy(e));
+  }
+  return SV_OK;
+}
+
 int64_t maximin_cluster_max_rows(int d) {
   if (d < 1 || d > 64) return 0;
   const int64_t budget = (int64_t)ro_max_smem() - kMcStaticSmem - mc_fixed_bytes(d);
@@ -1371,12 +1420,24 @@ extern "C" int sv_reorder_batched(const sv_reorder_desc* D, const sv_reorder_pro
                                                       D->dmax, Xe, Xs);
   SV_CUDA_TRY(cudaGetLastError());
 
-  // maximin: one launch per cluster size
-  for (int g = 0; g < 5; ++g) {
-    if (L.plist[g].empty()) continue;
-    rc = launch_maximin_cluster(1 << g, L.smem[g], (unsigned)L.plist[g].size(), dprobs,
-                                (const int32_t*)(ws + L.o_plist[g]), (const double*)Xs, ord, info, st);
-    if (rc != SV_OK) return rc;
+  cudaStream_t hs[kRoHelpers];
+  if ((rc = ro_helper_streams(hs)) != SV_OK) return rc;
+  // maximin: one launch per cluster size, side by side (the first on st)
+  {
+    int used = 0;
+    for (int g = 0; g < 5; ++g) used += L.plist[g].empty() ? 0 : 1;
+    const int nh = used > 1 ? used - 1 : 0;
+    if ((rc = ro_fork(st, hs, nh)) != SV_OK) return rc;
+    int slot = 0;
+    for (int g = 0; g < 5; ++g) {
+      if (L.plist[g].empty()) continue;
+      cudaStream_t sg = slot == 0 ? st : hs[slot - 1];
+      ++slot;
+      rc = launch_maximin_cluster(1 << g, L.smem[g], (unsigned)L.plist[g].size(), dprobs,
+                                  (const int32_t*)(ws + L.o_plist[g]), (const double*)Xs, ord, info, sg);
+      if (rc != SV_OK) return rc;
+    }
+    if ((rc = ro_join(st, hs, nh)) != SV_OK) return rc;
   }
 
   gx = (maxn + 255) / 256;
@@ -1385,12 +1446,23 @@ extern "C" int sv_reorder_batched(const sv_reorder_desc* D, const sv_reorder_pro
   SV_CUDA_TRY(cudaGetLastError());
   k_ro_knn_prep<<<dim3((unsigned)gx, np), 256, 0, st>>>(dprobs, Xs, v, B);
   SV_CUDA_TRY(cudaGetLastError());
-  for (int g = 0; g < 8; ++g) {
-    if (L.tiles[g].empty()) continue;
-    rc = launch_knn_batched(L.DPs[g], (const KnnBatchProb*)(ws + L.o_kprobs),
-                            (const int2*)(ws + L.o_tiles[g]), (int64_t)L.tiles[g].size(), Xs, v, B,
-                            nbr, D->ldnbr, L.kcap[g], st);
-    if (rc != SV_OK) return rc;
+  // neighbour search: one launch per dimension class, side by side
+  {
+    int used = 0;
+    for (int g = 0; g < 8; ++g) used += L.tiles[g].empty() ? 0 : 1;
+    const int nh = used > 1 ? used - 1 : 0;
+    if ((rc = ro_fork(st, hs, nh)) != SV_OK) return rc;
+    int slot = 0;
+    for (int g = 0; g < 8; ++g) {
+      if (L.tiles[g].empty()) continue;
+      cudaStream_t sg = slot == 0 ? st : hs[slot - 1];
+      ++slot;
+      rc = launch_knn_batched(L.DPs[g], (const KnnBatchProb*)(ws + L.o_kprobs),
+                              (const int2*)(ws + L.o_tiles[g]), (int64_t)L.tiles[g].size(), Xs, v, B,
+                              nbr, D->ldnbr, L.kcap[g], sg);
+      if (rc != SV_OK) return rc;
+    }
+    if ((rc = ro_join(st, hs, nh)) != SV_OK) return rc;
   }
   return SV_OK;
 }
