@@ -330,8 +330,12 @@ def run_fits(torch, lib, nprob, dump=""):
 
     plain, t_plain = timed(lambda: [model(pr).fit(X, y) for pr, X, y in zip(probs, Xs, ys)])
     forms = {}
-    b64, t = timed(lambda: fit_batched([model(pr) for pr in probs], Xs, ys, precision="float64"))
+    st64 = {}
+    b64, t = timed(lambda: fit_batched([model(pr) for pr in probs], Xs, ys, precision="float64",
+                                       stats=st64))
     forms["batched_float64"] = _form_stats(plain, b64, t, nprob)
+    forms["batched_float64"]["schedule"] = {k: (float(v) if isinstance(v, float) else v)
+                                            for k, v in st64.items() if k not in ("batch", "thetas")}
     st = {}
     spl, t = timed(lambda: fit_batched([model(pr) for pr in probs], Xs, ys, precision="split", stats=st))
     forms["batched_split"] = _form_stats(plain, spl, t, nprob)
