@@ -185,6 +185,16 @@ def to_dev(torch, arr, dtype):
 
 
 _HOST_READABLE = None
+_SIDE = None
+
+
+def side_stream(torch):
+    """A second stream of the library, for work that may overlap the host's
+    copies on the current one (created on first use)."""
+    global _SIDE
+    if _SIDE is None:
+        _SIDE = torch.cuda.Stream()
+    return _SIDE
 
 
 def device_reads_host_memory(lib):

@@ -108,19 +108,30 @@ class DeviceProblem:
             raise ValueError("X and y have incompatible shapes")
         self.has_Z = Zo is not None and np.asarray(Zo).ndim == 2 and np.asarray(Zo).shape[1] > 0
         self.q = int(np.asarray(Zo).shape[1]) if self.has_Z else 0
+        # the packing kernel first: it reads the groups while the host waits
+        # in the copies of X, y and Z
+        pending = self._pack_on_device(groups)
         self.X = _lib.to_dev(torch, Xo, np.float64)
         self.y = _lib.to_dev(torch, yo, np.float64)
         self.Z = _lib.to_dev(torch, np.asarray(Zo, dtype=np.float64), np.float64) if self.has_Z else None
-        self._pack_on_device(groups)
+        if pending is not None:
+            torch.cuda.current_stream().wait_stream(pending[1])
+            if int(pending[0].item()):  # waits for the packing
+                raise ValueError("conditioning sets reference rows outside the data")
+        del pending
         self._chunks = {}
         self._ws = None
         self.out = None
         self.info = _lib.new_info(torch)
 
     def _pack_on_device(self, groups):
-        """The block table of ``pack_groups`` built on the device (sv_pack_blocks)
-        from the groups' own arrays: warp-sized groups first, group order kept;
-        a row or neighbour index outside the data raises ValueError."""
+        """Enqueue the block table of ``pack_groups`` built on the device
+        (sv_pack_blocks) from the groups' own arrays, on the library's side
+        stream: warp-sized groups first, group order kept.  Returns (bad flag,
+        side stream, arrays the kernel reads): the current stream must wait
+        for the side stream before the tables or the flag are used, and the
+        arrays must live until then (flag nonzero: a row or neighbour index
+        outside the data); None when there are no blocks."""
         torch, lib = self.torch, self.lib
         rows_l, nb_l = [], []
         for rows, nb in groups:
@@ -145,12 +156,25 @@ class DeviceProblem:
         self._gk, self._gl = gk, gl
         self._goff = [0] * len(gk)  # first block of each group in the packed table
         if B == 0:
-            return
+            return None
+        bad = torch.empty(1, dtype=torch.int32, device="cuda")
+        side = _lib.side_stream(torch)
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            return self._pack_enqueue(groups_arrays=(rows_l, nb_l), order=order, gl=gl, gk=gk,
+                                      bad=bad, side=side)
+
+    def _pack_enqueue(self, groups_arrays, order, gl, gk, bad, side):
+        """sv_pack_blocks on the current (side) stream; see _pack_on_device."""
+        torch, lib = self.torch, self.lib
+        rows_l, nb_l = groups_arrays
         desc = (_lib.PackGroup * len(order))()
         if _lib.device_reads_host_memory(lib):
             # the packing kernel reads the groups' own arrays over the
-            # chip-to-chip link: no copies (the arrays outlive the wait below)
+            # chip-to-chip link: no copies (the arrays are returned to the
+            # caller, which keeps them until it has waited for the packing)
             src = {g: (rows_l[g].ctypes.data, nb_l[g].ctypes.data) for g in order}
+            keep = None
         else:
             # small groups travel in one copy, large ones in their own
             small = [g for g in order if gl[g] * max(gk[g], 1) < 65536]
@@ -177,13 +201,11 @@ class DeviceProblem:
             d.nb = src[g][1] if gl[g] * gk[g] else None
             d.count, d.out_off, d.k = gl[g], o, gk[g]
             o += gl[g]
-        bad = torch.empty(1, dtype=torch.int32, device="cuda")
         rc = lib.sv_pack_blocks(ctypes.cast(desc, ctypes.c_void_p), len(order), self.n, self.ldnbr,
                                 _lib.ptr(self.rowb), _lib.ptr(self.kb), _lib.ptr(self.nbr), _lib.ptr(bad),
                                 _lib.stream_handle(torch))
         _lib.check(lib, rc, "sv_pack_blocks")
-        if int(bad.item()):  # waits for the copies and the packing
-            raise ValueError("conditioning sets reference rows outside the data")
+        return bad, side, (rows_l, nb_l, src if keep is None else keep, desc)
 
     @property
     def _gid(self):
