@@ -33,13 +33,18 @@
 
 namespace sv {
 
-constexpr int kSplitMaxThreads = 512;
+// 12 warps per CTA (shared memory holds 24 teams at d = 10, m = 30): bounds
+// of 384 threads let the kernel use 144 registers without spills instead of
+// 128 (measured at C2: 5.71 against 5.80 ms); likelihood-only launches, whose
+// smaller team slots would hold more warps, are held to 12 as well
+constexpr int kSplitMaxThreads = 384;
 // Panel widths, measured at n = 200k, d = 10, m = 30 (ms per evaluation):
 // columns per factorisation step (kSplitW) and steps per forward-solve pass
 // (kSplitWF) 4/4 6.71, 6/4 6.54, 4/8 6.54, 6/8 6.42, 8/8 6.38; two later rows
 // per iteration of a forward-solve pass (kSplitJU, independent double-float
 // chains) 8/8 6.29, 8/12 6.27, 6/6 6.32; two trailing elements per lane per
-// factorisation round (kSplitU2) 7.24 against 6.71.
+// factorisation round (kSplitU2) 7.24 against 6.71 (6.11 against 5.71 with
+// 144 registers).
 constexpr int kSplitW = 8;
 constexpr int kSplitWF = 8;
 constexpr int kSplitJU = 2;
