@@ -44,9 +44,11 @@ constexpr int kSplitMaxThreads = 384;
 // per iteration of a forward-solve pass (kSplitJU, independent double-float
 // chains) 8/8 6.29, 8/12 6.27, 6/6 6.32; two trailing elements per lane per
 // factorisation round (kSplitU2) 7.24 against 6.71 (6.11 against 5.71 with
-// 144 registers).
+// 144 registers).  With the 384-thread bounds: kSplitW/kSplitWF/kSplitJU
+// 8/8/2 5.71, 8/16/2 5.61, 8/16/4 5.68, 8/24/2 6.07, 8/32/2 6.02, 12/8/2 5.70,
+// 16/8/2 6.16.
 constexpr int kSplitW = 8;
-constexpr int kSplitWF = 8;
+constexpr int kSplitWF = 16;
 constexpr int kSplitJU = 2;
 constexpr int kSplitU2 = 1;
 
