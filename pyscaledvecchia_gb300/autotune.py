@@ -79,7 +79,9 @@ def _save_file():
 
 def choose(times):
     """The width to use from {width: ms}: the fastest, unless the default is
-    within the margin of it."""
+    within the margin of it (the default when nothing was measured)."""
+    if not times:
+        return DEFAULT
     best = min(times, key=times.get)
     if DEFAULT in times and times[DEFAULT] <= (1.0 + _MARGIN) * times[best]:
         return DEFAULT
@@ -108,8 +110,11 @@ def measure(K, d, q, need_grad, nblocks=24000, seed=0):
     for w in WIDTHS:
         def run():
             prob.launch(th, P, 2.5, False, need_grad, 0.0, 0.0, True, precision="split", team_lanes=w)
-        run()
-        torch.cuda.synchronize()
+        try:
+            run()
+            torch.cuda.synchronize()
+        except (ValueError, RuntimeError):
+            continue  # a width the library refuses for this shape is not a candidate
         best = float("inf")
         for _ in range(3):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

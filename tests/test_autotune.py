@@ -19,6 +19,8 @@ def fresh(monkeypatch, tmp_path):
 
 
 def test_choose_keeps_the_default_within_the_margin():
+    assert autotune.choose({}) == autotune.DEFAULT
+    assert autotune.choose({4: 2.0, 8: 1.0}) == 8
     assert autotune.choose({4: 2.0, 8: 1.0, 16: 1.02, 32: 1.5}) == 16
     assert autotune.choose({4: 2.0, 8: 1.0, 16: 1.2, 32: 1.5}) == 8
     assert autotune.choose({4: 2.0, 8: 1.3, 16: 1.2, 32: 1.1}) == 32
