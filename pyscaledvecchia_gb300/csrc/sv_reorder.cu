@@ -1310,20 +1310,22 @@ int maximin_grid_single(const double* X, int64_t n, int d, int64_t first, int64_
 // joins them back before the work that needs their results.  Calls from
 // several host threads at once may serialise on the helpers, never misorder.
 constexpr int kRoHelpers = 7;
-static cudaStream_t g_ro_helper[kRoHelpers];
-static int g_ro_helper_dev = -1;
+constexpr int kRoMaxDevices = 64;
+static cudaStream_t g_ro_helper[kRoMaxDevices][kRoHelpers];
+static bool g_ro_helper_made[kRoMaxDevices];
 static std::mutex g_ro_mu;
 
 static int ro_helper_streams(cudaStream_t* out) {
   std::lock_guard<std::mutex> lk(g_ro_mu);
   int dev = 0;
   SV_CUDA_TRY(cudaGetDevice(&dev));
-  if (g_ro_helper_dev != dev) {
+  if (dev < 0 || dev >= kRoMaxDevices) return SV_EINVAL;
+  if (!g_ro_helper_made[dev]) {
     for (int i = 0; i < kRoHelpers; ++i)
-      SV_CUDA_TRY(cudaStreamCreateWithFlags(&g_ro_helper[i], cudaStreamNonBlocking));
-    g_ro_helper_dev = dev;
+      SV_CUDA_TRY(cudaStreamCreateWithFlags(&g_ro_helper[dev][i], cudaStreamNonBlocking));
+    g_ro_helper_made[dev] = true;
   }
-  for (int i = 0; i < kRoHelpers; ++i) out[i] = g_ro_helper[i];
+  for (int i = 0; i < kRoHelpers; ++i) out[i] = g_ro_helper[dev][i];
   return SV_OK;
 }
 
