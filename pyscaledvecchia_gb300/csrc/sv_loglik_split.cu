@@ -679,32 +679,49 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
       double* F = wzZ + P * q;
       for (int c = tl; c < 1 + q; c += G) rec[2 + q + c] = wkd[P + c];
       for (int p = tl; p < P; p += G) wK[p] = wkd[p];
-      const int nf = P * (P + 1) / 2;
-      const int ntot = nf + P * (1 + q);
-      for (int t = tl; t < ntot; t += G) {
-        int c1, c2;
-        if (t < nf) {
-          tri_index(t, c1, c2);
+      // Gram products G(c1, c2) = sum_i R32(i, c1) R32(i, c2) for c2 < P and
+      // c2 <= c1 < NR (the Fisher triangle, then the y and Z columns), by 2x2
+      // tiles: columns (c2, c2 + 1) for even c2, rows (c1, c1 + 1) for
+      // c1 = c2, c2 + 2, ...; a lane takes one tile at a time, one shared-
+      // memory load per FMA.  Each entry is the same sum in the same order as
+      // alone; tile entries above the diagonal or outside the set are dropped.
+      auto tiles_of = [&](int u) { return (NR - 2 * u + 1) / 2; };
+      const int npair = (P + 1) / 2;
+      int ntile = 0;
+      for (int u = 0; u < npair; ++u) ntile += tiles_of(u);
+      auto put = [&](int c1, int c2, float g) {
+        if (c1 >= NR || c2 >= P || c1 < c2) return;
+        if (c1 < P) {
+          F[tri_off(c1, c2)] = fma(-0.5 * wkd[c1], wkd[c2], (double)g);
+        } else if (c1 == P) {
+          wzy[c2] = (double)g;
         } else {
-          const int s3 = t - nf;
-          c1 = s3 / (1 + q);
-          c2 = P + (s3 - c1 * (1 + q));
+          wzZ[c2 * q + (c1 - P - 1)] = (double)g;
         }
-        const float* r1 = R32 + c1 * 33;
-        const float* r2 = R32 + c2 * 33;
-        float sacc = 0.0f;
-        for (int i = 0; i < K; ++i) sacc = fmaf(r1[i], r2[i], sacc);
-        if (t < nf) {
-          F[t] = fma(-0.5 * wkd[c1], wkd[c2], (double)sacc);
-        } else {
-          const int s3 = t - nf;
-          const int p = s3 / (1 + q);
-          const int cc = s3 - p * (1 + q);
-          if (cc == 0)
-            wzy[p] = (double)sacc;
-          else
-            wzZ[p * q + (cc - 1)] = (double)sacc;
+      };
+      for (int t = tl; t < ntile; t += G) {
+        int u = 0, rem = t;
+        while (rem >= tiles_of(u)) {
+          rem -= tiles_of(u);
+          ++u;
         }
+        const int c2 = 2 * u, c1 = 2 * u + 2 * rem;
+        const float* xa = R32 + c1 * 33;
+        const float* xb = R32 + min(c1 + 1, NR - 1) * 33;
+        const float* ya = R32 + c2 * 33;
+        const float* yb = R32 + min(c2 + 1, NR - 1) * 33;
+        float g00 = 0.0f, g01 = 0.0f, g10 = 0.0f, g11 = 0.0f;
+        for (int i = 0; i < K; ++i) {
+          const float a0 = xa[i], a1 = xb[i], b0 = ya[i], b1 = yb[i];
+          g00 = fmaf(a0, b0, g00);
+          g01 = fmaf(a0, b1, g01);
+          g10 = fmaf(a1, b0, g10);
+          g11 = fmaf(a1, b1, g11);
+        }
+        put(c1, c2, g00);
+        put(c1, c2 + 1, g01);
+        put(c1 + 1, c2, g10);
+        put(c1 + 1, c2 + 1, g11);
       }
     }
     __syncwarp();
