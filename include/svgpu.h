@@ -197,8 +197,8 @@ int sv_vecchia_loglik(const sv_loglik_desc* desc, const double* theta, const dou
                       void* workspace, size_t workspace_bytes, sv_stream_t stream);
 
 /* Batched form: many independent problems evaluated by one set of launches
- * (the spec batched fits; the reference fits problems one at a time, so
- * the per-problem arithmetic is likelihood.py:66-175 unchanged).  Problem p
+ * (batched fits of hundreds of problems; the reference fits problems one at
+ * a time, so the per-problem arithmetic is likelihood.py:66-175 unchanged).  Problem p
  * has its own inputs (offsets into the concatenated X, y, Z), its own
  * contiguous run of blocks [blk_off, blk_off + nblk) with row indices local
  * to the problem, its own parameter vector theta[p * theta_stride ..] and its
