@@ -184,28 +184,35 @@ def to_dev(torch, arr, dtype):
     return torch.from_numpy(a).to("cuda")
 
 
-_HOST_READABLE = None
-_SIDE = None
+_HOST_READABLE = None    # None: ask the current device; True / False: fixed
+_HOST_READABLE_DEV = {}  # device index -> answer
+_SIDE = {}               # device index -> side stream
 
 
 def side_stream(torch):
-    """A second stream of the library, for work that may overlap the host's
-    copies on the current one (created on first use)."""
-    global _SIDE
-    if _SIDE is None:
-        _SIDE = torch.cuda.Stream()
-    return _SIDE
+    """A second stream of the library on the current device, for work that
+    may overlap the host's copies on the current stream (created on first
+    use)."""
+    dev = torch.cuda.current_device()
+    s = _SIDE.get(dev)
+    if s is None:
+        s = _SIDE[dev] = torch.cuda.Stream(device=dev)
+    return s
 
 
 def device_reads_host_memory(lib):
-    """True when kernels may read ordinary NumPy memory directly (the device
-    reports coherent pageable access through the host's page tables)."""
-    global _HOST_READABLE
-    if _HOST_READABLE is None:
-        v = ctypes.c_int32(0)
-        check(lib, lib.sv_device_reads_host_memory(ctypes.byref(v)), "sv_device_reads_host_memory")
-        _HOST_READABLE = bool(v.value)
-    return _HOST_READABLE
+    """True when kernels may read ordinary NumPy memory directly (the current
+    device reports coherent pageable access through the host's page
+    tables)."""
+    if _HOST_READABLE is not None:
+        return _HOST_READABLE
+    dev = _torch().cuda.current_device()
+    v = _HOST_READABLE_DEV.get(dev)
+    if v is None:
+        c = ctypes.c_int32(0)
+        check(lib, lib.sv_device_reads_host_memory(ctypes.byref(c)), "sv_device_reads_host_memory")
+        v = _HOST_READABLE_DEV[dev] = bool(c.value)
+    return v
 
 
 def ptr(t):

@@ -61,3 +61,52 @@ def test_status_strings(lib):
 def test_library_is_sm103a_only():
     from pyscaledvecchia_gb300 import _build
     assert _build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_side_stream_and_host_memory_flag_are_per_device(monkeypatch):
+    """The library's side stream and the host-memory answer are kept per
+    device (stand-ins for torch and the library: no CUDA call)."""
+    import ctypes
+    from pyscaledvecchia_gb300 import _lib
+
+    class FakeStream:
+        def __init__(self, device=None):
+            self.device = device
+
+    class Cuda:
+        dev = 0
+        Stream = FakeStream
+
+        def current_device(self):
+            return self.dev
+
+    class Torch:
+        cuda = Cuda()
+
+    class Lib:
+        answers = {0: 1, 1: 0}
+        calls = []
+
+        def sv_device_reads_host_memory(self, ref):
+            Lib.calls.append(Torch.cuda.dev)
+            ref._obj.value = Lib.answers[Torch.cuda.dev]
+            return _lib.SV_OK
+
+    monkeypatch.setattr(_lib, "_SIDE", {})
+    monkeypatch.setattr(_lib, "_HOST_READABLE", None)
+    monkeypatch.setattr(_lib, "_HOST_READABLE_DEV", {})
+    monkeypatch.setattr(_lib, "_torch", lambda: Torch)
+    t, lib = Torch(), Lib()
+    s0 = _lib.side_stream(t)
+    assert s0.device == 0 and _lib.side_stream(t) is s0
+    assert _lib.device_reads_host_memory(lib) is True
+    assert _lib.device_reads_host_memory(lib) is True
+    Torch.cuda.dev = 1
+    s1 = _lib.side_stream(t)
+    assert s1 is not s0 and s1.device == 1
+    assert _lib.device_reads_host_memory(lib) is False
+    assert Lib.calls == [0, 1]
+    monkeypatch.setattr(_lib, "_HOST_READABLE", True)  # fixed answer: no query
+    assert _lib.device_reads_host_memory(lib) is True
+    assert Lib.calls == [0, 1]
+    Torch.cuda.dev = 0
