@@ -3,7 +3,8 @@
  * scaled Vecchia hot path (Katzfuss, Guinness & Lawrence 2020/22).
  *
  * Every entry point is a plain C function over caller-owned DEVICE buffers
- * (pointers + sizes), stream-ordered on `stream` (NULL = legacy default
+ * (pointers + sizes; sv_pack_blocks also takes host arrays where the device
+ * reads host memory), stream-ordered on `stream` (NULL = legacy default
  * stream).  Nothing here allocates device memory: each call that needs
  * scratch memory takes a caller-provided workspace whose size is returned by
  * the matching *_workspace_bytes query.  Errors detected on the device (a
