@@ -22,8 +22,10 @@
 // needs one reciprocal per step and no square roots; the Cholesky factor is
 // C = L D^(1/2), so a = C^-T e_K = L^-T e_K / sqrt(d_K), W = D^(-1/2) L^-1 V
 // (unit forward solves, the D^(-1/2) weights applied in the float32 Gram)
-// and L_KK = sqrt(d_K).  Blocks whose scale or data leave float32's exponent
-// range are left to the float64 pass.
+// and L_KK = sqrt(d_K).  Blocks whose smallest pivot ratio d_k / Sigma_kk
+// falls below rho_min (ill-conditioned: the float32 assembly would cost too
+// much), that do not factor even with jitter, or whose scale or data leave
+// float32's exponent range are left to the float64 pass.
 //
 // Warp-uniform outer loops (up to the warp's largest K) with team-local
 // predication keep every __syncwarp reached by all lanes when the blocks of a
