@@ -1,19 +1,20 @@
-"""Team-width autotuner of the split-precision block kernel.
+"""Team-width autotuner of the split-precision block kernels.
 
-The split kernel (csrc/sv_loglik_split.cu) gives every conditioning block a
-team of G lanes (4, 8, 16 or 32; 32/G blocks per warp).  The fastest G
-depends on the block size K = m + 1, the input dimension d and the number of
-right-hand sides: measured on GB300 with the double-float factorisation,
-8 lanes beat 16 by 24 % at d = 3, m = 10 and by 14 % at d = 3, m = 20, while
-16 is the fastest at m = 30 and for every d >= 6.
+The split kernels (csrc/sv_loglik_split64.cu, float64 factorisation, and
+csrc/sv_loglik_split.cu, double-float factorisation) give every conditioning
+block a team of G lanes (4, 8, 16 or 32; 32/G blocks per warp).  The fastest
+G depends on the kernel, the block size K = m + 1, the input dimension d and
+the number of right-hand sides: measured on GB300 with the double-float
+factorisation, 8 lanes beat 16 by 24 % at d = 3, m = 10 and by 14 % at d = 3,
+m = 20, while 16 is the fastest at m = 30 and for every d >= 6.
 
-``team_lanes(K, d, q, need_grad)`` times the four widths on a synthetic
-problem of that shape the first time the shape is seen on a device (exact
-nearest-neighbour conditioning sets of uniform points, about 24,000 blocks,
-best of three evaluations per width) and keeps the choice in memory and in
-a JSON file: ``$SV_AUTOTUNE_CACHE``, else
-``~/.cache/pyscaledvecchia_gb300/team_lanes.json``, keyed by device name and
-shape.  A width other than 16 is taken only when it is more than 3 % faster,
+``team_lanes(K, d, q, need_grad, precision)`` times the four widths on a
+synthetic problem of that shape the first time the shape is seen on a device
+(exact nearest-neighbour conditioning sets of uniform points, about 24,000
+blocks, best of three evaluations per width) and keeps the choice in memory
+and in a JSON file: ``$SV_AUTOTUNE_CACHE``, else
+``~/.cache/pyscaledvecchia_gb300/team_lanes.json``, keyed by device name,
+precision form and shape.  A width other than 16 is taken only when it is more than 3 % faster,
 so that timing noise does not flip choices.  ``SV_AUTOTUNE=0`` turns
 measurement off (16 lanes).
 
@@ -45,8 +46,8 @@ def cache_path():
     return os.path.join(os.path.expanduser("~"), ".cache", "pyscaledvecchia_gb300", "team_lanes.json")
 
 
-def shape_key(device, K, d, q, need_grad):
-    return f"{device}|K={int(K)}|d={int(d)}|q={int(q)}|grad={int(bool(need_grad))}"
+def shape_key(device, K, d, q, need_grad, precision="split"):
+    return f"{device}|{precision}|K={int(K)}|d={int(d)}|q={int(q)}|grad={int(bool(need_grad))}"
 
 
 def _load_file():
@@ -88,9 +89,9 @@ def choose(times):
     return best
 
 
-def measure(K, d, q, need_grad, nblocks=24000, seed=0):
-    """{width: ms} of one split-form evaluation of a synthetic problem with
-    blocks of K points in d dimensions and q trend columns."""
+def measure(K, d, q, need_grad, precision="split", nblocks=24000, seed=0):
+    """{width: ms} of one evaluation in the given split form of a synthetic
+    problem with blocks of K points in d dimensions and q trend columns."""
     from . import _lib
     from .likelihood import DeviceProblem
     from .ordering import _nn_groups, find_ordered_nn
@@ -109,7 +110,7 @@ def measure(K, d, q, need_grad, nblocks=24000, seed=0):
     times = {}
     for w in WIDTHS:
         def run():
-            prob.launch(th, P, 2.5, False, need_grad, 0.0, 0.0, True, precision="split", team_lanes=w)
+            prob.launch(th, P, 2.5, False, need_grad, 0.0, 0.0, True, precision=precision, team_lanes=w)
         try:
             run()
             torch.cuda.synchronize()
@@ -127,9 +128,9 @@ def measure(K, d, q, need_grad, nblocks=24000, seed=0):
     return times
 
 
-def team_lanes(K, d, q, need_grad, measure_fn=None, device=None):
-    """Team width for split-form blocks of up to K points (K <= 32) in d
-    dimensions with q trend columns."""
+def team_lanes(K, d, q, need_grad, precision="split", measure_fn=None, device=None):
+    """Team width for blocks of up to K points (K <= 32) in d dimensions with
+    q trend columns in the given split form ("split" or "split_df")."""
     if os.environ.get("SV_AUTOTUNE", "1") == "0":
         return DEFAULT
     if K <= 1:
@@ -139,14 +140,14 @@ def team_lanes(K, d, q, need_grad, measure_fn=None, device=None):
         _, torch = _lib.device_ready()
         if torch.cuda.is_current_stream_capturing():
             return _mem.get(shape_key(torch.cuda.get_device_name(torch.cuda.current_device()),
-                                      K, d, q, need_grad), DEFAULT)
+                                      K, d, q, need_grad, precision), DEFAULT)
         device = torch.cuda.get_device_name(torch.cuda.current_device())
-    key = shape_key(device, K, d, q, need_grad)
+    key = shape_key(device, K, d, q, need_grad, precision)
     with _lock:
         _load_file()
         if key in _mem:
             return _mem[key]
-    times = (measure_fn or measure)(K, d, q, need_grad)
+    times = (measure_fn or measure)(K, d, q, need_grad, precision=precision)
     w = choose(times)
     with _lock:
         _mem[key] = w

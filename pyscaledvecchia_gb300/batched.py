@@ -19,7 +19,7 @@ import numpy as np
 
 from . import _lib
 from ._covariance import _check_nu
-from .likelihood import _PRECISION, _WARP_K, chunk_ids, pack_groups
+from .likelihood import _PRECISION, _SPLIT, _WARP_K, chunk_ids, pack_groups
 from .ordering import _nn_groups
 
 __all__ = ["BatchProblem", "BatchedLikelihood", "ordered_groups"]
@@ -63,7 +63,7 @@ class BatchedLikelihood:
                  team_lanes=0, split_rho_min=0.0):
         for pr in precisions:
             if pr not in _PRECISION:
-                raise ValueError("precision must be 'float64' or 'split'")
+                raise ValueError("precision must be 'float64', 'split' or 'split_df'")
         if len(problems) == 0:
             raise ValueError("a batch needs at least one problem")
         lib, torch = _lib.device_ready()
@@ -137,15 +137,19 @@ class BatchedLikelihood:
         wlist = np.flatnonzero(~big).astype(np.int32)
         clist = np.flatnonzero(big).astype(np.int32)
         self.nwarp, self.ncta = wlist.shape[0], clist.shape[0]
-        if ("split" in self.precisions and self.team_lanes == 0 and self.nwarp > 0
-                and not self.any_est and self.Pmax + 1 + self.qmax <= 32):
-            # one team width per launch: the autotuner's choice for the
-            # problem with the most blocks of at most 32 points
-            from . import autotune
-            wp = bprob[wlist]
-            i = int(np.argmax(np.bincount(wp, minlength=self.nprob)))
-            Kw = int(kb[wlist][wp == i].max()) + 1
-            self.team_lanes = autotune.team_lanes(Kw, int(self.d[i]), int(self.q[i]), self.need_grad)
+        # one team width per launch of a split form: the given one, else the
+        # autotuner's choice for the problem with the most blocks of at most
+        # 32 points
+        self._lanes = {prec: self.team_lanes for prec in self.precisions}
+        for prec in self.precisions:
+            if (prec in _SPLIT and self.team_lanes == 0 and self.nwarp > 0
+                    and not self.any_est and self.Pmax + 1 + self.qmax <= 32):
+                from . import autotune
+                wp = bprob[wlist]
+                i = int(np.argmax(np.bincount(wp, minlength=self.nprob)))
+                Kw = int(kb[wlist][wp == i].max()) + 1
+                self._lanes[prec] = autotune.team_lanes(Kw, int(self.d[i]), int(self.q[i]),
+                                                        self.need_grad, precision=prec)
 
         xlen = np.array([a.shape[0] for a in xs], dtype=np.int64)
         self.x_off = np.concatenate([[0], np.cumsum(xlen)[:-1]]).astype(np.int64)
@@ -192,7 +196,7 @@ class BatchedLikelihood:
             Bd.nprob, Bd.nblk, Bd.nwarp, Bd.ncta, Bd.nx = self.nprob, B, self.nwarp, self.ncta, self.nx
             Bd.dmax, Bd.qmax, Bd.kmax, Bd.ldnbr = self.dmax, self.qmax, self.kmax, self.ldnbr
             Bd.need_grad, Bd.any_estimate_nu, Bd.chunked = int(self.need_grad), int(self.any_est), int(self.chunked)
-            Bd.precision, Bd.team_lanes = _PRECISION[prec], self.team_lanes
+            Bd.precision, Bd.team_lanes = _PRECISION[prec], self._lanes[prec]
             Bd.theta_stride, Bd.out_stride, Bd.pad = self.Pmax, self.ostride, 0
             Bd.split_rho_min = self.split_rho_min
             Bd.nblk_max = int(self.nblk.max())

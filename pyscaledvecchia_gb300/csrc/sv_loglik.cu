@@ -63,6 +63,8 @@ __global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, in
     }
     {
       const double dg = I.s2 * (1.0 + I.tau), s2t = I.s2 * I.tau;
+      I.dg = dg;
+      I.s2t = s2t;
       I.s2_hi = (float)I.s2;
       I.s2_lo = (float)(I.s2 - (double)I.s2_hi);
       I.dg_hi = (float)dg;
@@ -741,7 +743,7 @@ WsLayout ws_layout(const EvalShape& S) {
   L.sums = off;
   off = align256(off + sizeof(double) * (size_t)S.nprob * L.nfmax);
   L.xhl = off;
-  if (S.precision == 1) off = align256(off + sizeof(float) * 2 * (size_t)S.nx);
+  if (S.precision == 1 || S.precision == 2) off = align256(off + sizeof(float) * 2 * (size_t)S.nx);
   L.total = off;
   return L;
 }
@@ -852,9 +854,10 @@ int run_eval(const EvalCall& C, cudaStream_t st) {
   k_prob_params<<<(int)S.nprob, 64, 0, st>>>(C.probs, C.theta, C.tstride, (int)S.nprob, probs);
   SV_CUDA_TRY(cudaGetLastError());
 
-  // split form: closed-form nu for every problem and at most 32 right-hand
-  // sides (d + q <= 29); anything else runs the float64 kernels
-  const bool split = S.precision == 1 && !S.any_est && A.NRmax <= 32;
+  // split forms (1: float64 factorisation, 2: double-float factorisation):
+  // closed-form nu for every problem and at most 32 right-hand sides
+  // (d + q <= 29); anything else runs the float64 kernels
+  const bool split = (S.precision == 1 || S.precision == 2) && !S.any_est && A.NRmax <= 32;
   // 16 lanes per block is the fastest team width measured for every K from 6
   // to 31 (d = 3 and 10); 8 and 32 trail by up to 37 % and 12 %
   const int lanes = C.team_lanes > 0 ? C.team_lanes : 16;
@@ -866,7 +869,8 @@ int run_eval(const EvalCall& C, cudaStream_t st) {
     B.b0 = 0;
     B.b1 = C.nwarp;
     if (C.nwarp <= 0) return SV_OK;
-    if (split && !B.redo_mode) return launch_block_split(B, lanes, st);
+    if (split && !B.redo_mode)
+      return S.precision == 1 ? launch_block_split(B, lanes, st) : launch_block_split_df(B, lanes, st);
     return launch_warp_kernel(B, st);
   };
   auto cta_pass = [&](LikArgs B) -> int {
@@ -989,7 +993,7 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
   if (D->kmax > 0 && (!nbr || D->ldnbr < D->kmax)) return SV_EINVAL;
   if (D->chunked && !chunk) return SV_EINVAL;
   if (!D->estimate_nu && !(D->nu > 0.0)) return SV_EINVAL;
-  if (D->precision != 0 && D->precision != 1) return SV_EINVAL;
+  if (D->precision < 0 || D->precision > 2) return SV_EINVAL;
   const EvalShape S = single_shape(D);
   WsLayout W = ws_layout(S);
   if (!workspace || workspace_bytes < W.total) return SV_ENOSPC;
@@ -1061,7 +1065,7 @@ extern "C" int sv_vecchia_loglik_batched(const sv_batch_desc* B, const sv_prob_d
   if (B->kmax > 0 && (!nbr || B->ldnbr < B->kmax)) return SV_EINVAL;
   if ((B->nwarp > 0 && !wlist) || (B->ncta > 0 && !clist)) return SV_EINVAL;
   if (B->chunked && !chunk) return SV_EINVAL;
-  if (B->precision != 0 && B->precision != 1) return SV_EINVAL;
+  if (B->precision < 0 || B->precision > 2) return SV_EINVAL;
   const int Pmax = B->dmax + 2 + (B->any_estimate_nu ? 1 : 0);
   if (B->theta_stride < Pmax || B->out_stride < 1 + Pmax + Pmax * Pmax + B->qmax) return SV_EINVAL;
   const EvalShape S = batch_shape(B);

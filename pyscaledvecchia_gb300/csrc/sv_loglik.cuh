@@ -23,7 +23,8 @@ struct ProbInfo {
   int32_t d, q, P, estimate_nu, closed, skip;
   double nu_fixed, var_penalty, log_var_target;
   double s2, tau;
-  // split form: s2, s2 (1 + tau) and s2 tau as float32 (hi, lo) pairs
+  double dg, s2t;  // s2 (1 + tau) and s2 tau
+  // double-float split form: s2, s2 (1 + tau) and s2 tau as float32 (hi, lo) pairs
   float s2_hi, s2_lo, dg_hi, dg_lo, s2t_hi, s2t_lo;
   MaternMode mm;
   double invlam[kMaxD];
@@ -115,9 +116,12 @@ __host__ __device__ inline int split_slot_doubles(int d, int NR, int kc) {
   return s;
 }
 
-// launches the split-precision kernel over list entries [A.b0, A.b1) (all
-// K <= 32, closed-form nu); lanes = block team width (4, 8, 16 or 32)
+// launch the split-precision kernels over list entries [A.b0, A.b1) (all
+// K <= 32, closed-form nu); lanes = block team width (4, 8, 16 or 32).
+// launch_block_split: float64 factorisation and solves (the split form);
+// launch_block_split_df: double-float factorisation and solves
 int launch_block_split(const LikArgs& A, int lanes, cudaStream_t st);
+int launch_block_split_df(const LikArgs& A, int lanes, cudaStream_t st);
 
 // split form: fills A.xhl (X's n * d entries as float2) for every problem
 int launch_split_prep(const LikArgs& A, int64_t nx, cudaStream_t st);

@@ -30,8 +30,8 @@
 // Warp-uniform outer loops (up to the warp's largest K) with team-local
 // predication keep every __syncwarp reached by all lanes when the blocks of a
 // warp differ in size.
-#include "sv_loglik.cuh"
 #include "sv_df64.cuh"
+#include "sv_split.cuh"
 
 namespace sv {
 
@@ -55,108 +55,6 @@ constexpr int kSplitWF = 16;
 constexpr int kSplitJU = 2;
 constexpr int kSplitU2 = 1;
 
-__device__ __forceinline__ void matern_closed_f32(int code, float r, float& M, float& g) {
-  if (code == 0) {
-    if (r > 0.0f) {
-      const float e = expf(-r);
-      M = e;
-      g = -e / r;
-    } else {
-      M = 1.0f;
-      g = 0.0f;
-    }
-  } else if (code == 1) {
-    const float c = 1.7320508075688772f * r;
-    const float e = expf(-c);
-    M = (1.0f + c) * e;
-    g = -3.0f * e;
-  } else {
-    const float c = 2.23606797749979f * r;
-    const float e = expf(-c);
-    M = (1.0f + c + c * c * (1.0f / 3.0f)) * e;
-    g = -(5.0f / 3.0f) * (1.0f + c) * e;
-  }
-}
-
-// Correlation deficit D = 1 - M(r) with small relative error for every r
-// (for nearby points M is close to 1 and 1 - M would lose all of float32's
-// digits):  nu = 0.5: -expm1(-r);  for c = sqrt(2 nu) r <= 2,
-// nu = 1.5: e^-c c^2 P(c) with P(c) = sum_{k >= 2} c^(k-2) / k!,
-// nu = 2.5: e^-c c^2 (P(c) - 1/3)   (1 - M = e^-c (c^2/6 + sum_{k>=3} c^k/k!)),
-// P by Horner's rule in c with the constants 1/k!, k = 3 .. 14 (positive
-// terms, no cancellation; the terms beyond k = 14 are below 1e-8 of P at
-// c = 2).  Measured against 40-digit values on c in [1e-4, 2]: at most 4 ulp,
-// 0.8 ulp on average, as the exponential-tail sum it replaces.
-__device__ __forceinline__ float matern_deficit_f32(int code, float r) {
-  if (code == 0) return -expm1f(-r);
-  const float c = (code == 1 ? 1.7320508075688772f : 2.23606797749979f) * r;
-  if (c > 2.0f) {
-    float M, g;
-    matern_closed_f32(code, r, M, g);
-    return 1.0f - M;
-  }
-  constexpr float kInvFact[12] = {1.1470745597729725e-11f, 1.6059043836821613e-10f,
-                                  2.08767569878681e-09f,   2.505210838544172e-08f,
-                                  2.755731922398589e-07f,  2.7557319223985893e-06f,
-                                  2.48015873015873e-05f,   0.0001984126984126984f,
-                                  0.001388888888888889f,   0.008333333333333333f,
-                                  0.041666666666666664f,   0.16666666666666666f};  // 1/14! .. 1/3!
-  float P = kInvFact[0];
-#pragma unroll
-  for (int t = 1; t < 12; ++t) P = fmaf(P, c, kInvFact[t]);
-  P = fmaf(P, c, code == 1 ? 0.5f : 0.16666666666666666f);
-  return (expf(-c) * (c * c)) * P;
-}
-
-// Order tests on the bit patterns of positive numbers (integer pipe): for
-// x, y >= 0, x < y <=> bits(x) < bits(y).
-__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
-constexpr long long kBitsTiny = 0x39B4484BFEEBC2A0LL;  // 1e-30
-constexpr long long kBitsHuge = 0x46293E5939A08CEALL;  // 1e30
-constexpr int kFBitsInf = 0x7F800000;
-
-// |x| < 1e30 for a float64 x (bit test; NaN fails)
-__device__ __forceinline__ bool in_f32_range(double x) {
-  return (dbits(x) & 0x7FFFFFFFFFFFFFFFLL) < kBitsHuge;
-}
-
-// Rows i of the float32 right-hand sides dSigma_l a for l = 1..d:
-//   R(1 + l, i) = -s2 sum_{j != i} g_ij a_j (u_il - u_jl)^2,
-// one pass over the neighbours j with row i's coordinates, the squared
-// differences and the d sums in registers (DR >= d, zero padded); the same
-// roundings in the same order as a pass per l.
-template <int DR>
-__device__ __forceinline__ void split_dsig_row(int i, int K, int d, int code, float s2f,
-                                               const float* u, const float* a32, dfv* R) {
-  float ui[DR], S[DR];
-#pragma unroll
-  for (int l = 0; l < DR; ++l) {
-    ui[l] = l < d ? u[l * 32 + i] : 0.0f;
-    S[l] = 0.0f;
-  }
-  for (int j = 0; j < K; ++j) {
-    if (j == i) continue;  // g_ii a_i (u_i - u_i)^2 adds exactly nothing
-    float sq[DR];
-    float r2 = 0.0f;
-#pragma unroll
-    for (int l = 0; l < DR; ++l)
-      if (l < d) {
-        const float df = ui[l] - u[l * 32 + j];
-        r2 = fmaf(df, df, r2);
-        sq[l] = df * df;
-      }
-    float M, g;
-    matern_closed_f32(code, sqrtf(r2), M, g);
-    const float c = g * a32[j];
-#pragma unroll
-    for (int l = 0; l < DR; ++l)
-      if (l < d) S[l] = fmaf(c, sq[l], S[l]);
-  }
-#pragma unroll
-  for (int l = 0; l < DR; ++l)
-    if (l < d) R[(1 + l) * 33 + i] = df_make(-s2f * S[l], 0.0f);
-}
-
 // a pivot of the team's factorisation: LAPACK's criterion (a pivot that is
 // not > 0, i.e. negative, zero or NaN, fails: flag[0]), the conditioning
 // test against rho_min (flag[1]; rho_bits = bits of the float32 threshold)
@@ -171,13 +69,6 @@ __device__ __forceinline__ void split_pivot(dfv dkk, dfv* diag, int rho_bits, vo
     *diag = df_rcp(dkk);
   }
 }
-
-// L is stored packed by columns with capacity kc (the launch's largest K):
-// entry (i, j), i >= j, at cstart(j) + i - j.  Column walks (scaling,
-// trailing updates, forward solves) then touch consecutive words, free of
-// bank conflicts.  Once factored, the diagonal holds the pivots' reciprocals.
-__device__ __forceinline__ int cstart(int j, int kc) { return j * kc - (j * (j - 1)) / 2; }
-__device__ __forceinline__ int cm(int i, int j, int kc) { return cstart(j, kc) + (i - j); }
 
 // Entries (h, j < h) and (K-1-h, j < K-1-h) of Sigma below the diagonal,
 // s2 (1 - D(r_ij)), and both diagonal entries dj; u is [d][32] (row i at
@@ -226,7 +117,7 @@ __device__ __forceinline__ void split_sigma_rows(int h, int K, int d, int code, 
 }
 
 template <int G>
-__global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, int wpc) {
+__global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split_df(LikArgs A, int wpc) {
   extern __shared__ double smem[];
   constexpr int NB = 32 / G;
   if (!pass_has_work(A)) return;
@@ -570,45 +461,16 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split(LikArgs A, 
         R[i] = jit == 0.0 ? e : df_fms(e, jitd, a[i]);
       }
       // p = 1..d (float32): -s2 sum_j g_ij a_j (u_il - u_jl)^2
-      if (d <= 12) {
-        for (int i = tl; i < K; i += G) {
-          if (d <= 4)
-            split_dsig_row<4>(i, K, d, code, s2f, u, a32, R);
-          else if (d <= 8)
-            split_dsig_row<8>(i, K, d, code, s2f, u, a32, R);
-          else
-            split_dsig_row<12>(i, K, d, code, s2f, u, a32, R);
-        }
-      } else
       for (int i = tl; i < K; i += G) {
-        float cj[32];
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          float c = 0.0f;
-          if (j < K && j != i) {
-            float r2 = 0.0f;
-            for (int l = 0; l < d; ++l) {
-              const float df = u[l * 32 + i] - u[l * 32 + j];
-              r2 = fmaf(df, df, r2);
-            }
-            float M, g;
-            matern_closed_f32(code, sqrtf(r2), M, g);
-            c = g * a32[j];
-          }
-          cj[j] = c;
-        }
-        for (int l = 0; l < d; ++l) {
-          const float uil = u[l * 32 + i];
-          float s = 0.0f;
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            if (j < K) {
-              const float df = uil - u[l * 32 + j];
-              s = fmaf(cj[j], df * df, s);
-            }
-          }
-          R[(1 + l) * 33 + i] = df_make(-s2f * s, 0.0f);
-        }
+        auto store = [&](int c, float v) { R[c * 33 + i] = df_make(v, 0.0f); };
+        if (d <= 4)
+          split_dsig_row<4>(i, K, d, code, s2f, u, a32, store);
+        else if (d <= 8)
+          split_dsig_row<8>(i, K, d, code, s2f, u, a32, store);
+        else if (d <= 12)
+          split_dsig_row<12>(i, K, d, code, s2f, u, a32, store);
+        else
+          split_dsig_row_wide(i, K, d, code, s2f, u, a32, store);
       }
       // nugget row: dSigma_tau = s2 tau I
       const dfv s2taud = df_make(PI.s2t_hi, PI.s2t_lo);
@@ -759,7 +621,7 @@ int launch_split_prep(const LikArgs& A, int64_t nx, cudaStream_t st) {
   return SV_OK;
 }
 
-int launch_block_split(const LikArgs& A, int lanes, cudaStream_t st) {
+int launch_block_split_df(const LikArgs& A, int lanes, cudaStream_t st) {
   int dev = 0, maxsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -779,9 +641,9 @@ int launch_block_split(const LikArgs& A, int lanes, cudaStream_t st) {
   switch (lanes) {
 #define SV_SPLIT_CASE(GV)                                                                          \
   case GV:                                                                                         \
-    SV_CUDA_TRY(cudaFuncSetAttribute(k_block_split<GV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+    SV_CUDA_TRY(cudaFuncSetAttribute(k_block_split_df<GV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                      (int)smem));                                                  \
-    k_block_split<GV><<<(unsigned)grid, 32 * wpc, smem, st>>>(A, wpc);                            \
+    k_block_split_df<GV><<<(unsigned)grid, 32 * wpc, smem, st>>>(A, wpc);                            \
     break;
     SV_SPLIT_CASE(4)
     SV_SPLIT_CASE(8)

@@ -8,10 +8,11 @@ the schedule: every model's Fisher-scoring iteration runs as a generator
 objective requests of all models with one batched likelihood launch per
 precision (sv_vecchia_loglik_batched), replayed from a CUDA graph.
 
-precision="split" runs the iterations on the split-precision kernels and
-then continues each model in float64 from where it stopped ("polish", no
-reorders) until the float64 iteration stops too, so the reported loglik,
-theta and beta are float64 results.  precision="float64" runs float64
+precision="split" runs the iterations on the split-precision kernels
+(float32 assembly, float64 factorisation; "split_df": double-float
+factorisation) and then continues each model in float64 from where it
+stopped ("polish", no reorders) until the float64 iteration stops too, so the
+reported loglik, theta and beta are float64 results.  precision="float64" runs float64
 throughout (the fitted theta then follows the reference's own iteration).
 """
 from __future__ import annotations
@@ -63,7 +64,8 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
     """Fit ``models[i]`` to ``(Xs[i], ys[i])`` for every i, together.
 
     models : ScaledVecchiaGP instances (each keeps its own settings)
-    precision : "split" (split-precision iterations + float64 polish) or
+    precision : "split" (split-precision iterations + float64 polish),
+            "split_df" (the same on the double-float split kernel) or
             "float64" (every evaluation in float64: the fitted parameters are
             bit for bit those of ScaledVecchiaGP.fit)
     polish_iter : float64 Fisher-scoring iterations after the split phase
@@ -91,8 +93,8 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
     t_start = time.perf_counter()
     cnt = {"rounds": 0, "launches": 0, "reorder_calls": 0, "reordered_problems": 0,
            "t_setup": 0.0, "t_reorder": 0.0, "t_eval": 0.0, "t_host": 0.0}
-    if precision not in ("split", "float64"):
-        raise ValueError("precision must be 'split' or 'float64'")
+    if precision not in ("split", "split_df", "float64"):
+        raise ValueError("precision must be 'split', 'split_df' or 'float64'")
     if not (len(models) == len(Xs) == len(ys)):
         raise ValueError("models, Xs and ys must have the same length")
     if len(models) == 0:
@@ -121,7 +123,7 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
             f.st["theta0"] = f.model._clip_theta(t0, f.d, f.est)
             f.last_ranges = np.exp(f.st["theta0"][1:1 + f.d]).copy()
         cnt["t_warm_start"] = time.perf_counter() - t_ws
-    precs = ("split", "float64") if precision == "split" else ("float64",)
+    precs = (precision, "float64") if precision != "float64" else ("float64",)
     BL = BatchedLikelihood([f.problem() for f in fits], need_grad=True, precisions=precs,
                            team_lanes=team_lanes)
     BL.set_sources([f.st["Xe"] for f in fits], [f.st["ye"] for f in fits],
@@ -162,7 +164,7 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
             f.msg = f.gen.send(reply)
         except StopIteration as stop:
             theta, ll, beta = stop.value
-            if f.phase == "main" and precision == "split":
+            if f.phase == "main" and precision != "float64":
                 # float64 polish from the split iterate, no reorders
                 f.phase = "polish"
                 f.prec = "float64"
@@ -221,7 +223,7 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
         for i in pend:
             f = fits[i]
             st, ll, g, M, beta = BL.unpack(out, info, i)
-            f.evals[f.prec] += 1
+            f.evals["float64" if f.prec == "float64" else "split"] += 1
             if st == _lib.SV_ECHOL:
                 advance(f, EVAL_FAILED)
                 continue

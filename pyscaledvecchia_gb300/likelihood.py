@@ -25,7 +25,8 @@ from ._covariance import _check_nu, _chunks
 __all__ = ["vecchia_profile_loglik"]
 
 _WARP_K = 32  # blocks with K = k+1 <= 32 run one per warp, larger ones one per CTA
-_PRECISION = {"float64": 0, "split": 1}
+_PRECISION = {"float64": 0, "split": 1, "split_df": 2}
+_SPLIT = ("split", "split_df")
 
 
 def pack_groups(groups, n=None):
@@ -218,7 +219,7 @@ class DeviceProblem:
         """Number of library kernels one evaluation launches."""
         warp = self.nblk_warp > 0
         cta = self.nblk > self.nblk_warp
-        split = (precision == "split" and not estimate_nu and nu in (0.5, 1.5, 2.5)
+        split = (precision in _SPLIT and not estimate_nu and nu in (0.5, 1.5, 2.5)
                  and self.d + 3 + self.q <= 32)
         n = (1 if warp else 0) + (1 if cta else 0)
         if split and warp:
@@ -255,16 +256,19 @@ class DeviceProblem:
         """Enqueue one evaluation; results land in self.out / self.info.
 
         precision "float64" is the reference's arithmetic; "split" computes
-        distances, Matern terms, dSigma.a and the Gram products in float32,
-        the factorisation and solves in double-float (float32 pairs, about 46
-        bits) and the records and reductions in float64 (closed-form nu;
-        other cases, and blocks that are ill-conditioned or outside float32's
-        exponent range, are evaluated in float64 by the library)."""
+        distances, Matern terms, dSigma.a and the Gram products (trace
+        contractions) in float32, the factorisation, solves, log-determinant
+        and the likelihood sums in float64; "split_df" is "split" with the
+        factorisation and solves in double-float (float32 pairs, about 46
+        bits) instead of float64.  The split forms take closed-form nu; other
+        cases, and blocks that are ill-conditioned or outside float32's
+        exponent range, are evaluated in float64 by the library."""
         torch, lib = self.torch, self.lib
-        if (precision == "split" and not team_lanes and self.nblk_warp > 0 and not estimate_nu
+        if (precision in _SPLIT and not team_lanes and self.nblk_warp > 0 and not estimate_nu
                 and nu in (0.5, 1.5, 2.5) and self.d + 3 + self.q <= 32):
             from . import autotune
-            team_lanes = autotune.team_lanes(min(self.kmax + 1, 32), self.d, self.q, need_grad)
+            team_lanes = autotune.team_lanes(min(self.kmax + 1, 32), self.d, self.q, need_grad,
+                                             precision=precision)
         D = _lib.LoglikDesc()
         D.n, D.nblk, D.nblk_warp = self.n, self.nblk, self.nblk_warp
         D.d, D.q, D.ldnbr, D.kmax = self.d, self.q, self.ldnbr, self.kmax
@@ -326,15 +330,17 @@ def vecchia_profile_loglik(theta, Xo, yo, Zo, groups, nu, estimate_nu=False,
     groups : output of ``ordering._nn_groups``.
     nu : fixed Matern smoothness (ignored with ``estimate_nu``).
     precision (keyword only, not in the reference): "float64" (default, the
-            reference's arithmetic) or "split" (float32 assembly and Gram
-            products, double-float factorisation; see DeviceProblem.launch).
+            reference's arithmetic), "split" (float32 assembly and Gram
+            products, float64 factorisation, solves and log-determinant) or
+            "split_df" (the same with a double-float factorisation; see
+            DeviceProblem.launch).
     Returns (ll, grad, fisher, beta); grad and fisher are None when
     ``need_grad`` is False.  Raises numpy.linalg.LinAlgError when a block
     cannot be factorised even with jitter.
     """
     theta = np.asarray(theta, dtype=float)
     if precision not in _PRECISION:
-        raise ValueError("precision must be 'float64' or 'split'")
+        raise ValueError("precision must be 'float64', 'split' or 'split_df'")
     prob = DeviceProblem(Xo, yo, Zo, groups)
     return prob.evaluate(theta, nu, estimate_nu=estimate_nu, need_grad=need_grad,
                          var_penalty=var_penalty, log_var_target=log_var_target,

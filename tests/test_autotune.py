@@ -29,14 +29,14 @@ def test_choose_keeps_the_default_within_the_margin():
 def test_measures_once_per_shape_and_caches_on_disk(fresh):
     calls = []
 
-    def fake(K, d, q, g):
-        calls.append((K, d, q, g))
+    def fake(K, d, q, g, precision="split"):
+        calls.append((K, d, q, g, precision))
         return {4: 3.0, 8: 1.0, 16: 2.0, 32: 2.5} if d == 3 else {4: 3.0, 8: 2.0, 16: 1.0, 32: 2.5}
 
     assert autotune.team_lanes(11, 3, 1, True, measure_fn=fake, device="dev") == 8
     assert autotune.team_lanes(11, 3, 1, True, measure_fn=fake, device="dev") == 8
     assert autotune.team_lanes(31, 10, 1, True, measure_fn=fake, device="dev") == 16
-    assert calls == [(11, 3, 1, True), (31, 10, 1, True)]
+    assert calls == [(11, 3, 1, True, "split"), (31, 10, 1, True, "split")]
     data = json.loads(fresh.read_text())
     assert data[autotune.shape_key("dev", 11, 3, 1, True)] == 8
     # a new process reads the file instead of measuring
@@ -46,10 +46,14 @@ def test_measures_once_per_shape_and_caches_on_disk(fresh):
     # another device is another key
     assert autotune.team_lanes(11, 3, 1, True, measure_fn=fake, device="other") == 8
     assert len(calls) == 3
+    # another precision form is another key
+    assert autotune.team_lanes(11, 3, 1, True, precision="split_df", measure_fn=fake, device="dev") == 8
+    assert calls[-1] == (11, 3, 1, True, "split_df")
+    assert autotune.shape_key("dev", 11, 3, 1, True, "split_df") in json.loads(fresh.read_text())
 
 
 def test_switch_off_and_trivial_blocks(fresh, monkeypatch):
-    def boom(*a):
+    def boom(*a, **kw):
         raise AssertionError("no measurement expected")
 
     assert autotune.team_lanes(1, 3, 1, True, measure_fn=boom, device="dev") == autotune.DEFAULT
@@ -59,7 +63,7 @@ def test_switch_off_and_trivial_blocks(fresh, monkeypatch):
 
 def test_unreadable_cache_is_ignored(fresh):
     fresh.write_text("not json")
-    assert autotune.team_lanes(21, 4, 0, False, measure_fn=lambda *a: {4: 1.0, 8: 2.0, 16: 3.0, 32: 4.0},
+    assert autotune.team_lanes(21, 4, 0, False, measure_fn=lambda *a, **kw: {4: 1.0, 8: 2.0, 16: 3.0, 32: 4.0},
                                device="dev") == 4
 
 
@@ -70,4 +74,4 @@ def test_measurement_on_the_device(fresh):
     assert all(t > 0 for t in times.values())
     w = autotune.team_lanes(21, 3, 1, True)
     assert w in autotune.WIDTHS
-    assert autotune.team_lanes(21, 3, 1, True, measure_fn=lambda *a: pytest.fail("measured twice")) == w
+    assert autotune.team_lanes(21, 3, 1, True, measure_fn=lambda *a, **kw: pytest.fail("measured twice")) == w
