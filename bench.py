@@ -4,21 +4,25 @@ Workload (one "step"): the profile log-likelihood, its score and the Fisher
 information of a scaled Vecchia model with n = 200,000 points in d = 10,
 m = 30 neighbours (K = 31 blocks, P = 12 parameters), Matern nu = 2.5,
 sigma^2 = 2, tau = 1e-3, lambda log-uniform in [0.05, 50], X uniform in
-[0,1]^10 (seed 1), y an unconditional Vecchia draw made on the GPU; the
-ordering and neighbour sets are the exact maximin / kNN of the scaled
-inputs.  Throughput unit: conditioning blocks per second (one block per
-point).  Synthetic data (the reference publishes no dataset or numbers).
+[0,1]^10 (seed 1), y an unconditional Vecchia draw y = U^-T eps (computed
+on the host with NumPy, the same arrays in both arms); the ordering and
+neighbour sets are the exact maximin / kNN of the scaled inputs.  The timed
+form is the split form: float32 distances, Matern assembly, dSigma.a and
+Fisher / score Gram products, float64 LDL^T, triangular solves,
+log-determinant and likelihood sums.  Throughput unit: conditioning blocks
+per second (one block per point).  Synthetic data (the reference publishes
+no dataset or numbers).
 
   value : device-resident inputs, one sv_vecchia_loglik per step, CUDA
           events on the launching stream, L2 flushed (256 MB write) between
           steps and excluded from the step time
-  e2e   : the public call vecchia_profile_loglik(theta, X, y, Z, groups, nu)
-          on host NumPy arrays (conditioning-set packing, host->device
-          copies, kernels, device->host read of the results) per step
+  e2e   : the public call vecchia_profile_loglik(theta, X, y, Z, groups, nu,
+          precision="split") on host NumPy arrays (conditioning-set packing,
+          host->device copies, kernels, device->host read of the results)
 
 ``--impl reference`` times the reference algorithm's CPU form on the host
 cores instead: the C restatement of its Numba loops (oracle/sv_oracle.c,
-OpenMP over blocks, every host thread), on the same workload.
+OpenMP over blocks, every host thread), on the same ordered inputs.
 
 Multi-GPU (torchrun, N > 1): every rank evaluates its own independent
 problem (seed 1 + rank), there is no data-path collective; value = all
@@ -27,6 +31,7 @@ ranks' blocks / the slowest rank's time (weak scaling).
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import math
 import os
@@ -41,15 +46,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Vecchia fits/s, chosen vs plain form on GB300 at |dloglik|<1e-6; blocks/s"
-# float32 instructions per double-float multiply-add of the split kernel
-# (df_fms_acc in pyscaledvecchia_gb300/csrc/sv_df64.cuh: 1 MUL, 3 FMA, 8 ADD)
-DF_OPS = 12
-# DRAM bytes (read + write) per block of one k_block_split<16> launch at the
-# default size (n = 200,000; other sizes report no traffic: at 20,000 blocks
-# the records stay in L2), from the ncu capture summarised in
-# profiles/k_block_split16_n200k_traffic.md: (45.08 MB read + 134.42 MB
-# written) / 200,000 blocks
-SPLIT_TRAFFIC_PER_BLOCK = 897.5
+# DRAM bytes (read + write) per block of one k_block_split64<16> launch at the
+# default size (n = 200,000): an ncu capture of that launch (one pass,
+# dram__bytes_read.sum + dram__bytes_write.sum) divided by its 200,000 blocks
+SPLIT64_TRAFFIC_PER_BLOCK = None
+# the exact maximin order of the default workload, computed once by the
+# oracle (tests/golden/make_c2_order.py)
+C2_ORDER = os.path.join(ROOT, "tests", "golden", "c2_order.npz")
 
 
 def parse():
@@ -68,6 +71,9 @@ def parse():
     ap.add_argument("--fits-dump", default="",
                     help="write per-problem results of the batched-fits workload to this .npz")
     ap.add_argument("--no-predict", action="store_true", help="skip the prediction workload")
+    ap.add_argument("--no-c1", action="store_true", help="skip the n = 2000 fit + predict workload")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the other precision forms and smoothness values of the evaluation")
     return ap.parse_args()
 
 
@@ -87,8 +93,69 @@ def make_inputs(n, d, seed):
     return X, lam, theta, eps
 
 
+def matern_closed(nu, r):
+    if nu == 0.5:
+        return np.exp(-r)
+    if nu == 1.5:
+        c = math.sqrt(3.0) * r
+        return (1.0 + c) * np.exp(-c)
+    c = math.sqrt(5.0) * r
+    return (1.0 + c + c * c / 3.0) * np.exp(-c)
+
+
+def vecchia_response(Xo, nn, theta, nu, eps, chunk=4096):
+    """Unconditional Vecchia draw y = U^-T eps on the host (NumPy): column i
+    of U is a_i = L_i^-T e_K of block (neighbours of i, i) with covariance
+    sigma^2 (M_nu + tau I), so y_i = (eps_i - sum_j a_ij y_j) / a_ii in row
+    order.  The benchmark's response in both arms (identical arrays)."""
+    n, d = Xo.shape
+    m = nn.shape[1] - 1
+    s2, lam, tau = math.exp(theta[0]), np.exp(theta[1:1 + d]), math.exp(theta[-1])
+    U = Xo / lam
+    a_self = np.empty(n)
+    a_nb = np.zeros((n, max(m, 1)))
+    for k in range(0, m + 1):
+        rows = np.arange(k, k + 1) if k < m else np.arange(m, n)
+        rows = rows[rows < n]
+        for c0 in range(0, rows.shape[0], chunk):
+            r = rows[c0:c0 + chunk]
+            blk = np.concatenate([nn[r, 1:k + 1], r[:, None]], axis=1)  # (B, k+1)
+            P = U[blk] - U[r][:, None, :]  # centred on the block's own point
+            q = (P * P).sum(-1)
+            D = np.sqrt(np.maximum(q[:, :, None] + q[:, None, :] - 2.0 * (P @ np.transpose(P, (0, 2, 1))),
+                                   0.0))
+            S = s2 * (matern_closed(nu, D) + tau * np.eye(k + 1))
+            L = np.linalg.cholesky(S)
+            e = np.zeros((r.shape[0], k + 1, 1))
+            e[:, k, 0] = 1.0
+            a = np.linalg.solve(np.transpose(L, (0, 2, 1)), e)[:, :, 0]
+            a_self[r] = a[:, k]
+            a_nb[r, :k] = a[:, :k]
+    y = np.empty(n)
+    for i in range(n):
+        k = min(i, m)
+        s = eps[i]
+        if k:
+            s -= a_nb[i, :k] @ y[nn[i, 1:k + 1]]
+        y[i] = s / a_self[i]
+    return y
+
+
+def nn_digest(nn):
+    return hashlib.sha256(np.ascontiguousarray(nn, dtype=np.int32).tobytes()).hexdigest()
+
+
+def c2_fixture(n, d, m, seed):
+    """(order, neighbour-table digest) of the oracle for the default
+    workload, or None for other sizes."""
+    if (n, d, m, seed) != (200_000, 10, 30, 1) or not os.path.exists(C2_ORDER):
+        return None
+    f = np.load(C2_ORDER)
+    return f["order"].astype(np.int64), str(f["nn_sha256"])
+
+
 def block_flops(kb, P):
-    """float64 flops per block of size K = k+1: Cholesky K^3/3, a = L^-T e_K,
+    """float64 flops per block of size K = k+1: LDL^T K^3/3, a = L^-T e_K,
     W = L^-1 (dS a) for P rows, z = L^-1 y: K^3/3 + (P+2) K^2."""
     K = kb.astype(np.float64) + 1.0
     return float(np.sum(K ** 3 / 3.0 + (P + 2) * K ** 2))
@@ -177,6 +244,20 @@ def measured_peak(lib, torch, probe="fp64"):
     return best
 
 
+def errors_vs(ref, got):
+    """Per-output error of (ll, grad, fisher, beta) against a float64
+    reference: ll relative; score in units of its standard deviation
+    sqrt(F_ii) (the score is a sum of zero-mean terms); Fisher relative to
+    its largest entry; beta relative."""
+    ll0, g0, F0, b0 = ref
+    ll1, g1, F1, b1 = got
+    sd = np.sqrt(np.maximum(np.diag(F0), 1e-300))
+    return {"ll_rel": abs(ll1 - ll0) / abs(ll0),
+            "score_in_sd": float(np.max(np.abs(g1 - g0) / sd)),
+            "fisher_rel_max": float(np.abs(F1 - F0).max() / np.abs(F0).max()),
+            "beta_rel": float(np.max(np.abs(b1 - b0) / np.maximum(np.abs(b0), 1e-300)))}
+
+
 def cpu_reference_eval(Xo, yo, Zo, groups, theta, nu, threads):
     from oracle import oracle
     oracle.set_threads(threads)
@@ -185,46 +266,112 @@ def cpu_reference_eval(Xo, yo, Zo, groups, theta, nu, threads):
     return time.perf_counter() - t0, out
 
 
+# ---------------------------------------------------------------------------
+# C1: plain single fit + predict, n = 2000
+# ---------------------------------------------------------------------------
+def c1_inputs():
+    """X_train 2000 x 8 and X_test 500 x 8 uniform in [0,1]^8 (seed 0); y an
+    exact GP draw (dense Cholesky) of sigma^2 = 1, Matern 2.5, relative nugget
+    1e-4, lambda = (0.2, 0.3, 0.5, 1, 2, 5, 50, 100), constant mean 0.5, drawn
+    jointly at the training and test points."""
+    rng = np.random.default_rng(0)
+    Xtr = rng.random((2000, 8))
+    Xte = rng.random((500, 8))
+    lam = np.array([0.2, 0.3, 0.5, 1.0, 2.0, 5.0, 50.0, 100.0])
+    Xa = np.vstack([Xtr, Xte]) / lam
+    r = np.sqrt(((Xa[:, None, :] - Xa[None, :, :]) ** 2).sum(-1))
+    S = matern_closed(2.5, r) + 1e-4 * np.eye(Xa.shape[0])
+    y = 0.5 + np.linalg.cholesky(S) @ rng.standard_normal(Xa.shape[0])
+    return Xtr, y[:2000], Xte, y[2000:]
+
+
+C1_SETTINGS = dict(m_est=30, m_pred=140, n_est=2000, nu=2.5, trend="constant", nugget=None)
+C1_WORKLOAD = ("fit + predict, n_train 2000 x 8, n_test 500, Matern 2.5, exact GP draw "
+               "(tau 1e-4), m_est 30, m_pred 140, n_est 2000, constant trend, nugget estimated")
+
+
+def run_c1(make_model, reps):
+    Xtr, ytr, Xte, yte = c1_inputs()
+    make_model().fit(Xtr[:500], ytr[:500])  # warm-up (library, allocations)
+    tf, tp, res = [], [], None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        gp = make_model().fit(Xtr, ytr)
+        t1 = time.perf_counter()
+        mu, sd = gp.predict(Xte, return_std=True)
+        t2 = time.perf_counter()
+        tf.append(t1 - t0)
+        tp.append(t2 - t1)
+        res = (gp, mu, sd)
+    gp, mu, sd = res
+    t = float(np.mean(tf) + np.mean(tp))
+    return {"workload": C1_WORKLOAD, "fit_s": float(np.mean(tf)), "predict_s": float(np.mean(tp)),
+            "fit_predict_s": t, "fits_per_s": 1.0 / t, "loglik": float(gp.loglik_),
+            "theta": [float(v) for v in gp.theta_], "b": float(gp.b_),
+            "rmse_test": float(np.sqrt(np.mean((mu - yte) ** 2))), "reps": reps}
+
+
+# ---------------------------------------------------------------------------
+# reference arm
+# ---------------------------------------------------------------------------
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from oracle import oracle
     threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
     X, lam, theta, eps = make_inputs(args.n, args.d, 1)
     Xs = X / lam
-    order = oracle.maximin_order(Xs) if args.n <= 50_000 else None
-    if order is None:
-        # the exact O(n^2 d) ordering is not part of the timed step; a random
-        # permutation stands in for it on the CPU side (same block sizes)
-        order = np.random.default_rng(2).permutation(args.n)
+    fx = c2_fixture(args.n, args.d, args.m, 1)
+    t0 = time.perf_counter()
+    if fx is not None:
+        order = fx[0]  # the oracle's own maximin order, computed once
+        src = "oracle maximin order (tests/golden/c2_order.npz)"
+    else:
+        order = oracle.maximin_order(Xs)
+        src = "oracle maximin order"
+    t_order = time.perf_counter() - t0
+    t0 = time.perf_counter()
     nn = oracle.ordered_nn(Xs[order], args.m)
+    t_nn = time.perf_counter() - t0
+    nn_ok = (nn_digest(nn) == fx[1]) if fx is not None else None
     groups = oracle.nn_groups(nn, args.m)
-    Xo, Zo = X[order], np.ones((args.n, 1))
-    yo = eps[order]
+    Xo, Zo = np.ascontiguousarray(X[order]), np.ones((args.n, 1))
+    yo = vecchia_response(Xo, nn, theta, 2.5, eps)
     for _ in range(args.warmup):
         cpu_reference_eval(Xo, yo, Zo, groups, theta, args.nu, threads)
-    ts = []
+    ts, out = [], None
     for _ in range(args.steps):
-        ts.append(cpu_reference_eval(Xo, yo, Zo, groups, theta, args.nu, threads)[0])
+        t, out = cpu_reference_eval(Xo, yo, Zo, groups, theta, args.nu, threads)
+        ts.append(t)
     t = float(np.mean(ts))
     v = args.n / t
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "blocks/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic",
+        "data": "synthetic (seeded; y = Vecchia draw computed on the host, the same arrays as "
+                "the GPU arm)",
         "config": {"workload": f"loglik+score+Fisher, n={args.n}, d={args.d}, m={args.m}, "
                                f"nu={args.nu}", "n": args.n, "d": args.d, "m": args.m,
-                   "nu": args.nu},
+                   "nu": args.nu, "ordering": src},
         "cpu_baseline": {"value": v, "unit": "blocks/s", "cores": threads, "kind": "port",
                          "sample": f"full evaluation of all {args.n} blocks per step "
                                    "(C restatement of the reference's Numba loops, OpenMP)"},
         "e2e": {"value": v, "unit": "blocks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "extra": {"ll": out[0], "order_s": t_order, "knn_s": t_nn,
+                  "nn_matches_oracle_fixture": nn_ok},
     }
+    if not args.no_c1:
+        from oracle.fit import OracleGP
+        line["extra"]["c1"] = run_c1(lambda: OracleGP(**C1_SETTINGS), reps=1)
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# C3: batched fits
+# ---------------------------------------------------------------------------
 def make_fit_problems(nprob, seed=2):
     """The batched-fits workload: nprob independent problems, n log-uniform
     in [500, 20000], d uniform in {3..12}, m in {10, 20, 30}, X uniform in
@@ -328,26 +475,27 @@ def run_fits(torch, lib, nprob, dump=""):
         torch.cuda.synchronize()
         return out, time.perf_counter() - t0
 
+    def sched(st):
+        return {k: (float(v) if isinstance(v, float) else v) for k, v in st.items()
+                if k not in ("batch", "thetas")}
+
     plain, t_plain = timed(lambda: [model(pr).fit(X, y) for pr, X, y in zip(probs, Xs, ys)])
     forms = {}
     st64 = {}
     b64, t = timed(lambda: fit_batched([model(pr) for pr in probs], Xs, ys, precision="float64",
                                        stats=st64))
     forms["batched_float64"] = _form_stats(plain, b64, t, nprob)
-    forms["batched_float64"]["schedule"] = {k: (float(v) if isinstance(v, float) else v)
-                                            for k, v in st64.items() if k not in ("batch", "thetas")}
+    forms["batched_float64"]["schedule"] = sched(st64)
     st = {}
     spl, t = timed(lambda: fit_batched([model(pr) for pr in probs], Xs, ys, precision="split", stats=st))
     forms["batched_split"] = _form_stats(plain, spl, t, nprob)
-    forms["batched_split"]["schedule"] = {k: (float(v) if isinstance(v, float) else v)
-                                          for k, v in st.items() if k not in ("batch", "thetas")}
+    forms["batched_split"]["schedule"] = sched(st)
     if enc is not None:
         stw = {}
         warm, t = timed(lambda: fit_batched([model(pr) for pr in probs], Xs, ys, precision="split",
                                             warm_start=enc, stats=stw))
         forms["batched_split_warm"] = _form_stats(plain, warm, t, nprob)
-        forms["batched_split_warm"]["schedule"] = {k: (float(v) if isinstance(v, float) else v)
-                                                   for k, v in stw.items() if k not in ("batch", "thetas")}
+        forms["batched_split_warm"]["schedule"] = sched(stw)
         # both starts per model in one float64 batch, the better converged
         # loglik kept: never below the plain fit (whose path is the default one)
         judged, t = timed(lambda: fit_batched([model(pr) for pr in probs], Xs, ys, precision="float64",
@@ -405,6 +553,9 @@ def run_fits(torch, lib, nprob, dump=""):
     }
 
 
+# ---------------------------------------------------------------------------
+# C4: prediction and joint sampling
+# ---------------------------------------------------------------------------
 def run_predict(torch, lib):
     """Prediction and joint sampling: n_train = 100,000 points in [0,1]^6,
     y a Matern-2.5 Vecchia draw with lambda = (0.1, 0.2, 0.4, 0.8, 5, 100),
@@ -455,6 +606,38 @@ def run_predict(torch, lib):
             "sd_finite": bool(np.all(np.isfinite(sd))), "samples_shape": list(samples.shape)}
 
 
+# ---------------------------------------------------------------------------
+# C2 at the other smoothness values, and the Bessel K_nu against scipy
+# ---------------------------------------------------------------------------
+def bessel_error(torch, lib, Xo, nn, theta, nu, nblk=2000, seed=5):
+    """Largest relative error of the device K_nu (sv_bessel_k) against
+    scipy.special.kv on this workload's own arguments: c = sqrt(2 nu) r for
+    every pair of nblk random blocks (r floored at 1e-7 as in
+    _matern_general.py:92-116)."""
+    from scipy.special import kv
+
+    from pyscaledvecchia_gb300 import _lib
+    n, d = Xo.shape
+    U = Xo / np.exp(theta[1:1 + d])
+    rng = np.random.default_rng(seed)
+    rows = rng.choice(np.arange(nn.shape[1], n), nblk, replace=False)
+    blk = np.concatenate([nn[rows, 1:], rows[:, None]], axis=1)
+    P = U[blk]
+    r = np.sqrt(((P[:, :, None, :] - P[:, None, :, :]) ** 2).sum(-1))
+    iu = np.triu_indices(blk.shape[1], 1)
+    c = math.sqrt(2.0 * nu) * np.maximum(r[:, iu[0], iu[1]].ravel(), 1e-7)
+    xd = _lib.to_dev(torch, c, np.float64)
+    out = torch.empty_like(xd)
+    rc = lib.sv_bessel_k(_lib.ptr(xd), c.shape[0], float(nu), _lib.ptr(out), _lib.stream_handle(torch))
+    _lib.check(lib, rc, "sv_bessel_k")
+    got = out.cpu().numpy()
+    ref = kv(nu, c)
+    ok = ref > 0
+    return {"args": int(c.shape[0]), "c_min": float(c.min()), "c_max": float(c.max()),
+            "max_rel_err_vs_scipy_kv": float(np.max(np.abs(got[ok] - ref[ok]) / ref[ok])),
+            "underflow_both_zero": int(np.sum((ref == 0) & (got == 0)))}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -470,15 +653,14 @@ def main():
     import pyscaledvecchia_gb300 as sv
     from pyscaledvecchia_gb300 import _lib
     from pyscaledvecchia_gb300.likelihood import DeviceProblem
-    from pyscaledvecchia_gb300.ordering import (_nn_groups, maximin_order_device,
-                                                ordered_nn_device)
-    from pyscaledvecchia_gb300.sampling import vecchia_prior_sample_device
+    from pyscaledvecchia_gb300.ordering import _nn_groups, maximin_order_device, ordered_nn_device
 
     lib, _ = _lib.device_ready()
     n, d, m, nu = args.n, args.d, args.m, args.nu
-    X, lam, theta, eps = make_inputs(n, d, 1 + rank)
+    seed = 1 + rank
+    X, lam, theta, eps = make_inputs(n, d, seed)
 
-    # ---- setup: exact ordering, neighbours, Vecchia draw of y (timed once)
+    # ---- setup: exact ordering and neighbours on the GPU, the response on the host
     Xs = X / lam
     first = int(np.argmin(((Xs - Xs.mean(0)) ** 2).sum(1)))
     Xs_d = _lib.to_dev(torch, Xs, np.float64)
@@ -495,11 +677,11 @@ def main():
     _lib.check_info(lib, info.cpu().numpy(), "knn")
     order = order_d.cpu().numpy()
     nn = nn_d.cpu().numpy()
+    fx = c2_fixture(n, d, m, seed)
+    order_ok = bool(np.array_equal(order, fx[0])) if fx is not None else None
+    nn_ok = (nn_digest(nn) == fx[1]) if fx is not None else None
     Xo = np.ascontiguousarray(X[order])
-    Xo_d = _lib.to_dev(torch, Xo, np.float64)
-    yo = vecchia_prior_sample_device(torch, Xo_d, nn_d, theta, nu,
-                                     _lib.to_dev(torch, eps.reshape(n, 1), np.float64))
-    yo = yo.reshape(-1).cpu().numpy()
+    yo = vecchia_response(Xo, nn, theta, 2.5, eps)
     Zo = np.ones((n, 1))
     groups = _nn_groups(nn, m)
     prob = DeviceProblem(Xo, yo, Zo, groups)
@@ -512,9 +694,10 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
 
-    def time_form(precision, lanes, steps, warmup):
+    def time_form(precision, lanes, steps, warmup, nu_=None):
+        nu_ = nu if nu_ is None else nu_
         for _ in range(warmup):
-            prob.launch(th_d, P, nu, False, True, 0.0, 0.0, True, precision=precision,
+            prob.launch(th_d, P, nu_, False, True, 0.0, 0.0, True, precision=precision,
                         team_lanes=lanes)
         torch.cuda.synchronize()
         evs = []
@@ -523,21 +706,20 @@ def main():
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            prob.launch(th_d, P, nu, False, True, 0.0, 0.0, True, precision=precision,
+            prob.launch(th_d, P, nu_, False, True, 0.0, 0.0, True, precision=precision,
                         team_lanes=lanes)
             e1.record(stream)
             evs.append((e0, e1))
         torch.cuda.synchronize()
         return [a.elapsed_time(b) for a, b in evs]
 
-    # team width of the split kernel: pick the fastest on this problem
-    lane_ms = {}
-    for lanes in (4, 8, 16, 32):
-        lane_ms[lanes] = float(np.median(time_form("split", lanes, 2, 1)))
-    best_lanes = min(lane_ms, key=lane_ms.get)
+    # team width of the split kernels: the fastest on this problem
+    def best_width(prec):
+        ms = {w: float(np.median(time_form(prec, w, 2, 1))) for w in (4, 8, 16, 32)}
+        return min(ms, key=ms.get), ms
+    best_lanes, lane_ms = best_width("split")
     res64 = prob.evaluate(theta, nu)
     res = prob.evaluate(theta, nu, precision="split", team_lanes=best_lanes)
-    plain_ms = time_form("float64", 0, max(2, args.steps // 2), 1)
 
     if world > 1:
         torch.distributed.barrier()
@@ -575,46 +757,69 @@ def main():
         torch.distributed.destroy_process_group()
         return
 
+    # ---- the other forms and smoothness values of the same workload
+    forms = {}
+    if not args.no_forms:
+        ms64 = float(np.mean(time_form("float64", 0, max(2, args.steps // 2), 1)))
+        forms["float64"] = {"ms": ms64, "blocks_per_s": n / (ms64 * 1e-3)}
+        df_lanes, df_ms = best_width("split_df")
+        res_df = prob.evaluate(theta, nu, precision="split_df", team_lanes=df_lanes)
+        forms["split_df"] = {"ms": df_ms[df_lanes], "blocks_per_s": n / (df_ms[df_lanes] * 1e-3),
+                             "team_lanes": df_lanes, "team_lanes_ms": df_ms,
+                             "factorisation": "double-float (float32 pairs, ~46 bits)",
+                             "errors_vs_float64_form": errors_vs(res64, res_df)}
+        for nu_o in (1.5,):
+            ms_s = float(np.mean(time_form("split", best_lanes, max(2, args.steps // 2), 1, nu_o)))
+            ms_f = float(np.mean(time_form("float64", 0, max(2, args.steps // 2), 1, nu_o)))
+            r_s = prob.evaluate(theta, nu_o, precision="split", team_lanes=best_lanes)
+            r_f = prob.evaluate(theta, nu_o)
+            forms[f"nu{nu_o}"] = {"split_ms": ms_s, "split_blocks_per_s": n / (ms_s * 1e-3),
+                                  "float64_ms": ms_f, "float64_blocks_per_s": n / (ms_f * 1e-3),
+                                  "split_errors_vs_float64_form": errors_vs(r_f, r_s)}
+        # fixed nu = 0.8: the Bessel path (float64 kernels; the split forms
+        # take closed-form nu only)
+        ms08 = float(np.mean(time_form("float64", 0, max(2, args.steps // 2), 1, 0.8)))
+        forms["nu0.8"] = {"float64_ms": ms08, "float64_blocks_per_s": n / (ms08 * 1e-3),
+                          "kernel": "float64 block kernel with the device Bessel K_nu",
+                          "bessel_k": bessel_error(torch, lib, Xo, nn, theta, 0.8)}
+
     peak = measured_peak(lib, torch, "fp64")
     peak32 = measured_peak(lib, torch, "fp32")
-    # the split kernel computes its float64-grade work (factorisation and
-    # solves) in double-float on the FP32 pipe: one multiply-add (2 float64
-    # flops) takes DF_OPS float32 instructions (1 MUL, 3 FMA, 8 ADD)
-    peak_df = peak32 / DF_OPS
     achieved = flops / t_step / 1e12
     line = {
         "metric": METRIC, "value": value, "unit": "blocks/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 assembly/Gram + double-float (f32 pair) LDL^T/solves + f64 records (split form)",
-        "data": "synthetic (seeded; y = Vecchia draw on the GPU)",
-        "config": {"workload": f"loglik+score+Fisher, n={n}, d={d}, m={m}, nu={nu}, "
-                               "split-precision form",
+        "dtype": "f32 distances/Matern/dSigma.a/Gram + f64 LDL^T, solves, log-determinant, "
+                 "likelihood sums (split form)",
+        "data": "synthetic (seeded; y = Vecchia draw computed on the host, the same arrays as "
+                "the reference arm)",
+        "config": {"workload": f"loglik+score+Fisher, n={n}, d={d}, m={m}, nu={nu}, split form",
                    "n": n, "d": d, "m": m, "nu": nu, "blocks_per_step": n,
                    "l2": "flushed between steps (256 MB write, outside the step time)",
                    "parallelism": f"{world} independent problem(s), one per GPU"},
         "e2e": {"value": world * n / t_e2e, "unit": "blocks/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches_per_step * args.steps),
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_df, "unit": "TFLOP/s",
-                     "frac": achieved / peak_df,
-                     "traffic": SPLIT_TRAFFIC_PER_BLOCK * n if n == 200000 else None,
-                     "basis": "achieved = K^3/3 + (P+2)K^2 float64-grade flops per block "
-                              "(LDL^T, a, W, z), computed in double-float; peak = the FP32 FMA "
-                              f"probe measured in this run ({peak32:.1f} TFLOP/s) / {DF_OPS} "
-                              "float32 instructions per double-float multiply-add; traffic = "
-                              "DRAM bytes per block of an ncu capture at this size x blocks",
-                     "fp64_pipe_peak": peak, "fp64_pipe_frac": achieved / peak},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak,
+                     "traffic": (SPLIT64_TRAFFIC_PER_BLOCK * n
+                                 if SPLIT64_TRAFFIC_PER_BLOCK and n == 200000 else None),
+                     "peak_source": "float64 FMA probe measured in this run (sv_fp64_fma_probe); "
+                                    "MEASURED_PEAKS.json has no float64 figure",
+                     "basis": "achieved = K^3/3 + (P+2)K^2 float64 flops per block (LDL^T, a, "
+                              "W, z) / mean step time (the whole evaluation, of which the block "
+                              "kernel is the dominant launch); traffic = DRAM bytes per block of "
+                              "an ncu capture of the block kernel at this size x blocks",
+                     "fp32_probe_tflops": peak32},
         "clocks": clk,
         "extra": {"ll_split": res[0], "ll_float64": res64[0], "ll_e2e": ll_e2e,
-                  "rel_dll_split_vs_float64": abs(res[0] - res64[0]) / abs(res64[0]),
-                  "max_rel_dgrad": float(np.abs(res[1] - res64[1]).max() / np.abs(res64[1]).max()),
-                  "max_rel_dfisher": float(np.abs(res[2] - res64[2]).max() / np.abs(res64[2]).max()),
-                  "plain_float64_ms": float(np.mean(plain_ms)),
-                  "plain_float64_blocks_per_s": world * n / (float(np.mean(plain_ms)) * 1e-3),
-                  "plain_float64_roofline_frac": flops / (float(np.mean(plain_ms)) * 1e-3) / 1e12 / peak,
+                  "split_errors_vs_float64_form": errors_vs(res64, res),
+                  "blocks_refactored_in_float64": int(prob.last_info[3]),
                   "team_lanes_ms": lane_ms, "team_lanes": best_lanes,
-                  "maximin_s": t_maximin, "knn_s": t_knn, "step_ms_all": step_ms},
+                  "maximin_s": t_maximin, "knn_s": t_knn,
+                  "order_matches_oracle": order_ok, "nn_matches_oracle": nn_ok,
+                  "step_ms_all": step_ms, "forms": forms},
     }
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -626,6 +831,11 @@ def main():
                                 "sample": f"one full evaluation of all {n} blocks "
                                           "(C restatement of the reference's Numba loops, OpenMP)"}
         line["extra"]["ll_cpu"] = out[0]
+        line["extra"]["split_errors_vs_oracle"] = errors_vs(out, res)
+        line["extra"]["float64_errors_vs_oracle"] = errors_vs(out, res64)
+    if not args.no_c1:
+        from pyscaledvecchia_gb300 import ScaledVecchiaGP
+        line["c1"] = run_c1(lambda: ScaledVecchiaGP(**C1_SETTINGS), reps=3)
     if args.fits_problems > 0:
         line["fits"] = run_fits(torch, lib, args.fits_problems, args.fits_dump)
     if not args.no_predict:

@@ -61,7 +61,10 @@ int sv_maximin_order(const double* X, int64_t n, int32_t d, int64_t first, int64
                      int32_t* info, void* workspace, size_t workspace_bytes, sv_stream_t stream);
 /* The same with test aids that give the same order by other routes: bit 0
  * ranks every pivot choice by exact roots, bit 1 takes pivots by the tie
- * pass only, bit 2 runs the grid form even when one cluster would hold X. */
+ * pass only, bit 2 runs the grid form even when one cluster would hold X.
+ * Bit 3 (with bit 2) tests the grid barrier's bounded wait: one CTA does not
+ * arrive at the first barrier and every wait is limited to 4096 polls, so
+ * all waits run out, every CTA returns and info[0] = SV_ETIMEOUT. */
 int sv_maximin_order_flags(const double* X, int64_t n, int32_t d, int64_t first, int64_t* order,
                            int32_t* info, void* workspace, size_t workspace_bytes, int32_t flags,
                            sv_stream_t stream);
@@ -142,12 +145,15 @@ typedef struct sv_loglik_desc {
   int32_t need_grad;    /* 1: score and Fisher information too                 */
   int32_t estimate_nu;  /* 1: theta = [log s2, log lam.., log nu, log tau]     */
   int32_t chunked;      /* 1: chunk[] gives the jitter-sharing chunk of a block */
-  int32_t precision;    /* 0 = float64 throughout; 1 = split: float32 assembly, */
-                        /*   dSigma.a and Gram products, double-float (float32 */
-                        /*   pair) factorisation and solves, float64 records   */
-                        /*   (closed-form nu, k+1 <= 32 blocks)                */
-  int32_t team_lanes;   /* split form: lanes per block (4, 8, 16, 32; 0 = 16)  */
-  double split_rho_min; /* split form: blocks whose smallest pivot ratio      */
+  int32_t precision;    /* 0 = float64 throughout; 1 = split: float32         */
+                        /*   distances, Matern assembly, dSigma.a and Gram     */
+                        /*   products, float64 LDL^T, solves, log-determinant  */
+                        /*   and sums; 2 = split with a double-float (float32  */
+                        /*   pair) factorisation and solves.  The split forms  */
+                        /*   take closed-form nu and k+1 <= 32 blocks; other   */
+                        /*   blocks run in float64                             */
+  int32_t team_lanes;   /* split forms: lanes per block (4, 8, 16, 32; 0 = 16) */
+  double split_rho_min; /* split forms: blocks whose smallest pivot ratio     */
                         /*   L_kk^2 / Sigma_kk is below this (0 = 1e-4) are    */
                         /*   re-evaluated in float64; info[SV_INFO_AUX] counts */
   double nu;            /* fixed smoothness (estimate_nu = 0)                   */
@@ -161,7 +167,9 @@ typedef struct sv_loglik_desc {
  * _batch_chol, _backsolve_LT and _forward_solve on its path.
  *   theta : device float64[P], P = d+2 (+1 if estimate_nu)
  *   block b: self row rowb[b], neighbours nbr[b*ldnbr + 0..kb[b]-1]
- *   chunk : device int32[nblk] chunk ids (desc->chunked) or NULL
+ *   chunk : device int32[nblk] chunk ids in [0, nblk) (desc->chunked) or
+ *           NULL; an id outside that range sets info[SV_INFO_STATUS] to
+ *           SV_EINVAL when the chunk table is read (some block needed jitter)
  *   out   : device float64[1 + P + P*P + q] = ll, grad, fish (row-major), beta
  *   info  : device int32[4] (SV_INFO_*) */
 /* The block table of sv_vecchia_loglik from the groups of _nn_groups
@@ -249,8 +257,10 @@ int sv_vecchia_loglik_batched(const sv_batch_desc* desc, const sv_prob_desc* pro
  * outputs as above, but the scratch comes from a file-scope static device
  * array of SV_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library
  * until exit.  Returns SV_ENOSPC, launching nothing, when
- * sv_loglik_workspace_bytes(desc) exceeds it (about 35,000 blocks at
- * d = 10, m = 30).  The first call on a device looks up the array's address
+ * sv_loglik_workspace_bytes(desc) exceeds it: at d = 10, m = 30, q = 1 with
+ * score and Fisher, 34,995 blocks in float64 (precision 0) and 32,300 in the
+ * split forms (precision 1 and 2, whose scratch also holds the float32
+ * coordinate pairs).  The first call on a device looks up the array's address
  * (cudaGetSymbolAddress) and should come before any stream capture.  All
  * calls share the array: calls that overlap on the GPU race, so serialise
  * them. */
@@ -388,6 +398,14 @@ size_t sv_joint_solve_workspace_bytes(int64_t npred);
 int sv_joint_solve(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr, const int32_t* nbr,
                    const double* acol, const double* R, int32_t nrhs, double* X, int32_t* info,
                    void* workspace, size_t workspace_bytes, sv_stream_t stream);
+/* The same with a test aid for the bounded waits: flags bit 0 keeps row 0
+ * from publishing its result and limits every wait to 4096 polls, so the
+ * waits of the rows that depend on row 0 run out (info[0] = SV_ETIMEOUT,
+ * info[1] = the first such row); the kernel still finishes. */
+int sv_joint_solve_flags(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr, const int32_t* nbr,
+                         const double* acol, const double* R, int32_t nrhs, double* X,
+                         int32_t* info, void* workspace, size_t workspace_bytes, int32_t flags,
+                         sv_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
 /* Measurement                                                             */

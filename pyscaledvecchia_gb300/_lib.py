@@ -130,6 +130,8 @@ SIGNATURES = {
     "sv_device_reads_host_memory": (c_i32, [c_vp]),
     "sv_joint_solve": (c_i32, [c_i64, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp,
                                c_vp, c_sz, c_vp]),
+    "sv_joint_solve_flags": (c_i32, [c_i64, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp,
+                                     c_vp, c_vp, c_sz, c_i32, c_vp]),
 }
 
 

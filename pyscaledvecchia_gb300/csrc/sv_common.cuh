@@ -15,9 +15,13 @@
     if (e_ != cudaSuccess) return sv_record_cuda_error(e_); \
   } while (0)
 
-// Bounded spin-waits: a wait that runs out of iterations sets this status in
-// the kernel's error word and the kernel returns instead of hanging.
-#define SV_SPIN_LIMIT (1u << 26)
+// Bounded spin-waits: a wait that runs out of iterations sets SV_ETIMEOUT in
+// the kernel's error word and the kernel returns instead of hanging.  2^22
+// polls of a word in L2 (each a few hundred nanoseconds) take about a second,
+// far beyond any wait these kernels have when they work (microseconds).
+#define SV_SPIN_LIMIT (1u << 22)
+// the limit under the test aids that make a wait run out on purpose
+#define SV_SPIN_LIMIT_TEST (1u << 12)
 
 int sv_record_cuda_error(cudaError_t e);
 int sv_num_sms();

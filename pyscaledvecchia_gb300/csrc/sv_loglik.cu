@@ -25,6 +25,8 @@
 // batched evaluation can be captured in a CUDA graph.
 #include <stdio.h>
 
+#include <atomic>
+
 #include "sv_loglik.cuh"
 
 namespace sv {
@@ -88,6 +90,9 @@ __global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, in
   }
   for (int l = threadIdx.x; l < d; l += blockDim.x) I.invlam[l] = exp(-th[1 + l]);
 }
+
+// the problem table of a one-problem evaluation, passed by value
+__global__ void k_put_desc(sv_prob_desc pd, sv_prob_desc* out) { *out = pd; }
 
 // info words of every problem: status 0, first failing block -1, jitter 0, aux 0
 __global__ void k_info_init(int32_t* info, int nprob) {
@@ -209,7 +214,7 @@ __device__ void block_pass1(const LikArgs& A, int64_t b, double* sm) {
   const double s2 = PI.s2, tau = PI.tau;
   int lv = 0;
   if (A.fixup) {
-    lv = A.chunk_max[A.chunk[b]];
+    lv = chunk_level(A, b);
   } else if (A.redo_mode) {
     lv = A.level[b];
   }
@@ -378,7 +383,7 @@ __device__ void block_pass1(const LikArgs& A, int64_t b, double* sm) {
 // which blocks a launch of the block kernels processes
 __device__ __forceinline__ bool block_selected(const LikArgs& A, int64_t b, int kcap) {
   if (A.redo_mode) return A.redo[b] != 0;
-  if (A.fixup) return A.chunk_max[A.chunk[b]] > A.level[b];
+  if (A.fixup) return chunk_level(A, b) > A.level[b];
   return A.kb[b] + 1 <= kcap;
 }
 
@@ -418,14 +423,23 @@ __global__ void k_block_cta(LikArgs A) {
   }
 }
 
-// chunk-wide jitter: chunk_max[c] = max level over the chunk's blocks
+// chunk-wide jitter: chunk_max[c] = max level over the chunk's blocks.  A
+// chunk id outside [0, nblk) is the caller's error: it is skipped and its
+// problem's status set to SV_EINVAL (chunk ids are read only when some block
+// needed jitter)
 __global__ void k_chunk_max(const int32_t* flags, const int32_t* chunk, const int8_t* level,
-                            int64_t nblk, int32_t* chunk_max) {
+                            int64_t nblk, int32_t* chunk_max, const int32_t* bprob,
+                            int32_t* info) {
   if (flags[0] == 0) return;
   for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nblk;
        b += (int64_t)gridDim.x * blockDim.x) {
+    const int c = chunk[b];
+    if (c < 0 || c >= nblk) {
+      set_error(info + 4 * (bprob ? bprob[b] : 0) + SV_INFO_STATUS, SV_EINVAL);
+      continue;
+    }
     const int lv = level[b];
-    if (lv > 0 && lv <= 9) atomicMax(chunk_max + chunk[b], lv);
+    if (lv > 0 && lv <= 9) atomicMax(chunk_max + c, lv);
   }
 }
 
@@ -748,15 +762,24 @@ WsLayout ws_layout(const EvalShape& S) {
   return L;
 }
 
-int g_max_smem_optin = -1;
+// opt-in shared memory per block of the current device, read once per
+// device (devices may differ; calls may come from several host threads)
+constexpr int kMaxDevices = 64;
+std::atomic<int> g_max_smem_optin[kMaxDevices];
 int max_smem_optin() {
-  if (g_max_smem_optin < 0) {
-    int dev = 0, v = 0;
-    cudaGetDevice(&dev);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= kMaxDevices) {
+    int v = 0;
     cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    g_max_smem_optin = v;
+    return v;
   }
-  return g_max_smem_optin;
+  int v = g_max_smem_optin[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    g_max_smem_optin[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
 }
 
 struct EvalCall {
@@ -841,6 +864,7 @@ int run_eval(const EvalCall& C, cudaStream_t st) {
   A.need_grad = S.need_grad;
   A.any_estimate_nu = S.any_est;
   A.fixup = 0;
+  A.nchunk = S.nblk;
   A.redo_mode = 0;
   A.rho_min = C.rho_min > 0.0 ? C.rho_min : 1e-4;
   A.xhl = (float2*)(ws + W.xhl);
@@ -893,7 +917,8 @@ int run_eval(const EvalCall& C, cudaStream_t st) {
   if (C.chunked && S.nblk > 0) {
     int64_t g = (S.nblk + 255) / 256;
     if (g > 4096) g = 4096;
-    k_chunk_max<<<(int)g, 256, 0, st>>>(A.flags, C.chunk, A.level, S.nblk, A.chunk_max);
+    k_chunk_max<<<(int)g, 256, 0, st>>>(A.flags, C.chunk, A.level, S.nblk, A.chunk_max, C.bprob,
+                                         C.info);
     SV_CUDA_TRY(cudaGetLastError());
     LikArgs B = A;
     B.fixup = 1;
@@ -1014,7 +1039,10 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
   pd.nu = D->nu;
   pd.var_penalty = D->var_penalty;
   pd.log_var_target = D->log_var_target;
-  SV_CUDA_TRY(cudaMemcpyAsync(ws + W.desc, &pd, sizeof(pd), cudaMemcpyHostToDevice, st));
+  // written by a one-thread kernel that takes the descriptor by value (no
+  // copy from host memory on the stream)
+  k_put_desc<<<1, 1, 0, st>>>(pd, (sv_prob_desc*)(ws + W.desc));
+  SV_CUDA_TRY(cudaGetLastError());
   EvalCall C;
   C.S = S;
   C.probs = (const sv_prob_desc*)(ws + W.desc);

@@ -51,6 +51,7 @@ struct LikArgs {
   int nprob, ldnbr, CS, kt, dmax, NRmax;  // kt = team block capacity (32 or kmax+1)
   int need_grad, any_estimate_nu;
   int fixup;              // only blocks whose chunk needs a larger jitter level
+  int64_t nchunk;         // length of chunk_max: chunk ids lie in [0, nchunk)
   int redo_mode;          // float64 kernel: only blocks flagged by the split kernel
   double rho_min;
   float2* xhl;            // split form: x / lambda as float32 (hi, lo) pairs
@@ -64,6 +65,13 @@ __device__ __forceinline__ bool pass_has_work(const LikArgs& A) {
   if (A.fixup && A.flags[0] == 0) return false;
   if (A.redo_mode && A.flags[1] == 0) return false;
   return true;
+}
+
+// the jitter level the chunk of block b needs (chunk-wide jitter fix-up);
+// a chunk id outside [0, nchunk) has none (k_chunk_max reports it)
+__device__ __forceinline__ int chunk_level(const LikArgs& A, int64_t b) {
+  const int c = A.chunk[b];
+  return (c >= 0 && c < A.nchunk) ? A.chunk_max[c] : 0;
 }
 
 // block id of the t-th entry handled by a launch

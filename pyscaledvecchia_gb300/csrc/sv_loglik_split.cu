@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split_df(LikArgs 
     bool active = tix < nb;
     const int64_t b = active ? launch_block(A, A.b0 + tix) : 0;
     if (active && A.probs[block_problem(A, b)].skip) active = false;
-    if (active && A.fixup) active = A.chunk_max[A.chunk[b]] > A.level[b];
+    if (active && A.fixup) active = chunk_level(A, b) > A.level[b];
     const int K = active ? A.kb[b] + 1 : 0;
     const int Kw = __reduce_max_sync(full, K);
     if (Kw == 0) continue;
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split_df(LikArgs 
 
     // ---- Sigma (float32 deficit, double-float entries) and LDL^T with the
     //      jitter ladder of _covariance.py:235-252
-    int lv = (active && A.fixup) ? A.chunk_max[A.chunk[b]] : 0;
+    int lv = (active && A.fixup) ? chunk_level(A, b) : 0;
     bool done = !active || !range_ok, failed = active && !range_ok;
     double jit = 0.0;
     int rho_bits = 0;

@@ -31,35 +31,22 @@ constexpr double kPi = 3.141592653589793;
 constexpr double kLn2 = 0.6931471805599453;
 constexpr double kRFloor = 1e-7;  // _matern_general.py:87
 
-// 1/Gamma(1+z) = sum_k kRecipGammaTaylor[k] z^k, |z| <= 1/2
+// Taylor coefficients of 1/Gamma(1+z) about z = 0 (computed to 20 digits
+// with mpmath from A&S 6.1.34): 1/Gamma(1+z) = sum_k c_k z^k, |z| <= 1/2
+#define SV_RECIP_GAMMA_1P_COEFS \
+  1.0, 0.57721566490153286061, -0.65587807152025388108, \
+  -0.042002635034095235529, 0.1665386113822914895, -0.042197734555544336748, \
+  -0.0096219715278769735621, 0.0072189432466630995424, -0.0011651675918590651121, \
+  -0.00021524167411495097282, 0.00012805028238811618615, -0.000020134854780788238656, \
+  -1.2504934821426706573e-6, 1.1330272319816958824e-6, -2.0563384169776071035e-7, \
+  6.1160951044814158179e-9, 5.0020076444692229301e-9, -1.1812745704870201446e-9, \
+  1.0434267116911005105e-10, 7.782263439905071254e-12, -3.6968056186422057082e-12, \
+  5.100370287454475979e-13, -2.0583260535665067832e-14, -5.3481225394230179824e-15, \
+  1.2267786282382607902e-15, -1.1812593016974587695e-16, 1.1866922547516003326e-18
+
+// 1/Gamma(1+z) by Horner's rule in the coefficients above, |z| <= 1/2
 SV_HD double recip_gamma_1p(double z) {
-  const double c[27] = {1.0,
-                        0.57721566490153286061,
-                        -0.65587807152025388108,
-                        -0.042002635034095235529,
-                        0.1665386113822914895,
-                        -0.042197734555544336748,
-                        -0.0096219715278769735621,
-                        0.0072189432466630995424,
-                        -0.0011651675918590651121,
-                        -0.00021524167411495097282,
-                        0.00012805028238811618615,
-                        -0.000020134854780788238656,
-                        -1.2504934821426706573e-6,
-                        1.1330272319816958824e-6,
-                        -2.0563384169776071035e-7,
-                        6.1160951044814158179e-9,
-                        5.0020076444692229301e-9,
-                        -1.1812745704870201446e-9,
-                        1.0434267116911005105e-10,
-                        7.782263439905071254e-12,
-                        -3.6968056186422057082e-12,
-                        5.100370287454475979e-13,
-                        -2.0583260535665067832e-14,
-                        -5.3481225394230179824e-15,
-                        1.2267786282382607902e-15,
-                        -1.1812593016974587695e-16,
-                        1.1866922547516003326e-18};
+  const double c[27] = {SV_RECIP_GAMMA_1P_COEFS};
   double s = c[26];
   for (int k = 25; k >= 0; --k) s = s * z + c[k];
   return s;
@@ -68,33 +55,7 @@ SV_HD double recip_gamma_1p(double z) {
 // Gamma_1(mu) = (1/Gamma(1-mu) - 1/Gamma(1+mu)) / (2 mu)   (odd part, no cancellation)
 // Gamma_2(mu) = (1/Gamma(1-mu) + 1/Gamma(1+mu)) / 2         (even part)
 SV_HD void temme_gammas(double mu, double& g1, double& g2, double& rg_plus, double& rg_minus) {
-  const double c[27] = {1.0,
-                        0.57721566490153286061,
-                        -0.65587807152025388108,
-                        -0.042002635034095235529,
-                        0.1665386113822914895,
-                        -0.042197734555544336748,
-                        -0.0096219715278769735621,
-                        0.0072189432466630995424,
-                        -0.0011651675918590651121,
-                        -0.00021524167411495097282,
-                        0.00012805028238811618615,
-                        -0.000020134854780788238656,
-                        -1.2504934821426706573e-6,
-                        1.1330272319816958824e-6,
-                        -2.0563384169776071035e-7,
-                        6.1160951044814158179e-9,
-                        5.0020076444692229301e-9,
-                        -1.1812745704870201446e-9,
-                        1.0434267116911005105e-10,
-                        7.782263439905071254e-12,
-                        -3.6968056186422057082e-12,
-                        5.100370287454475979e-13,
-                        -2.0583260535665067832e-14,
-                        -5.3481225394230179824e-15,
-                        1.2267786282382607902e-15,
-                        -1.1812593016974587695e-16,
-                        1.1866922547516003326e-18};
+  const double c[27] = {SV_RECIP_GAMMA_1P_COEFS};
   const double m2 = mu * mu;
   // even part: c0 + c2 m^2 + c4 m^4 + ...
   double ev = c[26];

@@ -23,7 +23,8 @@ static int maximin_route(const double* X, int64_t n, int32_t d, int64_t first, i
                          sv_stream_t stream) {
   if (n < 0 || d < 1 || d > 64 || (n > 0 && (!X || !order)) || !info) return SV_EINVAL;
   if (n > 0 && (first < 0 || first >= n)) return SV_EINVAL;
-  if (n > 0x7fffffffLL || flags < 0 || flags > 7) return SV_EINVAL;
+  if (n > 0x7fffffffLL || flags < 0 || flags > 15) return SV_EINVAL;
+  if ((flags & 8) && !(flags & 4)) return SV_EINVAL;  // the barrier test aid is the grid form's
   cudaStream_t st = (cudaStream_t)stream;
   int32_t init_info[4] = {0, -1, 0, 0};
   SV_CUDA_TRY(cudaMemcpyAsync(info, init_info, sizeof(init_info), cudaMemcpyHostToDevice, st));

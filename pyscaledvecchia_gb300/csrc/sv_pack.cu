@@ -74,6 +74,13 @@ extern "C" int sv_pack_blocks(const sv_pack_group* groups, int32_t ngroups, int6
                               int32_t* rowb, int32_t* kb, int32_t* nbr, int32_t* bad,
                               sv_stream_t stream) {
   if (ngroups < 0 || n < 0 || ldnbr < 1 || !bad || (ngroups > 0 && !groups)) return SV_EINVAL;
+  // every group is checked before anything is launched, so a rejected call
+  // leaves the block table untouched
+  for (int g = 0; g < ngroups; ++g) {
+    const sv_pack_group& G = groups[g];
+    if (G.count < 0 || G.k < 0 || G.k > ldnbr || G.out_off < 0) return SV_EINVAL;
+    if (G.count > 0 && (!G.rows || (G.k > 0 && !G.nb) || !rowb || !kb || !nbr)) return SV_EINVAL;
+  }
   cudaStream_t st = (cudaStream_t)stream;
   SV_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int32_t), st));
   const int nsm = sv_num_sms();
@@ -91,9 +98,7 @@ extern "C" int sv_pack_blocks(const sv_pack_group* groups, int32_t ngroups, int6
   };
   for (int g = 0; g < ngroups; ++g) {
     const sv_pack_group& G = groups[g];
-    if (G.count < 0 || G.k < 0 || G.k > ldnbr || G.out_off < 0) return SV_EINVAL;
     if (G.count == 0) continue;
-    if (!G.rows || (G.k > 0 && !G.nb) || !rowb || !kb || !nbr) return SV_EINVAL;
     PB.g[PB.ng++] = G;
     maxtot = std::max<int64_t>(maxtot, G.count * (int64_t)ldnbr);
     if (PB.ng == kPackBatch) {
@@ -107,6 +112,10 @@ extern "C" int sv_pack_blocks(const sv_pack_group* groups, int32_t ngroups, int6
 extern "C" int sv_chunk_ids(const sv_chunk_group* groups, int32_t ngroups, int32_t* ids,
                             sv_stream_t stream) {
   if (ngroups < 0 || (ngroups > 0 && (!groups || !ids))) return SV_EINVAL;
+  for (int g = 0; g < ngroups; ++g) {
+    const sv_chunk_group& G = groups[g];
+    if (G.count < 0 || G.out_off < 0 || G.step < 1 || G.base < 0) return SV_EINVAL;
+  }
   cudaStream_t st = (cudaStream_t)stream;
   const int nsm = sv_num_sms();
   ChunkBatch CB;
@@ -123,7 +132,6 @@ extern "C" int sv_chunk_ids(const sv_chunk_group* groups, int32_t ngroups, int32
   };
   for (int g = 0; g < ngroups; ++g) {
     const sv_chunk_group& G = groups[g];
-    if (G.count < 0 || G.out_off < 0 || G.step < 1 || G.base < 0) return SV_EINVAL;
     if (G.count == 0) continue;
     CB.g[CB.ng++] = G;
     maxc = std::max<int64_t>(maxc, G.count);

@@ -8,8 +8,9 @@
 //                   -a[:k].r / a_K and variance 1 / a_K^2, or the column a of
 //                   the sparse inverse Cholesky factor U.
 //   k_joint_solve : U_pp^T x = rhs (gp.py:380-401, scipy spsolve_triangular),
-//                   one warp per row, rows claimed in order, bounded waits on
-//                   the rows it depends on.
+//                   one CTA per row (its threads split the right-hand sides),
+//                   rows claimed in order, bounded waits on the rows it
+//                   depends on.
 #include "sv_block.cuh"
 
 namespace sv {
@@ -193,49 +194,77 @@ struct JsArgs {
   double* X;
   int* ready;
   unsigned* counter;
+  unsigned* progress;    // rows published so far
   int32_t* info;
+  unsigned spin_limit;   // polls without progress anywhere before a wait gives up
+  int skip_ready_row0;   // test aid: row 0 never publishes, its dependants' waits run out
 };
 
+// One CTA per row at a time, rows claimed in order by an atomic counter (a
+// row depends only on rows claimed before it, so every awaited row is held
+// by a running CTA).  The row's earlier-prediction neighbours and their
+// coefficients go to shared memory, one thread waits per dependency, then
+// the threads split the right-hand sides; each right-hand side is the same
+// sum in the same order as a one-thread solve.  A wait gives up when neither
+// its row nor any other row has been published for spin_limit polls (a
+// stall, not a long dependency chain: a row's time grows with nrhs).
 __global__ void k_joint_solve(JsArgs A) {
-  const int lane = threadIdx.x & 31;
+  extern __shared__ double js_sm[];
+  double* s_a = js_sm;                              // [k] coefficients
+  int* s_p = (int*)(js_sm + (A.k > 0 ? A.k : 1));   // [k] earlier rows
+  __shared__ long long s_c;
+  __shared__ int s_np;
   const int K = A.k + 1;
   while (true) {
-    int64_t c = 0;
-    if (lane == 0) c = (int64_t)atomicAdd(A.counter, 1u);
-    c = __shfl_sync(0xffffffffu, c, 0);
+    if (threadIdx.x == 0) s_c = (long long)atomicAdd(A.counter, 1u);
+    __syncthreads();
+    const int64_t c = s_c;
     if (c >= A.npred) break;
     const double* ac = A.acol + c * (int64_t)K;
-    bool timed_out = false;
-    for (int r0 = 0; r0 < A.nrhs; r0 += 32) {
-      const int r = r0 + lane;
-      double s = (r < A.nrhs) ? A.R[c * (int64_t)A.nrhs + r] : 0.0;
+    if (threadIdx.x == 0) {
+      int np = 0;
       for (int i = 0; i < A.k; ++i) {
         const int64_t ix = A.nbr[c * (int64_t)A.ldnbr + i];
         if (ix < 0 || ix < A.nobs) continue;  // absent slot or observation
-        const int64_t p = ix - A.nobs;  // an earlier prediction row
-        if (r0 == 0) {
-          if (lane == 0) {
-            unsigned it = 0;
-            while (ld_acquire_s32(A.ready + p) == 0) {
-              if (++it > SV_SPIN_LIMIT) {
-                set_error(A.info + SV_INFO_STATUS, SV_ETIMEOUT);
-                atomicCAS(A.info + SV_INFO_BLOCK, -1, (int)c);
-                timed_out = true;
-                break;
-              }
-            }
-          }
-          timed_out = __shfl_sync(0xffffffffu, (int)timed_out, 0) != 0;
-          __syncwarp();
-        }
-        if (r < A.nrhs) s -= ac[i] * __ldcg(A.X + p * (int64_t)A.nrhs + r);
+        s_p[np] = (int)(ix - A.nobs);         // an earlier prediction row
+        s_a[np] = ac[i];
+        ++np;
       }
-      if (r < A.nrhs) A.X[c * (int64_t)A.nrhs + r] = s / ac[K - 1];
+      s_np = np;
     }
-    (void)timed_out;
+    __syncthreads();
+    const int np = s_np;
+    for (int j = threadIdx.x; j < np; j += blockDim.x) {
+      const int p = s_p[j];
+      unsigned it = 0, seen = ld_acquire_u32(A.progress);
+      while (ld_acquire_s32(A.ready + p) == 0) {
+        if (++it > A.spin_limit) {
+          const unsigned now = ld_acquire_u32(A.progress);
+          if (now != seen) {
+            seen = now;
+            it = 0;
+            continue;
+          }
+          set_error(A.info + SV_INFO_STATUS, SV_ETIMEOUT);
+          atomicCAS(A.info + SV_INFO_BLOCK, -1, (int)c);
+          break;
+        }
+      }
+    }
+    __syncthreads();
+    const double aK = ac[K - 1];
+    for (int r = threadIdx.x; r < A.nrhs; r += blockDim.x) {
+      double v = A.R[c * (int64_t)A.nrhs + r];
+#pragma unroll 4
+      for (int j = 0; j < np; ++j) v -= s_a[j] * __ldcg(A.X + (int64_t)s_p[j] * A.nrhs + r);
+      A.X[c * (int64_t)A.nrhs + r] = v / aK;
+    }
     __threadfence();
-    __syncwarp();
-    if (lane == 0) st_release_s32(A.ready + c, 1);
+    __syncthreads();
+    if (threadIdx.x == 0 && !(A.skip_ready_row0 && c == 0)) {
+      st_release_s32(A.ready + c, 1);
+      atomicAdd(A.progress, 1u);
+    }
   }
 }
 
@@ -310,11 +339,11 @@ extern "C" size_t sv_joint_solve_workspace_bytes(int64_t npred) {
   return 256 + ((sizeof(int) * (size_t)(npred > 0 ? npred : 1) + 255) & ~(size_t)255);
 }
 
-extern "C" int sv_joint_solve(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr,
-                              const int32_t* nbr, const double* acol, const double* R, int32_t nrhs,
-                              double* X, int32_t* info, void* workspace, size_t workspace_bytes,
-                              sv_stream_t stream) {
-  if (npred < 0 || nobs < 0 || k < 0 || nrhs < 1 || !info) return SV_EINVAL;
+static int joint_solve(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr, const int32_t* nbr,
+                       const double* acol, const double* R, int32_t nrhs, double* X, int32_t* info,
+                       void* workspace, size_t workspace_bytes, int32_t flags, sv_stream_t stream) {
+  if (npred < 0 || nobs < 0 || k < 0 || k > 4096 || nrhs < 1 || !info || flags < 0 || flags > 1)
+    return SV_EINVAL;
   if (npred > 0 && (!acol || !R || !X || (k > 0 && (!nbr || ldnbr < k)))) return SV_EINVAL;
   if (npred > 0x7fffffffLL) return SV_EINVAL;
   cudaStream_t st = (cudaStream_t)stream;
@@ -323,6 +352,7 @@ extern "C" int sv_joint_solve(int64_t npred, int64_t nobs, int32_t k, int32_t ld
   if (npred == 0) return SV_OK;
   if (!workspace || workspace_bytes < sv_joint_solve_workspace_bytes(npred)) return SV_ENOSPC;
   unsigned* counter = (unsigned*)workspace;
+  unsigned* progress = counter + 1;
   int* ready = (int*)((char*)workspace + 256);
   SV_CUDA_TRY(cudaMemsetAsync(workspace, 0, sv_joint_solve_workspace_bytes(npred), st));
   JsArgs A;
@@ -337,13 +367,37 @@ extern "C" int sv_joint_solve(int64_t npred, int64_t nobs, int32_t k, int32_t ld
   A.X = X;
   A.ready = ready;
   A.counter = counter;
+  A.progress = progress;
   A.info = info;
+  A.skip_ready_row0 = flags & 1;
+  A.spin_limit = (flags & 1) ? SV_SPIN_LIMIT_TEST : SV_SPIN_LIMIT;
   const int nsm = sv_num_sms();
-  int64_t warps = npred;
-  if (warps > 16LL * nsm) warps = 16LL * nsm;
-  const int tpb = 256;
-  const int64_t grid = (warps * 32 + tpb - 1) / tpb;
-  k_joint_solve<<<(unsigned)grid, tpb, 0, st>>>(A);
+  // threads per row: the right-hand sides, rounded to whole warps, at most 256
+  int tpb = ((nrhs + 31) / 32) * 32;
+  if (tpb > 256) tpb = 256;
+  const size_t smem = (size_t)(k > 0 ? k : 1) * (sizeof(double) + sizeof(int)) + 8;
+  int per_sm = 0;
+  SV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_joint_solve, tpb, smem));
+  if (per_sm < 1) return SV_EINVAL;
+  int64_t grid = (int64_t)per_sm * nsm;
+  if (grid > npred) grid = npred;
+  k_joint_solve<<<(unsigned)grid, tpb, smem, st>>>(A);
   SV_CUDA_TRY(cudaGetLastError());
   return SV_OK;
+}
+
+extern "C" int sv_joint_solve(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr,
+                              const int32_t* nbr, const double* acol, const double* R, int32_t nrhs,
+                              double* X, int32_t* info, void* workspace, size_t workspace_bytes,
+                              sv_stream_t stream) {
+  return joint_solve(npred, nobs, k, ldnbr, nbr, acol, R, nrhs, X, info, workspace, workspace_bytes,
+                     0, stream);
+}
+
+extern "C" int sv_joint_solve_flags(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr,
+                                    const int32_t* nbr, const double* acol, const double* R,
+                                    int32_t nrhs, double* X, int32_t* info, void* workspace,
+                                    size_t workspace_bytes, int32_t flags, sv_stream_t stream) {
+  return joint_solve(npred, nobs, k, ldnbr, nbr, acol, R, nrhs, X, info, workspace, workspace_bytes,
+                     flags, stream);
 }

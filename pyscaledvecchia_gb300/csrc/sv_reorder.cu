@@ -440,6 +440,10 @@ struct McRun {
   int64_t* order;
   int32_t* info;       // the problem's 4 status words
   int32_t d, flags;
+  // grid form: the iteration limit of a barrier wait, and a test aid: CTA 0
+  // does not arrive at the first barrier, so every wait there runs out
+  unsigned spin_limit;
+  int32_t skip_first_arrival;
   // grid form: candidate lists of every CTA [2][G][32], their bounds [2][G],
   // and the monotone arrival counter of the grid barrier
   long long* gl_b;
@@ -508,11 +512,11 @@ __device__ __forceinline__ void mc_run(const McRun& Q, int C, int r) {
       __syncthreads();
       if (threadIdx.x == 0) {
         __threadfence();
-        atomicAdd(Q.arrive, 1u);
+        if (!(Q.skip_first_arrival && r == 0 && s_epoch == 0)) atomicAdd(Q.arrive, 1u);
         const unsigned target = (unsigned)C * ++s_epoch;
         unsigned it = 0;
         while (ld_acquire_u32(Q.arrive) < target) {
-          if (++it > (SV_SPIN_LIMIT >> 4)) {
+          if (++it > Q.spin_limit) {
             set_error(Q.info + SV_INFO_STATUS, SV_ETIMEOUT);
             s_abort = 1;
             break;
@@ -1285,6 +1289,8 @@ int maximin_grid_single(const double* X, int64_t n, int d, int64_t first, int64_
   Q.info = info;
   Q.d = d;
   Q.flags = flags & 3;
+  Q.skip_first_arrival = (flags & 8) ? 1 : 0;
+  Q.spin_limit = (flags & 8) ? SV_SPIN_LIMIT_TEST : SV_SPIN_LIMIT;
   size_t off = 0;
   Q.gl_b = (long long*)(ws + off);
   off += ro_align(g2 * 32 * 8);

@@ -34,19 +34,21 @@ __all__ = ["ScaledVecchiaGP"]
 
 @dataclass
 class ScaledVecchiaGP:
-    """Scaled Vecchia GP emulator (Katzfuss, Guinness & Lawrence, 2020).
+    """Gaussian-process emulator with a scaled Vecchia approximation.
 
-    Parameters
-    ----------
-    m_est   : conditioning-set size for likelihood evaluation (paper default 30)
-    m_pred  : conditioning-set size for prediction            (paper default 140)
-    n_est   : subsample size used for parameter estimation    (paper default 5000)
-    nu      : Matern smoothness: 0.5, 1.5, 2.5 (closed forms), any other
-              positive value (Bessel form), or None to estimate it.
-    trend   : 'constant', 'linear' or 'zero'
-    nugget  : None -> estimate the relative nugget; a float -> hold it fixed
-    var_correction : estimate the predictive-variance factor b (Sec. 3.4)
-    lambda_max : ranges above this are treated as infinite
+    The fields are the reference model's settings, with the same names and
+    defaults: how many nearest earlier points condition each point when the
+    likelihood is evaluated (``m_est``) and when predicting (``m_pred``); how
+    many rows the parameters are estimated on (``n_est``, a random subset when
+    the data are larger); the Matern smoothness ``nu`` (a closed form for
+    0.5, 1.5 and 2.5, the Bessel form for any other positive value, estimated
+    when None); the mean model ``trend`` ('zero', 'constant' or 'linear' in
+    the inputs); the relative ``nugget`` (estimated when None, held at the
+    given value otherwise); the ``var_penalty`` pulling log sigma^2 towards
+    the data's variance; ``var_correction`` (fit the predictive-variance
+    factor b on an inner split); ``lambda_max`` (the largest range before an
+    input counts as irrelevant); the Fisher-scoring budget ``max_iter`` and
+    tolerance ``tol``; the seed of every random draw (``random_state``).
     """
 
     m_est: int = 30
@@ -476,16 +478,21 @@ class ScaledVecchiaGP:
             raise RuntimeError("call .fit(X, y) first")
 
     def summary(self):
+        """A text report of the fitted model: its settings, the Vecchia
+        log-likelihood of the standardised responses, the variance, smoothness,
+        nugget and variance factor, and each input's relevance 1/lambda."""
         self._check_fitted()
-        nu_label = "estimated" if self._estimate_nu else "fixed"
-        s = [f"ScaledVecchiaGP(nu={'estimate' if self.nu is None else self.nu}, "
-             f"m_est={self.m_est}, m_pred={self.m_pred}, trend='{self.trend}')",
-             f"  Vecchia loglik (standardised y) : {self.loglik_:.3f}",
-             f"  sigma^2 : {self.variance_:.6g}",
-             f"  nu      : {self.nu_:.4g}  ({nu_label})",
-             f"  nugget  : {self.nugget_:.6g}  (relative)",
-             f"  b       : {self.b_:.4g}  (variance correction)",
-             "  input relevances 1/lambda_l (unit-box scaling):"]
-        for l, rel in enumerate(self.relevance_):
-            s.append(f"      x[{l}] : {rel:10.4f}")
-        return "\n".join(s)
+        how = "estimated" if self._estimate_nu else "fixed"
+        nu_set = "estimate" if self.nu is None else self.nu
+        rows = [
+            f"ScaledVecchiaGP  nu={nu_set}  m_est={self.m_est}  m_pred={self.m_pred}  "
+            f"trend={self.trend!r}",
+            f"  loglik (Vecchia, standardised y)  {self.loglik_:.3f}",
+            f"  variance sigma^2                  {self.variance_:.6g}",
+            f"  smoothness nu ({how:9s})        {self.nu_:.4g}",
+            f"  relative nugget                   {self.nugget_:.6g}",
+            f"  variance factor b                 {self.b_:.4g}",
+            "  relevance 1/lambda per input (inputs scaled to the unit box):",
+        ]
+        rows += [f"    x{j:<3d} {r:12.4f}" for j, r in enumerate(self.relevance_)]
+        return "\n".join(rows)

@@ -25,7 +25,8 @@ __all__ = ["maximin_order", "find_ordered_nn"]
 def maximin_order_device(torch, Xd, first: int, flags: int = 0):
     """Maximin permutation of the rows of a device (n, d) float64 tensor.
     ``flags`` (test aids, same order): 1 ranks every pivot choice by exact
-    roots, 2 takes pivots by tie passes only, 4 forces the grid form."""
+    roots, 2 takes pivots by tie passes only, 4 forces the grid form; 8 (with
+    4) makes the grid barrier's bounded wait run out (SV_ETIMEOUT in info)."""
     lib = _lib.load_library()
     n, d = Xd.shape
     order = torch.empty(n, dtype=torch.int64, device="cuda")

@@ -152,6 +152,12 @@ def test_fit_parity_with_reference(golden_gp, name):
     assert abs(gp.loglik_ - ll_ref) <= ll_tol, (gp.loglik_, ll_ref)
     np.testing.assert_allclose(gp.theta_, g[name + "_theta"], rtol=th_tol, atol=th_tol)
     np.testing.assert_allclose(gp.beta_, g[name + "_beta"], rtol=th_tol, atol=th_tol)
+    # variance correction b of _estimate_b (gp.py:410-425): estimated when
+    # n >= 200 (the "sub" case), else 1; in the clipped cases it inherits the
+    # fit's sensitivity (the oracle's restatement lands 2e-4 away as well)
+    b_ref = float(g[name + "_b"])
+    b_tol = 2e-3 if clipped else 1e-8
+    assert abs(gp.b_ - b_ref) <= b_tol * b_ref, (gp.b_, b_ref)
 
 
 @pytest.mark.parametrize("name", ["sine", "linear", "fixnug", "sub", "nu175"])

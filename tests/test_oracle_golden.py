@@ -142,3 +142,33 @@ def test_oracle_joint_mean_vs_reference(golden_gp, oracle):
             Lt = U_pp.T.tocsr()
             mu = spsolve_triangular(Lt, -(U_op.T @ resid[order_obs]), lower=True)[inv] + Zs @ beta
             _close(ymu + ysd * mu, g[name + "_" + tag + "jmean"], rtol=1e-7, atol=1e-10)
+
+
+ORACLE_FIT_CASES = {
+    "sine": dict(m_est=10, m_pred=20, n_est=150, random_state=0),
+    "linear": dict(m_est=8, m_pred=15, n_est=100, trend="linear", random_state=0),
+    "fixnug": dict(m_est=10, m_pred=20, n_est=120, nugget=1e-8, random_state=0),
+    "sub": dict(m_est=10, m_pred=25, n_est=150, random_state=3),
+}
+
+
+@pytest.mark.parametrize("name", sorted(ORACLE_FIT_CASES))
+def test_oracle_fit_vs_reference(golden_gp, oracle, name):
+    """The oracle's restatement of fit / Fisher scoring / predict / _estimate_b
+    (oracle/fit.py) against the reference's own fits on the same data.  The
+    bands of the cases whose estimated nugget runs onto its 1e-12 clip are the
+    reference's own rounding sensitivity there (see tests/test_gp.py); the
+    fixed-nugget case is well posed."""
+    from oracle.fit import OracleGP
+    g = golden_gp
+    gp = OracleGP(**ORACLE_FIT_CASES[name]).fit(g[name + "_X"], g[name + "_y"])
+    ll_ref = float(g[name + "_loglik"])
+    clipped = g[name + "_theta"][-1] < np.log(1e-11)
+    ll_tol, th_tol, b_tol = (5e-3, 3e-4, 2e-3) if clipped else (1e-8 * abs(ll_ref), 1e-6, 1e-8)
+    assert abs(gp.loglik_ - ll_ref) <= ll_tol, (gp.loglik_, ll_ref)
+    np.testing.assert_allclose(gp.theta_, g[name + "_theta"], rtol=th_tol, atol=th_tol)
+    np.testing.assert_allclose(gp.beta_, g[name + "_beta"], rtol=th_tol, atol=th_tol)
+    assert abs(gp.b_ - float(g[name + "_b"])) <= b_tol * float(g[name + "_b"])
+    mu, sd = gp.predict(g[name + "_Xte"], return_std=True)
+    np.testing.assert_allclose(mu, g[name + "_mu"], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(sd, g[name + "_sd"], rtol=1e-6, atol=1e-6)

@@ -7,8 +7,11 @@ be those of sv_vecchia_loglik on the same inputs.
 
 Two calls in a row on different problems (the second also uses the CTA
 kernel, K = 41) check that the contents the first call leaves in the shared
-array do not leak into the second.  Collected last so that a run stopping at
-the first failure has run every other test.
+array do not leak into the second; the same for the split forms, whose
+scratch also holds the float32 coordinate pairs and which run the jitter
+fix-up and float64 re-evaluation passes, the last call filling most of the
+array.  Collected last so that a run stopping at the first failure has run
+every other test.
 """
 import math
 
@@ -32,21 +35,22 @@ def _problem(seed, n, d, m):
     return prob, theta
 
 
-def _desc(prob, P):
+def _desc(prob, P, precision=0):
     from pyscaledvecchia_gb300 import _lib
     D = _lib.LoglikDesc()
     D.n, D.nblk, D.nblk_warp = prob.n, prob.nblk, prob.nblk_warp
     D.d, D.q, D.ldnbr, D.kmax = prob.d, prob.q, prob.ldnbr, prob.kmax
-    D.need_grad, D.estimate_nu, D.chunked, D.precision = 1, 0, 1, 0
+    D.need_grad, D.estimate_nu, D.chunked, D.precision = 1, 0, 1, precision
+    D.team_lanes = 16
     D.nu, D.var_penalty, D.log_var_target = 2.5, 0.0, 0.0
     return D
 
 
-def _noalloc_call(prob, theta):
+def _noalloc_call(prob, theta, precision=0):
     from pyscaledvecchia_gb300 import _lib
     lib, torch = _lib.device_ready()
     P = prob.d + 2
-    D = _desc(prob, P)
+    D = _desc(prob, P, precision)
     th = _lib.to_dev(torch, theta, np.float64)
     out = torch.empty(1 + P + P * P + prob.q, dtype=torch.float64, device="cuda")
     info = _lib.new_info(torch)
@@ -66,6 +70,32 @@ def test_noalloc_matches_workspace_entry_point_on_two_calls():
         prob, theta = _problem(seed, n, d, m)
         ll0, g0, F0, b0 = prob.evaluate(theta, 2.5)
         ll, g, F, b = _noalloc_call(prob, theta)
+        assert abs(ll - ll0) <= 1e-10 * abs(ll0)
+        np.testing.assert_allclose(g, g0, rtol=1e-8, atol=1e-8 * np.abs(g0).max())
+        np.testing.assert_allclose(F, F0, rtol=1e-8, atol=1e-8 * np.abs(F0).max())
+        np.testing.assert_allclose(b, b0, rtol=1e-8, atol=1e-10)
+
+
+@pytest.mark.parametrize("form,code", [("split", 1), ("split_df", 2)])
+def test_noalloc_split_forms_on_two_calls(form, code):
+    """The split forms (float32 assembly; float64 or double-float
+    factorisation): the first problem has a fixed nugget of 1e-8, so blocks
+    fall below the pivot-ratio test and are re-evaluated in float64; the
+    second (n = 30,000, d = 10, m = 30) fills most of the fixed array."""
+    from pyscaledvecchia_gb300 import _lib
+    lib, _ = _lib.device_ready()
+    cases = ((4, 2500, 3, 20, 1e-8), (5, 30000, 10, 30, 1e-3))
+    for seed, n, d, m, tau in cases:
+        prob, theta = _problem(seed, n, d, m)
+        theta[-1] = math.log(tau)
+        if n == 30000:
+            need = lib.sv_loglik_workspace_bytes(_desc(prob, d + 2, code))
+            assert 0.8 * (32 << 20) < need <= (32 << 20)
+        ll0, g0, F0, b0 = prob.evaluate(theta, 2.5, precision=form, team_lanes=16)
+        aux0 = int(prob.last_info[3])
+        ll, g, F, b = _noalloc_call(prob, theta, code)
+        if n == 2500:
+            assert aux0 > 0  # the float64 re-evaluation pass ran
         assert abs(ll - ll0) <= 1e-10 * abs(ll0)
         np.testing.assert_allclose(g, g0, rtol=1e-8, atol=1e-8 * np.abs(g0).max())
         np.testing.assert_allclose(F, F0, rtol=1e-8, atol=1e-8 * np.abs(F0).max())
