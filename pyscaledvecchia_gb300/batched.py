@@ -25,13 +25,41 @@ from .ordering import _nn_groups
 __all__ = ["BatchProblem", "BatchedLikelihood", "ordered_groups"]
 
 
+class OrderedGroups(list):
+    """The _nn_groups structure (ordering.py:119-127) of an ordered
+    m-neighbour search over n rows, with placeholder (zero) neighbour
+    indices: row i alone in group i for i < m, rows m..n-1 in group m.  The
+    layout a device reorder fills in; BatchedLikelihood packs it without
+    walking the groups."""
+
+    def __init__(self, n, m):
+        n, m = int(n), int(m)
+        zero = np.zeros(1, dtype=np.int64)
+        groups = [(np.array([k], dtype=np.int64), np.broadcast_to(zero, (1, k)))
+                  for k in range(min(n, m))]
+        if n > m:
+            groups.append((np.arange(m, n, dtype=np.int64), np.broadcast_to(zero, (n - m, m))))
+        super().__init__(groups)
+        self.n, self.m = n, m
+
+
 def ordered_groups(n, m):
     """The _nn_groups structure of an ordered m-neighbour search over n rows
-    (row i has min(i, m) neighbours; ordering.py:119-127), with placeholder
-    neighbour indices: the layout a device reorder fills in."""
-    nn = np.zeros((n, m + 1), dtype=np.int64)
-    nn[:, 0] = np.arange(n)
-    return _nn_groups(nn, m)
+    (row i has min(i, m) neighbours), with placeholder neighbour indices."""
+    return OrderedGroups(n, m)
+
+
+def _pack_ordered(n, m):
+    """pack_groups of OrderedGroups(n, m) (m + 1 <= 32: no reordering of
+    large blocks), built directly: block i = row i with min(i, m)
+    neighbours, group i for i < m, group m for the rest.  The neighbour table
+    is None: its placeholders (row 0) are written straight into the batch's
+    table, and a device reorder writes every row's neighbours."""
+    kb = np.minimum(np.arange(n), m).astype(np.int32)
+    rowb = np.arange(n, dtype=np.int32)
+    gk = list(range(min(n, m))) + ([m] if n > m else [])
+    gl = [1] * min(n, m) + ([n - m] if n > m else [])
+    return rowb, kb, None, kb.copy(), gk, gl
 
 
 @dataclass
@@ -104,7 +132,10 @@ class BatchedLikelihood:
             ys.append(y)
             if Z is not None:
                 zs.append(Z.reshape(-1))
-            packs.append(pack_groups(pr.groups, X.shape[0]))
+            if isinstance(pr.groups, OrderedGroups) and pr.groups.n == X.shape[0] and pr.groups.m + 1 <= _WARP_K:
+                packs.append(_pack_ordered(pr.groups.n, pr.groups.m))
+            else:
+                packs.append(pack_groups(pr.groups, X.shape[0]))
         self.dmax = int(self.d.max())
         self.qmax = int(self.q.max())
         self.any_est = bool(self.estimate_nu.any())
@@ -128,7 +159,14 @@ class BatchedLikelihood:
             o, c = int(self.blk_off[i]), rb.shape[0]
             rowb[o:o + c] = rb
             kb[o:o + c] = k
-            nbr[o:o + c, :nb.shape[1]] = nb
+            if nb is not None:
+                nbr[o:o + c, :nb.shape[1]] = nb
+            else:  # ordered layout: row 0 as every neighbour placeholder
+                mm = int(k.max()) if c else 0
+                for r in range(min(c, mm)):
+                    nbr[o + r, :r] = 0
+                if c > mm:
+                    nbr[o + mm:o + c, :mm] = 0
             bprob[o:o + c] = i
             ids = chunk_ids(gid, gk, gl, int(self.P[i]) if self.need_grad else 1)
             chunk[o:o + c] = ids + nchunk
@@ -379,11 +417,16 @@ class BatchedLikelihood:
         """Capture one evaluation of a mode as a CUDA graph (replayed by ``run``)."""
         torch = self.torch
         prec = precision or self.precisions[0]
+        # warm-up launch outside the capture (it sets the kernels' attributes)
+        # with every problem switched off, so it does no evaluation work
+        saved = self._modes[prec]["active"].copy()
+        self.set_active(np.zeros(self.nprob, dtype=bool), prec)
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(s):
-            self.launch(prec)  # warm-up outside the capture (sets kernel attributes)
+            self.launch(prec)
         torch.cuda.current_stream().wait_stream(s)
+        self.set_active(saved, prec)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g, capture_error_mode="thread_local"):
             self.launch(prec)

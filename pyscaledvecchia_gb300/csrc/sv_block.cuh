@@ -15,10 +15,18 @@ namespace sv {
 
 template <int T>
 struct Team {
-  // T == 32: one warp; T > 32: the whole CTA (T == blockDim.x)
-  __device__ __forceinline__ static int lane() { return T == 32 ? (threadIdx.x & 31) : threadIdx.x; }
+  // T == 16: one half of a warp (two blocks per warp, each half with its own
+  // control flow); T == 32: one warp; T > 32: the whole CTA (T == blockDim.x)
+  __device__ __forceinline__ static int lane() {
+    return T == 16 ? (threadIdx.x & 15) : T == 32 ? (threadIdx.x & 31) : threadIdx.x;
+  }
+  __device__ __forceinline__ static unsigned mask() {
+    return T == 16 ? (0xFFFFu << (threadIdx.x & 16)) : 0xffffffffu;
+  }
   __device__ __forceinline__ static void sync() {
-    if (T == 32)
+    if (T == 16)
+      __syncwarp(mask());
+    else if (T == 32)
       __syncwarp();
     else
       __syncthreads();
@@ -128,17 +136,28 @@ __device__ bool cholesky_packed(int K, double* Lp, double* invd, volatile int* f
   return true;
 }
 
-// float64 reciprocal of a positive pivot without a division on the float64
-// pipe: float32 seed and two Newton steps y <- y + y (1 - d y) (quadratic
-// convergence: relative error ~2^-24 -> 2^-48 -> 2^-96, below float64
-// rounding); pivots outside the float32 range take the float64 division.
-__device__ __forceinline__ double rcp_pivot64(double d) {
-  if (d > 1e-30 && d < 1e30) {
-    double y = (double)(1.0f / (float)d);
-    y = fma(y, fma(-d, y, 1.0), y);
-    return fma(y, fma(-d, y, 1.0), y);
+// float64 reciprocal of a pivot inside [1e-30, 1e30]: the float32
+// reciprocal y of the rounded pivot (relative error e = 1 - d y, |e| below
+// ~2^-23) corrected by the third-order step y (1 + e + e^2), whose
+// truncation error y e^3 (~2^-69) lies far below float64 rounding: three
+// float64 FMAs (e exact to float64 rounding by the FMA, e + e^2, y + y t),
+// the result within an ulp of 1/d.  Pivots outside that range take the
+// float64 division.
+__device__ __forceinline__ double pivot_rcp64(double d) {
+  const long long b = dbits(d);
+  if (b > kBitsTiny && b < kBitsHuge) {
+    const double y = f2d_int(__frcp_rn(d2f_int(d)));
+    const double e = fma(-d, y, 1.0);
+    return fma(y, fma(e, e, e), y);
   }
   return 1.0 / d;
+}
+
+// LAPACK dpotrf's pivot criterion (a pivot that is not > 0 fails: negative,
+// zero or NaN) as a test of the bit pattern on the integer pipe
+__device__ __forceinline__ bool pivot_positive(double d) {
+  const long long b = dbits(d);
+  return b > 0 && b < kBitsInf;
 }
 
 // LDL^T of the packed lower triangle in place (unit L below the diagonal,
@@ -151,10 +170,10 @@ __device__ bool ldlt_packed(int K, double* Lp, double* invd, double* acc, volati
   for (int k = 0; k < K; ++k) {
     if (lane == 0) {
       const double dkk = Lp[tri_off(k, k)];
-      if (!(dkk > 0.0))
+      if (!pivot_positive(dkk))
         *flag = 1;
       else
-        invd[k] = rcp_pivot64(dkk);
+        invd[k] = pivot_rcp64(dkk);
     }
     Team<T>::sync();
     if (*flag) return false;
@@ -228,9 +247,32 @@ __device__ void forward_solve_multi(int K, const double* Lp, const double* invd,
   }
 }
 
-// Team-wide sum of a per-lane value (result valid in every lane).
+// Forward solve L W = R with a unit lower L (packed, diagonal ignored) for
+// NR right-hand sides stored column-major with leading dimension ldr, in place.
+template <int T>
+__device__ void forward_solve_unit_multi(int K, const double* Lp, double* R, int NR, int ldr) {
+  const int lane = Team<T>::lane();
+  for (int i = 0; i < K - 1; ++i) {
+    const int m = K - i - 1;
+    const int cnt = m * NR;
+    for (int t = lane; t < cnt; t += T) {
+      const int c = t / m;
+      const int j = i + 1 + (t - c * m);
+      R[c * ldr + j] -= Lp[tri_off(j, i)] * R[c * ldr + i];
+    }
+    Team<T>::sync();
+  }
+}
+
+// Team-wide sum of a per-lane value (result valid in every lane).  A
+// 16-lane team's tree is the 32-lane tree without its first step, which for
+// a block of at most 16 points adds the zeros of lanes 16..31.
 template <int T>
 __device__ double team_sum(double v, double* red) {
+  if (T == 16) {
+    for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(Team<16>::mask(), v, o, 16);
+    return v;
+  }
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   if (T == 32) return v;
   const int w = threadIdx.x >> 5;

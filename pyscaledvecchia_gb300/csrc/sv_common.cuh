@@ -63,6 +63,52 @@ __device__ __forceinline__ void tri_index(int t, int& i, int& j) {
 }
 __device__ __forceinline__ int tri_off(int i, int j) { return i * (i + 1) / 2 + j; }
 
+// Order tests on the bit patterns of positive numbers (integer pipe): for
+// x, y >= 0, x < y <=> bits(x) < bits(y).
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+constexpr long long kBitsTiny = 0x39B4484BFEEBC2A0LL;  // 1e-30
+constexpr long long kBitsHuge = 0x46293E5939A08CEALL;  // 1e30
+constexpr long long kBitsInf = 0x7FF0000000000000LL;
+constexpr int kFBitsInf = 0x7F800000;
+
+// |x| < 1e30 for a float64 x (bit test; NaN fails)
+__device__ __forceinline__ bool in_f32_range(double x) {
+  return (dbits(x) & 0x7FFFFFFFFFFFFFFFLL) < kBitsHuge;
+}
+
+// float32 -> float64 by bit manipulation (integer pipe; a float64 conversion
+// instruction would occupy the slow float64 pipe): exact for zero and normal
+// numbers, subnormals become a signed zero, infinities and NaN stay so.
+__device__ __forceinline__ double f2d_int(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  const unsigned s = b & 0x80000000u;
+  const unsigned e64 = e == 0xffu ? 0x7ffu : e + 896u;
+  const unsigned hi = e == 0u ? s : (s | (e64 << 20) | ((b & 0x7fffffu) >> 3));
+  const unsigned lo = e == 0u ? 0u : (b << 29);
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// float64 -> float32 rounded to nearest (halfway cases away from zero) by
+// bit manipulation (integer pipe): magnitudes below float32's normal range
+// give a signed zero, above it infinity; NaN stays NaN.
+__device__ __forceinline__ float d2f_int(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned s = (unsigned)(b >> 32) & 0x80000000u;
+  const unsigned long long mag = b & 0x7FFFFFFFFFFFFFFFull;
+  const unsigned long long r = mag + 0x10000000ull;  // half a float32 ulp
+  const unsigned e = (unsigned)(r >> 52);
+  const unsigned m = (unsigned)(r >> 29) & 0x7fffffu;
+  unsigned f;
+  if (e <= 896u)
+    f = s;
+  else if (e >= 1151u)
+    f = s | 0x7f800000u | (mag > 0x7FF0000000000000ull ? 0x400000u : 0u);
+  else
+    f = s | ((e - 896u) << 23) | m;
+  return __uint_as_float(f);
+}
+
 // exact maximin / kNN arithmetic (ordering.py:52-57): squared distance in
 // IEEE sequential float64, no FMA contraction
 __device__ __forceinline__ double sqdist_exact(const double* a, const double* b, int d) {

@@ -127,10 +127,12 @@ __host__ __device__ inline int64_t team_smem_doubles(int kt, int d, int NR, int 
 // pairs of round K/2 are met from both ends, each lane adding its own term).
 // Half the float64 work of a pass per (row, coordinate) over all partners;
 // the sums are those of the same terms in another (fixed) order.
-template <int DR>
+template <int DR, int T>
 __device__ __forceinline__ void dsig_pairs_warp(int K, int d, const double* u, const double* Gp,
                                                 const double* a, double* R, int ldr, int lane) {
-  const unsigned full = 0xffffffffu;
+  // T = 32: the whole warp, K <= 32; T = 16: one half of the warp, K <= 16
+  // (shuffles within the half)
+  const unsigned full = Team<T>::mask();
   const bool own = lane < K;
   double ui[DR], S[DR];
 #pragma unroll
@@ -164,7 +166,7 @@ __device__ __forceinline__ void dsig_pairs_warp(int K, int d, const double* u, c
 #pragma unroll
       for (int l = 0; l < DR; ++l)
         if (l < d) {
-          const double rv = __shfl_sync(full, sq[l], src & 31);
+          const double rv = __shfl_sync(full, sq[l], src & (T - 1), T);
           if (own) S[l] = fma(cji, rv, S[l]);
         }
     }
@@ -175,12 +177,13 @@ __device__ __forceinline__ void dsig_pairs_warp(int K, int d, const double* u, c
 }
 
 // One block, processed by a team (float64 throughout).  Writes the block's record.
+// kt is the block capacity of the team's slot (its shared-memory layout).
 template <int T>
-__device__ void block_pass1(const LikArgs& A, int64_t b, double* sm) {
+__device__ void block_pass1(const LikArgs& A, int64_t b, double* sm, int kt) {
   const int lane = Team<T>::lane();
   const int p = block_problem(A, b);
   const ProbInfo& PI = A.probs[p];
-  const int d = PI.d, q = PI.q, P = PI.P, NR = A.need_grad ? (P + 1 + q) : 0, kt = A.kt;
+  const int d = PI.d, q = PI.q, P = PI.P, NR = A.need_grad ? (P + 1 + q) : 0;
   const int dmax = A.dmax;
   const int k = A.kb[b];
   const int K = k + 1;
@@ -231,7 +234,11 @@ __device__ void block_pass1(const LikArgs& A, int64_t b, double* sm) {
     if (lane == 0) *flag = 0;
     assemble_sigma<T>(K, d, u, nullptr, s2, tau, jit, PI.mm, Lp, Gp, Dp);
     Team<T>::sync();
-    ok = cholesky_packed<T>(K, Lp, invd, flag);
+    // LDL^T (one three-FMA reciprocal per pivot on one lane, where a
+    // Cholesky pivot takes a square root and a division); the Cholesky
+    // factor is L D^(1/2), with the same failure criterion (dpotrf: a pivot
+    // that is not > 0)
+    ok = ldlt_packed<T>(K, Lp, invd, acc, flag);
     Team<T>::sync();
     if (ok) break;
   }
@@ -259,8 +266,12 @@ __device__ void block_pass1(const LikArgs& A, int64_t b, double* sm) {
     jit_used = jitter_pow10(lv) * (sc / (double)K);
   }
 
-  // ---- a = L^-T e_K  (likelihood.py:125-127)
-  backsolve_eK<T>(K, Lp, invd, a, acc);
+  // ---- a = C^-T e_K = L^-T e_K / sqrt(d_K)  (likelihood.py:125-127);
+  //      L_KK = sqrt(d_K)
+  backsolve_unit_eK<T>(K, Lp, a, acc);
+  const double lKK = sqrt(Lp[tri_off(K - 1, K - 1)]);
+  const double sK = sqrt(invd[K - 1]);
+  for (int i = lane; i < K; i += T) a[i] *= sK;
   Team<T>::sync();
 
   // ---- GLS parts a.y, a.Z (likelihood.py:129-134)
@@ -269,7 +280,7 @@ __device__ void block_pass1(const LikArgs& A, int64_t b, double* sm) {
     for (int i = lane; i < K; i += T) vy += a[i] * Y[idx[i]];
     vy = team_sum<T>(vy, red);
     if (lane == 0) {
-      rec[0] = Lp[tri_off(K - 1, K - 1)];  // L_KK; the log is taken in the reduction
+      rec[0] = lKK;  // L_KK; the log is taken in the reduction
       rec[1] = vy;
     }
     for (int c = 0; c < q; ++c) {
@@ -291,19 +302,18 @@ __device__ void block_pass1(const LikArgs& A, int64_t b, double* sm) {
   // ---- right-hand sides dSigma_p a (likelihood.py:138), then y and Z
   // R columns: p = 0..P-1 (dSigma rows), P: y, P+1..P+q: Z
   const int ldr = kt;
-  // p = 0: dSigma_0 = Sigma (un-jittered) = L L^T - jit I, so Sigma a = L_KK e_K - jit a
-  for (int i = lane; i < K; i += T)
-    R[i] = ((i == K - 1) ? Lp[tri_off(K - 1, K - 1)] : 0.0) - jit_used * a[i];
+  // p = 0: dSigma_0 = Sigma (un-jittered) = C C^T - jit I, so Sigma a = L_KK e_K - jit a
+  for (int i = lane; i < K; i += T) R[i] = ((i == K - 1) ? lKK : 0.0) - jit_used * a[i];
   // p = 1..d: (dSigma_l a)_i = sum_j G_ij (u_il - u_jl)^2 a_j   (_covariance.py:142-146)
   bool dsig_done = false;
-  if constexpr (T == 32) {
-    if (K <= 32 && d <= 12) {
+  if constexpr (T == 32 || T == 16) {
+    if (K <= T && d <= 12) {
       if (d <= 4)
-        dsig_pairs_warp<4>(K, d, u, Gp, a, R, ldr, lane);
+        dsig_pairs_warp<4, T>(K, d, u, Gp, a, R, ldr, lane);
       else if (d <= 8)
-        dsig_pairs_warp<8>(K, d, u, Gp, a, R, ldr, lane);
+        dsig_pairs_warp<8, T>(K, d, u, Gp, a, R, ldr, lane);
       else
-        dsig_pairs_warp<12>(K, d, u, Gp, a, R, ldr, lane);
+        dsig_pairs_warp<12, T>(K, d, u, Gp, a, R, ldr, lane);
       dsig_done = true;
     }
   }
@@ -336,8 +346,16 @@ __device__ void block_pass1(const LikArgs& A, int64_t b, double* sm) {
   }
   Team<T>::sync();
 
-  // ---- W = L^-1 [dSigma a], z parts = L^-1 [y, Z]  (likelihood.py:139, 154)
-  forward_solve_multi<T>(K, Lp, invd, R, NR, ldr);
+  // ---- W = C^-1 [dSigma a], z parts = C^-1 [y, Z]  (likelihood.py:139, 154):
+  //      unit forward solves, then row i times d_i^(-1/2)
+  forward_solve_unit_multi<T>(K, Lp, R, NR, ldr);
+  for (int i = lane; i < K; i += T) invd[i] = sqrt(invd[i]);
+  Team<T>::sync();
+  for (int t = lane; t < K * NR; t += T) {
+    const int c = t / K, i = t - c * K;
+    R[c * ldr + i] *= invd[i];
+  }
+  Team<T>::sync();
 
   // ---- record: zK parts, wK, W.zy, W.zZ, Fisher (likelihood.py:140-142)
   double* wK = rec + 3 + 2 * q;
@@ -387,22 +405,44 @@ __device__ __forceinline__ bool block_selected(const LikArgs& A, int64_t b, int 
   return A.kb[b] + 1 <= kcap;
 }
 
+// Blocks of up to 32 points, two list entries per warp at a time: when both
+// have at most 16 points each half of the warp takes one (16-lane teams,
+// slots of capacity 16), else the whole warp takes them in turn.  A block's
+// arithmetic is the same either way (every step's per-element order is fixed
+// by the block, not by the team), so the results do not depend on the pairing.
 __global__ void k_block_warp(LikArgs A) {
   extern __shared__ double smem[];
   if (!pass_has_work(A)) return;
   const int64_t per_team = team_smem_doubles(32, A.dmax, A.NRmax, A.need_grad, A.any_estimate_nu);
-  const int w = threadIdx.x >> 5;
+  const int64_t per_half = team_smem_doubles(16, A.dmax, A.NRmax, A.need_grad, A.any_estimate_nu);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* sm = smem + w * per_team;
   const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t t = A.b0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + w; t < A.b1; t += nw) {
-    const int64_t b = launch_block(A, t);
-    if (A.probs[block_problem(A, b)].skip) continue;
+  // whether list entry t is a block for this launch (and its block id)
+  auto take = [&](int64_t t, int64_t& b) -> bool {
+    if (t >= A.b1) return false;
+    b = launch_block(A, t);
+    if (A.probs[block_problem(A, b)].skip) return false;
     if (!block_selected(A, b, 32)) {
-      if (!A.redo_mode && !A.fixup && (threadIdx.x & 31) == 0)
+      if (!A.redo_mode && !A.fixup && lane == 0)
         set_error(A.info + 4 * block_problem(A, b) + SV_INFO_STATUS, SV_EINVAL);
-      continue;
+      return false;
     }
-    block_pass1<32>(A, b, sm);
+    return true;
+  };
+  for (int64_t t = A.b0 + 2 * ((int64_t)blockIdx.x * (blockDim.x >> 5) + w); t < A.b1; t += 2 * nw) {
+    int64_t b0 = 0, b1 = 0;
+    const bool h0 = take(t, b0), h1 = take(t + 1, b1);
+    if (h0 && h1 && A.kb[b0] + 1 <= 16 && A.kb[b1] + 1 <= 16) {
+      const int half = lane >> 4;
+      block_pass1<16>(A, half ? b1 : b0, sm + half * per_half, 16);
+    } else {
+      if (h0) {
+        block_pass1<32>(A, b0, sm, 32);
+        __syncwarp();
+      }
+      if (h1) block_pass1<32>(A, b1, sm, 32);
+    }
     __syncwarp();
   }
 }
@@ -418,7 +458,7 @@ __global__ void k_block_cta(LikArgs A) {
         set_error(A.info + 4 * block_problem(A, b) + SV_INFO_STATUS, SV_EINVAL);
       continue;
     }
-    block_pass1<128>(A, b, smem);
+    block_pass1<128>(A, b, smem, A.kt);
     __syncthreads();
   }
 }
@@ -805,11 +845,21 @@ int launch_warp_kernel(LikArgs A, cudaStream_t st) {
   // needs every resident warp it can get to cover its latency
   int wpc = 16;
   while (wpc > 1 && wpc * team > (size_t)max_smem_optin()) --wpc;
+  // and no more threads than the kernel's registers allow in one CTA
+  cudaFuncAttributes fa;
+  SV_CUDA_TRY(cudaFuncGetAttributes(&fa, k_block_warp));
+  while (wpc > 1 && 32 * wpc > fa.maxThreadsPerBlock) --wpc;
   const size_t smem = wpc * team;
   if (smem > (size_t)max_smem_optin()) return SV_EINVAL;
   SV_CUDA_TRY(cudaFuncSetAttribute(k_block_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int64_t grid = (A.b1 - A.b0 + wpc - 1) / wpc;
-  if (grid > 64LL * nsm) grid = 64LL * nsm;
+  // persistent grid: the CTAs that fit on the SMs at once, each warp taking
+  // pairs of blocks in a grid-stride loop
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_block_warp, 32 * wpc, smem) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  int64_t grid = (A.b1 - A.b0 + 2 * wpc - 1) / (2 * wpc);
+  if (grid > (int64_t)per_sm * nsm) grid = (int64_t)per_sm * nsm;
   if (grid < 1) grid = 1;
   k_block_warp<<<(int)grid, 32 * wpc, smem, st>>>(A);
   SV_CUDA_TRY(cudaGetLastError());

@@ -53,23 +53,6 @@ constexpr int kS64W = 8;    // columns per factorisation panel
 constexpr int kS64WF = 16;  // steps per forward-solve pass
 constexpr int kS64JU = 2;   // later rows per iteration of a forward-solve pass
 
-// float64 reciprocal of a pivot inside [1e-30, 1e30]: the float32
-// reciprocal y of the rounded pivot (relative error e = 1 - d y, |e| below
-// ~2^-23) corrected by the third-order step y (1 + e + e^2), whose
-// truncation error y e^3 (~2^-69) lies far below float64 rounding: three
-// float64 FMAs (e exact to float64 rounding by the FMA, e + e^2, y + y t),
-// the result within an ulp of 1/d.  Pivots outside that range take the
-// float64 division.
-__device__ __forceinline__ double pivot_rcp64(double d) {
-  const long long b = dbits(d);
-  if (b > kBitsTiny && b < kBitsHuge) {
-    const double y = f2d_int(__frcp_rn(d2f_int(d)));
-    const double e = fma(-d, y, 1.0);
-    return fma(y, fma(e, e, e), y);
-  }
-  return 1.0 / d;
-}
-
 // a pivot of the team's factorisation: LAPACK's criterion (a pivot that is
 // not > 0, i.e. negative, zero or NaN, fails: flag[0]), the conditioning
 // test against rho_min (flag[1]; rho_bits = bits of rho_min Sigma_kk) and the
