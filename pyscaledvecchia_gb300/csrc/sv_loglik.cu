@@ -405,45 +405,49 @@ __device__ __forceinline__ bool block_selected(const LikArgs& A, int64_t b, int 
   return A.kb[b] + 1 <= kcap;
 }
 
-// Blocks of up to 32 points, two list entries per warp at a time: when both
-// have at most 16 points each half of the warp takes one (16-lane teams,
-// slots of capacity 16), else the whole warp takes them in turn.  A block's
-// arithmetic is the same either way (every step's per-element order is fixed
-// by the block, not by the team), so the results do not depend on the pairing.
+// Blocks of 17 to 32 points, one per warp (blocks of up to 16 points are
+// k_block_half's).
 __global__ void k_block_warp(LikArgs A) {
   extern __shared__ double smem[];
   if (!pass_has_work(A)) return;
   const int64_t per_team = team_smem_doubles(32, A.dmax, A.NRmax, A.need_grad, A.any_estimate_nu);
-  const int64_t per_half = team_smem_doubles(16, A.dmax, A.NRmax, A.need_grad, A.any_estimate_nu);
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
   double* sm = smem + w * per_team;
   const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-  // whether list entry t is a block for this launch (and its block id)
-  auto take = [&](int64_t t, int64_t& b) -> bool {
-    if (t >= A.b1) return false;
-    b = launch_block(A, t);
-    if (A.probs[block_problem(A, b)].skip) return false;
+  for (int64_t t = A.b0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + w; t < A.b1; t += nw) {
+    const int64_t b = launch_block(A, t);
+    if (A.probs[block_problem(A, b)].skip) continue;
     if (!block_selected(A, b, 32)) {
-      if (!A.redo_mode && !A.fixup && lane == 0)
+      if (!A.redo_mode && !A.fixup && (threadIdx.x & 31) == 0)
         set_error(A.info + 4 * block_problem(A, b) + SV_INFO_STATUS, SV_EINVAL);
-      return false;
+      continue;
     }
-    return true;
-  };
-  for (int64_t t = A.b0 + 2 * ((int64_t)blockIdx.x * (blockDim.x >> 5) + w); t < A.b1; t += 2 * nw) {
-    int64_t b0 = 0, b1 = 0;
-    const bool h0 = take(t, b0), h1 = take(t + 1, b1);
-    if (h0 && h1 && A.kb[b0] + 1 <= 16 && A.kb[b1] + 1 <= 16) {
-      const int half = lane >> 4;
-      block_pass1<16>(A, half ? b1 : b0, sm + half * per_half, 16);
-    } else {
-      if (h0) {
-        block_pass1<32>(A, b0, sm, 32);
-        __syncwarp();
-      }
-      if (h1) block_pass1<32>(A, b1, sm, 32);
-    }
+    if (A.kb[b] + 1 <= 16) continue;
+    block_pass1<32>(A, b, sm, 32);
     __syncwarp();
+  }
+}
+
+// Blocks of up to 16 points, two per warp: each half of the warp takes its
+// own list entry (16-lane teams with slots of capacity 16, their own control
+// flow).  A block's arithmetic does not depend on the team width (every
+// step's per-element order is fixed by the block), so the results are those
+// of a whole warp on the block.
+__global__ void k_block_half(LikArgs A) {
+  extern __shared__ double smem[];
+  if (!pass_has_work(A)) return;
+  const int64_t per_half = team_smem_doubles(16, A.dmax, A.NRmax, A.need_grad, A.any_estimate_nu);
+  const int h = threadIdx.x >> 4;  // half-warp index in the CTA
+  double* sm = smem + h * per_half;
+  const int64_t nh = (int64_t)gridDim.x * (blockDim.x >> 4);
+  for (int64_t t = A.b0 + (int64_t)blockIdx.x * (blockDim.x >> 4) + h; t < A.b1; t += nh) {
+    const int64_t b = launch_block(A, t);
+    if (A.probs[block_problem(A, b)].skip) continue;
+    // larger blocks are k_block_warp's (which reports sizes beyond 32); the
+    // fix-up and re-evaluation passes select by chunk and flag, not by size
+    if (A.kb[b] + 1 > 16 || !block_selected(A, b, 16)) continue;
+    block_pass1<16>(A, b, sm, 16);
+    __syncwarp(Team<16>::mask());
   }
 }
 
@@ -838,32 +842,36 @@ struct EvalCall {
   char* ws;
 };
 
-int launch_warp_kernel(LikArgs A, cudaStream_t st) {
+// launch of a block kernel whose CTAs are teams of `tw` threads: as many
+// teams per CTA as shared memory and the kernel's registers allow (the
+// float64 pipe needs every resident warp it can get to cover its latency),
+// a persistent grid of the CTAs that fit on the SMs at once
+template <typename Kern>
+int launch_team_kernel(Kern kern, LikArgs A, int kt, int tw, int max_teams, cudaStream_t st) {
   const int nsm = sv_num_sms();
-  const size_t team = sizeof(double) * team_smem_doubles(32, A.dmax, A.NRmax, A.need_grad, A.any_estimate_nu);
-  // as many warps (teams) per CTA as shared memory holds: the float64 pipe
-  // needs every resident warp it can get to cover its latency
-  int wpc = 16;
-  while (wpc > 1 && wpc * team > (size_t)max_smem_optin()) --wpc;
-  // and no more threads than the kernel's registers allow in one CTA
+  const size_t team = sizeof(double) * team_smem_doubles(kt, A.dmax, A.NRmax, A.need_grad, A.any_estimate_nu);
   cudaFuncAttributes fa;
-  SV_CUDA_TRY(cudaFuncGetAttributes(&fa, k_block_warp));
-  while (wpc > 1 && 32 * wpc > fa.maxThreadsPerBlock) --wpc;
-  const size_t smem = wpc * team;
+  SV_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
+  int tpc = max_teams;
+  while (tpc > 1 && (tpc * team > (size_t)max_smem_optin() || tpc * tw > fa.maxThreadsPerBlock)) --tpc;
+  const size_t smem = tpc * team;
   if (smem > (size_t)max_smem_optin()) return SV_EINVAL;
-  SV_CUDA_TRY(cudaFuncSetAttribute(k_block_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  // persistent grid: the CTAs that fit on the SMs at once, each warp taking
-  // pairs of blocks in a grid-stride loop
+  SV_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_block_warp, 32 * wpc, smem) != cudaSuccess ||
-      per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, tw * tpc, smem) != cudaSuccess || per_sm < 1)
     per_sm = 1;
-  int64_t grid = (A.b1 - A.b0 + 2 * wpc - 1) / (2 * wpc);
+  int64_t grid = (A.b1 - A.b0 + tpc - 1) / tpc;
   if (grid > (int64_t)per_sm * nsm) grid = (int64_t)per_sm * nsm;
   if (grid < 1) grid = 1;
-  k_block_warp<<<(int)grid, 32 * wpc, smem, st>>>(A);
+  kern<<<(int)grid, tw * tpc, smem, st>>>(A);
   SV_CUDA_TRY(cudaGetLastError());
   return SV_OK;
+}
+
+int launch_warp_kernel(LikArgs A, cudaStream_t st) {
+  int rc = launch_team_kernel(k_block_half, A, 16, 16, 32, st);
+  if (rc != SV_OK) return rc;
+  return launch_team_kernel(k_block_warp, A, 32, 32, 16, st);
 }
 
 int launch_cta_kernel(LikArgs A, cudaStream_t st) {
