@@ -48,8 +48,9 @@ sys.path.insert(0, ROOT)
 METRIC = "Vecchia fits/s, chosen vs plain form on GB300 at |dloglik|<1e-6; blocks/s"
 # DRAM bytes (read + write) per block of one k_block_split64<16> launch at the
 # default size (n = 200,000): an ncu capture of that launch (one pass,
-# dram__bytes_read.sum + dram__bytes_write.sum) divided by its 200,000 blocks
-SPLIT64_TRAFFIC_PER_BLOCK = None
+# dram__bytes_read.sum 45.10 MB + dram__bytes_write.sum 132.88 MB) divided by
+# its 200,000 blocks
+SPLIT64_TRAFFIC_PER_BLOCK = 889.9
 # the exact maximin order of the default workload, computed once by the
 # oracle (tests/golden/make_c2_order.py)
 C2_ORDER = os.path.join(ROOT, "tests", "golden", "c2_order.npz")
