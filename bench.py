@@ -777,6 +777,35 @@ def main():
             forms[f"nu{nu_o}"] = {"split_ms": ms_s, "split_blocks_per_s": n / (ms_s * 1e-3),
                                   "float64_ms": ms_f, "float64_blocks_per_s": n / (ms_f * 1e-3),
                                   "split_errors_vs_float64_form": errors_vs(r_f, r_s)}
+        # linear trend (gp.py:99-100: Z = [1, x], q = d + 1 = 11 columns of
+        # the GLS profiling gathered per block, likelihood.py:129-134)
+        Zl = np.concatenate([np.ones((n, 1)), Xo], axis=1)
+        prob_l = DeviceProblem(Xo, yo, Zl, groups)
+        tl = {}
+        for prec in ("split", "float64"):
+            for _ in range(2):
+                prob_l.launch(th_d, P, nu, False, True, 0.0, 0.0, True, precision=prec,
+                              team_lanes=best_lanes if prec == "split" else 0)
+            torch.cuda.synchronize()
+            ev = []
+            for _ in range(max(2, args.steps // 2)):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                prob_l.launch(th_d, P, nu, False, True, 0.0, 0.0, True, precision=prec,
+                              team_lanes=best_lanes if prec == "split" else 0)
+                e1.record(stream)
+                ev.append((e0, e1))
+            torch.cuda.synchronize()
+            tl[prec] = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+        rl_s = prob_l.evaluate(theta, nu, precision="split", team_lanes=best_lanes)
+        rl_f = prob_l.evaluate(theta, nu)
+        forms["trend_linear"] = {"q": int(Zl.shape[1]), "split_ms": tl["split"],
+                                 "split_blocks_per_s": n / (tl["split"] * 1e-3),
+                                 "float64_ms": tl["float64"],
+                                 "float64_blocks_per_s": n / (tl["float64"] * 1e-3),
+                                 "split_errors_vs_float64_form": errors_vs(rl_f, rl_s)}
+        del prob_l
         # fixed nu = 0.8: the Bessel path (float64 kernels; the split forms
         # take closed-form nu only)
         ms08 = float(np.mean(time_form("float64", 0, max(2, args.steps // 2), 1, 0.8)))

@@ -205,6 +205,39 @@ int sv_vecchia_loglik(const sv_loglik_desc* desc, const double* theta, const dou
                       const int32_t* nbr, const int32_t* chunk, double* out, int32_t* info,
                       void* workspace, size_t workspace_bytes, sv_stream_t stream);
 
+/* Sharded form of sv_vecchia_loglik: one problem's blocks split across
+ * several GPUs (one process each; no counterpart in the reference, which
+ * evaluates on one host; the arithmetic is likelihood.py:66-175 unchanged).
+ * The evaluation's reduction partitions (the `parts` of
+ * sv_loglik_shard_sizes: contiguous runs of blocks, fixed by nblk) are
+ * divided among the ranks: a rank owns partitions [part_begin, part_end)
+ * and every rank holds the whole of X, y, Z and the block table.  Four
+ * stages with three exchanges between them, each an element-wise
+ * all-reduce over the ranks:
+ *   stage 1: blocks of the rank's partitions; their chunks' jitter levels
+ *            into chunk_max (int32[nblk], zeroed first)  -> all-reduce MAX
+ *   stage 2: chunk-wide jitter fix-up of the rank's blocks from the exchanged
+ *            chunk_max, split-form re-evaluation, pass-1 partial sums of its
+ *            partitions into rows [part_begin, part_end) of part1
+ *            (double[parts][part1_len]; the other rows must be 0)  -> SUM
+ *   stage 3: XtX, Zty, Fisher and beta from all of part1; pass-2 partial sums
+ *            of its partitions into part2 (double[parts][part2_len], other
+ *            rows 0)                                            -> SUM
+ *   stage 4: ll, score, Fisher and beta from all of part2 into out.
+ * Each partition's partial sums are computed by the same kernels as in one
+ * GPU's evaluation and the sums of the SUM exchanges add exact zeros, so
+ * the result is bit for bit that of sv_vecchia_loglik.  The workspace must
+ * persist from stage 1 to stage 4 of an evaluation; info is per rank
+ * (combine the status words, e.g. by MAX). */
+int sv_loglik_shard_sizes(const sv_loglik_desc* desc, int32_t* parts, int32_t* part1_len,
+                          int32_t* part2_len);
+int sv_vecchia_loglik_stage(const sv_loglik_desc* desc, int32_t stage, int32_t part_begin,
+                            int32_t part_end, const double* theta, const double* X, const double* y,
+                            const double* Z, const int32_t* rowb, const int32_t* kb,
+                            const int32_t* nbr, const int32_t* chunk, int32_t* chunk_max,
+                            double* part1, double* part2, double* out, int32_t* info,
+                            void* workspace, size_t workspace_bytes, sv_stream_t stream);
+
 /* Batched form: many independent problems evaluated by one set of launches
  * (batched fits of hundreds of problems; the reference fits problems one at
  * a time, so the per-problem arithmetic is likelihood.py:66-175 unchanged).  Problem p

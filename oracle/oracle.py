@@ -66,6 +66,9 @@ def lib():
         L.or_vecchia_loglik.restype = i32
         L.or_predict_blocks.argtypes = [vp, vp, vp, i64, i32, i32, vp, vp, dbl, dbl, dbl, vp, vp]
         L.or_predict_blocks.restype = i32
+        L.or_block_records.argtypes = [vp, vp, vp, vp, i64, i32, i32, vp, vp, vp, i32, i64, i64, vp,
+                                       dbl, i32, vp, vp]
+        L.or_block_records.restype = i32
         L.or_num_threads.restype = i32
         L.or_set_num_threads.argtypes = [i32]
         _lib = L

@@ -19,6 +19,7 @@
  *                       _covariance.py:111-147 (Sigma, dSigma/dlog theta),
  *                       _batch_chol :235-252 (per-block jitter), the solves
  *                       _forward_solve/_backsolve_LT :205-232
+ *   or_block_records    the per-block first pass of or_vecchia_loglik
  *   or_predict_blocks   gp.py:242-277 (_predict_scaled: marginal mean/var)
  *
  * Closed-form Matern smoothness only (nu in {0.5, 1.5, 2.5}); the Bessel path
@@ -508,6 +509,38 @@ int or_vecchia_loglik(const double* theta, const double* X, const double* y, con
   free(cache);
   free(level);
   return 0;
+}
+
+/*
+ * Per-block records of blocks [b0, b1) (the first pass of or_vecchia_loglik,
+ * likelihood.py:111-144): [log L_KK, a.y, a.Z(q), (L^-1 y)_K, (L^-1 Z)_K(q),
+ * w_K(P), W (L^-1 y)(P), W (L^-1 Z)(P q), F(P P)] per block, the jitter search
+ * starting at force_level[b - b0] (NULL: 0; the chunk-wide redo of
+ * _covariance.py:235-252 passes the chunk's level), the level used in
+ * level_out.  Returns the record length, or -1 when a block fails even with
+ * jitter.
+ */
+int or_block_records(const double* theta, const double* X, const double* y, const double* Z,
+                     int64_t n, int d, int q, const int64_t* rowb, const int32_t* kb,
+                     const int64_t* nbr, int ldnbr, int64_t b0, int64_t b1,
+                     const int32_t* force_level, double nu, int need_grad, double* records,
+                     int32_t* level_out) {
+  int P = d + 2;
+  double ranges[256];
+  if (d > 256) return -2;
+  for (int l = 0; l < d; l++) ranges[l] = exp(theta[1 + l]);
+  lik_args A = {X, y, Z, n, d, q, rowb, kb, nbr, ldnbr, exp(theta[0]), exp(theta[1 + d]), nu,
+                ranges, need_grad};
+  int cs = block_stride(q, P, need_grad);
+  int failed = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(| : failed)
+  for (int64_t b = b0; b < b1; b++) {
+    int lv = 0;
+    if (eval_block(&A, b, force_level ? force_level[b - b0] : 0, records + (b - b0) * cs, &lv) != 0)
+      failed |= 1;
+    level_out[b - b0] = lv;
+  }
+  return failed ? -1 : cs;
 }
 
 /*

@@ -101,6 +101,9 @@ SIGNATURES = {
     "sv_chunk_ids": (c_i32, [c_vp, c_i32, c_vp, c_vp]),
     "sv_vecchia_loglik": (c_i32, [ctypes.POINTER(LoglikDesc), c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
                                   c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+    "sv_loglik_shard_sizes": (c_i32, [ctypes.POINTER(LoglikDesc), c_vp, c_vp, c_vp]),
+    "sv_vecchia_loglik_stage": (c_i32, [ctypes.POINTER(LoglikDesc), c_i32, c_i32, c_i32] + [c_vp] * 14
+                                + [c_sz, c_vp]),
     "sv_loglik_batched_workspace_bytes": (c_sz, [ctypes.POINTER(BatchDesc)]),
     "sv_vecchia_loglik_batched": (c_i32, [ctypes.POINTER(BatchDesc)] + [c_vp] * 15 + [c_sz, c_vp]),
     "sv_vecchia_loglik_noalloc": (c_i32, [ctypes.POINTER(LoglikDesc), c_vp, c_vp, c_vp, c_vp, c_vp,

@@ -25,6 +25,7 @@
 // batched evaluation can be captured in a CUDA graph.
 #include <stdio.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "sv_loglik.cuh"
@@ -472,10 +473,10 @@ __global__ void k_block_cta(LikArgs A) {
 // problem's status set to SV_EINVAL (chunk ids are read only when some block
 // needed jitter)
 __global__ void k_chunk_max(const int32_t* flags, const int32_t* chunk, const int8_t* level,
-                            int64_t nblk, int32_t* chunk_max, const int32_t* bprob,
-                            int32_t* info) {
+                            int64_t nblk, int64_t bb0, int64_t bb1, int32_t* chunk_max,
+                            const int32_t* bprob, int32_t* info) {
   if (flags[0] == 0) return;
-  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nblk;
+  for (int64_t b = bb0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < bb1;
        b += (int64_t)gridDim.x * blockDim.x) {
     const int c = chunk[b];
     if (c < 0 || c >= nblk) {
@@ -487,6 +488,15 @@ __global__ void k_chunk_max(const int32_t* flags, const int32_t* chunk, const in
   }
 }
 
+// flags[0] = 1 when any chunk of the (exchanged) chunk table needs jitter:
+// the fix-up pass of a shard must run when another shard's block raised the
+// level of a chunk this shard shares
+__global__ void k_any_jitter(const int32_t* chunk_max, int64_t nchunk, int32_t* flags) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nchunk;
+       c += (int64_t)gridDim.x * blockDim.x)
+    if (chunk_max[c] > 0) flags[0] = 1;
+}
+
 // ---------------------------------------------------------------------------
 // reductions (grid row = problem, R.parts partitions of its blocks)
 // ---------------------------------------------------------------------------
@@ -495,6 +505,7 @@ struct RedArgs {
   const ProbInfo* probs;
   int CS, need_grad, nfmax, qmax, Pmax;
   int parts;      // partitions of every problem's blocks
+  int pbeg;       // the partitions this launch reduces: pbeg + blockIdx.x (< parts)
   double* part1;  // [nprob][parts][nfmax]
   double* part2;  // [nprob][parts][Pmax + 1]
   double* beta;   // [nprob][qmax + 1]
@@ -531,9 +542,10 @@ __global__ void k_reduce1(RedArgs R) {
   const int nf = nfield1(q, P, R.need_grad);
   const int nwarp = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int parts = red_parts_n(PI.nblk);
-  if ((int)blockIdx.x >= parts) return;
+  const int part = R.pbeg + (int)blockIdx.x;
+  if (part >= parts) return;
   const int64_t per = (PI.nblk + parts - 1) / parts;
-  const int64_t b0 = PI.blk_off + blockIdx.x * per;
+  const int64_t b0 = PI.blk_off + part * per;
   const int64_t b1 = min(PI.blk_off + PI.nblk, b0 + per);
   double* acc = racc + (int64_t)w * R.nfmax;
   const int foff = 3 + 2 * q + P * (2 + q);
@@ -593,11 +605,11 @@ __global__ void k_reduce1(RedArgs R) {
   for (int r = 0; r < kFr; ++r)
     if (lane + 32 * r < nf) acc[lane + 32 * r] = a[r];
   __syncthreads();
-  double* part = R.part1 + ((int64_t)p * R.parts + blockIdx.x) * R.nfmax;
+  double* partv = R.part1 + ((int64_t)p * R.parts + part) * R.nfmax;
   for (int f = threadIdx.x; f < nf; f += blockDim.x) {
     double s = 0.0;
     for (int k = 0; k < nwarp; ++k) s += racc[(int64_t)k * R.nfmax + f];
-    part[f] = s;
+    partv[f] = s;
   }
 }
 
@@ -658,9 +670,10 @@ __global__ void k_reduce2(RedArgs R) {
   for (int i = threadIdx.x; i < q; i += blockDim.x) sbeta[i] = R.beta[(int64_t)p * (R.qmax + 1) + i];
   __syncthreads();
   const int parts = red_parts_n(PI.nblk);
-  if ((int)blockIdx.x >= parts) return;
+  const int part = R.pbeg + (int)blockIdx.x;
+  if (part >= parts) return;
   const int64_t per = (PI.nblk + parts - 1) / parts;
-  const int64_t b0 = PI.blk_off + blockIdx.x * per;
+  const int64_t b0 = PI.blk_off + part * per;
   const int64_t b1 = min(PI.blk_off + PI.nblk, b0 + per);
   double acc[kMaxP + 1];
   for (int i = 0; i <= np; ++i) acc[i] = 0.0;
@@ -691,7 +704,7 @@ __global__ void k_reduce2(RedArgs R) {
   for (int i = threadIdx.x; i <= np; i += blockDim.x) {
     double s = 0.0;
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k][i];
-    R.part2[((int64_t)p * R.parts + blockIdx.x) * (R.Pmax + 1) + i] = s;
+    R.part2[((int64_t)p * R.parts + part) * (R.Pmax + 1) + i] = s;
   }
 }
 
@@ -887,12 +900,25 @@ int launch_cta_kernel(LikArgs A, cudaStream_t st) {
   return SV_OK;
 }
 
-// Enqueues one evaluation.  Only kernels and memsets: capturable in a graph.
-int run_eval(const EvalCall& C, cudaStream_t st) {
+// One stage of a sharded one-problem evaluation (sv_vecchia_loglik_stage):
+// the shard is reduction partitions [pb, pe); the exchanged tables live in
+// caller buffers.
+struct ShardStage {
+  int stage;           // 1 .. 4
+  int pb, pe;          // the shard's partitions
+  int32_t* chunk_max;  // [nblk] chunk levels (stage 1 writes the shard's, stage 2 reads all)
+  double* part1;       // [parts][nfield1]
+  double* part2;       // [parts][P + 1]
+};
+
+// Enqueues one evaluation (sh == nullptr), or one stage of a sharded one.
+// Only kernels and memsets: capturable in a graph.
+int run_eval(const EvalCall& C, cudaStream_t st, const ShardStage* sh = nullptr) {
   const EvalShape& S = C.S;
   WsLayout W = ws_layout(S);
   char* ws = C.ws;
   ProbInfo* probs = (ProbInfo*)(ws + W.probs);
+  const int stage = sh ? sh->stage : 0;  // 0: the whole evaluation
 
   LikArgs A;
   A.X = C.X;
@@ -908,7 +934,7 @@ int run_eval(const EvalCall& C, cudaStream_t st) {
   A.cache = (double*)(ws + W.cache);
   A.level = (int8_t*)(ws + W.level);
   A.redo = (int8_t*)(ws + W.redo);
-  A.chunk_max = (int32_t*)(ws + W.chunk_max);
+  A.chunk_max = sh ? sh->chunk_max : (int32_t*)(ws + W.chunk_max);
   A.flags = (int32_t*)(ws + W.flags);
   A.info = C.info;
   A.b0 = 0;
@@ -928,13 +954,14 @@ int run_eval(const EvalCall& C, cudaStream_t st) {
   A.xhl = (float2*)(ws + W.xhl);
   A.kcap = S.kmax + 1 < 32 ? (S.kmax + 1 > 0 ? S.kmax + 1 : 1) : 32;
 
-  k_info_init<<<(int)((S.nprob + 255) / 256), 256, 0, st>>>(C.info, (int)S.nprob);
-  SV_CUDA_TRY(cudaGetLastError());
-  SV_CUDA_TRY(cudaMemsetAsync(A.flags, 0, 4 * sizeof(int32_t), st));
-  if (C.chunked)
-    SV_CUDA_TRY(cudaMemsetAsync(A.chunk_max, 0, sizeof(int32_t) * (S.nblk > 0 ? S.nblk : 1), st));
-  k_prob_params<<<(int)S.nprob, 64, 0, st>>>(C.probs, C.theta, C.tstride, (int)S.nprob, probs);
-  SV_CUDA_TRY(cudaGetLastError());
+  // the blocks of this call: all, or those of the shard's partitions
+  const int parts = red_parts(S);
+  int64_t blo = 0, bhi = S.nblk;
+  if (sh) {
+    const int64_t per = (S.nblk + parts - 1) / parts;
+    blo = std::min<int64_t>((int64_t)sh->pb * per, S.nblk);
+    bhi = std::min<int64_t>((int64_t)sh->pe * per, S.nblk);
+  }
 
   // split forms (1: float64 factorisation, 2: double-float factorisation):
   // closed-form nu for every problem and at most 32 right-hand sides
@@ -945,12 +972,14 @@ int run_eval(const EvalCall& C, cudaStream_t st) {
   const int lanes = C.team_lanes > 0 ? C.team_lanes : 16;
   if (split && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32) return SV_EINVAL;
 
+  // list ranges: the warp-kernel blocks are [0, nwarp) (or wlist), the CTA
+  // blocks the rest; a shard (one problem, no lists) takes its part of each
   auto warp_pass = [&](LikArgs B) -> int {
     B.kt = 32;
     B.list = C.wlist;
-    B.b0 = 0;
-    B.b1 = C.nwarp;
-    if (C.nwarp <= 0) return SV_OK;
+    B.b0 = sh ? std::min<int64_t>(blo, C.nwarp) : 0;
+    B.b1 = sh ? std::min<int64_t>(bhi, C.nwarp) : C.nwarp;
+    if (B.b1 <= B.b0) return SV_OK;
     if (split && !B.redo_mode)
       return S.precision == 1 ? launch_block_split(B, lanes, st) : launch_block_split_df(B, lanes, st);
     return launch_warp_kernel(B, st);
@@ -960,34 +989,57 @@ int run_eval(const EvalCall& C, cudaStream_t st) {
     B.list = C.clist;
     B.b0 = C.clist ? 0 : C.nwarp;
     B.b1 = C.clist ? C.ncta : C.nwarp + C.ncta;
-    if (C.ncta <= 0) return SV_OK;
+    if (sh) {
+      B.b0 = std::max<int64_t>(blo, C.nwarp);
+      B.b1 = std::min<int64_t>(bhi, C.nwarp + C.ncta);
+    }
+    if (B.b1 <= B.b0) return SV_OK;
     return launch_cta_kernel(B, st);
   };
 
   int rc;
-  if (split && C.nwarp > 0) {
-    rc = launch_split_prep(A, S.nx, st);
-    if (rc != SV_OK) return rc;
-  }
-  if ((rc = warp_pass(A)) != SV_OK) return rc;
-  if ((rc = cta_pass(A)) != SV_OK) return rc;
-  // reference chunk-wide jitter: redo blocks whose chunk needed a larger level
-  if (C.chunked && S.nblk > 0) {
-    int64_t g = (S.nblk + 255) / 256;
-    if (g > 4096) g = 4096;
-    k_chunk_max<<<(int)g, 256, 0, st>>>(A.flags, C.chunk, A.level, S.nblk, A.chunk_max, C.bprob,
-                                         C.info);
+  if (stage == 0 || stage == 1) {
+    k_info_init<<<(int)((S.nprob + 255) / 256), 256, 0, st>>>(C.info, (int)S.nprob);
     SV_CUDA_TRY(cudaGetLastError());
-    LikArgs B = A;
-    B.fixup = 1;
-    if ((rc = warp_pass(B)) != SV_OK) return rc;
-    if ((rc = cta_pass(B)) != SV_OK) return rc;
+    SV_CUDA_TRY(cudaMemsetAsync(A.flags, 0, 4 * sizeof(int32_t), st));
+    if (C.chunked)
+      SV_CUDA_TRY(cudaMemsetAsync(A.chunk_max, 0, sizeof(int32_t) * (S.nblk > 0 ? S.nblk : 1), st));
+    k_prob_params<<<(int)S.nprob, 64, 0, st>>>(C.probs, C.theta, C.tstride, (int)S.nprob, probs);
+    SV_CUDA_TRY(cudaGetLastError());
+    if (split && C.nwarp > 0) {
+      rc = launch_split_prep(A, S.nx, st);
+      if (rc != SV_OK) return rc;
+    }
+    if ((rc = warp_pass(A)) != SV_OK) return rc;
+    if ((rc = cta_pass(A)) != SV_OK) return rc;
+    // the largest jitter level of every chunk (of this call's blocks)
+    if (C.chunked && bhi > blo) {
+      int64_t g = (bhi - blo + 255) / 256;
+      if (g > 4096) g = 4096;
+      k_chunk_max<<<(int)g, 256, 0, st>>>(A.flags, C.chunk, A.level, S.nblk, blo, bhi, A.chunk_max,
+                                           C.bprob, C.info);
+      SV_CUDA_TRY(cudaGetLastError());
+    }
   }
-  // split form: float64 re-evaluation of the blocks it flagged as ill-conditioned
-  if (split && C.nwarp > 0) {
-    LikArgs B = A;
-    B.redo_mode = 1;
-    if ((rc = warp_pass(B)) != SV_OK) return rc;
+  if (stage == 0 || stage == 2) {
+    // reference chunk-wide jitter: redo blocks whose chunk needed a larger level
+    if (C.chunked && bhi > blo) {
+      if (sh) {
+        const int64_t g = std::min<int64_t>((S.nblk + 255) / 256, 4096);
+        k_any_jitter<<<(int)(g > 0 ? g : 1), 256, 0, st>>>(A.chunk_max, S.nblk, A.flags);
+        SV_CUDA_TRY(cudaGetLastError());
+      }
+      LikArgs B = A;
+      B.fixup = 1;
+      if ((rc = warp_pass(B)) != SV_OK) return rc;
+      if ((rc = cta_pass(B)) != SV_OK) return rc;
+    }
+    // split form: float64 re-evaluation of the blocks it flagged as ill-conditioned
+    if (split && C.nwarp > 0) {
+      LikArgs B = A;
+      B.redo_mode = 1;
+      if ((rc = warp_pass(B)) != SV_OK) return rc;
+    }
   }
 
   RedArgs R;
@@ -998,29 +1050,41 @@ int run_eval(const EvalCall& C, cudaStream_t st) {
   R.nfmax = W.nfmax;
   R.qmax = S.qmax;
   R.Pmax = S.Pmax;
-  R.part1 = (double*)(ws + W.part1);
-  R.part2 = (double*)(ws + W.part2);
+  R.part1 = sh ? sh->part1 : (double*)(ws + W.part1);
+  R.part2 = sh ? sh->part2 : (double*)(ws + W.part2);
   R.beta = (double*)(ws + W.beta);
   R.sums = (double*)(ws + W.sums);
   R.theta = C.theta;
   R.tstride = C.tstride;
   R.out = C.out;
   R.ostride = C.ostride;
-  R.parts = red_parts(S);
-  const dim3 rgrid((unsigned)R.parts, (unsigned)S.nprob);
-  int rwarps = kRedThreads / 32;
-  while (rwarps > 1 && sizeof(double) * (size_t)rwarps * W.nfmax > (size_t)max_smem_optin()) --rwarps;
-  const size_t rsmem = sizeof(double) * (size_t)rwarps * W.nfmax;
-  if (rsmem > (size_t)max_smem_optin()) return SV_EINVAL;
-  SV_CUDA_TRY(cudaFuncSetAttribute(k_reduce1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
-  k_reduce1<<<rgrid, 32 * rwarps, rsmem, st>>>(R);
-  SV_CUDA_TRY(cudaGetLastError());
-  k_final1<<<(unsigned)S.nprob, kRedThreads, 0, st>>>(R);
-  SV_CUDA_TRY(cudaGetLastError());
-  k_reduce2<<<rgrid, kRedThreads, 0, st>>>(R);
-  SV_CUDA_TRY(cudaGetLastError());
-  k_final2<<<(unsigned)S.nprob, 64, 0, st>>>(R);
-  SV_CUDA_TRY(cudaGetLastError());
+  R.parts = parts;
+  R.pbeg = sh ? sh->pb : 0;
+  const int npart = sh ? sh->pe - sh->pb : parts;
+  const dim3 rgrid((unsigned)(npart > 0 ? npart : 1), (unsigned)S.nprob);
+  if (stage == 0 || stage == 2) {
+    int rwarps = kRedThreads / 32;
+    while (rwarps > 1 && sizeof(double) * (size_t)rwarps * W.nfmax > (size_t)max_smem_optin()) --rwarps;
+    const size_t rsmem = sizeof(double) * (size_t)rwarps * W.nfmax;
+    if (rsmem > (size_t)max_smem_optin()) return SV_EINVAL;
+    if (npart > 0) {
+      SV_CUDA_TRY(cudaFuncSetAttribute(k_reduce1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
+      k_reduce1<<<rgrid, 32 * rwarps, rsmem, st>>>(R);
+      SV_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  if (stage == 0 || stage == 3) {
+    k_final1<<<(unsigned)S.nprob, kRedThreads, 0, st>>>(R);
+    SV_CUDA_TRY(cudaGetLastError());
+    if (npart > 0) {
+      k_reduce2<<<rgrid, kRedThreads, 0, st>>>(R);
+      SV_CUDA_TRY(cudaGetLastError());
+    }
+  }
+  if (stage == 0 || stage == 4) {
+    k_final2<<<(unsigned)S.nprob, 64, 0, st>>>(R);
+    SV_CUDA_TRY(cudaGetLastError());
+  }
   return SV_OK;
 }
 
@@ -1063,11 +1127,14 @@ extern "C" size_t sv_loglik_workspace_bytes(const sv_loglik_desc* D) {
   return ws_layout(single_shape(D)).total;
 }
 
-extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, const double* X,
-                                 const double* y, const double* Z, const int32_t* rowb,
-                                 const int32_t* kb, const int32_t* nbr, const int32_t* chunk,
-                                 double* out, int32_t* info, void* workspace,
-                                 size_t workspace_bytes, sv_stream_t stream) {
+namespace {
+
+// Checks of a one-problem call and its EvalCall (the problem table is written
+// into the workspace by a one-thread kernel that takes it by value).
+int single_call(const sv_loglik_desc* D, const double* theta, const double* X, const double* y,
+                const double* Z, const int32_t* rowb, const int32_t* kb, const int32_t* nbr,
+                const int32_t* chunk, double* out, int32_t* info, void* workspace,
+                size_t workspace_bytes, cudaStream_t st, EvalCall& C) {
   if (!D || !theta || !X || !y || !rowb || !kb || !out || !info) return SV_EINVAL;
   if (D->d < 1 || D->d > kMaxD || D->q < 0 || D->q > kMaxQ || D->nblk < 0 || D->n < 0)
     return SV_EINVAL;
@@ -1080,9 +1147,7 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
   const EvalShape S = single_shape(D);
   WsLayout W = ws_layout(S);
   if (!workspace || workspace_bytes < W.total) return SV_ENOSPC;
-  cudaStream_t st = (cudaStream_t)stream;
   char* ws = (char*)workspace;
-  // the problem table of a one-problem batch lives in the workspace
   sv_prob_desc pd;
   pd.n = D->n;
   pd.x_off = 0;
@@ -1101,7 +1166,6 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
   // copy from host memory on the stream)
   k_put_desc<<<1, 1, 0, st>>>(pd, (sv_prob_desc*)(ws + W.desc));
   SV_CUDA_TRY(cudaGetLastError());
-  EvalCall C;
   C.S = S;
   C.probs = (const sv_prob_desc*)(ws + W.desc);
   C.theta = theta;
@@ -1126,7 +1190,61 @@ extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, c
   C.ostride = 1 + S.Pmax + S.Pmax * S.Pmax + S.qmax;
   C.info = info;
   C.ws = ws;
+  return SV_OK;
+}
+
+}  // namespace
+
+extern "C" int sv_vecchia_loglik(const sv_loglik_desc* D, const double* theta, const double* X,
+                                 const double* y, const double* Z, const int32_t* rowb,
+                                 const int32_t* kb, const int32_t* nbr, const int32_t* chunk,
+                                 double* out, int32_t* info, void* workspace,
+                                 size_t workspace_bytes, sv_stream_t stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  EvalCall C;
+  const int rc = single_call(D, theta, X, y, Z, rowb, kb, nbr, chunk, out, info, workspace,
+                             workspace_bytes, st, C);
+  if (rc != SV_OK) return rc;
   return run_eval(C, st);
+}
+
+extern "C" int sv_loglik_shard_sizes(const sv_loglik_desc* D, int32_t* parts, int32_t* part1_len,
+                                     int32_t* part2_len) {
+  if (!D || !parts || !part1_len || !part2_len || D->nblk < 0 || D->d < 1 || D->d > kMaxD ||
+      D->q < 0 || D->q > kMaxQ)
+    return SV_EINVAL;
+  const EvalShape S = single_shape(D);
+  *parts = red_parts(S);
+  *part1_len = nfield1(S.qmax, S.Pmax, S.need_grad);
+  *part2_len = S.Pmax + 1;
+  return SV_OK;
+}
+
+extern "C" int sv_vecchia_loglik_stage(const sv_loglik_desc* D, int32_t stage, int32_t part_begin,
+                                       int32_t part_end, const double* theta, const double* X,
+                                       const double* y, const double* Z, const int32_t* rowb,
+                                       const int32_t* kb, const int32_t* nbr, const int32_t* chunk,
+                                       int32_t* chunk_max, double* part1, double* part2,
+                                       double* out, int32_t* info, void* workspace,
+                                       size_t workspace_bytes, sv_stream_t stream) {
+  if (!D || stage < 1 || stage > 4) return SV_EINVAL;
+  int32_t parts = 0, l1 = 0, l2 = 0;
+  if (sv_loglik_shard_sizes(D, &parts, &l1, &l2) != SV_OK) return SV_EINVAL;
+  if (part_begin < 0 || part_end < part_begin || part_end > parts) return SV_EINVAL;
+  if (!part1 || !part2 || (D->chunked && !chunk_max)) return SV_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  EvalCall C;
+  const int rc = single_call(D, theta, X, y, Z, rowb, kb, nbr, chunk, out, info, workspace,
+                             workspace_bytes, st, C);
+  if (rc != SV_OK) return rc;
+  ShardStage sh;
+  sh.stage = stage;
+  sh.pb = part_begin;
+  sh.pe = part_end;
+  sh.chunk_max = chunk_max;
+  sh.part1 = part1;
+  sh.part2 = part2;
+  return run_eval(C, st, &sh);
 }
 
 extern "C" size_t sv_loglik_batched_workspace_bytes(const sv_batch_desc* B) {
