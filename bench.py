@@ -557,14 +557,12 @@ def run_fits(torch, lib, nprob, dump=""):
 # ---------------------------------------------------------------------------
 # C4: prediction and joint sampling
 # ---------------------------------------------------------------------------
-def run_predict(torch, lib):
-    """Prediction and joint sampling: n_train = 100,000 points in [0,1]^6,
-    y a Matern-2.5 Vecchia draw with lambda = (0.1, 0.2, 0.4, 0.8, 5, 100),
-    sigma^2 = 1, tau = 1e-6 (seed 3); the default fit (m_est 30, n_est 5000,
-    variance correction b on the reference's inner split); then 50,000 test
-    points in [-0.1, 1.1]^6: marginal mean/sd with m_pred = 140 (141-point
-    blocks) and 100 joint sample paths."""
-    from pyscaledvecchia_gb300 import ScaledVecchiaGP, _lib as L
+def c4_inputs(torch):
+    """The prediction workload's data: n_train = 100,000 points in [0,1]^6,
+    y a Matern-2.5 Vecchia draw (m = 30) with lambda = (0.1, 0.2, 0.4, 0.8,
+    5, 100), sigma^2 = 1, tau = 1e-6, and 50,000 test points in
+    [-0.1, 1.1]^6 (seed 3).  Returns (X, y, Xte)."""
+    from pyscaledvecchia_gb300 import _lib as L
     from pyscaledvecchia_gb300.ordering import maximin_order_device, ordered_nn_device
     from pyscaledvecchia_gb300.sampling import vecchia_prior_sample_device
     rng = np.random.default_rng(3)
@@ -584,6 +582,19 @@ def run_predict(torch, lib):
                                      L.to_dev(torch, eps.reshape(ntr, 1), np.float64))
     y = np.empty(ntr)
     y[o] = yo.reshape(-1).cpu().numpy()
+    return X, y, Xte
+
+
+def run_predict(torch, lib, check_oracle=True):
+    """Prediction and joint sampling on c4_inputs: the default fit (m_est 30,
+    n_est 5000, variance correction b on the reference's inner split); then
+    the 50,000 test points: marginal mean/sd with m_pred = 140 (141-point
+    blocks) in float64 and in the split form (float32 assembly, float64
+    LDL^T and solves), their differences and their errors against the
+    oracle on a sample of 2,000 points, and 100 joint sample paths."""
+    from pyscaledvecchia_gb300 import ScaledVecchiaGP
+    X, y, Xte = c4_inputs(torch)
+    nte = Xte.shape[0]
 
     def timed(fn):
         torch.cuda.synchronize()
@@ -594,17 +605,104 @@ def run_predict(torch, lib):
 
     gp = ScaledVecchiaGP(m_est=30, m_pred=140, nu=2.5)
     _, t_fit = timed(lambda: gp.fit(X, y))
-    gp.predict(Xte[:2000], return_std=True)  # warm-up
-    (mu, sd), t_pred = timed(lambda: gp.predict(Xte, return_std=True))
-    samples, t_joint = timed(lambda: gp.sample_joint(Xte, n_sim=100, random_state=0))
+    res = {"workload": "n_train 100000 x 6, n_test 50000, m_pred 140, 100 joint paths, nu 2.5",
+           "fit_s": t_fit, "b": float(gp.b_), "fitted_ranges": [float(v) for v in gp.ranges_],
+           "nugget": float(gp.nugget_)}
     K = 141
-    flops = nte * (K ** 3 / 3 + K ** 2)
-    return {"workload": "n_train 100000 x 6, n_test 50000, m_pred 140, 100 joint paths, nu 2.5",
-            "fit_s": t_fit, "predict_s": t_pred, "predict_points_per_s": nte / t_pred,
-            "predict_fp64_tflops": flops / t_pred / 1e12,
-            "sample_joint_s": t_joint, "b": float(gp.b_),
-            "fitted_ranges": [float(v) for v in gp.ranges_], "nugget": float(gp.nugget_),
-            "sd_finite": bool(np.all(np.isfinite(sd))), "samples_shape": list(samples.shape)}
+    flops = K ** 3 / 3 + K ** 2  # LDL^T and the solve of one block (float64)
+    pred = {}
+    for prec in ("float64", "split"):
+        gp.precision = prec
+        gp.predict(Xte[:2000], return_std=True)  # warm-up
+        (mu, sd), t = timed(lambda: gp.predict(Xte, return_std=True))
+        ms = predict_kernel_ms(torch, lib, gp, Xte)
+        pred[prec] = (mu, sd)
+        res[prec] = {"predict_s": t, "predict_points_per_s": nte / t, "kernel_ms": ms,
+                     "kernel_fp64_tflops": nte * flops / (ms * 1e-3) / 1e12,
+                     "blocks_redone_in_float64": gp.pred_stats_["redone_float64"],
+                     "sd_finite": bool(np.all(np.isfinite(sd)))}
+    mu64, sd64 = pred["float64"]
+    mu32, sd32 = pred["split"]
+    res["split_vs_float64"] = pred_errors(mu32, sd32, mu64, sd64)
+    if check_oracle:
+        # the oracle (C restatement of gp.py:242-277, OpenMP on the host's
+        # cores) on every 25th test point: the checker of both forms
+        from oracle import oracle
+        oracle.build()
+        oracle.set_threads(os.cpu_count() or 1)
+        sub = np.arange(0, nte, 25)
+        Xs_te = (Xte[sub] - gp._lo) / gp._span
+        Ztr = gp._design(gp.X_)
+        resid = gp.y_ - (Ztr @ gp.beta_ if gp.beta_.size else 0.0)
+        t0 = time.perf_counter()
+        mo, vo, _ = oracle.predict_marginal(gp.X_, resid, Xs_te, gp._pred_theta(), 2.5, 140)
+        t_or = time.perf_counter() - t0
+        mo = gp._ymu + gp._ysd * (mo + (gp._design(Xs_te) @ gp.beta_ if gp.beta_.size else 0.0))
+        so = gp._ysd * np.sqrt(gp.b_ * vo)
+        res["oracle_sample"] = f"every 25th test point ({sub.size}), {os.cpu_count()} threads"
+        res["oracle_points_per_s"] = sub.size / t_or
+        for prec in ("float64", "split"):
+            res[prec + "_vs_oracle"] = pred_errors(pred[prec][0][sub], pred[prec][1][sub], mo, so)
+    gp.precision = "float64"
+    samples, t_joint = timed(lambda: gp.sample_joint(Xte, n_sim=100, random_state=0))
+    res["sample_joint_s"] = t_joint
+    res["samples_shape"] = list(samples.shape)
+    return res
+
+
+def pred_errors(mu, sd, mu_ref, sd_ref):
+    """Prediction differences in units of the reference sd: |mean - mean_ref|
+    / sd_ref and |sd - sd_ref| / sd_ref (median, 99th percentile, max)."""
+    em = np.abs(mu - mu_ref) / sd_ref
+    es = np.abs(sd - sd_ref) / sd_ref
+
+    def q(e):
+        return [float(np.median(e)), float(np.quantile(e, 0.99)), float(e.max())]
+    return {"mean_err_over_sd": q(em), "sd_rel_err": q(es), "points": int(mu.shape[0])}
+
+
+def predict_kernel_ms(torch, lib, gp, Xte, reps=5):
+    """Device time of the prediction-block launch alone (sv_predict_blocks,
+    the model's precision) on the whole test set: neighbours searched once,
+    CUDA events around each launch on the launching stream, median of reps."""
+    from pyscaledvecchia_gb300 import _lib as L
+    from pyscaledvecchia_gb300.ordering import knn_query_device
+    Xs_te = (Xte - gp._lo) / gp._span
+    Ztr = gp._design(gp.X_)
+    resid = gp.y_ - (Ztr @ gp.beta_ if gp.beta_.size else 0.0)
+    ntr, d = gp.X_.shape
+    nte = Xs_te.shape[0]
+    m = min(gp.m_pred, ntr)
+    nb, _ = knn_query_device(torch, L.to_dev(torch, gp.X_ / gp.ranges_, np.float64),
+                             L.to_dev(torch, Xs_te / gp.ranges_, np.float64), m)
+    Xall = torch.cat([L.to_dev(torch, gp.X_, np.float64), L.to_dev(torch, Xs_te, np.float64)])
+    tgt = torch.arange(ntr, ntr + nte, dtype=torch.int32, device="cuda")
+    nbr = nb.to(torch.int32).contiguous()
+    rd = L.to_dev(torch, resid, np.float64)
+    th = L.to_dev(torch, gp._pred_theta(), np.float64)
+    D = L.PredDesc()
+    D.nall, D.nobs, D.nblk = ntr + nte, ntr, nte
+    D.d, D.k, D.ldnbr = d, m, m
+    D.general, D.nu = int(gp._general()), float(gp.nu_)
+    D.precision = int(gp.precision == "split")
+    mean = torch.empty(nte, dtype=torch.float64, device="cuda")
+    var = torch.empty_like(mean)
+    info = L.new_info(torch)
+    st = torch.cuda.current_stream()
+    ts = []
+    for _ in range(reps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        rc = lib.sv_predict_blocks(D, L.ptr(th), L.ptr(Xall), L.ptr(tgt), L.ptr(nbr), L.ptr(rd),
+                                   L.ptr(mean), L.ptr(var), None, None, L.ptr(info),
+                                   L.stream_handle(torch))
+        e1.record(st)
+        torch.cuda.synchronize()
+        L.check(lib, rc, "sv_predict_blocks")
+        ts.append(e0.elapsed_time(e1))
+    L.check_info(lib, info.cpu().numpy(), "sv_predict_blocks")
+    return float(np.median(ts[1:]))
 
 
 # ---------------------------------------------------------------------------
@@ -869,7 +967,7 @@ def main():
     if args.fits_problems > 0:
         line["fits"] = run_fits(torch, lib, args.fits_problems, args.fits_dump)
     if not args.no_predict:
-        line["predict"] = run_predict(torch, lib)
+        line["predict"] = run_predict(torch, lib, check_oracle=not args.no_cpu_baseline)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

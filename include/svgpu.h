@@ -42,6 +42,10 @@ typedef struct CUstream_st* sv_stream_t; /* identical to cudaStream_t */
 #define SV_INFO_JITTER 2     /* largest jitter level used (0 = none, 1..9 = 1e-12..1e-4) */
 #define SV_INFO_AUX 3        /* split form: blocks re-evaluated in float64 */
 
+/* version of this interface: sv_abi_version() returns it; bumped whenever a
+ * signature or a structure layout changes */
+#define SV_ABI_VERSION 2
+
 const char* sv_status_string(int status);
 int sv_abi_version(void);
 /* last cudaError_t recorded by a call that returned SV_ECUDA */
@@ -398,7 +402,18 @@ typedef struct sv_pred_desc {
   int32_t general;  /* 1: Bessel Matern                                */
   int32_t target_nugget; /* 1: the target row carries the nugget too     */
                          /*    (prior / unconditional draws)              */
+  int32_t precision;     /* 0: float64; 1: split (closed-form nu only,   */
+                         /*    float64 otherwise): entries below the      */
+                         /*    diagonal from coordinates centred on the   */
+                         /*    target as float32 (hi, lo) pairs and the   */
+                         /*    float32 correlation deficit, one float64   */
+                         /*    FMA each; diagonal, LDL^T and solves in    */
+                         /*    float64                                    */
   double nu;
+  double split_rho_min;  /* split: a block whose smallest pivot ratio     */
+                         /*    d_k / Sigma_kk falls below this (<= 0:     */
+                         /*    1e-4), or that does not factor, is redone  */
+                         /*    in float64; info[SV_INFO_AUX] counts them  */
 } sv_pred_desc;
 
 /* One prediction block per target row tgt[b] (noise-free unless

@@ -77,8 +77,12 @@ class ReorderDesc(ctypes.Structure):
 class PredDesc(ctypes.Structure):
     """Mirror of sv_pred_desc (include/svgpu.h)."""
     _fields_ = [("nall", c_i64), ("nobs", c_i64), ("nblk", c_i64), ("d", c_i32), ("k", c_i32),
-                ("ldnbr", c_i32), ("general", c_i32), ("target_nugget", c_i32), ("nu", c_dbl)]
+                ("ldnbr", c_i32), ("general", c_i32), ("target_nugget", c_i32),
+                ("precision", c_i32), ("nu", c_dbl), ("split_rho_min", c_dbl)]
 
+
+# SV_ABI_VERSION of include/svgpu.h that the structures above mirror
+ABI_VERSION = 2
 
 # name -> (restype, argtypes); every symbol declared in include/svgpu.h
 SIGNATURES = {
@@ -160,6 +164,9 @@ def load_library(check_current: bool = True):
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
+        if lib.sv_abi_version() != ABI_VERSION:
+            raise RuntimeError(f"{path} implements interface version {lib.sv_abi_version()}, "
+                               f"these bindings version {ABI_VERSION}: rebuild it")
         _lib = lib
         return lib
 

@@ -37,7 +37,7 @@ extern "C" const char* sv_status_string(int s) {
   }
 }
 
-extern "C" int sv_abi_version(void) { return 1; }
+extern "C" int sv_abi_version(void) { return SV_ABI_VERSION; }
 
 extern "C" int sv_last_cuda_error(void) { return g_last_cuda_error; }
 

@@ -163,15 +163,21 @@ __device__ __forceinline__ bool pivot_positive(double d) {
 // LDL^T of the packed lower triangle in place (unit L below the diagonal,
 // D = diag(d_k) on it): one reciprocal per step instead of a square root and
 // a division.  Fails as the Cholesky does (LAPACK dpotrf: a pivot that is not
-// > 0, d_k = L_kk^2).  acc is K doubles of scratch.
+// > 0, d_k = L_kk^2).  acc is K doubles of scratch.  With rb (the bit
+// patterns of per-row thresholds), a pivot below its row's threshold stops
+// the factorisation too (*flag = 2: too ill-conditioned for the entries'
+// precision).
 template <int T>
-__device__ bool ldlt_packed(int K, double* Lp, double* invd, double* acc, volatile int* flag) {
+__device__ bool ldlt_packed(int K, double* Lp, double* invd, double* acc, volatile int* flag,
+                            const long long* rb = nullptr) {
   const int lane = Team<T>::lane();
   for (int k = 0; k < K; ++k) {
     if (lane == 0) {
       const double dkk = Lp[tri_off(k, k)];
       if (!pivot_positive(dkk))
         *flag = 1;
+      else if (rb && dbits(dkk) < rb[k])
+        *flag = 2;
       else
         invd[k] = pivot_rcp64(dkk);
     }
@@ -191,6 +197,75 @@ __device__ bool ldlt_packed(int K, double* Lp, double* invd, double* acc, volati
       tri_index(t, ii, jj);
       const int i = k + 1 + ii, j = k + 1 + jj;
       Lp[tri_off(i, j)] -= Lp[tri_off(i, k)] * acc[j];  // a_ij -= l_ik d_k l_jk
+    }
+    Team<T>::sync();
+  }
+  return true;
+}
+
+// The same LDL^T by panels of W columns: the panel's columns are factored
+// one by one (pivot, scaling, updates of the panel's later columns), then
+// every element right of the panel takes the panel's W updates in one visit,
+// a_ij - l_is (d_s l_js) for s = kk, kk+1, ... in order, so every element
+// sees the same operations in the same order as in ldlt_packed (the results
+// are bitwise equal).  One load and one store of a_ij per panel instead of
+// per column, and three barriers per column only over the panel's W columns.
+// accs: W columns of ldacc doubles holding the panel's unscaled columns
+// d_s l_js (accs column 0 doubles as ldlt_packed's acc).
+template <int T, int W>
+__device__ bool ldlt_blocked(int K, double* Lp, double* invd, double* accs, int ldacc,
+                             volatile int* flag, const long long* rb = nullptr) {
+  const int lane = Team<T>::lane();
+  for (int kk = 0; kk < K; kk += W) {
+    const int ke = kk + W < K ? kk + W : K;
+    for (int c = kk; c < ke; ++c) {
+      if (lane == 0) {
+        const double dcc = Lp[tri_off(c, c)];
+        if (!pivot_positive(dcc))
+          *flag = 1;
+        else if (rb && dbits(dcc) < rb[c])
+          *flag = 2;
+        else
+          invd[c] = pivot_rcp64(dcc);
+      }
+      Team<T>::sync();
+      if (*flag) return false;
+      const double inv = invd[c];
+      double* ac = accs + (c - kk) * ldacc;
+      for (int i = c + 1 + lane; i < K; i += T) {
+        const double v = Lp[tri_off(i, c)];
+        ac[i] = v;
+        Lp[tri_off(i, c)] = v * inv;
+      }
+      Team<T>::sync();
+      // the panel's later columns j in (c, ke), rows i >= j
+      const int np = ke - c - 1;
+      if (np > 0) {
+        const int cnt = (K - c - 1) * np;
+        for (int t = lane; t < cnt; t += T) {
+          const int i = c + 1 + t / np, j = c + 1 + t % np;
+          if (j <= i) Lp[tri_off(i, j)] -= Lp[tri_off(i, c)] * ac[j];
+        }
+        Team<T>::sync();
+      }
+    }
+    // everything right of the panel: rows and columns >= ke
+    const int m = K - ke;
+    const int cnt = m * (m + 1) / 2;
+    const int w = ke - kk;
+    for (int t = lane; t < cnt; t += T) {
+      int ii, jj;
+      tri_index(t, ii, jj);
+      const int i = ke + ii, j = ke + jj;
+      const double* li = Lp + tri_off(i, kk);
+      double v = Lp[tri_off(i, j)];
+      if (w == W) {
+#pragma unroll
+        for (int p = 0; p < W; ++p) v -= li[p] * accs[p * ldacc + j];
+      } else {
+        for (int p = 0; p < w; ++p) v -= li[p] * accs[p * ldacc + j];
+      }
+      Lp[tri_off(i, j)] = v;
     }
     Team<T>::sync();
   }

@@ -7,6 +7,13 @@
 //                   Cholesky with jitter retry, a = L^-T e_K; marginal mean
 //                   -a[:k].r / a_K and variance 1 / a_K^2, or the column a of
 //                   the sparse inverse Cholesky factor U.
+//                   Split form (closed-form nu): the entries below the
+//                   diagonal from coordinates centred on the target, held as
+//                   float32 (hi, lo) pairs, and the float32 correlation
+//                   deficit, one float64 FMA each; the diagonal,
+//                   the LDL^T and every solve in float64.  A block with a
+//                   pivot ratio d_k / Sigma_kk below rho_min, or that does not
+//                   factor, is redone in float64 from the start.
 //   k_joint_solve : U_pp^T x = rhs (gp.py:380-401, scipy spsolve_triangular),
 //                   one CTA per row (its threads split the right-hand sides),
 //                   rows claimed in order, bounded waits on the rows it
@@ -30,6 +37,8 @@ struct PredArgs {
   int d, k, ldnbr, kt;
   int closed;
   int target_nugget;
+  int split;       // 1: float32 assembly (closed-form nu only)
+  double rho_min;  // split: smallest pivot ratio d_k / Sigma_kk kept
   double nu;
 };
 
@@ -56,8 +65,76 @@ __device__ void pred_params(const PredArgs& A, PredPrm* prm) {
   __syncthreads();
 }
 
+// columns per panel of the blocked LDL^T
+constexpr int kPredW = 8;
+
 __host__ __device__ inline int64_t pred_team_doubles(int kt, int d) {
-  return (int64_t)kt * d + (int64_t)kt * (kt + 1) / 2 + 5 * (int64_t)kt + (kt + 1) / 2 + 1 + 40;
+  return (int64_t)kt * d + (int64_t)kt * (kt + 1) / 2 + (4 + kPredW) * (int64_t)kt + (kt + 1) / 2 +
+         1 + 40;
+}
+
+// |x| below 2^60: d <= 64 squared float32 differences of such coordinates
+// stay finite
+constexpr long long kBitsCoordMax = 0x43B0000000000000LL;
+
+// The split form's attempt at a block: coordinates centred on the target
+// (scaled differences formed in float64, kept as float32 (hi, lo) pairs), the entries
+// below the diagonal s2 (1 - D(r_ij)) with D the float32 correlation deficit
+// (accurate for close pairs), the diagonal s2 (1 + tau mask_i) in float64,
+// then the LDL^T with the pivot-ratio guard (thresholds rho_min Sigma_kk in
+// rb).  Returns false when the block must be redone in float64: a coordinate
+// out of range, a pivot that is not > 0 or below its threshold.
+template <int T>
+__device__ bool pred_split_factor(const PredArgs& A, const PredPrm* prm, int K, double* u,
+                                  double* Lp, double* invd, double* acc, const double* mask,
+                                  long long* rb, const int* idx, volatile int* flag) {
+  const int lane = Team<T>::lane();
+  const int d = A.d;
+  float2* u2 = (float2*)u;
+  const double* xt = A.Xall + (int64_t)idx[K - 1] * d;
+  if (lane == 0) flag[1] = 0;
+  Team<T>::sync();
+  bool in_range = true;
+  for (int t = lane; t < K * d; t += T) {
+    const int i = t / d, l = t - (t / d) * d;
+    const double v = (A.Xall[(int64_t)idx[i] * d + l] - xt[l]) * prm->invlam[l];
+    in_range = in_range && (dbits(v) & 0x7FFFFFFFFFFFFFFFLL) < kBitsCoordMax;
+    const float hi = d2f_int(v);
+    u2[t] = make_float2(hi, d2f_int(v - f2d_int(hi)));
+  }
+  if (!in_range) flag[1] = 1;
+  const double s2 = prm->s2, tau = prm->tau;
+  for (int i = lane; i < K; i += T) rb[i] = dbits(A.rho_min * (s2 * (1.0 + tau * mask[i])));
+  Team<T>::sync();
+  if (flag[1]) return false;
+  const int code = A.closed;
+  const int npair = K * (K + 1) / 2;
+  for (int t = lane; t < npair; t += T) {
+    int i, j;
+    tri_index(t, i, j);
+    double v;
+    if (i == j) {
+      v = s2 * (1.0 + tau * mask[i]);
+    } else {
+      const float2* ui = u2 + i * d;
+      const float2* uj = u2 + j * d;
+      float r2 = 0.0f;
+      for (int l = 0; l < d; ++l) {
+        // (hi_i - hi_j) + (lo_i - lo_j): the difference to about one float32
+        // rounding of itself, however far the pair lies from the target
+        const float2 a = ui[l], c = uj[l];
+        const float df = (a.x - c.x) + (a.y - c.y);
+        r2 = fmaf(df, df, r2);
+      }
+      v = fma(-s2, f2d_int(matern_deficit_f32(code, sqrtf(r2))), s2);
+    }
+    Lp[t] = v;
+  }
+  if (lane == 0) *flag = 0;
+  Team<T>::sync();
+  const bool ok = ldlt_blocked<T, kPredW>(K, Lp, invd, acc, A.kt, flag, rb);
+  Team<T>::sync();
+  return ok;
 }
 
 template <int T>
@@ -68,8 +145,8 @@ __device__ void pred_block(const PredArgs& A, const PredPrm* prm, int64_t b, dou
   double* Lp = u + (int64_t)kt * d;
   double* a = Lp + (int64_t)kt * (kt + 1) / 2;
   double* invd = a + kt;
-  double* acc = invd + kt;
-  double* mask = acc + kt;
+  double* acc = invd + kt;                 // kPredW columns of kt
+  double* mask = acc + kPredW * kt;
   double* rv = mask + kt;
   int* idx = (int*)(rv + kt);
   volatile int* flag = idx + kt;
@@ -95,14 +172,18 @@ __device__ void pred_block(const PredArgs& A, const PredPrm* prm, int64_t b, dou
     rv[i] = (A.resid && i < k && ix < A.nobs) ? A.resid[ix] : 0.0;
   }
   Team<T>::sync();
-  for (int t = lane; t < K * d; t += T) {
-    const int i = t / d, l = t - (t / d) * d;
-    u[i * d + l] = A.Xall[(int64_t)idx[i] * d + l] * prm->invlam[l];
-  }
-  Team<T>::sync();
   const double s2 = prm->s2, tau = prm->tau;
   bool ok = false;
-  for (int lv = 0; lv <= 9; ++lv) {
+  if (A.split) ok = pred_split_factor<T>(A, prm, K, u, Lp, invd, acc, mask, (long long*)a, idx, flag);
+  if (!ok) {
+    if (A.split && lane == 0) atomicAdd(A.info + SV_INFO_AUX, 1);
+    for (int t = lane; t < K * d; t += T) {
+      const int i = t / d, l = t - (t / d) * d;
+      u[i * d + l] = A.Xall[(int64_t)idx[i] * d + l] * prm->invlam[l];
+    }
+    Team<T>::sync();
+  }
+  for (int lv = 0; lv <= 9 && !ok; ++lv) {
     double jit = 0.0;
     if (lv > 0) {
       // 10^p * mean(diag Sigma)   (_covariance.py:245-249)
@@ -114,7 +195,7 @@ __device__ void pred_block(const PredArgs& A, const PredPrm* prm, int64_t b, dou
     if (lane == 0) *flag = 0;
     assemble_sigma<T>(K, d, u, mask, s2, tau, jit, prm->mm, Lp, nullptr, nullptr);
     Team<T>::sync();
-    ok = ldlt_packed<T>(K, Lp, invd, acc, flag);
+    ok = ldlt_blocked<T, kPredW>(K, Lp, invd, acc, kt, flag);
     Team<T>::sync();
     if (ok) {
       if (lv > 0 && lane == 0) atomicMax(A.info + SV_INFO_JITTER, lv);
@@ -306,6 +387,9 @@ extern "C" int sv_predict_blocks(const sv_pred_desc* D, const double* theta, con
   A.closed = D->general ? -1 : closed;
   A.target_nugget = D->target_nugget;
   A.nu = D->nu;
+  if (D->precision < 0 || D->precision > 1) return SV_EINVAL;
+  A.split = (D->precision == 1 && A.closed >= 0) ? 1 : 0;
+  A.rho_min = D->split_rho_min > 0.0 ? D->split_rho_min : 1e-4;
   int dev = 0, maxsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);

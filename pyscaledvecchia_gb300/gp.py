@@ -49,6 +49,13 @@ class ScaledVecchiaGP:
     factor b on an inner split); ``lambda_max`` (the largest range before an
     input counts as irrelevant); the Fisher-scoring budget ``max_iter`` and
     tolerance ``tol``; the seed of every random draw (``random_state``).
+
+    One setting has no counterpart in the reference: ``precision``, the
+    arithmetic of the likelihood blocks in fit and of the prediction blocks:
+    "float64" (the reference's) or "split" (closed-form nu: block entries
+    assembled in float32 from centred coordinates and the correlation
+    deficit, the factorisation, solves and sums in float64; ill-conditioned
+    blocks are redone in float64).
     """
 
     m_est: int = 30
@@ -64,6 +71,7 @@ class ScaledVecchiaGP:
     tol: float = 1e-4
     random_state: int | None = 0
     verbose: bool = False
+    precision: str = "float64"
 
     # fitted state -----------------------------------------------------------
     X_: np.ndarray = field(default=None, init=False, repr=False)
@@ -74,6 +82,11 @@ class ScaledVecchiaGP:
     d_: int = field(default=None, init=False, repr=False)
     _estimate_nu: bool = field(default=False, init=False, repr=False)
     _nu_fit: float = field(default=None, init=False, repr=False)
+
+    def _precision(self):
+        if self.precision not in ("float64", "split"):
+            raise ValueError("precision must be 'float64' or 'split'")
+        return self.precision
 
     # ---------------- basis / scaling helpers ------------------------------
     def _design(self, X):
@@ -138,7 +151,8 @@ class ScaledVecchiaGP:
             th = self._objective_theta(th, d, estimate_nu)
             ll, g, M, beta = state["prob"].evaluate(
                 th, self.nu, estimate_nu=estimate_nu, need_grad=True,
-                var_penalty=self.var_penalty, log_var_target=st["log_var_target"])
+                var_penalty=self.var_penalty, log_var_target=st["log_var_target"],
+                precision=self._precision())
             g, M = self._freeze_nugget(g, M)
             return ll, g, M, beta
 
@@ -154,7 +168,8 @@ class ScaledVecchiaGP:
         theta, ll, beta = _fisher_scoring(
             theta, objective, max_iter=self.max_iter, tol=self.tol,
             verbose=self.verbose, reorder_hook=reorder_hook)
-        self.fit_stats_ = {"split": 0, "float64": nev[0]}
+        split = self._precision() != "float64"
+        self.fit_stats_ = {"split": nev[0] if split else 0, "float64": 0 if split else nev[0]}
         return self._fit_finish(st, theta, ll, beta)
 
     # ---------------- pieces of fit shared with the batched fitter ----------
@@ -296,6 +311,7 @@ class ScaledVecchiaGP:
         D.nall, D.nobs, D.nblk = ntr + nq, (ntr if noise_free else ntr + nq), nq
         D.d, D.k, D.ldnbr = d, m, m
         D.general, D.nu = int(self._general()), float(self.nu_)
+        D.precision = int(self._precision() == "split")
         th = _lib.to_dev(torch, self._pred_theta(), np.float64)
         info2 = _lib.new_info(torch)
         rc = lib.sv_predict_blocks(D, _lib.ptr(th), _lib.ptr(Xall), _lib.ptr(tgt), _lib.ptr(nbr),
@@ -304,7 +320,9 @@ class ScaledVecchiaGP:
         _lib.check(lib, rc, "sv_predict_blocks")
         res = torch.cat([mean, var]).cpu().numpy()
         _lib.check_info(lib, info.cpu().numpy(), "sv_knn_query")
-        _lib.check_info(lib, info2.cpu().numpy(), "sv_predict_blocks")
+        inf2 = info2.cpu().numpy()
+        _lib.check_info(lib, inf2, "sv_predict_blocks")
+        self.pred_stats_ = {"blocks": int(nq), "redone_float64": int(inf2[3])}
         return res[:nq], res[nq:]
 
     def predict(self, Xstar, return_std=False, return_var=False, m=None):
@@ -358,6 +376,7 @@ class ScaledVecchiaGP:
         D.nall, D.nobs, D.nblk = n + ns, n, ns
         D.d, D.k, D.ldnbr = d, k, k
         D.general, D.nu = int(self._general()), float(self.nu_)
+        D.precision = int(self._precision() == "split")
         th = _lib.to_dev(torch, self._pred_theta(), np.float64)
         info2 = _lib.new_info(torch)
         rc = lib.sv_predict_blocks(D, _lib.ptr(th), _lib.ptr(Xo), _lib.ptr(tgt), _lib.ptr(nbr),

@@ -33,7 +33,8 @@ import numpy as np
 
 from . import _lib
 
-__all__ = ["SetEncoder", "draw_training_problems", "problem_features", "DEFAULT_WEIGHTS"]
+__all__ = ["SetEncoder", "draw_training_problems", "draw_problems", "problem_features",
+           "evaluate_warm_start", "DEFAULT_WEIGHTS"]
 
 S_POINTS = 512
 MAX_D = 12
@@ -114,6 +115,75 @@ def standardise(X, y):
     return (X - lo) / span, (y - y.mean()) / ysd, span, ysd
 
 
+def _draw_specs(rng, B, n, d_range, lam_range, tau_range, s2_range):
+    """B problem specifications (d, X, lambda, tau, sigma^2, eps, eps2)."""
+    spec = []
+    for _ in range(B):
+        d = int(rng.integers(d_range[0], d_range[1] + 1))
+        X = rng.random((n, d))
+        lam = np.exp(rng.uniform(math.log(lam_range[0]), math.log(lam_range[1]), d))
+        tau = float(np.exp(rng.uniform(math.log(tau_range[0]), math.log(tau_range[1]))))
+        s2 = float(np.exp(rng.uniform(math.log(s2_range[0]), math.log(s2_range[1]))))
+        spec.append((d, X, lam, tau, s2, rng.standard_normal(n), rng.standard_normal(n)))
+    return spec
+
+
+def _draw_responses(spec, n, m):
+    """y of every specified problem: one batched device reorder orders them
+    all, one prior draw draws them all (see draw_training_problems)."""
+    lib, torch = _lib.device_ready()
+    from .batched import BatchedLikelihood, BatchProblem, ordered_groups
+    from .sampling import vecchia_prior_sample_device
+    B = len(spec)
+    tau0 = 1e-8
+    mm = min(m, n - 1)
+    BL = BatchedLikelihood([BatchProblem(sp[1], np.zeros(n), None, ordered_groups(n, mm))
+                            for sp in spec], need_grad=False, chunked=False)
+    BL.set_sources([sp[1] for sp in spec], [np.zeros(n)] * B, [None] * B, [mm] * B)
+    orders = BL.reorder(list(range(B)),
+                        [np.concatenate([[0.0], np.log(sp[2]), [math.log(sp[3])]]) for sp in spec],
+                        return_orders=True)
+    Xall = BL.X.cpu().numpy()
+    nbr = BL.nbr.cpu().numpy().astype(np.int64)
+    N = B * n
+    Xs = np.zeros((N, MAX_D))
+    nn = np.full((N, mm + 1), -1, dtype=np.int64)
+    for p, sp in enumerate(spec):
+        d, lam = sp[0], sp[2]
+        xo = int(BL.x_off[p])
+        Xs[p * n:(p + 1) * n, :d] = Xall[xo:xo + n * d].reshape(n, d) / lam
+        o = int(BL.blk_off[p])
+        loc = nbr[o:o + n, :mm]
+        nn[p * n:(p + 1) * n, 0] = np.arange(p * n, (p + 1) * n)
+        nn[p * n:(p + 1) * n, 1:] = np.where(loc >= 0, loc + p * n, -1)
+    eps = np.concatenate([sp[5] for sp in spec]).reshape(N, 1)
+    th = np.concatenate([[0.0], np.zeros(MAX_D), [math.log(tau0)]])
+    f = vecchia_prior_sample_device(torch, _lib.to_dev(torch, Xs, np.float64),
+                                    _lib.to_dev(torch, nn, np.int64), th, 2.5,
+                                    _lib.to_dev(torch, eps, np.float64)).reshape(-1).cpu().numpy()
+    ys = []
+    for p, sp in enumerate(spec):
+        d, X, lam, tau, s2, _, e2 = sp
+        yo = math.sqrt(s2) * (f[p * n:(p + 1) * n] + math.sqrt(max(tau - tau0, 0.0)) * e2)
+        y = np.empty(n)
+        y[orders[p]] = yo
+        ys.append(y)
+    return ys
+
+
+def draw_problems(nprob, seed=0, n=2000, d_range=(3, 12), lam_range=(0.05, 100.0),
+                  tau_range=(1e-8, 1e-1), s2_range=(0.1, 10.0), m=30, chunk=512):
+    """(Xs, ys) of nprob problems drawn as draw_training_problems draws them
+    (the held-out problems of the warm-start evaluation)."""
+    rng = np.random.default_rng(seed)
+    Xs, ys = [], []
+    for c0 in range(0, nprob, chunk):
+        spec = _draw_specs(rng, min(chunk, nprob - c0), n, d_range, lam_range, tau_range, s2_range)
+        ys += _draw_responses(spec, n, m)
+        Xs += [sp[1] for sp in spec]
+    return Xs, ys
+
+
 def draw_training_problems(nprob, seed=0, n=2000, d_range=(3, 12), lam_range=(0.05, 100.0),
                            tau_range=(1e-8, 1e-1), s2_range=(0.1, 10.0), m=30, chunk=512,
                            fit_targets=False):
@@ -133,58 +203,17 @@ def draw_training_problems(nprob, seed=0, n=2000, d_range=(3, 12), lam_range=(0.
     precision with float64 polish, nugget estimated, nu = 2.5, n_est = None),
     so the encoder learns where Fisher scoring ends, clipped ranges of
     irrelevant inputs included."""
-    lib, torch = _lib.device_ready()
-    from .batched import BatchedLikelihood, BatchProblem, ordered_groups
-    from .sampling import vecchia_prior_sample_device
+    _lib.device_ready()
     rng = np.random.default_rng(seed)
     feats = np.zeros((nprob, S_POINTS, N_FEAT))
     cnt = np.zeros(nprob, dtype=np.int32)
     tg = np.zeros((nprob, N_OUT))
     wt = np.zeros((nprob, N_OUT))
     dims = np.zeros(nprob, dtype=np.int64)
-    tau0 = 1e-8
-    mm = min(m, n - 1)
     for c0 in range(0, nprob, chunk):
         B = min(chunk, nprob - c0)
-        spec = []
-        for _ in range(B):
-            d = int(rng.integers(d_range[0], d_range[1] + 1))
-            X = rng.random((n, d))
-            lam = np.exp(rng.uniform(math.log(lam_range[0]), math.log(lam_range[1]), d))
-            tau = float(np.exp(rng.uniform(math.log(tau_range[0]), math.log(tau_range[1]))))
-            s2 = float(np.exp(rng.uniform(math.log(s2_range[0]), math.log(s2_range[1]))))
-            spec.append((d, X, lam, tau, s2, rng.standard_normal(n), rng.standard_normal(n)))
-        BL = BatchedLikelihood([BatchProblem(sp[1], np.zeros(n), None, ordered_groups(n, mm))
-                                for sp in spec], need_grad=False, chunked=False)
-        BL.set_sources([sp[1] for sp in spec], [np.zeros(n)] * B, [None] * B, [mm] * B)
-        orders = BL.reorder(list(range(B)),
-                            [np.concatenate([[0.0], np.log(sp[2]), [math.log(sp[3])]]) for sp in spec],
-                            return_orders=True)
-        Xall = BL.X.cpu().numpy()
-        nbr = BL.nbr.cpu().numpy().astype(np.int64)
-        N = B * n
-        Xs = np.zeros((N, MAX_D))
-        nn = np.full((N, mm + 1), -1, dtype=np.int64)
-        for p, sp in enumerate(spec):
-            d, lam = sp[0], sp[2]
-            xo = int(BL.x_off[p])
-            Xs[p * n:(p + 1) * n, :d] = Xall[xo:xo + n * d].reshape(n, d) / lam
-            o = int(BL.blk_off[p])
-            loc = nbr[o:o + n, :mm]
-            nn[p * n:(p + 1) * n, 0] = np.arange(p * n, (p + 1) * n)
-            nn[p * n:(p + 1) * n, 1:] = np.where(loc >= 0, loc + p * n, -1)
-        eps = np.concatenate([sp[5] for sp in spec]).reshape(N, 1)
-        th = np.concatenate([[0.0], np.zeros(MAX_D), [math.log(tau0)]])
-        f = vecchia_prior_sample_device(torch, _lib.to_dev(torch, Xs, np.float64),
-                                        _lib.to_dev(torch, nn, np.int64), th, 2.5,
-                                        _lib.to_dev(torch, eps, np.float64)).reshape(-1).cpu().numpy()
-        ys = []
-        for p, sp in enumerate(spec):
-            d, X, lam, tau, s2, _, e2 = sp
-            yo = math.sqrt(s2) * (f[p * n:(p + 1) * n] + math.sqrt(max(tau - tau0, 0.0)) * e2)
-            y = np.empty(n)
-            y[orders[p]] = yo
-            ys.append(y)
+        spec = _draw_specs(rng, B, n, d_range, lam_range, tau_range, s2_range)
+        ys = _draw_responses(spec, n, m)
         fitted = None
         if fit_targets:
             from .fit_batched import fit_batched
@@ -399,6 +428,64 @@ class SetEncoder:
         return res
 
 
+def evaluate_warm_start(enc, nprob=1000, seed=1, n=2000, precisions=("float64", "split"),
+                        tol_ll=1e-6):
+    """Held-out comparison of the encoder's start with the default start:
+    nprob problems drawn as the training problems are (another seed), each
+    fitted with fit_batched (nugget estimated, nu = 2.5, n_est = None, no
+    variance correction) from the default start, from the encoder's start,
+    and in the judged form (both, the larger loglik kept).  Per precision:
+    wall time of each form, objective evaluations per fit, and how the warm
+    fits' converged loglik compares with the default fits' (within tol_ll,
+    better, worse)."""
+    import time
+
+    import torch
+
+    from .fit_batched import fit_batched
+    from .gp import ScaledVecchiaGP
+    t0 = time.time()
+    Xs, ys = draw_problems(nprob, seed=seed, n=n)
+    out = {"problems": nprob, "n": n, "seed": seed, "draw_s": time.time() - t0}
+
+    def models():
+        return [ScaledVecchiaGP(n_est=None, nu=2.5, var_correction=False) for _ in Xs]
+
+    def timed(**kw):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r = fit_batched(models(), Xs, ys, **kw)
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t
+
+    def evals(fits):
+        return np.array([g.fit_stats_["split"] + g.fit_stats_["float64"] for g in fits], dtype=float)
+
+    fit_batched(models()[:4], Xs[:4], ys[:4], precision="float64", warm_start=enc)  # warm-up
+    for prec in precisions:
+        base, tb = timed(precision=prec)
+        warm, tw = timed(precision=prec, warm_start=enc)
+        judged, tj = timed(precision=prec, warm_start=enc, warm_judge=True)
+        dll = np.array([w.loglik_ - b.loglik_ for w, b in zip(warm, base)])
+        djl = np.array([j.loglik_ - b.loglik_ for j, b in zip(judged, base)])
+        eb, ew = evals(base), evals(warm)
+        out[prec] = {
+            "default_s": tb, "warm_s": tw, "judged_s": tj,
+            "default_fits_per_s": nprob / tb, "warm_fits_per_s": nprob / tw,
+            "judged_fits_per_s": nprob / tj,
+            "evals_default_mean": float(eb.mean()), "evals_warm_mean": float(ew.mean()),
+            "evals_default_median": float(np.median(eb)), "evals_warm_median": float(np.median(ew)),
+            "frac_warm_within_tol": float(np.mean(np.abs(dll) < tol_ll)),
+            "frac_warm_better": float(np.mean(dll >= tol_ll)),
+            "frac_warm_worse": float(np.mean(dll <= -tol_ll)),
+            "warm_dll_median": float(np.median(dll)),
+            "frac_judged_within_tol": float(np.mean(np.abs(djl) < tol_ll)),
+            "frac_judged_better": float(np.mean(djl >= tol_ll)),
+            "judged_min_dll": float(djl.min()),
+        }
+    return out
+
+
 def main(argv=None):
     """Train the encoder on problems drawn by the method and save it:
     python -m pyscaledvecchia_gb300.warmstart --problems 50000 --out <path>"""
@@ -414,10 +501,22 @@ def main(argv=None):
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     ap.add_argument("--fit-targets", action="store_true",
                     help="train on the fitted parameters of every drawn problem")
+    ap.add_argument("--evaluate", type=int, default=0,
+                    help="only compare the saved encoder's start with the default start on this "
+                         "many held-out problems (evaluate_warm_start) and exit")
+    ap.add_argument("--eval-out", default=None, help="JSON file for the --evaluate results")
     ap.add_argument("--infer", type=int, default=0,
                     help="only run the inference forward (tcgen05) on this many random sets "
                          "with the saved weights, timed, and exit")
     a = ap.parse_args(argv)
+    if a.evaluate:
+        import json
+        res = evaluate_warm_start(SetEncoder.load(a.out), nprob=a.evaluate, seed=a.seed + 1, n=a.n)
+        print(json.dumps(res, indent=1))
+        if a.eval_out:
+            with open(a.eval_out, "w") as fh:
+                json.dump(res, fh, indent=1)
+        return
     if a.infer:
         import torch
         enc = SetEncoder.load(a.out) if os.path.exists(a.out) else SetEncoder(seed=a.seed)

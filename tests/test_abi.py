@@ -53,7 +53,8 @@ def test_binding_argument_counts_match_the_prototypes():
 
 
 def test_status_strings(lib):
-    assert lib.sv_abi_version() == 1
+    from pyscaledvecchia_gb300 import _lib
+    assert lib.sv_abi_version() == _lib.ABI_VERSION
     assert lib.sv_status_string(0) == b"ok"
     assert b"Cholesky" in lib.sv_status_string(2)
 
@@ -110,3 +111,37 @@ def test_side_stream_and_host_memory_flag_are_per_device(monkeypatch):
     assert _lib.device_reads_host_memory(lib) is True
     assert Lib.calls == [0, 1]
     Torch.cuda.dev = 0
+
+
+def test_structure_layouts_match_the_header(tmp_path):
+    """Every ctypes mirror in _lib has the size and field offsets that a C
+    compiler gives the header's structure."""
+    import ctypes
+    import shutil
+    import subprocess
+
+    from pyscaledvecchia_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = {"sv_loglik_desc": _lib.LoglikDesc, "sv_prob_desc": _lib.ProbDesc,
+             "sv_batch_desc": _lib.BatchDesc, "sv_reorder_prob": _lib.ReorderProb,
+             "sv_pack_group": _lib.PackGroup, "sv_chunk_group": _lib.ChunkGroup,
+             "sv_reorder_desc": _lib.ReorderDesc, "sv_pred_desc": _lib.PredDesc}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "svgpu.h"', "int main(void) {"]
+    expect = []
+    for cname, py in pairs.items():
+        lines.append(f'  printf("%zu\\n", sizeof({cname}));')
+        expect.append(ctypes.sizeof(py))
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("%zu\\n", offsetof({cname}, {fname}));')
+            expect.append(getattr(py, fname).offset)
+    lines += ["  printf(\"%d\\n\", SV_ABI_VERSION);", "  return 0;", "}"]
+    expect.append(_lib.ABI_VERSION)
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True,
+                                          text=True).stdout.split()]
+    assert got == expect
