@@ -647,6 +647,15 @@ def run_predict(torch, lib, check_oracle=True):
     samples, t_joint = timed(lambda: gp.sample_joint(Xte, n_sim=100, random_state=0))
     res["sample_joint_s"] = t_joint
     res["samples_shape"] = list(samples.shape)
+    # exact marginal variances of the joint law, diag((U_pp U_pp^T)^-1)
+    # (gp.py:391-393 forms the dense 50,000 x 50,000 U_pp^-T for this)
+    F = gp._joint_factor_device((Xte - gp._lo) / gp._span, gp.m_pred)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    v = gp._joint_var_diag(F)
+    torch.cuda.synchronize()
+    res["exact_var_diag_s"] = time.perf_counter() - t0
+    res["exact_var_finite_positive"] = bool(torch.all(v > 0).item() and torch.isfinite(v).all().item())
     return res
 
 

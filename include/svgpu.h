@@ -44,7 +44,7 @@ typedef struct CUstream_st* sv_stream_t; /* identical to cudaStream_t */
 
 /* version of this interface: sv_abi_version() returns it; bumped whenever a
  * signature or a structure layout changes */
-#define SV_ABI_VERSION 2
+#define SV_ABI_VERSION 3
 
 const char* sv_status_string(int status);
 int sv_abi_version(void);
@@ -454,6 +454,23 @@ int sv_joint_solve_flags(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr, 
                          const double* acol, const double* R, int32_t nrhs, double* X,
                          int32_t* info, void* workspace, size_t workspace_bytes, int32_t flags,
                          sv_stream_t stream);
+
+/* diag((U_pp U_pp^T)^-1), the marginal variances of the joint predictive
+ * law N(mean, (U_pp U_pp^T)^-1) in the elimination ordering: replaces the
+ * dense S = U_pp^-T of gp.py:391-393 (predict_joint(exact_var=True),
+ * var = (S**2).sum(1)) without forming it.  Rows of S come from the
+ * recurrence of sv_joint_solve against identity columns, in column panels:
+ * a panel [c0, c0 + w) needs only rows >= c0 (S is lower triangular) and
+ * row i only its columns <= i - c0; w is the widest panel whose rows
+ * c0 .. npred-1 fit in `panel` ((npred - c0) w doubles; at least npred
+ * doubles, else SV_ENOSPC).  npred * npred doubles do it in one launch.
+ *   var       : device float64[npred]
+ *   workspace : sv_joint_solve_workspace_bytes(npred) bytes
+ *   panel     : device scratch of panel_bytes */
+int sv_joint_var_diag(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr, const int32_t* nbr,
+                      const double* acol, double* var, int32_t* info, void* workspace,
+                      size_t workspace_bytes, double* panel, size_t panel_bytes,
+                      sv_stream_t stream);
 
 /* ---------------------------------------------------------------------- */
 /* Measurement                                                             */

@@ -82,7 +82,7 @@ class PredDesc(ctypes.Structure):
 
 
 # SV_ABI_VERSION of include/svgpu.h that the structures above mirror
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 # name -> (restype, argtypes); every symbol declared in include/svgpu.h
 SIGNATURES = {
@@ -139,6 +139,8 @@ SIGNATURES = {
                                c_vp, c_sz, c_vp]),
     "sv_joint_solve_flags": (c_i32, [c_i64, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp,
                                      c_vp, c_vp, c_sz, c_i32, c_vp]),
+    "sv_joint_var_diag": (c_i32, [c_i64, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz,
+                                  c_vp, c_sz, c_vp]),
 }
 
 

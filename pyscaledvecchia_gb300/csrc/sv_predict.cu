@@ -349,6 +349,102 @@ __global__ void k_joint_solve(JsArgs A) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// diag((U_pp U_pp^T)^-1): rows of S = U_pp^-T against identity columns
+// ---------------------------------------------------------------------------
+struct JvArgs {
+  int64_t npred, nobs, row0;  // panel: identity columns row0 .. row0 + w - 1
+  int k, ldnbr, w;
+  const int32_t* nbr;
+  const double* acol;
+  double* S;        // rows row0 .. npred-1 of the panel, row stride w
+  double* var;      // += the panel's sum of squares of each row
+  int* ready;
+  unsigned* counter;
+  unsigned* progress;
+  int32_t* info;
+  unsigned spin_limit;
+};
+
+// Row c of S = U_pp^-T restricted to the panel's columns: the recurrence of
+// k_joint_solve with the identity as right-hand side, S_cr = (delta(c, row0
+// + r) - sum_j a_j S_{p_j r}) / a_K.  S is lower triangular, so rows before
+// row0 are zero in the panel (never formed, their dependencies skipped) and
+// row c is zero beyond column c - row0 (never formed; a dependency p is read
+// only where r <= p - row0).  The row's sum of squares is added to var[c].
+__global__ void k_joint_inv_rows(JvArgs A) {
+  extern __shared__ double jv_sm[];
+  double* s_a = jv_sm;
+  int* s_p = (int*)(jv_sm + (A.k > 0 ? A.k : 1));
+  __shared__ long long s_c;
+  __shared__ int s_np;
+  __shared__ double s_red[32];
+  const int K = A.k + 1;
+  while (true) {
+    if (threadIdx.x == 0) s_c = A.row0 + (long long)atomicAdd(A.counter, 1u);
+    __syncthreads();
+    const int64_t c = s_c;
+    if (c >= A.npred) break;
+    const double* ac = A.acol + c * (int64_t)K;
+    if (threadIdx.x == 0) {
+      int np = 0;
+      for (int i = 0; i < A.k; ++i) {
+        const int64_t ix = A.nbr[c * (int64_t)A.ldnbr + i];
+        if (ix < 0 || ix < A.nobs || ix - A.nobs < A.row0) continue;  // zero in this panel
+        s_p[np] = (int)(ix - A.nobs);
+        s_a[np] = ac[i];
+        ++np;
+      }
+      s_np = np;
+    }
+    __syncthreads();
+    const int np = s_np;
+    for (int j = threadIdx.x; j < np; j += blockDim.x) {
+      const int p = s_p[j];
+      unsigned it = 0, seen = ld_acquire_u32(A.progress);
+      while (ld_acquire_s32(A.ready + p) == 0) {
+        if (++it > A.spin_limit) {
+          const unsigned now = ld_acquire_u32(A.progress);
+          if (now != seen) {
+            seen = now;
+            it = 0;
+            continue;
+          }
+          set_error(A.info + SV_INFO_STATUS, SV_ETIMEOUT);
+          atomicCAS(A.info + SV_INFO_BLOCK, -1, (int)c);
+          break;
+        }
+      }
+    }
+    __syncthreads();
+    const double aK = ac[K - 1];
+    const int64_t own = c - A.row0;
+    const int64_t lim = own < A.w - 1 ? own : A.w - 1;
+    double sq = 0.0;
+    for (int64_t r = threadIdx.x; r <= lim; r += blockDim.x) {
+      double v = (r == own) ? 1.0 : 0.0;
+      for (int j = 0; j < np; ++j) {
+        const int64_t pr = s_p[j] - A.row0;
+        if (r <= pr) v -= s_a[j] * __ldcg(A.S + pr * A.w + r);
+      }
+      v = v / aK;
+      A.S[own * A.w + r] = v;
+      sq = fma(v, v, sq);
+    }
+    for (int o = 16; o > 0; o >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = sq;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_red[w];
+      A.var[c] += t;
+      st_release_s32(A.ready + c, 1);
+      atomicAdd(A.progress, 1u);
+    }
+  }
+}
+
 }  // namespace sv
 
 using namespace sv;
@@ -484,4 +580,58 @@ extern "C" int sv_joint_solve_flags(int64_t npred, int64_t nobs, int32_t k, int3
                                     size_t workspace_bytes, int32_t flags, sv_stream_t stream) {
   return joint_solve(npred, nobs, k, ldnbr, nbr, acol, R, nrhs, X, info, workspace, workspace_bytes,
                      flags, stream);
+}
+
+extern "C" int sv_joint_var_diag(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr,
+                                 const int32_t* nbr, const double* acol, double* var, int32_t* info,
+                                 void* workspace, size_t workspace_bytes, double* panel,
+                                 size_t panel_bytes, sv_stream_t stream) {
+  if (npred < 0 || nobs < 0 || k < 0 || k > 4096 || !info) return SV_EINVAL;
+  if (npred > 0 && (!acol || !var || !panel || (k > 0 && (!nbr || ldnbr < k)))) return SV_EINVAL;
+  if (npred > 0x7fffffffLL) return SV_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  int32_t init_info[4] = {0, -1, 0, 0};
+  SV_CUDA_TRY(cudaMemcpyAsync(info, init_info, sizeof(init_info), cudaMemcpyHostToDevice, st));
+  if (npred == 0) return SV_OK;
+  if (!workspace || workspace_bytes < sv_joint_solve_workspace_bytes(npred)) return SV_ENOSPC;
+  const int64_t pd = (int64_t)(panel_bytes / sizeof(double));
+  if (pd < npred) return SV_ENOSPC;  // one column of all rows at least
+  SV_CUDA_TRY(cudaMemsetAsync(var, 0, sizeof(double) * (size_t)npred, st));
+  JvArgs A;
+  A.npred = npred;
+  A.nobs = nobs;
+  A.k = k;
+  A.ldnbr = ldnbr;
+  A.nbr = nbr;
+  A.acol = acol;
+  A.S = panel;
+  A.var = var;
+  A.counter = (unsigned*)workspace;
+  A.progress = A.counter + 1;
+  A.ready = (int*)((char*)workspace + 256);
+  A.info = info;
+  A.spin_limit = SV_SPIN_LIMIT;
+  const int nsm = sv_num_sms();
+  const size_t smem = (size_t)(k > 0 ? k : 1) * (sizeof(double) + sizeof(int)) + 8;
+  for (int64_t c0 = 0; c0 < npred;) {
+    // the widest panel whose rows c0 .. npred-1 fit
+    const int64_t rows = npred - c0;
+    int64_t w = pd / rows;
+    if (w > rows) w = rows;
+    if (w > 0x7fffffffLL) w = 0x7fffffffLL;
+    A.row0 = c0;
+    A.w = (int)w;
+    SV_CUDA_TRY(cudaMemsetAsync(workspace, 0, sv_joint_solve_workspace_bytes(npred), st));
+    int tpb = (int)(((w + 31) / 32) * 32);
+    if (tpb > 256) tpb = 256;
+    int per_sm = 0;
+    SV_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_joint_inv_rows, tpb, smem));
+    if (per_sm < 1) return SV_EINVAL;
+    int64_t grid = (int64_t)per_sm * nsm;
+    if (grid > rows) grid = rows;
+    k_joint_inv_rows<<<(unsigned)grid, tpb, smem, st>>>(A);
+    SV_CUDA_TRY(cudaGetLastError());
+    c0 += w;
+  }
+  return SV_OK;
 }

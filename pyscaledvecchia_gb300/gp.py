@@ -416,6 +416,26 @@ class ScaledVecchiaGP:
         _lib.check(lib, rc, "sv_joint_solve")
         return X, info
 
+    def _joint_var_diag(self, F, panel_bytes=None):
+        """diag((U_pp U_pp^T)^-1) in the elimination ordering (device tensor).
+        The panel scratch holds at most a quarter of the free device memory
+        (and never more than the whole lower triangle needs)."""
+        lib, torch = _lib.device_ready()
+        ns = F["ns"]
+        if panel_bytes is None:
+            free = torch.cuda.mem_get_info()[0]
+            panel_bytes = min(8 * ns * ns, max(8 * ns, free // 4))
+        panel = _lib.workspace(torch, int(panel_bytes))
+        ws = _lib.workspace(torch, lib.sv_joint_solve_workspace_bytes(ns))
+        v = torch.empty(ns, dtype=torch.float64, device="cuda")
+        info = _lib.new_info(torch)
+        rc = lib.sv_joint_var_diag(ns, F["n"], F["k"], F["k"], _lib.ptr(F["nbr"]), _lib.ptr(F["acol"]),
+                                   _lib.ptr(v), _lib.ptr(info), _lib.ptr(ws), ws.numel(),
+                                   _lib.ptr(panel), panel.numel(), _lib.stream_handle(torch))
+        _lib.check(lib, rc, "sv_joint_var_diag")
+        _lib.check_info(lib, info.cpu().numpy(), "sv_joint_var_diag")
+        return v
+
     def predict_joint(self, Xstar, m=None, n_sim=0, exact_var=False,
                       random_state=None):
         """Joint Vecchia predictive distribution (Sec. 3.3).
@@ -446,17 +466,9 @@ class ScaledVecchiaGP:
         rng = np.random.default_rng(self.random_state if random_state is None
                                     else random_state)
         if exact_var:
-            # rows of U_pp^-T: solve against identity columns in chunks
-            v = torch.zeros(ns, dtype=torch.float64, device="cuda")
-            chunk = max(1, min(ns, (1 << 27) // max(ns, 1)))
-            for c0 in range(0, ns, chunk):
-                c1 = min(ns, c0 + chunk)
-                E = torch.zeros((ns, c1 - c0), dtype=torch.float64, device="cuda")
-                E[torch.arange(c0, c1, device="cuda"), torch.arange(c1 - c0, device="cuda")] = 1.0
-                S, info = self._joint_solve(F, E)
-                v += (S * S).sum(1)
-                _lib.check_info(lib, info.cpu().numpy(), "sv_joint_solve")
-            v = v.cpu().numpy()[inv]
+            # diag((U_pp U_pp^T)^-1) = (S**2).sum(1), S = U_pp^-T (gp.py:391-393),
+            # from rows of S in column panels, never the whole of S at once
+            v = self._joint_var_diag(F).cpu().numpy()[inv]
             out["var"] = (self._ysd ** 2) * self.b_ * v
         if n_sim > 0:
             eps = rng.standard_normal((ns, n_sim))

@@ -150,7 +150,7 @@ def _heldout(nprob, seed):
 
 @pytest.mark.gpu
 def test_warm_start_gain_on_heldout_problems():
-    """Shipped weights (trained on the fitted parameters of 12,000 problems
+    """Shipped weights (trained on the fitted parameters of 50,000 problems
     drawn by the method), held-out problems drawn the same way: the
     encoder's start lies much closer to where Fisher scoring converges than
     the default start and the fits need fewer objective evaluations; the
@@ -202,7 +202,7 @@ def test_warm_start_gain_on_heldout_problems():
     ew = np.array([g.fit_stats_["float64"] for g in warm])
     print(f"start-to-optimum distance^2: default {d0.mean():.2f}, encoder {dw.mean():.2f}; "
           f"objective evaluations: default {eb.mean():.2f}, encoder {ew.mean():.2f}")
-    # measured with the shipped weights (32 problems): distance^2 136.8 -> 46.6,
+    # measured with the shipped weights (32 problems): distance^2 136.8 -> 51.2,
     # evaluations 24.5 -> 22.3
     assert dw.mean() < 0.5 * d0.mean(), (dw.mean(), d0.mean())
     assert ew.mean() < 0.95 * eb.mean(), (ew.mean(), eb.mean())
