@@ -65,16 +65,23 @@ int sv_maximin_order(const double* X, int64_t n, int32_t d, int64_t first, int64
                      int32_t* info, void* workspace, size_t workspace_bytes, sv_stream_t stream);
 /* The same with test aids that give the same order by other routes: bit 0
  * ranks every pivot choice by exact roots, bit 1 takes pivots by the tie
- * pass only, bit 2 runs the grid form even when one cluster would hold X.
- * Bit 3 (with bit 2) tests the grid barrier's bounded wait: one CTA does not
- * arrive at the first barrier and every wait is limited to 4096 polls, so
- * all waits run out, every CTA returns and info[0] = SV_ETIMEOUT. */
+ * pass only, bit 2 runs the grid form even when one cluster would hold X,
+ * bit 4 runs the tree form (not with bit 2).  Bit 3 (with bit 2) tests the
+ * grid barrier's bounded wait: one CTA does not arrive at the first barrier
+ * and every wait is limited to 4096 polls, so all waits run out, every CTA
+ * returns and info[0] = SV_ETIMEOUT.  The workspace of a call with flags is
+ * sv_maximin_workspace_bytes_flags(n, d, flags) bytes. */
 int sv_maximin_order_flags(const double* X, int64_t n, int32_t d, int64_t first, int64_t* order,
                            int32_t* info, void* workspace, size_t workspace_bytes, int32_t flags,
                            sv_stream_t stream);
-/* largest n sv_maximin_order accepts for dimension d (rows held in the
- * shared memory of all SMs); SV_EINVAL above it */
+size_t sv_maximin_workspace_bytes_flags(int64_t n, int32_t d, int32_t flags);
+/* largest n sv_maximin_order accepts (int32 row indices): rows beyond the
+ * shared memory of all SMs (sv_maximin_grid_max_rows) take the tree form,
+ * whose workspace grows with n (about 260 bytes per row at d = 10) */
 int64_t sv_maximin_max_rows(int32_t d);
+/* largest n the grid form holds for dimension d (rows in the shared memory
+ * of all SMs) */
+int64_t sv_maximin_grid_max_rows(int32_t d);
 
 /* Ordered nearest neighbours: replaces ordering.py:76-116 (find_ordered_nn).
  * nn is (n, m+1) int64: column 0 = row index, columns 1..min(i,m) the nearest

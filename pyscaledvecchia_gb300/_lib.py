@@ -93,6 +93,8 @@ SIGNATURES = {
     "sv_maximin_order": (c_i32, [c_vp, c_i64, c_i32, c_i64, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "sv_maximin_order_flags": (c_i32, [c_vp, c_i64, c_i32, c_i64, c_vp, c_vp, c_vp, c_sz, c_i32, c_vp]),
     "sv_maximin_max_rows": (c_i64, [c_i32]),
+    "sv_maximin_grid_max_rows": (c_i64, [c_i32]),
+    "sv_maximin_workspace_bytes_flags": (c_sz, [c_i64, c_i32, c_i32]),
     "sv_ordered_knn_workspace_bytes": (c_sz, [c_i64, c_i32]),
     "sv_ordered_knn": (c_i32, [c_vp, c_i64, c_i32, c_i32, c_i64, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "sv_knn_query_workspace_bytes": (c_sz, [c_i64, c_i64, c_i32]),

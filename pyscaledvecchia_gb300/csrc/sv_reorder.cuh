@@ -38,5 +38,9 @@ int maximin_grid_single(const double* X, int64_t n, int d, int64_t first, int64_
                         int32_t* info, char* ws, size_t ws_bytes, int flags, cudaStream_t st);
 size_t maximin_grid_workspace_bytes();
 int64_t maximin_grid_max_rows(int d);
+// single-problem maximin through the tree form (any n >= 2)
+int maximin_tree_single(const double* X, int64_t n, int d, int64_t first, int64_t* order,
+                        int32_t* info, char* ws, size_t ws_bytes, int flags, cudaStream_t st);
+size_t maximin_tree_workspace_bytes(int64_t n, int d);
 
 }  // namespace sv

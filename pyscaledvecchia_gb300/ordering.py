@@ -25,13 +25,14 @@ __all__ = ["maximin_order", "find_ordered_nn"]
 def maximin_order_device(torch, Xd, first: int, flags: int = 0):
     """Maximin permutation of the rows of a device (n, d) float64 tensor.
     ``flags`` (test aids, same order): 1 ranks every pivot choice by exact
-    roots, 2 takes pivots by tie passes only, 4 forces the grid form; 8 (with
-    4) makes the grid barrier's bounded wait run out (SV_ETIMEOUT in info)."""
+    roots, 2 takes pivots by tie passes only, 4 forces the grid form, 16 the
+    tree form; 8 (with 4) makes the grid barrier's bounded wait run out
+    (SV_ETIMEOUT in info)."""
     lib = _lib.load_library()
     n, d = Xd.shape
     order = torch.empty(n, dtype=torch.int64, device="cuda")
     info = _lib.new_info(torch)
-    ws = _lib.workspace(torch, lib.sv_maximin_workspace_bytes(n, d))
+    ws = _lib.workspace(torch, lib.sv_maximin_workspace_bytes_flags(n, d, int(flags)))
     if flags:
         rc = lib.sv_maximin_order_flags(_lib.ptr(Xd), n, d, int(first), _lib.ptr(order), _lib.ptr(info),
                                         _lib.ptr(ws), ws.numel(), int(flags), _lib.stream_handle(torch))

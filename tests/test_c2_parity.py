@@ -43,3 +43,25 @@ def test_maximin_and_neighbours_match_the_oracle_at_200k():
     nn_d, info = ordered_nn_device(torch, Xs_d[order_d].contiguous(), m)
     _lib.check_info(lib, info.cpu().numpy(), "knn")
     assert nn_digest(nn_d.cpu().numpy()) == fx[1]
+
+
+def test_tree_form_maximin_at_200k():
+    """The tree form (the route beyond the grid form's shared memory) on the
+    same 200,000 rows gives the oracle's order too."""
+    import sys
+    sys.path.insert(0, ROOT)
+    import torch
+
+    from bench import c2_fixture, make_inputs
+    from pyscaledvecchia_gb300 import _lib
+    from pyscaledvecchia_gb300.ordering import maximin_order_device
+    n, d, m, seed = 200_000, 10, 30, 1
+    fx = c2_fixture(n, d, m, seed)
+    assert fx is not None, "tests/golden/c2_order.npz is missing"
+    lib, _ = _lib.device_ready()
+    X, lam, _, _ = make_inputs(n, d, seed)
+    Xs = X / lam
+    first = int(np.argmin(((Xs - Xs.mean(0)) ** 2).sum(1)))
+    order_d, info = maximin_order_device(torch, _lib.to_dev(torch, Xs, np.float64), first, 16)
+    _lib.check_info(lib, info.cpu().numpy(), "maximin")
+    np.testing.assert_array_equal(order_d.cpu().numpy(), fx[0])

@@ -106,12 +106,14 @@ def _maximin_routed(X, flags):
     return o.cpu().numpy()
 
 
-@pytest.mark.parametrize("flags", [4, 5, 6, 1, 2])
+@pytest.mark.parametrize("flags", [4, 5, 6, 1, 2, 16, 17, 18])
 def test_maximin_routes_vs_oracle(oracle, flags):
     """The grid form (flag 4: lists through global memory behind a grid
-    barrier, one CTA per SM from 9,728 rows) and the exact-root and tie-pass
-    routes (flags 1, 2) give the reference's order on random rows, a lattice
-    with duplicates and rows on a coarse grid of values."""
+    barrier, one CTA per SM from 9,728 rows), the tree form (flag 16: one CTA
+    over a 32-ary tree of the rows) and the exact-root and tie-pass routes
+    (flags 1, 2, alone and with either form) give the reference's order on
+    random rows, a lattice with duplicates and rows on a coarse grid of
+    values."""
     rng = np.random.default_rng(11)
     g = np.arange(30, dtype=float)
     lattice = np.array([[a, b] for a in g for b in g])
@@ -123,12 +125,13 @@ def test_maximin_routes_vs_oracle(oracle, flags):
         np.testing.assert_array_equal(_maximin_routed(X, flags), oracle.maximin_order(X))
 
 
-def test_maximin_grid_form_limits():
+def test_maximin_form_limits():
     from pyscaledvecchia_gb300 import _lib
     lib, _ = _lib.device_ready()
     for d in (2, 10, 64):
-        assert lib.sv_maximin_max_rows(d) > lib.sv_maximin_cluster_max_rows(d)
-    assert lib.sv_maximin_max_rows(10) > 500_000
+        assert lib.sv_maximin_grid_max_rows(d) > lib.sv_maximin_cluster_max_rows(d)
+        assert lib.sv_maximin_max_rows(d) == 2 ** 31 - 1
+    assert lib.sv_maximin_grid_max_rows(10) > 500_000
 
 
 @pytest.mark.parametrize("n,d,m,start", [(20000, 10, 30, 0), (5000, 3, 140, 0),
