@@ -783,6 +783,28 @@ def main():
     torch.cuda.synchronize()
     t_knn = time.perf_counter() - t0
     _lib.check_info(lib, info.cpu().numpy(), "knn")
+    # the same rows through the tree form of the maximin (the route beyond the
+    # grid form's shared memory), and the tree form at a million rows
+    t0 = time.perf_counter()
+    order_t, info = maximin_order_device(torch, Xs_d, first, 16)
+    torch.cuda.synchronize()
+    t_tree = time.perf_counter() - t0
+    _lib.check_info(lib, info.cpu().numpy(), "maximin")
+    tree_same = bool(torch.equal(order_t, order_d))
+    maximin_tree = {"rows": n, "tree_s": t_tree, "default_route_s": t_maximin,
+                    "same_order_as_default_route": tree_same}
+    if not args.no_forms:
+        X1, lam1, _, _ = make_inputs(1_000_000, d, seed + 100)
+        Xs1 = X1 / lam1
+        f1 = int(np.argmin(((Xs1 - Xs1.mean(0)) ** 2).sum(1)))
+        Xs1_d = _lib.to_dev(torch, Xs1, np.float64)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        o1, info = maximin_order_device(torch, Xs1_d, f1)
+        torch.cuda.synchronize()
+        maximin_tree["rows_1M_s"] = time.perf_counter() - t0
+        _lib.check_info(lib, info.cpu().numpy(), "maximin")
+        del Xs1_d, o1
     order = order_d.cpu().numpy()
     nn = nn_d.cpu().numpy()
     fx = c2_fixture(n, d, m, seed)
@@ -954,7 +976,7 @@ def main():
                   "split_errors_vs_float64_form": errors_vs(res64, res),
                   "blocks_refactored_in_float64": int(prob.last_info[3]),
                   "team_lanes_ms": lane_ms, "team_lanes": best_lanes,
-                  "maximin_s": t_maximin, "knn_s": t_knn,
+                  "maximin_s": t_maximin, "knn_s": t_knn, "maximin_tree": maximin_tree,
                   "order_matches_oracle": order_ok, "nn_matches_oracle": nn_ok,
                   "step_ms_all": step_ms, "forms": forms},
     }
