@@ -75,7 +75,67 @@ def parse():
     ap.add_argument("--no-c1", action="store_true", help="skip the n = 2000 fit + predict workload")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the other precision forms and smoothness values of the evaluation")
+    ap.add_argument("--kernel-case", default="", choices=["", "pred", "pred64", "tree", "jvar"],
+                    help="run one small case of a kernel for a profiler capture and exit: "
+                         "pred / pred64 (sv_predict_blocks, split / float64, 20,000 blocks of "
+                         "141), tree (tree-form maximin, 100,000 rows, d = 10), jvar "
+                         "(sv_joint_var_diag, 5,000 points)")
     return ap.parse_args()
+
+
+def kernel_case(name):
+    """Small cases for profiler captures (a few hundred MB on the device)."""
+    import torch
+
+    from pyscaledvecchia_gb300 import ScaledVecchiaGP
+    from pyscaledvecchia_gb300 import _lib as L
+    from pyscaledvecchia_gb300.ordering import knn_query_device, maximin_order_device
+    lib, _ = L.device_ready()
+    if name in ("pred", "pred64"):
+        rng = np.random.default_rng(0)
+        ntr, nte, d, m = 100_000, 20_000, 6, 140
+        Xtr, Xte = rng.random((ntr, d)), rng.random((nte, d))
+        # the fitted parameters of the prediction workload (standardised frame)
+        theta = np.array([-0.38, -2.30, -1.63, -0.93, -0.17, 1.96, 6.9, -5.87])
+        ranges = np.exp(theta[1:1 + d])
+        nb, _ = knn_query_device(torch, L.to_dev(torch, Xtr / ranges, np.float64),
+                                 L.to_dev(torch, Xte / ranges, np.float64), m)
+        Xall = torch.cat([L.to_dev(torch, Xtr, np.float64), L.to_dev(torch, Xte, np.float64)])
+        tgt = torch.arange(ntr, ntr + nte, dtype=torch.int32, device="cuda")
+        nbr = nb.to(torch.int32).contiguous()
+        rd = L.to_dev(torch, rng.standard_normal(ntr), np.float64)
+        th = L.to_dev(torch, theta, np.float64)
+        D = L.PredDesc()
+        D.nall, D.nobs, D.nblk = ntr + nte, ntr, nte
+        D.d, D.k, D.ldnbr = d, m, m
+        D.general, D.nu, D.precision = 0, 2.5, int(name == "pred")
+        mean = torch.empty(nte, dtype=torch.float64, device="cuda")
+        var = torch.empty_like(mean)
+        info = L.new_info(torch)
+        for _ in range(3):
+            L.check(lib, lib.sv_predict_blocks(D, L.ptr(th), L.ptr(Xall), L.ptr(tgt), L.ptr(nbr),
+                                               L.ptr(rd), L.ptr(mean), L.ptr(var), None, None,
+                                               L.ptr(info), L.stream_handle(torch)),
+                    "sv_predict_blocks")
+        torch.cuda.synchronize()
+        L.check_info(lib, info.cpu().numpy(), "sv_predict_blocks")
+    elif name == "tree":
+        n, d = 100_000, 10
+        rng = np.random.default_rng(1)
+        Xs = rng.random((n, d)) / np.exp(rng.uniform(math.log(0.05), math.log(50.0), d))
+        first = int(np.argmin(((Xs - Xs.mean(0)) ** 2).sum(1)))
+        _, info = maximin_order_device(torch, L.to_dev(torch, Xs, np.float64), first, 16)
+        torch.cuda.synchronize()
+        L.check_info(lib, info.cpu().numpy(), "sv_maximin_order")
+    elif name == "jvar":
+        rng = np.random.default_rng(2)
+        X = rng.random((20_000, 4))
+        y = np.sin(5 * X[:, 0]) + X[:, 1] + 0.1 * rng.standard_normal(20_000)
+        gp = ScaledVecchiaGP(m_est=20, n_est=2000, var_correction=False).fit(X, y)
+        F = gp._joint_factor_device((rng.random((5000, 4)) - gp._lo) / gp._span, 40)
+        gp._joint_var_diag(F)
+        torch.cuda.synchronize()
+    print(json.dumps({"kernel_case": name, "status": "ok"}))
 
 
 def dist_env():
@@ -748,6 +808,9 @@ def bessel_error(torch, lib, Xo, nn, theta, nu, nblk=2000, seed=5):
 
 def main():
     args = parse()
+    if args.kernel_case:
+        kernel_case(args.kernel_case)
+        return
     if args.impl == "reference":
         run_reference(args)
         return

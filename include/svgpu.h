@@ -305,9 +305,11 @@ int sv_vecchia_loglik_batched(const sv_batch_desc* desc, const sv_prob_desc* pro
  * score and Fisher, 34,995 blocks in float64 (precision 0) and 32,300 in the
  * split forms (precision 1 and 2, whose scratch also holds the float32
  * coordinate pairs).  The first call on a device looks up the array's address
- * (cudaGetSymbolAddress) and should come before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race, so serialise
- * them. */
+ * (cudaGetSymbolAddress) and must come before any stream capture; later calls
+ * enqueue only kernels (the problem descriptor passed by value, the status
+ * words cleared by a kernel) and can be captured in a CUDA graph and
+ * replayed.  All calls share the array: calls that overlap on the GPU race,
+ * so serialise them. */
 #define SV_NOALLOC_SCRATCH_BYTES (32u << 20)
 int sv_vecchia_loglik_noalloc(const sv_loglik_desc* desc, const double* theta, const double* X,
                               const double* y, const double* Z, const int32_t* rowb,

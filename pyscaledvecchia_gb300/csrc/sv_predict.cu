@@ -248,9 +248,11 @@ __global__ void k_pred_warp(PredArgs A) {
 }
 
 // threads of the CTA that owns one large prediction block: two CTAs of a
-// 141-point block fill an SM's shared memory, so 8 warps each keep 16 warps
-// resident to cover the float64 latency
-constexpr int kPredCta = 256;
+// 141-point block fill an SM's shared memory, so 12 warps each keep 24 warps
+// resident to cover the float64 and shared-memory latency (measured at 50,000
+// blocks of 141: 256 threads 58.9 ms, 384 57.8 ms, 512 86 ms, where the
+// registers allow one CTA per SM)
+constexpr int kPredCta = 384;
 
 __global__ void __launch_bounds__(kPredCta) k_pred_cta(PredArgs A) {
   extern __shared__ double smem[];

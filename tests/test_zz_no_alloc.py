@@ -102,6 +102,43 @@ def test_noalloc_split_forms_on_two_calls(form, code):
         np.testing.assert_allclose(b, b0, rtol=1e-8, atol=1e-10)
 
 
+@pytest.mark.parametrize("code", [0, 1])
+def test_noalloc_call_captured_in_a_graph(code):
+    """After the first call on a device (the scratch address lookup), the
+    call enqueues only kernels (the problem descriptor goes in by value, the
+    status words are cleared by a kernel): captured in a CUDA graph it
+    replays with new parameters and gives the bits of direct calls."""
+    from pyscaledvecchia_gb300 import _lib
+    lib, torch = _lib.device_ready()
+    prob, theta = _problem(6, 2000, 4, 15)
+    _noalloc_call(prob, theta, code)
+    P = prob.d + 2
+    D = _desc(prob, P, code)
+    th = _lib.to_dev(torch, theta, np.float64)
+    out = torch.empty(1 + P + P * P + prob.q, dtype=torch.float64, device="cuda")
+    info = _lib.new_info(torch)
+    chunk = prob.chunk_tensor(P)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        rc = lib.sv_vecchia_loglik_noalloc(D, _lib.ptr(th), _lib.ptr(prob.X), _lib.ptr(prob.y),
+                                           _lib.ptr(prob.Z), _lib.ptr(prob.rowb), _lib.ptr(prob.kb),
+                                           _lib.ptr(prob.nbr), _lib.ptr(chunk), _lib.ptr(out),
+                                           _lib.ptr(info), _lib.stream_handle(torch))
+    assert rc == 0, lib.sv_status_string(rc)
+    rng = np.random.default_rng(0)
+    for _ in range(3):
+        t = theta + rng.uniform(-0.2, 0.2, theta.shape)
+        th.copy_(torch.from_numpy(t))
+        g.replay()
+        torch.cuda.synchronize()
+        assert int(info.cpu().numpy()[0]) == 0
+        got = out.cpu().numpy()
+        ll, gr, F, b = _noalloc_call(prob, t, code)
+        want = np.concatenate([[ll], gr, F.ravel(), b])
+        np.testing.assert_array_equal(got, want)
+
+
 def test_noalloc_rejects_problems_beyond_the_fixed_scratch():
     from pyscaledvecchia_gb300 import _lib
     lib, torch = _lib.device_ready()
