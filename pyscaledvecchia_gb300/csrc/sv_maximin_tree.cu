@@ -51,6 +51,8 @@ constexpr int kMtLeaf = 32;      // points per leaf, children per node
 struct MtRun {
   int64_t n;
   int d, DV, H, flags;
+  int hdesc;             // the level the descent starts at
+  int hcand;             // the level the candidate rounds start at (0: the rows)
   int64_t first;         // original index of the first row (ordering.py:72)
   const int* first_pos;  // its position in tree order (device word)
   int64_t* order;
@@ -106,7 +108,7 @@ __global__ void __launch_bounds__(kMtThreads, 1) k_maximin_tree(MtRun Q) {
   __shared__ long long Ub[32], w_Kb[kMtWarps], s_Kb, s_top;
   __shared__ int Ui[32], Upos[32], w_Ki[kMtWarps], s_Ki, s_sel[32], piv_slot[32], P_pos[32];
   __shared__ float UB[32], Uthr[32], P_B[32];
-  __shared__ int s_k, s_tie, s_err, s_qn[2], s_nleaf;
+  __shared__ int s_k, s_tie, s_err, s_qn[2];
   const unsigned FULL = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float growth = mc_growth(d);
@@ -186,40 +188,51 @@ __global__ void __launch_bounds__(kMtThreads, 1) k_maximin_tree(MtRun Q) {
     }
   };
 
-  // ---- the 31 largest point keys (slots 0..30, positions Upos) and R
+  // ---- the 31 largest point keys (slots 0..30, positions Upos) and R.
+  //      The first round takes every node of level hc (the lowest level with
+  //      at most 32 nodes per thread), each thread keeping its three largest;
+  //      later rounds the children of the 31 nodes chosen, then their points.
+  //      Whatever a round leaves out is bounded by its Kb (a key left in a
+  //      thread's third place included).
+  const int hc = Q.hcand;
   auto candidates = [&](long long& Rb, int& Ri) {
     Rb = -1LL;
     Ri = kMcNone;
     int nsel = 0;
-    for (int h = H; h >= 0; --h) {
-      long long b = -1LL;
-      int i = kMcNone;
-      int64_t id = -1;
-      if (h == H) {
-        if (threadIdx.x < Q.nn[H]) id = threadIdx.x;
-      } else if (warp < nsel) {
-        id = (int64_t)s_sel[warp] * kMtLeaf + lane;
-        if (id >= (h > 0 ? Q.nn[h] : n)) id = -1;
-      }
-      if (id >= 0) {
-        if (h > 0) {
-          b = __ldcg(Q.kb[h] + id);
-          i = __ldcg(Q.ki[h] + id);
-        } else {
-          const long long bits = dbits(__ldcg(Q.dist + id));
-          if (bits >= 0 && bits < kBitsInf) {
-            b = bits;
-            i = Q.gidx[id];
-          }
+    for (int h = hc; h >= 0; --h) {
+      long long b = -1LL, b2 = -1LL, b3 = -1LL;
+      int i = kMcNone, i2 = kMcNone, i3 = kMcNone;
+      if (h == hc) {
+        for (int64_t id = threadIdx.x; id < Q.nn[h]; id += blockDim.x) {
+          const long long kb = __ldcg(Q.kb[h] + id);
+          if (kb >= 0) mc_insert3(kb, __ldcg(Q.ki[h] + id), b, i, b2, i2, b3, i3);
         }
-        if (b < 0) {
-          b = -1LL;
-          i = kMcNone;
+      } else {
+        int64_t id = -1;
+        if (warp < nsel) {
+          id = (int64_t)s_sel[warp] * kMtLeaf + lane;
+          if (id >= (h > 0 ? Q.nn[h] : n)) id = -1;
+        }
+        if (id >= 0) {
+          if (h > 0) {
+            b = __ldcg(Q.kb[h] + id);
+            i = __ldcg(Q.ki[h] + id);
+          } else {
+            const long long bits = dbits(__ldcg(Q.dist + id));
+            if (bits >= 0 && bits < kBitsInf) {
+              b = bits;
+              i = Q.gidx[id];
+            }
+          }
+          if (b < 0) {
+            b = -1LL;
+            i = kMcNone;
+          }
         }
       }
       long long Kb;
       int Ki;
-      collect(b, i, -1LL, kMcNone, -1LL, kMcNone, Kb, Ki);
+      collect(b, i, b2, i2, b3, i3, Kb, Ki);
       if (mc_greater(Kb, Ki, Rb, Ri)) {
         Rb = Kb;
         Ri = Ki;
@@ -326,12 +339,15 @@ __global__ void __launch_bounds__(kMtThreads, 1) k_maximin_tree(MtRun Q) {
   for (int l = threadIdx.x; l < d; l += blockDim.x) Px[l] = Q.xs[(size_t)P_pos[0] * d + l];
   __syncthreads();
 
+  const int hd = Q.hdesc;
   int64_t nsel = 1;
   while (nsel < n) {
     const int k = s_k;
     // 1. (CTA 0) the pivots are ordered (ordering.py:58) and their leaves
-    //    listed (mask bit 31: to be keyed again, no pivot); the top level's
-    //    items: every top node with every pivot
+    //    listed (mask bit 31: to be keyed again, no pivot); the first items:
+    //    every node of level hd with every pivot (hd: the highest level whose
+    //    nodes times 31 pivots are at most two items per thread of the
+    //    cluster, which saves the barriers of the levels above)
     if (r == 0) {
       if (threadIdx.x < 24) Q.cnt[threadIdx.x] = 0;
       __syncthreads();
@@ -341,17 +357,18 @@ __global__ void __launch_bounds__(kMtThreads, 1) k_maximin_tree(MtRun Q) {
         const int leaf = p / kMtLeaf;
         if (atomicOr(&Q.lmask[leaf], 0x80000000u) == 0u) Q.leaves[atomicAdd(cleaf, 1)] = leaf;
       }
-      for (int e = threadIdx.x; e < (int)Q.nn[H] * k; e += blockDim.x) {
+      for (int e = threadIdx.x; e < (int)Q.nn[hd] * k; e += blockDim.x) {
         Q.q[0][e] = e / k;
         Q.qm[0][e] = (unsigned)(e % k);
       }
-      if (threadIdx.x == 0) cdesc[H] = (int)Q.nn[H] * k;
+      if (threadIdx.x == 0) cdesc[hd] = (int)Q.nn[hd] * k;
     }
     cl.sync();
-    // 2. the descent, a thread per (node, pivot) item; a leaf reached takes
-    //    the pivot into its mask (the first bit puts it on the list)
-    for (int h = H; h >= 1; --h) {
-      const int buf = (H - h) & 1;
+    // 2. the descent from level hd, a thread per (node, pivot) item; a leaf
+    //    reached takes the pivot into its mask (the first bit puts it on the
+    //    list)
+    for (int h = hd; h >= 1; --h) {
+      const int buf = (hd - h) & 1;
       const int nin = __ldcg(cdesc + h);
       for (int64_t e = gt; e < nin; e += gs) {
         const int node = __ldcg(Q.q[buf] + e);
@@ -995,6 +1012,22 @@ int maximin_tree_single(const double* X, int64_t n, int d, int64_t first, int64_
                       (size_t)2 * 32 * DV * 4;
   SV_CUDA_TRY(cudaFuncSetAttribute(k_maximin_tree, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int C = mt_cluster_size(smem);
+  // the descent starts at the lowest level whose nodes times 31 pivots are at
+  // most two items per thread of the cluster, the candidate rounds at the
+  // lowest level of at most 32 nodes per thread (the top level always
+  // qualifies: at most 32 nodes)
+  Q.hdesc = H;
+  for (int h = 1; h <= H; ++h)
+    if (Q.nn[h] * kMcU <= 2LL * C * kMtThreads) {
+      Q.hdesc = h;
+      break;
+    }
+  Q.hcand = H;
+  for (int h = 1; h <= H; ++h)
+    if (Q.nn[h] <= 32LL * kMtThreads) {
+      Q.hcand = h;
+      break;
+    }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)C);
   cfg.blockDim = dim3(kMtThreads);
