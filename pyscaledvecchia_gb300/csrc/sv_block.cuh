@@ -42,12 +42,20 @@ struct MaternMode {
   double nu_p, nu_m;   // nu +- h
   double lc_p, lc_m;   // log_coef at nu +- h
   double inv2h;        // 1 / (2h)
+  const double* tab;   // fixed general nu: the table of M and g (or null)
+  int tab_elo;         // its first octave
+  double s2n;          // sqrt(2 nu)
 };
 
 __device__ __forceinline__ void matern_eval(const MaternMode& mm, double r, double& M, double& g,
                                             double& dMnu, bool want_g) {
   if (mm.closed >= 0) {
     matern_closed(mm.closed, r, M, g);
+    dMnu = 0.0;
+    return;
+  }
+  if (mm.tab && !mm.estimate_nu) {
+    matern_table_Mg(mm.tab, mm.tab_elo, mm.s2n, mm.nu, mm.log_coef, r, M, g, want_g);
     dMnu = 0.0;
     return;
   }

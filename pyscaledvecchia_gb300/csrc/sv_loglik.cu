@@ -34,7 +34,7 @@ namespace sv {
 
 // theta -> per-problem parameters (sigma^2, tau, nu, 1/lambda)
 __global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, int tstride,
-                              int nprob, ProbInfo* out) {
+                              int nprob, ProbInfo* out, const double* mtab, int mtab_elo) {
   const int p = blockIdx.x;
   if (p >= nprob) return;
   const sv_prob_desc& D = descs[p];
@@ -87,9 +87,40 @@ __global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, in
     mm.lc_p = D.estimate_nu ? matern_log_coef(mm.nu_p) : 0.0;
     mm.lc_m = D.estimate_nu ? matern_log_coef(mm.nu_m) : 0.0;
     mm.inv2h = 1.0 / (2.0 * h);
+    // fixed general nu with a table of M and g built for this call
+    mm.tab = (mtab && mm.closed < 0 && !D.estimate_nu) ? mtab : nullptr;
+    mm.tab_elo = mtab_elo;
+    mm.s2n = sqrt(2.0 * nu);
     I.mm = mm;
   }
   for (int l = threadIdx.x; l < d; l += blockDim.x) I.invlam[l] = exp(-th[1 + l]);
+}
+
+// the table of nu (mtab_intervals(elo) intervals x [16 of M, 16 of G]): one
+// CTA of kMtabN threads per interval, node values e^c M(c), e^c G(c) at the
+// Chebyshev points, then their Chebyshev coefficients
+__global__ void k_matern_table(double nu, double log_coef, int elo, double* tab) {
+  __shared__ double fm[kMtabN], fg[kMtabN];
+  const int iv = blockIdx.x, j = threadIdx.x;
+  const int e = elo + iv / 2, half = iv & 1;
+  const double tj = cospi((j + 0.5) / kMtabN);
+  const double m = half ? (tj - kMtabO1) / kMtabS1 : (tj - kMtabO0) / kMtabS0;
+  const double c = ldexp(m, e);
+  double knu, knm1;
+  bessel_k_nu_and_prev(nu, c, knu, knm1);
+  const double sc = exp(c + log_coef + nu * log(c));  // e^c times the prefactor
+  fm[j] = sc * knu;
+  fg[j] = -(2.0 * nu / c) * sc * knm1;
+  __syncthreads();
+  double am = 0.0, ag = 0.0;
+  for (int i = 0; i < kMtabN; ++i) {
+    const double w = cospi((double)j * (i + 0.5) / kMtabN);
+    am = fma(fm[i], w, am);
+    ag = fma(fg[i], w, ag);
+  }
+  const double sc2 = (j == 0 ? 1.0 : 2.0) / kMtabN;
+  tab[(size_t)iv * 2 * kMtabN + j] = am * sc2;
+  tab[(size_t)iv * 2 * kMtabN + kMtabN + j] = ag * sc2;
 }
 
 // the problem table of a one-problem evaluation, passed by value
@@ -774,13 +805,14 @@ namespace {
 struct EvalShape {
   int64_t nprob, nblk, nx, nblk_max;
   int dmax, qmax, Pmax, kmax, need_grad, any_est, precision;
+  double tab_nu;  // one problem of fixed general nu: the nu of its Matern table (0: none)
 };
 
 // reduction grid rows: the partitions of the largest problem
 int red_parts(const EvalShape& S) { return red_parts_n(S.nblk_max); }
 
 struct WsLayout {
-  size_t desc, probs, cache, level, redo, chunk_max, flags, part1, part2, beta, sums, xhl, total;
+  size_t desc, probs, cache, level, redo, chunk_max, flags, part1, part2, beta, sums, xhl, mtab, total;
   int CS, nfmax;
 };
 
@@ -815,6 +847,8 @@ WsLayout ws_layout(const EvalShape& S) {
   off = align256(off + sizeof(double) * (size_t)S.nprob * L.nfmax);
   L.xhl = off;
   if (S.precision == 1 || S.precision == 2) off = align256(off + sizeof(float) * 2 * (size_t)S.nx);
+  L.mtab = off;
+  if (S.tab_nu > 0.0) off = align256(off + sizeof(double) * (size_t)kMtabMaxDoubles);
   L.total = off;
   return L;
 }
@@ -1004,7 +1038,18 @@ int run_eval(const EvalCall& C, cudaStream_t st, const ShardStage* sh = nullptr)
     SV_CUDA_TRY(cudaMemsetAsync(A.flags, 0, 4 * sizeof(int32_t), st));
     if (C.chunked)
       SV_CUDA_TRY(cudaMemsetAsync(A.chunk_max, 0, sizeof(int32_t) * (S.nblk > 0 ? S.nblk : 1), st));
-    k_prob_params<<<(int)S.nprob, 64, 0, st>>>(C.probs, C.theta, C.tstride, (int)S.nprob, probs);
+    double* mtab = nullptr;
+    int elo = 0;
+    if (S.tab_nu > 0.0) {
+      // the Matern table of this call's fixed general nu
+      mtab = (double*)(ws + W.mtab);
+      elo = mtab_elo(S.tab_nu);
+      k_matern_table<<<mtab_intervals(elo), kMtabN, 0, st>>>(S.tab_nu, matern_log_coef(S.tab_nu), elo,
+                                                            mtab);
+      SV_CUDA_TRY(cudaGetLastError());
+    }
+    k_prob_params<<<(int)S.nprob, 64, 0, st>>>(C.probs, C.theta, C.tstride, (int)S.nprob, probs, mtab,
+                                              elo);
     SV_CUDA_TRY(cudaGetLastError());
     if (split && C.nwarp > 0) {
       rc = launch_split_prep(A, S.nx, st);
@@ -1101,6 +1146,11 @@ EvalShape single_shape(const sv_loglik_desc* D) {
   S.need_grad = D->need_grad;
   S.any_est = D->estimate_nu;
   S.precision = D->precision;
+  // a fixed nu without a closed form: its Matern is interpolated from a table
+  S.tab_nu = (!D->estimate_nu && D->nu > 0.0 && matern_closed_code(D->nu) < 0 &&
+              mtab_elo(D->nu) >= kMtabEloMin)
+                 ? D->nu
+                 : 0.0;
   return S;
 }
 
@@ -1117,6 +1167,7 @@ EvalShape batch_shape(const sv_batch_desc* B) {
   S.need_grad = B->need_grad;
   S.any_est = B->any_estimate_nu;
   S.precision = B->precision;
+  S.tab_nu = 0.0;  // problems may differ in nu: the Bessel routine for all
   return S;
 }
 

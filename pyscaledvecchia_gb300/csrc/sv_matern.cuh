@@ -212,6 +212,93 @@ SV_HD void matern_general_Mg(double r, double nu, double log_coef, double& M, do
 
 SV_HD double matern_log_coef(double nu) { return (1.0 - nu) * kLn2 - lgamma(nu); }
 
+// ---------------------------------------------------------------------------
+// Table of the general-smoothness Matern for a fixed nu (no counterpart in
+// the reference, whose _matern_general.py:87-116 calls scipy's kv for every
+// entry).  M(c) and G(c) = g(r) = -(2 nu / c) 2^(1-nu)/Gamma(nu) c^nu
+// K_{nu-1}(c), c = sqrt(2 nu) r, depend on nu alone: for a fixed nu they are
+// interpolated instead of evaluated.  Half-octave intervals [2^e, 2^e sqrt2),
+// [2^e sqrt2, 2^(e+1)) of c from 2^elo (elo = floor(log2(sqrt(2 nu) 1e-7)), the
+// smallest c the r floor lets through) to 2^9; on each, e^c M(c) and e^c G(c)
+// as 16-term Chebyshev series (functions analytic but for c = 0, which lies
+// about six half-widths away: the series converge like 12^-k, far below
+// float64 rounding at 16 terms).  M = e^-c P(t), G = e^-c Q(t), one
+// exponential per entry; c >= 2^9 (M < 1e-220) takes the Bessel routine.
+// ---------------------------------------------------------------------------
+constexpr int kMtabN = 16;       // Chebyshev terms per interval and function
+constexpr int kMtabEhi = 9;      // the table covers c < 2^9
+constexpr int kMtabEloMin = -40; // smaller nu (c floor below 2^-40): no table
+constexpr int kMtabMaxDoubles = 2 * (kMtabEhi - kMtabEloMin) * 2 * kMtabN;
+
+// floor(log2(sqrt(2 nu) * 1e-7)): the table's first octave
+SV_HD int mtab_elo(double nu) {
+  int e = 0;
+  frexp(sqrt(2.0 * nu) * kRFloor, &e);
+  return e - 1;
+}
+SV_HD int mtab_intervals(int elo) { return 2 * (kMtabEhi - elo); }
+
+// t in [-1, 1] on the lower ([1, sqrt2)) and upper ([sqrt2, 2)) half of the
+// octave, from the mantissa m in [1, 2): t = m S + O
+constexpr double kMtabS0 = 4.82842712474619;       // 2 / (sqrt2 - 1)
+constexpr double kMtabO0 = -5.82842712474619;      // -(1 + sqrt2) / (sqrt2 - 1)
+constexpr double kMtabS1 = 3.414213562373095;      // 2 / (2 - sqrt2)
+constexpr double kMtabO1 = -5.82842712474619;      // -(2 + sqrt2) / (2 - sqrt2)
+constexpr long long kMtabSqrt2Bits = 0x3FF6A09E667F3BCDLL;  // bits of sqrt(2)
+
+// M(c) and G(c) by the Bessel routine (c > 0)
+SV_HD void matern_general_MG_c(double c, double nu, double log_coef, double& M, double& G) {
+  double knu, knm1;
+  bessel_k_nu_and_prev(nu, c, knu, knm1);
+  const double pre = exp(log_coef + nu * log(c));
+  M = pre * knu;
+  G = -(2.0 * nu / c) * pre * knm1;
+}
+
+#ifdef __CUDACC__
+__device__ __forceinline__ double mtab_clenshaw(const double* cf, double t) {
+  const double t2 = t + t;
+  double b1 = 0.0, b2 = 0.0;
+#pragma unroll
+  for (int k = kMtabN - 1; k >= 1; --k) {
+    const double b0 = fma(t2, b1, __ldg(cf + k) - b2);
+    b2 = b1;
+    b1 = b0;
+  }
+  return fma(t, b1, __ldg(cf) - b2);
+}
+
+// M and g = G of matern_general_Mg at r from the table (r floored as
+// _matern_general.py:87 does: below 1e-7, M = 1 and g = 0)
+__device__ __forceinline__ void matern_table_Mg(const double* tab, int elo, double s2n, double nu,
+                                                double log_coef, double r, double& M, double& g,
+                                                bool want_g) {
+  if (r < kRFloor) {
+    M = 1.0;
+    g = 0.0;
+    return;
+  }
+  const double c = s2n * r;
+  const long long b = __double_as_longlong(c);
+  const int e = (int)(b >> 52) - 1023;
+  if (e < elo || e >= kMtabEhi) {
+    double G;
+    matern_general_MG_c(c, nu, log_coef, M, G);
+    g = want_g ? G : 0.0;
+    return;
+  }
+  const long long mb = (b & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL;
+  const double m = __longlong_as_double(mb);
+  const int j = mb >= kMtabSqrt2Bits ? 1 : 0;
+  const double t = j ? fma(m, kMtabS1, kMtabO1) : fma(m, kMtabS0, kMtabO0);
+  const double* cf = tab + (size_t)(2 * (e - elo) + j) * (2 * kMtabN);
+  const double ex = exp(-c);
+  M = ex * mtab_clenshaw(cf, t);
+  g = want_g ? ex * mtab_clenshaw(cf + kMtabN, t) : 0.0;
+}
+
+#endif
+
 // nu in {0.5, 1.5, 2.5} -> 0/1/2, else -1
 SV_HD int matern_closed_code(double nu) {
   if (nu == 0.5) return 0;

@@ -59,6 +59,9 @@ __device__ void pred_params(const PredArgs& A, PredPrm* prm) {
     mm.log_coef = A.closed < 0 ? matern_log_coef(A.nu) : 0.0;
     mm.nu_p = mm.nu_m = mm.lc_p = mm.lc_m = 0.0;
     mm.inv2h = 0.0;
+    mm.tab = nullptr;
+    mm.tab_elo = 0;
+    mm.s2n = 0.0;
     prm->mm = mm;
   }
   for (int l = threadIdx.x; l < A.d; l += blockDim.x) prm->invlam[l] = exp(-A.theta[1 + l]);

@@ -1,0 +1,56 @@
+"""The Matern table of a fixed general smoothness (one-problem evaluations,
+sv_vecchia_loglik with nu outside {0.5, 1.5, 2.5}) against the per-entry
+Bessel routine (the batched evaluation, which keeps it for every nu) and the
+oracle (scipy.special.kv, _matern_general.py:87-116 of the reference).
+
+The table interpolates e^c M(c) and e^c g(c), c = sqrt(2 nu) r, by 16-term
+Chebyshev series on half-octave intervals; its error is at the level of
+float64 rounding, so the likelihood, score and Fisher information agree
+with the Bessel routine to about 1e-13 relative."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _problem(seed, n, d, m, nu):
+    from pyscaledvecchia_gb300.ordering import _nn_groups, find_ordered_nn, maximin_order
+    rng = np.random.default_rng(seed)
+    X = rng.random((n, d))
+    y = np.sin(3 * X[:, 0]) + X[:, 1] ** 2 + 0.1 * rng.standard_normal(n)
+    lam = np.exp(rng.uniform(math.log(0.05), math.log(2.0), d))
+    theta = np.concatenate([[math.log(1.3)], np.log(lam), [math.log(2e-3)]])
+    order = maximin_order(X / lam)
+    nn = find_ordered_nn((X / lam)[order], m)
+    return X[order], y[order], np.ones((n, 1)), _nn_groups(nn, m), theta
+
+
+@pytest.mark.parametrize("nu", [0.3, 0.8, 1.75, 3.2])
+def test_table_matches_the_bessel_routine(nu):
+    from pyscaledvecchia_gb300.batched import BatchedLikelihood, BatchProblem
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    Xo, yo, Zo, groups, theta = _problem(3, 4000, 4, 25, nu)
+    ll_t, g_t, F_t, b_t = DeviceProblem(Xo, yo, Zo, groups).evaluate(theta, nu)
+    BL = BatchedLikelihood([BatchProblem(Xo, yo, Zo, groups, nu=nu)])
+    st, ll_b, g_b, F_b, b_b = BL.evaluate([theta])[0]
+    assert st == 0
+    assert abs(ll_t - ll_b) <= 1e-12 * abs(ll_b), (ll_t, ll_b)
+    np.testing.assert_allclose(g_t, g_b, rtol=1e-10, atol=1e-11 * np.abs(g_b).max())
+    np.testing.assert_allclose(F_t, F_b, rtol=1e-10, atol=1e-11 * np.abs(F_b).max())
+    np.testing.assert_allclose(b_t, b_b, rtol=1e-11, atol=1e-13)
+
+
+def test_table_against_the_oracle():
+    """scipy's kv through the oracle at nu = 0.8 (the benchmark's general
+    smoothness), a small problem."""
+    from oracle import oracle
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    nu = 0.8
+    Xo, yo, Zo, groups, theta = _problem(4, 600, 3, 15, nu)
+    ll, g, F, b = DeviceProblem(Xo, yo, Zo, groups).evaluate(theta, nu)
+    ll_o, g_o, F_o, b_o = oracle.vecchia_loglik_np(theta, Xo, yo, Zo, groups, nu)[:4]
+    assert abs(ll - ll_o) <= 1e-10 * abs(ll_o), (ll, ll_o)
+    np.testing.assert_allclose(g, g_o, rtol=1e-8, atol=1e-8 * np.abs(g_o).max())
+    np.testing.assert_allclose(F, F_o, rtol=1e-8, atol=1e-8 * np.abs(F_o).max())
