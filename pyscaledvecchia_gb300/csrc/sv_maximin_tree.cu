@@ -53,6 +53,7 @@ struct MtRun {
   int d, DV, H, flags;
   int hdesc;             // the level the descent starts at
   int hcand;             // the level the candidate rounds start at (0: the rows)
+  int cdist;             // the first candidate round split over the cluster's CTAs
   int64_t first;         // original index of the first row (ordering.py:72)
   const int* first_pos;  // its position in tree order (device word)
   int64_t* order;
@@ -74,6 +75,10 @@ struct MtRun {
   int* q[2];                          // queues of nodes, 32 nn[1] entries each
   unsigned* qm[2];                    // with a pivot index (descent) or mask
   int* cnt;                           // [24] counters of the cluster's queues
+  long long* cl_b;                    // [16][32] each CTA's largest keys of level hcand
+  int* cl_i;
+  long long* cl_Kb;                   // [16] and the bound of the rest
+  int* cl_Ki;
   int* leaves;                        // [nn[1]] leaves reached by a pass
   unsigned* lmask;                    // [nn[1]] their pivot masks (zero between passes)
 };
@@ -195,6 +200,7 @@ __global__ void __launch_bounds__(kMtThreads, 1) k_maximin_tree(MtRun Q) {
   //      Whatever a round leaves out is bounded by its Kb (a key left in a
   //      thread's third place included).
   const int hc = Q.hcand;
+  const int ncta = (int)cg::this_cluster().num_blocks();
   auto candidates = [&](long long& Rb, int& Ri) {
     Rb = -1LL;
     Ri = kMcNone;
@@ -202,7 +208,17 @@ __global__ void __launch_bounds__(kMtThreads, 1) k_maximin_tree(MtRun Q) {
     for (int h = hc; h >= 0; --h) {
       long long b = -1LL, b2 = -1LL, b3 = -1LL;
       int i = kMcNone, i2 = kMcNone, i3 = kMcNone;
-      if (h == hc) {
+      if (h == hc && Q.cdist) {
+        // the CTAs' lists of this round (step 5a): warp w merges CTA w's
+        if (warp < ncta) {
+          b = __ldcg(Q.cl_b + warp * 32 + lane);
+          i = __ldcg(Q.cl_i + warp * 32 + lane);
+          if (lane == 0) {
+            b3 = __ldcg(Q.cl_Kb + warp);
+            i3 = __ldcg(Q.cl_Ki + warp);
+          }
+        }
+      } else if (h == hc) {
         for (int64_t id = threadIdx.x; id < Q.nn[h]; id += blockDim.x) {
           const long long kb = __ldcg(Q.kb[h] + id);
           if (kb >= 0) mc_insert3(kb, __ldcg(Q.ki[h] + id), b, i, b2, i2, b3, i3);
@@ -496,6 +512,30 @@ __global__ void __launch_bounds__(kMtThreads, 1) k_maximin_tree(MtRun Q) {
       cl.sync();
     }
 
+    if (Q.cdist) {
+      // 5a. the first candidate round, every node of level hc, split over
+      //     the CTAs: each keeps its 32 largest keys and the bound of the rest
+      const int64_t per = (Q.nn[hc] + C - 1) / C;
+      const int64_t i0 = (int64_t)r * per, i1 = min(i0 + per, Q.nn[hc]);
+      long long b1 = -1LL, b2 = -1LL, b3 = -1LL;
+      int x1 = kMcNone, x2 = kMcNone, x3 = kMcNone;
+      for (int64_t id = i0 + threadIdx.x; id < i1; id += blockDim.x) {
+        const long long kb = __ldcg(Q.kb[hc] + id);
+        if (kb >= 0) mc_insert3(kb, __ldcg(Q.ki[hc] + id), b1, x1, b2, x2, b3, x3);
+      }
+      long long Kb;
+      int Ki;
+      collect(b1, x1, b2, x2, b3, x3, Kb, Ki);
+      if (threadIdx.x < 32) {
+        Q.cl_b[r * 32 + threadIdx.x] = Ub[threadIdx.x];
+        Q.cl_i[r * 32 + threadIdx.x] = Ui[threadIdx.x];
+      }
+      if (threadIdx.x == 0) {
+        Q.cl_Kb[r] = Kb;
+        Q.cl_Ki[r] = Ki;
+      }
+      cl.sync();
+    }
     if (r == 0) {
       // 5. candidates U = slots 0..30; R bounds every other point's bits
       long long R;
@@ -877,6 +917,7 @@ size_t maximin_tree_workspace_bytes(int64_t n, int d) {
   b += 4 * mt_align(4 * 32 * (size_t)nn[1]);   // queues and their pivots / masks
   b += 2 * mt_align(4 * (size_t)nn[1]);        // leaf list and leaf masks
   b += mt_align(4 * 24);                       // queue counters
+  b += 4 * mt_align(16 * 32 * 8);              // the CTAs' candidate lists
   b += 256;                                    // first position
   return b;
 }
@@ -954,6 +995,10 @@ int maximin_tree_single(const double* X, int64_t n, int d, int64_t first, int64_
   }
   Q.leaves = (int*)take(4 * (size_t)Q.nn[1]);
   int* mt_cnt = (int*)take(4 * 24);
+  Q.cl_b = (long long*)take(16 * 32 * 8);
+  Q.cl_i = (int*)take(16 * 32 * 8);
+  Q.cl_Kb = (long long*)take(16 * 32 * 8);
+  Q.cl_Ki = (int*)take(16 * 32 * 8);
   Q.lmask = (unsigned*)take(4 * (size_t)Q.nn[1]);
   int* first_pos = (int*)take(4);
   if (off > ws_bytes) return SV_ENOSPC;
@@ -1028,6 +1073,9 @@ int maximin_tree_single(const double* X, int64_t n, int d, int64_t first, int64_
       Q.hcand = h;
       break;
     }
+  // with more than 8 nodes per thread there, the first round is split over
+  // the cluster (one more barrier per pass)
+  Q.cdist = (C > 1 && Q.nn[Q.hcand] > 8LL * kMtThreads) ? 1 : 0;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)C);
   cfg.blockDim = dim3(kMtThreads);
