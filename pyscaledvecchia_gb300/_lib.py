@@ -47,7 +47,7 @@ class BatchDesc(ctypes.Structure):
                 ("nx", c_i64), ("dmax", c_i32), ("qmax", c_i32), ("kmax", c_i32),
                 ("ldnbr", c_i32), ("need_grad", c_i32), ("any_estimate_nu", c_i32),
                 ("chunked", c_i32), ("precision", c_i32), ("team_lanes", c_i32),
-                ("theta_stride", c_i32), ("out_stride", c_i32), ("pad", c_i32),
+                ("theta_stride", c_i32), ("out_stride", c_i32), ("general_nu", c_i32),
                 ("split_rho_min", c_dbl), ("nblk_max", c_i64)]
 
 

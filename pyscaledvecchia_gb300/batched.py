@@ -12,6 +12,7 @@ at different times.
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass
 from typing import Optional
 
@@ -21,6 +22,18 @@ from . import _lib
 from ._covariance import _check_nu
 from .likelihood import _PRECISION, _SPLIT, _WARP_K, chunk_ids, pack_groups
 from .ordering import _nn_groups
+
+_POOL = None
+
+
+def _host_pool():
+    """Worker threads for per-problem host arithmetic (numpy), created once."""
+    global _POOL
+    if _POOL is None:
+        import concurrent.futures as cf
+        _POOL = cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)))
+    return _POOL
+
 
 __all__ = ["BatchProblem", "BatchedLikelihood", "ordered_groups"]
 
@@ -88,7 +101,7 @@ class BatchedLikelihood:
     """
 
     def __init__(self, problems, need_grad=True, chunked=True, precisions=("float64",),
-                 team_lanes=0, split_rho_min=0.0):
+                 team_lanes=0, split_rho_min=0.0, matern_tables=True):
         for pr in precisions:
             if pr not in _PRECISION:
                 raise ValueError("precision must be 'float64', 'split' or 'split_df'")
@@ -139,6 +152,12 @@ class BatchedLikelihood:
         self.dmax = int(self.d.max())
         self.qmax = int(self.q.max())
         self.any_est = bool(self.estimate_nu.any())
+        # a fixed nu without a closed form in some problem: the evaluation
+        # interpolates its Matern from a per-problem table
+        # (matern_tables=False keeps the per-entry Bessel routine: the check
+        # of the tables)
+        self.general_nu = matern_tables and any(
+            not pr.estimate_nu and float(pr.nu) not in (0.5, 1.5, 2.5) for pr in problems)
         self.Pmax = self.dmax + 2 + (1 if self.any_est else 0)
         self.ostride = 1 + self.Pmax + self.Pmax * self.Pmax + self.qmax
 
@@ -235,7 +254,8 @@ class BatchedLikelihood:
             Bd.dmax, Bd.qmax, Bd.kmax, Bd.ldnbr = self.dmax, self.qmax, self.kmax, self.ldnbr
             Bd.need_grad, Bd.any_estimate_nu, Bd.chunked = int(self.need_grad), int(self.any_est), int(self.chunked)
             Bd.precision, Bd.team_lanes = _PRECISION[prec], self._lanes[prec]
-            Bd.theta_stride, Bd.out_stride, Bd.pad = self.Pmax, self.ostride, 0
+            Bd.theta_stride, Bd.out_stride = self.Pmax, self.ostride
+            Bd.general_nu = int(self.general_nu)
             Bd.split_rho_min = self.split_rho_min
             Bd.nblk_max = int(self.nblk.max())
             wsb = max(wsb, int(lib.sv_loglik_batched_workspace_bytes(Bd)))
@@ -359,14 +379,24 @@ class BatchedLikelihood:
             return [] if return_orders else None
         probs = (_lib.ReorderProb * len(ids))()
         ranges = np.ones((len(ids), self.dmax), dtype=np.float64)
-        for j, i in enumerate(ids):
+        for i in ids:
             if not self.device_reorderable(i):
                 raise ValueError(f"problem {i} is too large for the batched maximin")
+
+        def first_row(j):
+            i = ids[j]
             d = int(self.d[i])
-            th = np.asarray(thetas[j], dtype=float)
-            r = np.exp(th[1:1 + d])                      # gp.py:183
-            Xs = self._Xe_host[i] / r                    # gp.py:184
-            first = int(np.argmin(((Xs - Xs.mean(0)) ** 2).sum(1)))  # ordering.py:72
+            r = np.exp(np.asarray(thetas[j], dtype=float)[1:1 + d])  # gp.py:183
+            Xs = self._Xe_host[i] / r                                # gp.py:184
+            return r, int(np.argmin(((Xs - Xs.mean(0)) ** 2).sum(1)))  # ordering.py:72
+
+        # the host's share (numpy, which releases the interpreter lock in
+        # these array operations): the problems' first rows side by side
+        firsts = list(_host_pool().map(first_row, range(len(ids)))) if len(ids) > 1 \
+            else [first_row(0)]
+        for j, i in enumerate(ids):
+            d = int(self.d[i])
+            r, first = firsts[j]
             ranges[j, :d] = r
             P = probs[j]
             P.n, P.xe_off, P.ye_off, P.ze_off = int(self.n[i]), int(self.x_off[i]), int(self.y_off[i]), int(self.z_off[i])

@@ -32,9 +32,16 @@
 
 namespace sv {
 
+// whether problem D interpolates its Matern from a table: a fixed nu without
+// a closed form whose floor octave the table reaches
+__device__ __forceinline__ bool uses_matern_table(const sv_prob_desc& D) {
+  return !D.estimate_nu && D.nu > 0.0 && matern_closed_code(D.nu) < 0 &&
+         mtab_elo(D.nu) >= kMtabEloMin;
+}
+
 // theta -> per-problem parameters (sigma^2, tau, nu, 1/lambda)
 __global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, int tstride,
-                              int nprob, ProbInfo* out, const double* mtab, int mtab_elo) {
+                              int nprob, ProbInfo* out, const double* mtabs) {
   const int p = blockIdx.x;
   if (p >= nprob) return;
   const sv_prob_desc& D = descs[p];
@@ -87,21 +94,28 @@ __global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, in
     mm.lc_p = D.estimate_nu ? matern_log_coef(mm.nu_p) : 0.0;
     mm.lc_m = D.estimate_nu ? matern_log_coef(mm.nu_m) : 0.0;
     mm.inv2h = 1.0 / (2.0 * h);
-    // fixed general nu with a table of M and g built for this call
-    mm.tab = (mtab && mm.closed < 0 && !D.estimate_nu) ? mtab : nullptr;
-    mm.tab_elo = mtab_elo;
+    // fixed general nu: M and g from the table built for this call
+    mm.tab = (mtabs && uses_matern_table(D)) ? mtabs + (size_t)p * kMtabMaxDoubles : nullptr;
+    mm.tab_elo = mm.tab ? mtab_elo(nu) : 0;
     mm.s2n = sqrt(2.0 * nu);
     I.mm = mm;
   }
   for (int l = threadIdx.x; l < d; l += blockDim.x) I.invlam[l] = exp(-th[1 + l]);
 }
 
-// the table of nu (mtab_intervals(elo) intervals x [16 of M, 16 of G]): one
-// CTA of kMtabN threads per interval, node values e^c M(c), e^c G(c) at the
-// Chebyshev points, then their Chebyshev coefficients
-__global__ void k_matern_table(double nu, double log_coef, int elo, double* tab) {
+// the Matern tables of the problems that use one (kMtabMaxDoubles each, at
+// problem p's slot): CTA (interval, p) of kMtabN threads takes the node values
+// e^c M(c), e^c G(c) at the interval's Chebyshev points, then their
+// Chebyshev coefficients ([16 of M, 16 of G] per interval)
+__global__ void k_matern_tables(const sv_prob_desc* descs, double* tabs) {
   __shared__ double fm[kMtabN], fg[kMtabN];
+  const sv_prob_desc& D = descs[blockIdx.y];
+  if (!uses_matern_table(D)) return;
+  const double nu = D.nu;
+  const int elo = mtab_elo(nu);
   const int iv = blockIdx.x, j = threadIdx.x;
+  if (iv >= mtab_intervals(elo)) return;
+  const double log_coef = matern_log_coef(nu);
   const int e = elo + iv / 2, half = iv & 1;
   const double tj = cospi((j + 0.5) / kMtabN);
   const double m = half ? (tj - kMtabO1) / kMtabS1 : (tj - kMtabO0) / kMtabS0;
@@ -119,6 +133,7 @@ __global__ void k_matern_table(double nu, double log_coef, int elo, double* tab)
     ag = fma(fg[i], w, ag);
   }
   const double sc2 = (j == 0 ? 1.0 : 2.0) / kMtabN;
+  double* tab = tabs + (size_t)blockIdx.y * kMtabMaxDoubles;
   tab[(size_t)iv * 2 * kMtabN + j] = am * sc2;
   tab[(size_t)iv * 2 * kMtabN + kMtabN + j] = ag * sc2;
 }
@@ -805,7 +820,7 @@ namespace {
 struct EvalShape {
   int64_t nprob, nblk, nx, nblk_max;
   int dmax, qmax, Pmax, kmax, need_grad, any_est, precision;
-  double tab_nu;  // one problem of fixed general nu: the nu of its Matern table (0: none)
+  int tabs;  // a Matern table per problem (problems of fixed general nu fill theirs)
 };
 
 // reduction grid rows: the partitions of the largest problem
@@ -848,7 +863,7 @@ WsLayout ws_layout(const EvalShape& S) {
   L.xhl = off;
   if (S.precision == 1 || S.precision == 2) off = align256(off + sizeof(float) * 2 * (size_t)S.nx);
   L.mtab = off;
-  if (S.tab_nu > 0.0) off = align256(off + sizeof(double) * (size_t)kMtabMaxDoubles);
+  if (S.tabs) off = align256(off + sizeof(double) * (size_t)kMtabMaxDoubles * (size_t)S.nprob);
   L.total = off;
   return L;
 }
@@ -1038,18 +1053,15 @@ int run_eval(const EvalCall& C, cudaStream_t st, const ShardStage* sh = nullptr)
     SV_CUDA_TRY(cudaMemsetAsync(A.flags, 0, 4 * sizeof(int32_t), st));
     if (C.chunked)
       SV_CUDA_TRY(cudaMemsetAsync(A.chunk_max, 0, sizeof(int32_t) * (S.nblk > 0 ? S.nblk : 1), st));
-    double* mtab = nullptr;
-    int elo = 0;
-    if (S.tab_nu > 0.0) {
-      // the Matern table of this call's fixed general nu
-      mtab = (double*)(ws + W.mtab);
-      elo = mtab_elo(S.tab_nu);
-      k_matern_table<<<mtab_intervals(elo), kMtabN, 0, st>>>(S.tab_nu, matern_log_coef(S.tab_nu), elo,
-                                                            mtab);
+    double* mtabs = nullptr;
+    if (S.tabs) {
+      // the Matern tables of the problems of fixed general nu
+      mtabs = (double*)(ws + W.mtab);
+      k_matern_tables<<<dim3(2 * (kMtabEhi - kMtabEloMin), (unsigned)S.nprob), kMtabN, 0, st>>>(C.probs,
+                                                                                               mtabs);
       SV_CUDA_TRY(cudaGetLastError());
     }
-    k_prob_params<<<(int)S.nprob, 64, 0, st>>>(C.probs, C.theta, C.tstride, (int)S.nprob, probs, mtab,
-                                              elo);
+    k_prob_params<<<(int)S.nprob, 64, 0, st>>>(C.probs, C.theta, C.tstride, (int)S.nprob, probs, mtabs);
     SV_CUDA_TRY(cudaGetLastError());
     if (split && C.nwarp > 0) {
       rc = launch_split_prep(A, S.nx, st);
@@ -1147,10 +1159,10 @@ EvalShape single_shape(const sv_loglik_desc* D) {
   S.any_est = D->estimate_nu;
   S.precision = D->precision;
   // a fixed nu without a closed form: its Matern is interpolated from a table
-  S.tab_nu = (!D->estimate_nu && D->nu > 0.0 && matern_closed_code(D->nu) < 0 &&
-              mtab_elo(D->nu) >= kMtabEloMin)
-                 ? D->nu
-                 : 0.0;
+  S.tabs = (!D->estimate_nu && D->nu > 0.0 && matern_closed_code(D->nu) < 0 &&
+            mtab_elo(D->nu) >= kMtabEloMin)
+               ? 1
+               : 0;
   return S;
 }
 
@@ -1167,7 +1179,7 @@ EvalShape batch_shape(const sv_batch_desc* B) {
   S.need_grad = B->need_grad;
   S.any_est = B->any_estimate_nu;
   S.precision = B->precision;
-  S.tab_nu = 0.0;  // problems may differ in nu: the Bessel routine for all
+  S.tabs = B->general_nu ? 1 : 0;
   return S;
 }
 

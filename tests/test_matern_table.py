@@ -1,7 +1,8 @@
-"""The Matern table of a fixed general smoothness (one-problem evaluations,
-sv_vecchia_loglik with nu outside {0.5, 1.5, 2.5}) against the per-entry
-Bessel routine (the batched evaluation, which keeps it for every nu) and the
-oracle (scipy.special.kv, _matern_general.py:87-116 of the reference).
+"""The Matern table of a fixed general smoothness (nu outside {0.5, 1.5,
+2.5}) against the per-entry Bessel routine (a batched evaluation built with
+matern_tables=False) and the oracle (scipy.special.kv,
+_matern_general.py:87-116 of the reference); batched evaluations with tables
+equal the one-problem evaluation bit for bit.
 
 The table interpolates e^c M(c) and e^c g(c), c = sqrt(2 nu) r, by 16-term
 Chebyshev series on half-octave intervals; its error is at the level of
@@ -33,7 +34,12 @@ def test_table_matches_the_bessel_routine(nu):
     from pyscaledvecchia_gb300.likelihood import DeviceProblem
     Xo, yo, Zo, groups, theta = _problem(3, 4000, 4, 25, nu)
     ll_t, g_t, F_t, b_t = DeviceProblem(Xo, yo, Zo, groups).evaluate(theta, nu)
-    BL = BatchedLikelihood([BatchProblem(Xo, yo, Zo, groups, nu=nu)])
+    BT = BatchedLikelihood([BatchProblem(Xo, yo, Zo, groups, nu=nu)])
+    st, ll_2, g_2, F_2, b_2 = BT.evaluate([theta])[0]
+    assert st == 0 and ll_2 == ll_t
+    np.testing.assert_array_equal(g_2, g_t)
+    np.testing.assert_array_equal(F_2, F_t)
+    BL = BatchedLikelihood([BatchProblem(Xo, yo, Zo, groups, nu=nu)], matern_tables=False)
     st, ll_b, g_b, F_b, b_b = BL.evaluate([theta])[0]
     assert st == 0
     assert abs(ll_t - ll_b) <= 1e-12 * abs(ll_b), (ll_t, ll_b)
