@@ -365,14 +365,18 @@ class BatchedLikelihood:
             self._max_rows[d] = int(self.lib.sv_maximin_cluster_max_rows(d))
         return int(self.n[i]) <= self._max_rows[d]
 
-    def reorder(self, ids, thetas, return_orders=False, maximin_flags=0):
+    def reorder(self, ids, thetas, return_orders=False, maximin_flags=0, stream=None,
+                deferred=False):
         """Rebuild the Vecchia structure of problems ``ids`` at their
         parameters (gp.py:182-191) on the device: scaled inputs, maximin
         order, reordered X/y/Z and neighbour columns.  ``thetas[j]`` belongs
         to ``ids[j]``.  Returns the orders (list of int64 arrays) on request.
         maximin_flags are test aids that give the same orders by other
         routes: 1 ranks every choice of pivot by exact square roots, 2 takes
-        one pivot per pass by a full scan of the problem's points."""
+        one pivot per pass by a full scan of the problem's points.
+        stream: the CUDA stream of the work (default: the current one);
+        deferred: return at once a function that waits for the work and
+        checks its status (the problems' buffers must not be read before)."""
         lib, torch = self.lib, self.torch
         ids = [int(i) for i in ids]
         if not ids:
@@ -411,12 +415,24 @@ class BatchedLikelihood:
         if self._ro_ws is None or self._ro_ws.numel() < nbytes:
             self._ro_ws = _lib.workspace(torch, nbytes)
         P_ = _lib.ptr
+        sh = ctypes.c_void_p(stream.cuda_stream) if stream is not None else _lib.stream_handle(torch)
         rc = lib.sv_reorder_batched(D, ctypes.cast(probs, ctypes.c_void_p),
                                     ranges.ctypes.data_as(ctypes.c_void_p), P_(self.Xe), P_(self.ye),
                                     P_(self.Ze), P_(self.X), P_(self.y), P_(self.Z), P_(self.nbr),
                                     P_(self._ro_order), P_(self._ro_info), P_(self._ro_ws),
-                                    self._ro_ws.numel(), _lib.stream_handle(torch))
+                                    self._ro_ws.numel(), sh)
         _lib.check(lib, rc, "sv_reorder_batched")
+        if deferred:
+            done = torch.cuda.Event()
+            done.record(stream if stream is not None else torch.cuda.current_stream())
+            nids = len(ids)
+
+            def finish():
+                done.synchronize()
+                inf = self._ro_info[:nids].cpu().numpy()
+                for j in range(nids):
+                    _lib.check_info(lib, inf[j], "sv_reorder_batched")
+            return finish
         info = self._ro_info[:len(ids)].cpu().numpy()
         for j in range(len(ids)):
             _lib.check_info(lib, info[j], "sv_reorder_batched")

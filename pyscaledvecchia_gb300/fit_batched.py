@@ -60,7 +60,7 @@ class _Fit:
 
 def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=None,
                 warm_start=None, warm_judge=False, team_lanes=0, polish_iter=5, verbose=False,
-                stats=None):
+                stats=None, overlap_reorders=True):
     """Fit ``models[i]`` to ``(Xs[i], ys[i])`` for every i, together.
 
     models : ScaledVecchiaGP instances (each keeps its own settings)
@@ -86,6 +86,11 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
     stats : optional dict that receives the schedule's counters (rounds,
             batched launches, reorder calls, seconds in each part) and the
             batch itself under "batch" (for diagnostics)
+    overlap_reorders : rebuild the problems that asked for a reorder on a
+            side stream while the others' evaluation round runs; they join
+            the next round.  Every problem takes the same steps either way
+            (its own evaluations and reorders in its own order), so the
+            fitted parameters are the same bit for bit
     Returns the list of fitted models.  Per-model counters are left in
     ``model.fit_stats_`` (objective evaluations per precision).
     """
@@ -129,15 +134,26 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
     BL.set_sources([f.st["Xe"] for f in fits], [f.st["ye"] for f in fits],
                    [f.st["Ze"] for f in fits], [f.st["m"] for f in fits])
 
-    def rebuild(ids, thetas):
+    import torch
+    side = torch.cuda.Stream() if overlap_reorders else None
+
+    def rebuild(ids, thetas, deferred=False):
         """gp.py:182-191 for several fits: one batched device call for the
-        problems that fit a cluster, the one-problem path for the rest."""
+        problems that fit a cluster, the one-problem path for the rest.
+        deferred: the device call on the side stream, returned unfinished
+        (a function that waits for it), or None when there was none."""
         t0 = time.perf_counter()
         cnt["reorder_calls"] += 1
         cnt["reordered_problems"] += len(ids)
         dev = [(i, th) for i, th in zip(ids, thetas) if BL.device_reorderable(i)]
+        finish = None
         if dev:
-            BL.reorder([i for i, _ in dev], [th for _, th in dev])
+            if deferred:
+                side.wait_stream(torch.cuda.current_stream())
+                finish = BL.reorder([i for i, _ in dev], [th for _, th in dev], stream=side,
+                                    deferred=True)
+            else:
+                BL.reorder([i for i, _ in dev], [th for _, th in dev])
         for i, th in zip(ids, thetas):
             if BL.device_reorderable(i):
                 continue
@@ -145,6 +161,7 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
             order, groups = f.model._order_and_neighbours(f.st["Xe"], th, f.d, f.st["m"])
             BL.update_problem(i, f.st["Xe"][order], f.st["ye"][order], f.st["Ze"][order], groups)
         cnt["t_reorder"] += time.perf_counter() - t0
+        return finish
 
     rebuild(list(range(len(fits))), [f.st["theta0"] for f in fits])
     if graphs:
@@ -177,10 +194,12 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
                 f.result = (theta, ll, beta)
 
     nprob = len(fits)
+    inflight = None  # (fits being rebuilt on the side stream, the wait for it)
     while True:
         # reorder requests (gp.py:211-221): the ones whose ranges moved are
-        # rebuilt together in one batched call
-        while True:
+        # rebuilt together in one batched call (on the side stream, those
+        # fits sitting out this round, when overlap_reorders)
+        while inflight is None:
             req = [i for i, f in enumerate(fits) if f.msg is not None and f.msg[0] == "reorder"]
             if not req:
                 break
@@ -196,11 +215,29 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
                 ths.append(th)
                 f.last_ranges = r.copy()
             if todo:
+                if overlap_reorders:
+                    finish = rebuild(todo, ths, deferred=True)
+                    inflight = (todo, finish)
+                    break
                 rebuild(todo, ths)
                 for i in todo:
                     advance(fits[i], True)
-        pend = [i for i, f in enumerate(fits) if f.msg is not None]
+        waiting = set(inflight[0]) if inflight is not None else set()
+        pend = [i for i, f in enumerate(fits)
+                if f.msg is not None and f.msg[0] != "reorder" and i not in waiting]
         if not pend:
+            if inflight is not None:
+                todo, finish = inflight
+                inflight = None
+                t0 = time.perf_counter()
+                if finish is not None:
+                    finish()
+                cnt["t_reorder"] += time.perf_counter() - t0
+                for i in todo:
+                    advance(fits[i], True)
+                continue
+            if any(f.msg is not None for f in fits):
+                continue
             break
         thetas = [None] * nprob
         masks = {p: np.zeros(nprob, dtype=bool) for p in precs}
@@ -231,6 +268,16 @@ def fit_batched(models, Xs, ys, *, precision="split", graphs=True, init_thetas=N
                 _lib.check_info(BL.lib, info[i], "sv_vecchia_loglik_batched")
             g, M = f.model._freeze_nugget(g, M)
             advance(f, (ll, g, M, beta))
+        if inflight is not None:
+            # the side stream's rebuild: its fits take the next round
+            todo, finish = inflight
+            inflight = None
+            t0 = time.perf_counter()
+            if finish is not None:
+                finish()
+            cnt["t_reorder"] += time.perf_counter() - t0
+            for i in todo:
+                advance(fits[i], True)
 
     cnt["t_total"] = time.perf_counter() - t_start
     cnt["t_host"] = cnt["t_total"] - cnt["t_setup"] - cnt["t_reorder"] - cnt["t_eval"]
