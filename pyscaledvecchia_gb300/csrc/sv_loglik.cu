@@ -1013,8 +1013,9 @@ int run_eval(const EvalCall& C, cudaStream_t st, const ShardStage* sh = nullptr)
   }
 
   // split forms (1: float64 factorisation, 2: double-float factorisation):
-  // closed-form nu for every problem and at most 32 right-hand sides
-  // (d + q <= 29); anything else runs the float64 kernels
+  // no estimated nu and at most 32 right-hand sides (d + q <= 29); anything
+  // else runs the float64 kernels.  In a batch, the blocks of a problem whose
+  // nu has no closed form are sent by the split kernels to the float64 pass
   const bool split = (S.precision == 1 || S.precision == 2) && !S.any_est && A.NRmax <= 32;
   // 16 lanes per block is the fastest team width measured for every K from 6
   // to 31 (d = 3 and 10); 8 and 32 trail by up to 37 % and 12 %
@@ -1157,7 +1158,9 @@ EvalShape single_shape(const sv_loglik_desc* D) {
   S.kmax = D->kmax;
   S.need_grad = D->need_grad;
   S.any_est = D->estimate_nu;
-  S.precision = D->precision;
+  // the split forms assemble in float32 only the closed forms (nu 0.5, 1.5,
+  // 2.5); a problem with another nu runs the float64 kernels directly
+  S.precision = (D->estimate_nu || matern_closed_code(D->nu) < 0) ? 0 : D->precision;
   // a fixed nu without a closed form: its Matern is interpolated from a table
   S.tabs = (!D->estimate_nu && D->nu > 0.0 && matern_closed_code(D->nu) < 0 &&
             mtab_elo(D->nu) >= kMtabEloMin)

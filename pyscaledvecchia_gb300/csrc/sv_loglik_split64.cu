@@ -169,9 +169,10 @@ __global__ void __launch_bounds__(kS64MaxThreads, 1) k_block_split64(LikArgs A, 
     const float2* XH = A.xhl + PI.x_off;
     int32_t* info = A.info + 4 * pid;
     // scale inside [1e-30, 1e30] and data below 1e30 in magnitude keep every
-    // float32 quantity inside float32's exponent range; other blocks go to
-    // the float64 pass
-    bool range_ok = dbits(diag) > kBitsTiny && dbits(diag) < kBitsHuge;
+    // float32 quantity inside float32's exponent range; other blocks, and
+    // the blocks of a problem whose nu has no float32 form here, go to the
+    // float64 pass
+    bool range_ok = code >= 0 && dbits(diag) > kBitsTiny && dbits(diag) < kBitsHuge;
 
     // ---- gather: neighbours first, self last; coordinates centred on self
     if (active)

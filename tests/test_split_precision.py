@@ -139,3 +139,36 @@ def test_split_against_oracle(oracle, lanes):
     assert e_g <= 1e-3, e_g
     assert e_F <= 1e-5, e_F
     assert e_b <= 1e-4, e_b
+
+
+@pytest.mark.parametrize("form", SPLIT_FORMS)
+def test_split_general_nu_runs_float64(form):
+    """The split forms assemble in float32 only the closed forms (nu 0.5,
+    1.5, 2.5).  A one-problem call with another nu runs the float64 kernels
+    (the result is the float64 form's bit for bit); in a batch, the split
+    kernels send that problem's blocks to the float64 pass, counted as
+    redone, while a closed-form problem beside it stays in the split form."""
+    from pyscaledvecchia_gb300.batched import BatchedLikelihood, BatchProblem
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    from pyscaledvecchia_gb300.ordering import _nn_groups
+    Xo, y, Z, nn, theta = _inputs(3000, 4, 20, 1e-3, seed=77)
+    groups = _nn_groups(nn, 20)
+    prob = DeviceProblem(Xo, y, Z, groups)
+    a = prob.evaluate(theta, 0.8)
+    b = prob.evaluate(theta, 0.8, precision=form)
+    assert b[0] == a[0]
+    for u, v in zip(a[1:], b[1:]):
+        np.testing.assert_array_equal(u, v)
+    c25 = prob.evaluate(theta, 2.5)
+    BL = BatchedLikelihood([BatchProblem(Xo, y, Z, groups, nu=0.8),
+                            BatchProblem(Xo, y, Z, groups, nu=2.5)], precisions=(form,))
+    (s1, ll1, g1, F1, b1), (s2, ll2, g2, F2, b2) = BL.evaluate([theta, theta])
+    assert s1 == 0 and s2 == 0
+    # every block has at most 21 points, so every block runs the split kernels
+    assert int(BL.last_info[0, 3]) == Xo.shape[0]
+    assert int(BL.last_info[1, 3]) < Xo.shape[0] // 10
+    assert abs(ll1 - a[0]) <= 1e-12 * abs(a[0]), (ll1, a[0])
+    np.testing.assert_allclose(g1, a[1], rtol=1e-10, atol=1e-10 * np.abs(a[1]).max())
+    np.testing.assert_allclose(F1, a[2], rtol=1e-10, atol=1e-10 * np.abs(a[2]).max())
+    assert abs(ll2 - c25[0]) <= 5e-6 * abs(c25[0])
+    assert ll2 != c25[0]  # the closed-form problem ran in the split form
