@@ -76,13 +76,13 @@ def parse():
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the other precision forms and smoothness values of the evaluation")
     ap.add_argument("--kernel-case", default="",
-                    choices=["", "pred", "pred64", "tree", "jvar", "nu08"],
+                    choices=["", "pred", "pred64", "tree", "jvar", "nu08", "nu08s"],
                     help="run one small case of a kernel for a profiler capture and exit: "
                          "pred / pred64 (sv_predict_blocks, split / float64, 20,000 blocks of "
                          "141), tree (tree-form maximin, 100,000 rows, d = 10), jvar "
-                         "(sv_joint_var_diag, 5,000 points), nu08 (the float64 evaluation at "
-                         "fixed nu = 0.8 with its Matern table, 20,000 rows of the benchmark's "
-                         "distribution, three calls)")
+                         "(sv_joint_var_diag, 5,000 points), nu08 / nu08s (the float64 / "
+                         "split evaluation at fixed nu = 0.8 with its Matern table, 20,000 "
+                         "rows of the benchmark's distribution, three calls)")
     return ap.parse_args()
 
 
@@ -138,7 +138,7 @@ def kernel_case(name):
         F = gp._joint_factor_device((rng.random((5000, 4)) - gp._lo) / gp._span, 40)
         gp._joint_var_diag(F)
         torch.cuda.synchronize()
-    elif name == "nu08":
+    elif name in ("nu08", "nu08s"):
         from pyscaledvecchia_gb300.likelihood import DeviceProblem
         from pyscaledvecchia_gb300.ordering import _nn_groups, ordered_nn_device
         n, d, m = 20_000, 10, 30
@@ -150,8 +150,9 @@ def kernel_case(name):
         nn, _ = ordered_nn_device(torch, Xs_d[o].contiguous(), m)
         order = o.cpu().numpy()
         prob = DeviceProblem(X[order], eps, np.ones((n, 1)), _nn_groups(nn.cpu().numpy(), m))
+        prec = "split" if name == "nu08s" else "float64"
         for _ in range(3):
-            prob.evaluate(theta, 0.8)
+            prob.evaluate(theta, 0.8, precision=prec, team_lanes=16 if prec == "split" else 0)
         torch.cuda.synchronize()
     print(json.dumps({"kernel_case": name, "status": "ok"}))
 
@@ -1020,10 +1021,14 @@ def main():
                                  "float64_blocks_per_s": n / (tl["float64"] * 1e-3),
                                  "split_errors_vs_float64_form": errors_vs(rl_f, rl_s)}
         del prob_l
-        # fixed nu = 0.8: general smoothness (float64 kernels; the split forms
-        # take closed-form nu only), M and g from the call's Matern table
-        # built from the device K_nu; the per-entry Bessel routine (a batched
-        # evaluation without tables) once, as its check
+        # fixed nu = 0.8: general smoothness.  The split form assembles from
+        # the call's float32 Matern table (deficit and g), the float64 form
+        # takes M and g from its float64 table; both tables are built from the
+        # device K_nu.  The per-entry Bessel routine (a batched evaluation
+        # without tables) once, as the float64 table's check
+        ms08s = float(np.mean(time_form("split", best_lanes, max(2, args.steps // 2), 1, 0.8)))
+        r_s08 = prob.evaluate(theta, 0.8, precision="split", team_lanes=best_lanes)
+        redone08 = int(prob.last_info[3])
         ms08 = float(np.mean(time_form("float64", 0, max(2, args.steps // 2), 1, 0.8)))
         from pyscaledvecchia_gb300.batched import BatchedLikelihood, BatchProblem
         r_tab = prob.evaluate(theta, 0.8)
@@ -1034,9 +1039,13 @@ def main():
         torch.cuda.synchronize()
         ms_bes = (time.perf_counter() - t0) * 1e3
         del BL08
-        forms["nu0.8"] = {"float64_ms": ms08, "float64_blocks_per_s": n / (ms08 * 1e-3),
-                          "kernel": "float64 block kernels, Matern from a Chebyshev table of "
-                                    "the device K_nu for the fixed nu",
+        forms["nu0.8"] = {"split_ms": ms08s, "split_blocks_per_s": n / (ms08s * 1e-3),
+                          "split_blocks_redone_in_float64": redone08,
+                          "split_errors_vs_float64_form": errors_vs(r_tab, r_s08),
+                          "float64_ms": ms08, "float64_blocks_per_s": n / (ms08 * 1e-3),
+                          "kernel": "split: float32 deficit and g from an 8-term float32 "
+                                    "Chebyshev table; float64: M and g from a 16-term float64 "
+                                    "table; both of the device K_nu for the fixed nu",
                           "per_entry_bessel_ms": ms_bes,
                           "table_vs_per_entry_bessel": errors_vs(tuple(r_bes), r_tab),
                           "bessel_k": bessel_error(torch, lib, Xo, nn, theta, 0.8)}

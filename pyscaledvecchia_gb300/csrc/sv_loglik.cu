@@ -33,15 +33,14 @@
 namespace sv {
 
 // whether problem D interpolates its Matern from a table: a fixed nu without
-// a closed form whose floor octave the table reaches
+// a closed form, at most 10, whose floor octave the table reaches
 __device__ __forceinline__ bool uses_matern_table(const sv_prob_desc& D) {
-  return !D.estimate_nu && D.nu > 0.0 && matern_closed_code(D.nu) < 0 &&
-         mtab_elo(D.nu) >= kMtabEloMin;
+  return !D.estimate_nu && mtab_ok(D.nu);
 }
 
 // theta -> per-problem parameters (sigma^2, tau, nu, 1/lambda)
 __global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, int tstride,
-                              int nprob, ProbInfo* out, const double* mtabs) {
+                              int nprob, ProbInfo* out, const double* mtabs, int ftabs) {
   const int p = blockIdx.x;
   if (p >= nprob) return;
   const sv_prob_desc& D = descs[p];
@@ -95,10 +94,22 @@ __global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, in
     mm.lc_m = D.estimate_nu ? matern_log_coef(mm.nu_m) : 0.0;
     mm.inv2h = 1.0 / (2.0 * h);
     // fixed general nu: M and g from the table built for this call
-    mm.tab = (mtabs && uses_matern_table(D)) ? mtabs + (size_t)p * kMtabMaxDoubles : nullptr;
+    mm.tab = (mtabs && uses_matern_table(D)) ? mtabs + (size_t)p * kMtabSlotDoubles : nullptr;
     mm.tab_elo = mm.tab ? mtab_elo(nu) : 0;
     mm.s2n = sqrt(2.0 * nu);
     I.mm = mm;
+    // split kernels: a closed form, the float32 table, or none
+    MaternF32 mf;
+    mf.code = mm.closed;
+    mf.elo = mm.tab_elo;
+    mf.esw = ftab_switch(nu);
+    mf.s2n = (float)mm.s2n;
+    mf.tab = nullptr;
+    if (mf.code < 0 && mm.tab && ftabs && ftab_ok(nu)) {
+      mf.code = 3;
+      mf.tab = (const float4*)(mm.tab + kMtabMaxDoubles);
+    }
+    I.mf32 = mf;
   }
   for (int l = threadIdx.x; l < d; l += blockDim.x) I.invlam[l] = exp(-th[1 + l]);
 }
@@ -133,9 +144,27 @@ __global__ void k_matern_tables(const sv_prob_desc* descs, double* tabs) {
     ag = fma(fg[i], w, ag);
   }
   const double sc2 = (j == 0 ? 1.0 : 2.0) / kMtabN;
-  double* tab = tabs + (size_t)blockIdx.y * kMtabMaxDoubles;
+  double* tab = tabs + (size_t)blockIdx.y * kMtabSlotDoubles;
   tab[(size_t)iv * 2 * kMtabN + j] = am * sc2;
   tab[(size_t)iv * 2 * kMtabN + kMtabN + j] = ag * sc2;
+}
+
+// the float32 tables of the split kernels (after the float64 table in each
+// problem's slot): CTA (interval, p) of kFtabN threads takes the node values
+// F (the deficit D below 2^esw, e^c M above) and e^c G, then their Chebyshev
+// coefficients rounded to float32 ([8 of F, 8 of Q] per interval)
+__global__ void k_matern_ftabs(const sv_prob_desc* descs, double* tabs) {
+  __shared__ double ff[kFtabN], fq[kFtabN];
+  const sv_prob_desc& D = descs[blockIdx.y];
+  if (!uses_matern_table(D) || !ftab_ok(D.nu)) return;
+  const int elo = mtab_elo(D.nu);
+  const int iv = blockIdx.x, j = threadIdx.x;
+  if (iv >= ftab_intervals(elo)) return;
+  ftab_node(D.nu, elo, ftab_switch(D.nu), iv, j, ff[j], fq[j]);
+  __syncthreads();
+  float* ft = (float*)(tabs + (size_t)blockIdx.y * kMtabSlotDoubles + kMtabMaxDoubles);
+  ft[(size_t)iv * 2 * kFtabN + j] = ftab_coef(ff, j);
+  ft[(size_t)iv * 2 * kFtabN + kFtabN + j] = ftab_coef(fq, j);
 }
 
 // the problem table of a one-problem evaluation, passed by value
@@ -863,7 +892,7 @@ WsLayout ws_layout(const EvalShape& S) {
   L.xhl = off;
   if (S.precision == 1 || S.precision == 2) off = align256(off + sizeof(float) * 2 * (size_t)S.nx);
   L.mtab = off;
-  if (S.tabs) off = align256(off + sizeof(double) * (size_t)kMtabMaxDoubles * (size_t)S.nprob);
+  if (S.tabs) off = align256(off + sizeof(double) * (size_t)kMtabSlotDoubles * (size_t)S.nprob);
   L.total = off;
   return L;
 }
@@ -1015,7 +1044,8 @@ int run_eval(const EvalCall& C, cudaStream_t st, const ShardStage* sh = nullptr)
   // split forms (1: float64 factorisation, 2: double-float factorisation):
   // no estimated nu and at most 32 right-hand sides (d + q <= 29); anything
   // else runs the float64 kernels.  In a batch, the blocks of a problem whose
-  // nu has no closed form are sent by the split kernels to the float64 pass
+  // nu has neither a closed form nor the float32 table go from the split
+  // kernels to the float64 pass
   const bool split = (S.precision == 1 || S.precision == 2) && !S.any_est && A.NRmax <= 32;
   // 16 lanes per block is the fastest team width measured for every K from 6
   // to 31 (d = 3 and 10); 8 and 32 trail by up to 37 % and 12 %
@@ -1061,8 +1091,14 @@ int run_eval(const EvalCall& C, cudaStream_t st, const ShardStage* sh = nullptr)
       k_matern_tables<<<dim3(2 * (kMtabEhi - kMtabEloMin), (unsigned)S.nprob), kMtabN, 0, st>>>(C.probs,
                                                                                                mtabs);
       SV_CUDA_TRY(cudaGetLastError());
+      if (split) {
+        k_matern_ftabs<<<dim3(2 * (kFtabEhi - kMtabEloMin), (unsigned)S.nprob), kFtabN, 0, st>>>(C.probs,
+                                                                                                 mtabs);
+        SV_CUDA_TRY(cudaGetLastError());
+      }
     }
-    k_prob_params<<<(int)S.nprob, 64, 0, st>>>(C.probs, C.theta, C.tstride, (int)S.nprob, probs, mtabs);
+    k_prob_params<<<(int)S.nprob, 64, 0, st>>>(C.probs, C.theta, C.tstride, (int)S.nprob, probs, mtabs,
+                                               split ? 1 : 0);
     SV_CUDA_TRY(cudaGetLastError());
     if (split && C.nwarp > 0) {
       rc = launch_split_prep(A, S.nx, st);
@@ -1158,14 +1194,12 @@ EvalShape single_shape(const sv_loglik_desc* D) {
   S.kmax = D->kmax;
   S.need_grad = D->need_grad;
   S.any_est = D->estimate_nu;
-  // the split forms assemble in float32 only the closed forms (nu 0.5, 1.5,
-  // 2.5); a problem with another nu runs the float64 kernels directly
-  S.precision = (D->estimate_nu || matern_closed_code(D->nu) < 0) ? 0 : D->precision;
+  // the split forms assemble in float32 the closed forms (nu 0.5, 1.5, 2.5)
+  // and a fixed nu of the float32 table; another nu runs the float64 kernels
+  const bool f32 = matern_closed_code(D->nu) >= 0 || ftab_ok(D->nu);
+  S.precision = (D->estimate_nu || !f32) ? 0 : D->precision;
   // a fixed nu without a closed form: its Matern is interpolated from a table
-  S.tabs = (!D->estimate_nu && D->nu > 0.0 && matern_closed_code(D->nu) < 0 &&
-            mtab_elo(D->nu) >= kMtabEloMin)
-               ? 1
-               : 0;
+  S.tabs = (!D->estimate_nu && mtab_ok(D->nu)) ? 1 : 0;
   return S;
 }
 

@@ -27,6 +27,7 @@ struct ProbInfo {
   // double-float split form: s2, s2 (1 + tau) and s2 tau as float32 (hi, lo) pairs
   float s2_hi, s2_lo, dg_hi, dg_lo, s2t_hi, s2t_lo;
   MaternMode mm;
+  MaternF32 mf32;  // the split kernels' float32 Matern (code -1: the float64 pass)
   double invlam[kMaxD];
 };
 

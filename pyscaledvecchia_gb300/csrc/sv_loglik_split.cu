@@ -76,7 +76,7 @@ __device__ __forceinline__ void split_pivot(dfv dkk, dfv* diag, int rho_bits, vo
 // 0: read from shared memory).  The same value per entry as any other
 // traversal.
 template <int DR>
-__device__ __forceinline__ void split_sigma_rows(int h, int K, int d, int code, dfv s2, dfv dj,
+__device__ __forceinline__ void split_sigma_rows(int h, int K, int d, const MaternF32& mf, dfv s2, dfv dj,
                                                  const float* u, dfv* Lp, int kc) {
   const int ib = K - 1 - h;            // >= h
   const int na = ib == h ? 0 : h;      // entries of row h when it is a row of its own
@@ -110,7 +110,7 @@ __device__ __forceinline__ void split_sigma_rows(int h, int K, int d, int code, 
         r2 = fmaf(df, df, r2);
       }
     }
-    Lp[cm(i, j, kc)] = df_scaled_deficit(s2, matern_deficit_f32(code, sqrtf(r2)));
+    Lp[cm(i, j, kc)] = df_scaled_deficit(s2, matern_deficit_f32(mf, sqrtf(r2)));
   }
   Lp[cm(h, h, kc)] = dj;
   if (ib != h) Lp[cm(ib, ib, kc)] = dj;
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split_df(LikArgs 
     const int d = PI.d, q = PI.q, P = PI.P, NR = P + 1 + q;
     const double s2 = PI.s2, tau = PI.tau;
     const float s2f = (float)s2;
-    const int code = PI.closed;
+    const MaternF32 mf = PI.mf32;
     const double diag = s2 * (1.0 + tau);
     const dfv s2d = df_make(PI.s2_hi, PI.s2_lo);
     const double* Y = A.y + PI.y_off;
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split_df(LikArgs 
     // scale inside [1e-30, 1e30] and data below 1e30 in magnitude keep every
     // pair inside float32's exponent range; other blocks, and the blocks of a
     // problem whose nu has no float32 form here, go to the float64 pass
-    bool range_ok = code >= 0 && dbits(diag) > kBitsTiny && dbits(diag) < kBitsHuge;
+    bool range_ok = mf.code >= 0 && dbits(diag) > kBitsTiny && dbits(diag) < kBitsHuge;
 
     // ---- gather: neighbours first, self last; coordinates centred on self
     if (active)
@@ -228,13 +228,13 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split_df(LikArgs 
         // close pairs
         for (int h = tl; 2 * h < K; h += G) {
           if (d <= 4)
-            split_sigma_rows<4>(h, K, d, code, s2d, dj, u, Lp, kc);
+            split_sigma_rows<4>(h, K, d, mf, s2d, dj, u, Lp, kc);
           else if (d <= 8)
-            split_sigma_rows<8>(h, K, d, code, s2d, dj, u, Lp, kc);
+            split_sigma_rows<8>(h, K, d, mf, s2d, dj, u, Lp, kc);
           else if (d <= 12)
-            split_sigma_rows<12>(h, K, d, code, s2d, dj, u, Lp, kc);
+            split_sigma_rows<12>(h, K, d, mf, s2d, dj, u, Lp, kc);
           else
-            split_sigma_rows<0>(h, K, d, code, s2d, dj, u, Lp, kc);
+            split_sigma_rows<0>(h, K, d, mf, s2d, dj, u, Lp, kc);
         }
         if (tl == 0) {
           tflag[0] = 0;  // a pivot failed
@@ -465,13 +465,13 @@ __global__ void __launch_bounds__(kSplitMaxThreads, 1) k_block_split_df(LikArgs 
       for (int i = tl; i < K; i += G) {
         auto store = [&](int c, float v) { R[c * 33 + i] = df_make(v, 0.0f); };
         if (d <= 4)
-          split_dsig_row<4>(i, K, d, code, s2f, u, a32, store);
+          split_dsig_row<4>(i, K, d, mf, s2f, u, a32, store);
         else if (d <= 8)
-          split_dsig_row<8>(i, K, d, code, s2f, u, a32, store);
+          split_dsig_row<8>(i, K, d, mf, s2f, u, a32, store);
         else if (d <= 12)
-          split_dsig_row<12>(i, K, d, code, s2f, u, a32, store);
+          split_dsig_row<12>(i, K, d, mf, s2f, u, a32, store);
         else
-          split_dsig_row_wide(i, K, d, code, s2f, u, a32, store);
+          split_dsig_row_wide(i, K, d, mf, s2f, u, a32, store);
       }
       // nugget row: dSigma_tau = s2 tau I
       const dfv s2taud = df_make(PI.s2t_hi, PI.s2t_lo);

@@ -73,7 +73,7 @@ __device__ __forceinline__ void split64_pivot(double dkk, double* diag, long lon
 // diagonal entries dj; u is [d][32] (row i at column i), the current row's
 // coordinates are held in registers (DR >= d, 0: read from shared memory).
 template <int DR>
-__device__ __forceinline__ void split64_sigma_rows(int h, int K, int d, int code, double s2,
+__device__ __forceinline__ void split64_sigma_rows(int h, int K, int d, const MaternF32& mf, double s2,
                                                    double dj, const float* u, double* Lp, int kc) {
   const int ib = K - 1 - h;            // >= h
   const int na = ib == h ? 0 : h;      // entries of row h when it is a row of its own
@@ -107,7 +107,7 @@ __device__ __forceinline__ void split64_sigma_rows(int h, int K, int d, int code
         r2 = fmaf(df, df, r2);
       }
     }
-    Lp[cm(i, j, kc)] = fma(-s2, f2d_int(matern_deficit_f32(code, sqrtf(r2))), s2);
+    Lp[cm(i, j, kc)] = fma(-s2, f2d_int(matern_deficit_f32(mf, sqrtf(r2))), s2);
   }
   Lp[cm(h, h, kc)] = dj;
   if (ib != h) Lp[cm(ib, ib, kc)] = dj;
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(kS64MaxThreads, 1) k_block_split64(LikArgs A, 
     const int d = PI.d, q = PI.q, P = PI.P, NR = P + 1 + q;
     const double s2 = PI.s2;
     const float s2f = d2f_int(s2);
-    const int code = PI.closed;
+    const MaternF32 mf = PI.mf32;
     const double diag = PI.dg;
     const double* Y = A.y + PI.y_off;
     const double* Zm = A.Z + PI.z_off;
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(kS64MaxThreads, 1) k_block_split64(LikArgs A, 
     // float32 quantity inside float32's exponent range; other blocks, and
     // the blocks of a problem whose nu has no float32 form here, go to the
     // float64 pass
-    bool range_ok = code >= 0 && dbits(diag) > kBitsTiny && dbits(diag) < kBitsHuge;
+    bool range_ok = mf.code >= 0 && dbits(diag) > kBitsTiny && dbits(diag) < kBitsHuge;
 
     // ---- gather: neighbours first, self last; coordinates centred on self
     if (active)
@@ -213,13 +213,13 @@ __global__ void __launch_bounds__(kS64MaxThreads, 1) k_block_split64(LikArgs A, 
         // between them)
         for (int h = tl; 2 * h < K; h += G) {
           if (d <= 4)
-            split64_sigma_rows<4>(h, K, d, code, s2, dj, u, Lp, kc);
+            split64_sigma_rows<4>(h, K, d, mf, s2, dj, u, Lp, kc);
           else if (d <= 8)
-            split64_sigma_rows<8>(h, K, d, code, s2, dj, u, Lp, kc);
+            split64_sigma_rows<8>(h, K, d, mf, s2, dj, u, Lp, kc);
           else if (d <= 12)
-            split64_sigma_rows<12>(h, K, d, code, s2, dj, u, Lp, kc);
+            split64_sigma_rows<12>(h, K, d, mf, s2, dj, u, Lp, kc);
           else
-            split64_sigma_rows<0>(h, K, d, code, s2, dj, u, Lp, kc);
+            split64_sigma_rows<0>(h, K, d, mf, s2, dj, u, Lp, kc);
         }
         if (tl == 0) {
           tflag[0] = 0;  // a pivot failed
@@ -416,13 +416,13 @@ __global__ void __launch_bounds__(kS64MaxThreads, 1) k_block_split64(LikArgs A, 
       for (int i = tl; i < K; i += G) {
         auto store = [&](int c, float v) { R[c * 33 + i] = f2d_int(v); };
         if (d <= 4)
-          split_dsig_row<4>(i, K, d, code, s2f, u, a32, store);
+          split_dsig_row<4>(i, K, d, mf, s2f, u, a32, store);
         else if (d <= 8)
-          split_dsig_row<8>(i, K, d, code, s2f, u, a32, store);
+          split_dsig_row<8>(i, K, d, mf, s2f, u, a32, store);
         else if (d <= 12)
-          split_dsig_row<12>(i, K, d, code, s2f, u, a32, store);
+          split_dsig_row<12>(i, K, d, mf, s2f, u, a32, store);
         else
-          split_dsig_row_wide(i, K, d, code, s2f, u, a32, store);
+          split_dsig_row_wide(i, K, d, mf, s2f, u, a32, store);
       }
       // nugget row: dSigma_tau = s2 tau I
       for (int i = tl; i < K; i += G) R[(P - 1) * 33 + i] = PI.s2t * a[i];

@@ -221,13 +221,17 @@ SV_HD double matern_log_coef(double nu) { return (1.0 - nu) * kLn2 - lgamma(nu);
 // [2^e sqrt2, 2^(e+1)) of c from 2^elo (elo = floor(log2(sqrt(2 nu) 1e-7)), the
 // smallest c the r floor lets through) to 2^9; on each, e^c M(c) and e^c G(c)
 // as 16-term Chebyshev series (functions analytic but for c = 0, which lies
-// about six half-widths away: the series converge like 12^-k, far below
-// float64 rounding at 16 terms).  M = e^-c P(t), G = e^-c Q(t), one
+// about six half-widths away).  M = e^-c P(t), G = e^-c Q(t), one
 // exponential per entry; c >= 2^9 (M < 1e-220) takes the Bessel routine.
+// For nu <= 10 the series are within 6e-15 relative of 40-digit values; for
+// larger nu, e^c M (close to exp(c - c^2 / (4 nu))) spans too many orders of
+// magnitude on an interval (2e-14 at nu = 12.6, 3e-11 at 25.5), so nu > 10
+// keeps the per-entry Bessel routine.
 // ---------------------------------------------------------------------------
 constexpr int kMtabN = 16;       // Chebyshev terms per interval and function
 constexpr int kMtabEhi = 9;      // the table covers c < 2^9
 constexpr int kMtabEloMin = -40; // smaller nu (c floor below 2^-40): no table
+constexpr double kMtabNuMax = 10.0;  // larger nu: no table
 constexpr int kMtabMaxDoubles = 2 * (kMtabEhi - kMtabEloMin) * 2 * kMtabN;
 
 // floor(log2(sqrt(2 nu) * 1e-7)): the table's first octave
@@ -363,5 +367,175 @@ __device__ __forceinline__ float matern_deficit_f32(int code, float r) {
   P = fmaf(P, c, code == 1 ? 0.5f : 0.16666666666666666f);
   return (expf(-c) * (c * c)) * P;
 }
+
+// ---------------------------------------------------------------------------
+// float32 table of a fixed general nu (the split kernels; no counterpart in
+// the reference, which calls scipy's kv for every entry,
+// _matern_general.py:87-116).  On the float64 table's half-octave intervals
+// of c = sqrt(2 nu) r, from 2^elo up to 2^6 (for c >= 64, M < 1e-24: D = 1
+// and g = 0 in float32), 8-term Chebyshev series with float32 coefficients
+//   F(c) = D(c) = 1 - M(c)     on the intervals below 2^esw,
+//   F(c) = e^c M(c)            on the others (D = 1 - e^-c F),
+//   Q(c) = e^c G(c)            on all of them (g = e^-c Q),
+// sixteen floats (four float4) per interval.  2^esw is the first octave at
+// or above sqrt(2 max(nu - 1, 1)), where D >= 0.45 for nu <= 50 (D ~ c^2 /
+// (4 (nu - 1)) for nu > 1): above it 1 - e^-c F keeps D's relative accuracy.
+// Below it, D comes from the series of K_nu through I_-nu and I_nu with the
+// leading 1 of M taken out,
+//   D(c) = A (c/2)^(2 nu) sum_k x^k / (k! (1+nu)_k) - sum_{k>=1} x^k / (k! (1-nu)_k),
+//   x = c^2 / 4,  A = Gamma(1-nu) / Gamma(1+nu) = pi / (sin(pi nu) nu Gamma(nu)^2),
+// which keeps D's relative accuracy however small c is (1 - M keeps none of
+// it as c -> 0).  Near an integer nu the two sums cancel (the digits lost
+// grow as 1 / dist(nu, Z)): the table is built for dist(nu, Z) >= 1e-3 and
+// nu <= 8 (at eight terms e^c M and e^c G are within 9e-9 relative up to
+// nu = 8.4, 5e-7 at 10.3); other general nu run the float64 kernels.  The
+// float64 series is within 1e-13 of 40-digit values below 2^esw for nu from
+// 0.3 to 49.7 (at most 52 terms).  Measured in float32 against 40-digit
+// values (nu 0.3, 0.8, 1.75, 3.2; c in [2^-20, 64) at the float32 c and t the
+// kernels compute): D within 3 ulp and g within 4.2 ulp.
+// ---------------------------------------------------------------------------
+constexpr int kFtabN = 8;       // Chebyshev terms per interval and function
+constexpr int kFtabEhi = 6;     // the float32 table covers c < 2^6
+constexpr double kFtabNuMax = 8.0;  // larger nu: no float32 table
+constexpr int kFtabMaxFloats = 2 * (kFtabEhi - kMtabEloMin) * 2 * kFtabN;
+// one problem's slot in the table region: the float64 table, then the float32 one
+constexpr int kMtabSlotDoubles = kMtabMaxDoubles + kFtabMaxFloats / 2;
+static_assert((kMtabMaxDoubles * 8) % 16 == 0 && (kMtabSlotDoubles * 8) % 16 == 0,
+              "the float32 tables are read as float4");
+
+// whether a fixed nu gets the float64 table, and the float32 one
+SV_HD bool mtab_ok(double nu) {
+  return nu > 0.0 && nu <= kMtabNuMax && matern_closed_code(nu) < 0 && mtab_elo(nu) >= kMtabEloMin;
+}
+SV_HD bool ftab_ok(double nu) {
+  return mtab_ok(nu) && nu <= kFtabNuMax && fabs(nu - rint(nu)) >= 1e-3;
+}
+SV_HD int ftab_intervals(int elo) { return 2 * (kFtabEhi - elo); }
+// the first octave whose F is e^c M (at least 1)
+SV_HD int ftab_switch(double nu) {
+  int e = 0;
+  frexp(sqrt(2.0 * fmax(nu - 1.0, 1.0)), &e);
+  return e < 1 ? 1 : e;
+}
+
+// float32 Matern of a split kernel's block: a closed form, or the table
+struct MaternF32 {
+  int code;           // 0/1/2: nu = 0.5/1.5/2.5; 3: the float32 table; -1: none
+  int elo;            // the table's first octave
+  int esw;            // its first octave of F = e^c M
+  float s2n;          // sqrt(2 nu)
+  const float4* tab;  // four float4 per interval: F, then Q (global or shared)
+};
+
+#ifdef __CUDACC__
+// D(c) for c < 2^esw by the series above (nu at least 1e-3 from an
+// integer): terms until both are below 1e-18 of their sums past k = nu + 2
+// (at most 52 for nu <= 50), 96 at most
+__device__ __forceinline__ double matern_deficit_series(double c, double nu) {
+  const double x = 0.25 * c * c;
+  const double A = kPi / (sinpi(nu) * nu) * exp(2.0 * nu * log(0.5 * c) - 2.0 * lgamma(nu));
+  double s1 = 1.0, t = 1.0, s2 = 0.0, u = 1.0;
+  for (int k = 1; k <= 96; ++k) {
+    t *= x / (k * (k + nu));
+    u *= x / (k * (k - nu));
+    s1 += t;
+    s2 += u;
+    if (k > nu + 2.0 && fabs(t) < 1e-18 * fabs(s1) && fabs(u) < 1e-18 * fabs(s2)) break;
+  }
+  return A * s1 - s2;
+}
+
+// node j of interval iv of the float32 table: F and Q at the interval's
+// j-th Chebyshev point
+__device__ inline void ftab_node(double nu, int elo, int esw, int iv, int j, double& F,
+                                 double& Q) {
+  const int e = elo + iv / 2, half = iv & 1;
+  const double tj = cospi((j + 0.5) / kFtabN);
+  const double m = half ? (tj - kMtabO1) / kMtabS1 : (tj - kMtabO0) / kMtabS0;
+  const double c = ldexp(m, e);
+  double M, G;
+  matern_general_MG_c(c, nu, matern_log_coef(nu), M, G);
+  const double ec = exp(c);
+  F = e < esw ? matern_deficit_series(c, nu) : ec * M;
+  Q = ec * G;
+}
+
+// Chebyshev coefficient j of an interval from its kFtabN node values f
+__device__ inline float ftab_coef(const double* f, int j) {
+  double a = 0.0;
+  for (int i = 0; i < kFtabN; ++i) a = fma(f[i], cospi((double)j * (i + 0.5) / kFtabN), a);
+  return (float)(a * ((j == 0 ? 1.0 : 2.0) / kFtabN));
+}
+
+constexpr float kFtabS0 = 4.82842712474619f;   // t = m S + O, as the float64 table
+constexpr float kFtabO0 = -5.82842712474619f;
+constexpr float kFtabS1 = 3.414213562373095f;
+constexpr float kFtabO1 = -5.82842712474619f;
+constexpr int kFtabSqrt2Bits = 0x3FB504F4;     // the smallest float >= sqrt(2)
+
+// interval of c in the float32 table and t in [-1, 1] (a rounding outside
+// for c just below 2^elo); -1 for c >= 2^6
+__device__ __forceinline__ int ftab_locate(int elo, float c, float& t, int& e) {
+  const int bits = __float_as_int(c);
+  e = (bits >> 23) - 127;
+  if (e >= kFtabEhi) return -1;
+  float m;
+  int jh = 0;
+  if (e < elo) {
+    m = c * __int_as_float((127 - elo) << 23);  // c 2^-elo, exact
+    e = elo;
+  } else {
+    const int mb = (bits & 0x007FFFFF) | 0x3F800000;
+    m = __int_as_float(mb);
+    jh = mb >= kFtabSqrt2Bits ? 1 : 0;
+  }
+  t = jh ? fmaf(m, kFtabS1, kFtabO1) : fmaf(m, kFtabS0, kFtabO0);
+  return 2 * (e - elo) + jh;
+}
+
+__device__ __forceinline__ float ftab_clenshaw(float4 lo, float4 hi, float t) {
+  const float cf[kFtabN] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+  const float t2 = t + t;
+  float b1 = 0.0f, b2 = 0.0f;
+#pragma unroll
+  for (int k = kFtabN - 1; k >= 1; --k) {
+    const float b0 = fmaf(t2, b1, cf[k] - b2);
+    b2 = b1;
+    b1 = b0;
+  }
+  return fmaf(t, b1, cf[0] - b2);
+}
+
+// D and g of a split kernel's Matern (r floored as _matern_general.py:87
+// does: below 1e-7, M = 1 and g = 0)
+__device__ __forceinline__ float matern_deficit_f32(const MaternF32& mf, float r) {
+  if (mf.code != 3) return matern_deficit_f32(mf.code, r);
+  if (r < 1e-7f) return 0.0f;
+  const float c = mf.s2n * r;
+  float t;
+  int e;
+  const int iv = ftab_locate(mf.elo, c, t, e);
+  if (iv < 0) return 1.0f;
+  const float4* p = mf.tab + 4 * iv;
+  const float F = ftab_clenshaw(p[0], p[1], t);
+  return e < mf.esw ? F : 1.0f - expf(-c) * F;
+}
+
+__device__ __forceinline__ float matern_g_f32(const MaternF32& mf, float r) {
+  if (mf.code != 3) {
+    float M, g;
+    matern_closed_f32(mf.code, r, M, g);
+    return g;
+  }
+  if (r < 1e-7f) return 0.0f;
+  const float c = mf.s2n * r;
+  float t;
+  int e;
+  const int iv = ftab_locate(mf.elo, c, t, e);
+  if (iv < 0) return 0.0f;
+  const float4* p = mf.tab + 4 * iv + 2;
+  return expf(-c) * ftab_clenshaw(p[0], p[1], t);
+}
+#endif
 
 }  // namespace sv

@@ -15,7 +15,7 @@ namespace sv {
 // roundings in the same order as a pass per l.  store(1 + l, value) writes
 // the value into column 1 + l of the caller's right-hand sides.
 template <int DR, typename Store>
-__device__ __forceinline__ void split_dsig_row(int i, int K, int d, int code, float s2f,
+__device__ __forceinline__ void split_dsig_row(int i, int K, int d, const MaternF32& mf, float s2f,
                                                const float* u, const float* a32, Store store) {
   float ui[DR], S[DR];
 #pragma unroll
@@ -34,9 +34,7 @@ __device__ __forceinline__ void split_dsig_row(int i, int K, int d, int code, fl
         r2 = fmaf(df, df, r2);
         sq[l] = df * df;
       }
-    float M, g;
-    matern_closed_f32(code, sqrtf(r2), M, g);
-    const float c = g * a32[j];
+    const float c = matern_g_f32(mf, sqrtf(r2)) * a32[j];
 #pragma unroll
     for (int l = 0; l < DR; ++l)
       if (l < d) S[l] = fmaf(c, sq[l], S[l]);
@@ -49,7 +47,7 @@ __device__ __forceinline__ void split_dsig_row(int i, int K, int d, int code, fl
 // The same for d > 12: row i's g_ij a_j for all j in registers, then one
 // pass per coordinate.
 template <typename Store>
-__device__ __forceinline__ void split_dsig_row_wide(int i, int K, int d, int code, float s2f,
+__device__ __forceinline__ void split_dsig_row_wide(int i, int K, int d, const MaternF32& mf, float s2f,
                                                     const float* u, const float* a32, Store store) {
   float cj[32];
 #pragma unroll
@@ -61,9 +59,7 @@ __device__ __forceinline__ void split_dsig_row_wide(int i, int K, int d, int cod
         const float df = u[l * 32 + i] - u[l * 32 + j];
         r2 = fmaf(df, df, r2);
       }
-      float M, g;
-      matern_closed_f32(code, sqrtf(r2), M, g);
-      c = g * a32[j];
+      c = matern_g_f32(mf, sqrtf(r2)) * a32[j];
     }
     cj[j] = c;
   }

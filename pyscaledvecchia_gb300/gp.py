@@ -52,10 +52,13 @@ class ScaledVecchiaGP:
 
     One setting has no counterpart in the reference: ``precision``, the
     arithmetic of the likelihood blocks in fit and of the prediction blocks:
-    "float64" (the reference's) or "split" (closed-form nu: block entries
-    assembled in float32 from centred coordinates and the correlation
-    deficit, the factorisation, solves and sums in float64; ill-conditioned
-    blocks are redone in float64).
+    "float64" (the reference's) or "split" (block entries assembled in
+    float32 from centred coordinates and the correlation deficit, the
+    factorisation, solves and sums in float64; ill-conditioned blocks are
+    redone in float64).  The likelihood takes the split form for the closed
+    forms and for a fixed nu of the library's float32 table (at most 8 and
+    at least 1e-3 from an integer), the prediction blocks for the closed
+    forms; any other nu runs in float64.
     """
 
     m_est: int = 30

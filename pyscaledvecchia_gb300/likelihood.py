@@ -16,6 +16,7 @@ libsvgpu.so (sv_vecchia_loglik); the host only packs the conditioning sets.
 from __future__ import annotations
 
 import ctypes
+import math
 
 import numpy as np
 
@@ -27,6 +28,29 @@ __all__ = ["vecchia_profile_loglik"]
 _WARP_K = 32  # blocks with K = k+1 <= 32 run one per warp, larger ones one per CTA
 _PRECISION = {"float64": 0, "split": 1, "split_df": 2}
 _SPLIT = ("split", "split_df")
+
+
+def matern_table_nu(nu, estimate_nu=False):
+    """Whether the library interpolates this fixed nu's Matern from a
+    per-evaluation table (no closed form, nu <= 10, and sqrt(2 nu) 1e-7 >=
+    2^-40)."""
+    if (estimate_nu or nu is None or not 0.0 < nu <= 10.0
+            or float(nu) in (0.5, 1.5, 2.5)):
+        return False
+    return math.frexp(math.sqrt(2.0 * nu) * 1e-7)[1] - 1 >= -40
+
+
+def split_nu(nu, estimate_nu=False):
+    """Whether the split forms assemble this nu in float32: a closed form
+    (0.5, 1.5, 2.5), or a fixed nu of the library's float32 table (at most 8
+    and at least 1e-3 from an integer: near an integer the table's series
+    loses its digits).  Any other nu runs the float64 kernels."""
+    if estimate_nu or nu is None:
+        return False
+    if float(nu) in (0.5, 1.5, 2.5):
+        return True
+    return (matern_table_nu(nu) and float(nu) <= 8.0
+            and abs(float(nu) - round(float(nu))) >= 1e-3)
 
 
 def pack_groups(groups, n=None):
@@ -219,9 +243,11 @@ class DeviceProblem:
         """Number of library kernels one evaluation launches."""
         warp = self.nblk_warp > 0
         cta = self.nblk > self.nblk_warp
-        split = (precision in _SPLIT and not estimate_nu and nu in (0.5, 1.5, 2.5)
+        split = (precision in _SPLIT and split_nu(nu, estimate_nu)
                  and self.d + 3 + self.q <= 32)
         n = (1 if warp else 0) + (1 if cta else 0)
+        if matern_table_nu(nu, estimate_nu):
+            n += 2 if split else 1  # the Matern tables: float64, and float32 for the split kernels
         if split and warp:
             n += 1  # coordinate pre-pass
         if chunked:
@@ -260,12 +286,13 @@ class DeviceProblem:
         contractions) in float32, the factorisation, solves, log-determinant
         and the likelihood sums in float64; "split_df" is "split" with the
         factorisation and solves in double-float (float32 pairs, about 46
-        bits) instead of float64.  The split forms take closed-form nu; other
-        cases, and blocks that are ill-conditioned or outside float32's
-        exponent range, are evaluated in float64 by the library."""
+        bits) instead of float64.  The split forms take a closed-form nu or a
+        fixed nu of the float32 table (split_nu); other cases, and blocks that
+        are ill-conditioned or outside float32's exponent range, are evaluated
+        in float64 by the library."""
         torch, lib = self.torch, self.lib
-        if (precision in _SPLIT and not team_lanes and self.nblk_warp > 0 and not estimate_nu
-                and nu in (0.5, 1.5, 2.5) and self.d + 3 + self.q <= 32):
+        if (precision in _SPLIT and not team_lanes and self.nblk_warp > 0
+                and split_nu(nu, estimate_nu) and self.d + 3 + self.q <= 32):
             from . import autotune
             team_lanes = autotune.team_lanes(min(self.kmax + 1, 32), self.d, self.q, need_grad,
                                              precision=precision)

@@ -60,3 +60,39 @@ def test_table_against_the_oracle():
     assert abs(ll - ll_o) <= 1e-10 * abs(ll_o), (ll, ll_o)
     np.testing.assert_allclose(g, g_o, rtol=1e-8, atol=1e-8 * np.abs(g_o).max())
     np.testing.assert_allclose(F, F_o, rtol=1e-8, atol=1e-8 * np.abs(F_o).max())
+
+
+def test_split_table_against_the_oracle():
+    """The split form with the float32 table at nu = 0.8 against the oracle
+    (scipy's kv), with test_split_against_oracle's bounds: ll within 1e-7
+    relative, each score entry within 1e-3 of its standard deviation
+    sqrt(F_ii), Fisher within 1e-5 of its largest entry, beta within 1e-4."""
+    from oracle import oracle
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    nu = 0.8
+    Xo, yo, Zo, groups, theta = _problem(4, 600, 3, 15, nu)
+    prob = DeviceProblem(Xo, yo, Zo, groups)
+    ll, g, F, b = prob.evaluate(theta, nu, precision="split")
+    ll_o, g_o, F_o, b_o = oracle.vecchia_loglik_np(theta, Xo, yo, Zo, groups, nu)[:4]
+    assert ll != prob.evaluate(theta, nu)[0]  # the split form ran
+    assert abs(ll - ll_o) <= 1e-7 * abs(ll_o), (ll, ll_o)
+    sd = np.sqrt(np.diag(F_o))
+    assert np.all(np.abs(g - g_o) <= 1e-3 * sd), np.abs(g - g_o) / sd
+    assert np.abs(F - F_o).max() <= 1e-5 * np.abs(F_o).max()
+    np.testing.assert_allclose(b, b_o, rtol=1e-4, atol=1e-8)
+
+
+def test_no_table_above_nu_10():
+    """Above nu = 10 the 16-term series lose float64 accuracy, so the
+    evaluation keeps the per-entry Bessel routine: bit for bit the batched
+    evaluation built without tables."""
+    from pyscaledvecchia_gb300.batched import BatchedLikelihood, BatchProblem
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    nu = 12.5
+    Xo, yo, Zo, groups, theta = _problem(5, 2000, 3, 15, nu)
+    ll, g, F, b = DeviceProblem(Xo, yo, Zo, groups).evaluate(theta, nu)
+    BL = BatchedLikelihood([BatchProblem(Xo, yo, Zo, groups, nu=nu)], matern_tables=False)
+    st, ll_b, g_b, F_b, b_b = BL.evaluate([theta])[0]
+    assert st == 0 and ll == ll_b
+    np.testing.assert_array_equal(g, g_b)
+    np.testing.assert_array_equal(F, F_b)

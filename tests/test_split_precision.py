@@ -142,33 +142,52 @@ def test_split_against_oracle(oracle, lanes):
 
 
 @pytest.mark.parametrize("form", SPLIT_FORMS)
-def test_split_general_nu_runs_float64(form):
-    """The split forms assemble in float32 only the closed forms (nu 0.5,
-    1.5, 2.5).  A one-problem call with another nu runs the float64 kernels
-    (the result is the float64 form's bit for bit); in a batch, the split
-    kernels send that problem's blocks to the float64 pass, counted as
-    redone, while a closed-form problem beside it stays in the split form."""
+def test_split_general_nu(form):
+    """A fixed general nu runs the split forms through the float32 Matern
+    table (nu = 0.8: the float64 form's bounds of test_split_matches_float64);
+    within 1e-3 of an integer (nu = 2.0) there is no table and a one-problem
+    call runs the float64 kernels (the float64 form's result bit for bit).  In
+    a batch, the split kernels send the nu = 2.0 problem's blocks to the
+    float64 pass (all counted as redone) while the nu = 0.8 and nu = 2.5
+    problems beside it stay in the split form, each equal bit for bit to its
+    one-problem evaluation."""
     from pyscaledvecchia_gb300.batched import BatchedLikelihood, BatchProblem
     from pyscaledvecchia_gb300.likelihood import DeviceProblem
     from pyscaledvecchia_gb300.ordering import _nn_groups
     Xo, y, Z, nn, theta = _inputs(3000, 4, 20, 1e-3, seed=77)
     groups = _nn_groups(nn, 20)
     prob = DeviceProblem(Xo, y, Z, groups)
-    a = prob.evaluate(theta, 0.8)
-    b = prob.evaluate(theta, 0.8, precision=form)
-    assert b[0] == a[0]
-    for u, v in zip(a[1:], b[1:]):
-        np.testing.assert_array_equal(u, v)
-    c25 = prob.evaluate(theta, 2.5)
-    BL = BatchedLikelihood([BatchProblem(Xo, y, Z, groups, nu=0.8),
-                            BatchProblem(Xo, y, Z, groups, nu=2.5)], precisions=(form,))
-    (s1, ll1, g1, F1, b1), (s2, ll2, g2, F2, b2) = BL.evaluate([theta, theta])
-    assert s1 == 0 and s2 == 0
+    one = {}
+    for nu in (0.8, 2.0, 2.5):
+        a = prob.evaluate(theta, nu)
+        b = prob.evaluate(theta, nu, precision=form, team_lanes=16)
+        one[nu] = b
+        if nu == 2.0:
+            assert b[0] == a[0]
+            for u, v in zip(a[1:], b[1:]):
+                np.testing.assert_array_equal(u, v)
+            continue
+        assert b[0] != a[0]  # the split form ran
+        assert int(prob.last_info[3]) < Xo.shape[0] // 10
+        assert abs(b[0] - a[0]) <= 5e-6 * abs(a[0]), (nu, b[0], a[0])
+        assert np.abs(b[1] - a[1]).max() <= 1e-3 * np.abs(a[1]).max()
+        assert np.abs(b[2] - a[2]).max() <= 1e-3 * np.abs(a[2]).max()
+        np.testing.assert_allclose(b[3], a[3], rtol=2e-4, atol=1e-6)
+    nus = (2.0, 0.8, 2.5)
+    BL = BatchedLikelihood([BatchProblem(Xo, y, Z, groups, nu=nu) for nu in nus],
+                           precisions=(form,), team_lanes=16)
+    res = BL.evaluate([theta] * 3)
+    a20 = prob.evaluate(theta, 2.0)
+    st, ll, g, F, b = res[0]
+    assert st == 0
+    assert abs(ll - a20[0]) <= 1e-12 * abs(a20[0]), (ll, a20[0])
+    np.testing.assert_allclose(g, a20[1], rtol=1e-10, atol=1e-10 * np.abs(a20[1]).max())
+    np.testing.assert_allclose(F, a20[2], rtol=1e-10, atol=1e-10 * np.abs(a20[2]).max())
     # every block has at most 21 points, so every block runs the split kernels
     assert int(BL.last_info[0, 3]) == Xo.shape[0]
-    assert int(BL.last_info[1, 3]) < Xo.shape[0] // 10
-    assert abs(ll1 - a[0]) <= 1e-12 * abs(a[0]), (ll1, a[0])
-    np.testing.assert_allclose(g1, a[1], rtol=1e-10, atol=1e-10 * np.abs(a[1]).max())
-    np.testing.assert_allclose(F1, a[2], rtol=1e-10, atol=1e-10 * np.abs(a[2]).max())
-    assert abs(ll2 - c25[0]) <= 5e-6 * abs(c25[0])
-    assert ll2 != c25[0]  # the closed-form problem ran in the split form
+    for i, nu in ((1, 0.8), (2, 2.5)):
+        st, ll, g, F, b = res[i]
+        assert st == 0 and ll == one[nu][0], (nu, ll, one[nu][0])
+        np.testing.assert_array_equal(g, one[nu][1])
+        np.testing.assert_array_equal(F, one[nu][2])
+        assert int(BL.last_info[i, 3]) < Xo.shape[0] // 10
