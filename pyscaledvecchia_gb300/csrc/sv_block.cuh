@@ -85,19 +85,30 @@ __device__ void assemble_sigma(int K, int d, const double* u, const double* nugm
                                double* Gp, double* Dp) {
   const int lane = Team<T>::lane();
   const int npair = K * (K + 1) / 2;
+  // g at r = 0 (the diagonal): the closed forms' -3 (nu = 1.5) and -5/3
+  // (nu = 2.5); 0 for nu = 0.5 and the general form (r below its floor)
+  const double g0 = mm.closed == 1 ? -3.0 : mm.closed == 2 ? -(5.0 / 3.0) : 0.0;
   for (int t = lane; t < npair; t += T) {
     int i, j;
     tri_index(t, i, j);
-    const double* ui = u + i * d;
-    const double* uj = u + j * d;
-    double s = 0.0;
-    for (int l = 0; l < d; ++l) {
-      const double df = ui[l] - uj[l];
-      s += df * df;
-    }
-    const double r = sqrt(s);
     double M, g, dMnu;
-    matern_eval(mm, r, M, g, dMnu, Gp != nullptr);
+    if (i == j) {
+      // r = 0: M = 1 and dM/dnu = 0, the values the routines below return
+      // there, without their square root and exponential
+      M = 1.0;
+      g = g0;
+      dMnu = 0.0;
+    } else {
+      const double* ui = u + i * d;
+      const double* uj = u + j * d;
+      double s = 0.0;
+      for (int l = 0; l < d; ++l) {
+        const double df = ui[l] - uj[l];
+        s += df * df;
+      }
+      const double r = sqrt(s);
+      matern_eval(mm, r, M, g, dMnu, Gp != nullptr);
+    }
     double nug = 0.0;
     if (i == j) nug = tau * (nugmask ? nugmask[i] : 1.0);
     double v = s2 * (M + nug);

@@ -178,9 +178,12 @@ SV_HD void matern_closed(int nu_code, double r, double& M, double& g) {
     M = (1.0 + c) * e;
     g = -3.0 * e;
   } else {
+    // c^2 / 3 as c^2 times 1/3 (a float64 division costs about ten float64
+    // instructions; the reference's kernels, compiled with fastmath, may
+    // make the same substitution)
     const double c = kSqrt5 * r;
     const double e = exp(-c);
-    M = (1.0 + c + c * c / 3.0) * e;
+    M = (1.0 + c + c * c * (1.0 / 3.0)) * e;
     g = -(5.0 / 3.0) * (1.0 + c) * e;
   }
 }
