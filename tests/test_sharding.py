@@ -177,13 +177,16 @@ def test_problem_sharded_fits_give_every_rank_every_model(tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("nu", [2.5, 0.8])
 @pytest.mark.parametrize("precision", ["float64", "split"])
 @pytest.mark.parametrize("nshard", [2, 3])
-def test_device_shards_give_the_one_gpu_bits(precision, nshard):
+def test_device_shards_give_the_one_gpu_bits(precision, nshard, nu):
     """Shards of one problem run stage by stage on the one GPU, the exchanges
     done in between (MAX of the chunk tables, SUM of the partial-sum rows):
     the result is sv_vecchia_loglik's bit for bit, for a problem whose
-    duplicated rows need chunk-wide jitter as well."""
+    duplicated rows need chunk-wide jitter as well; at nu = 0.8 each shard
+    builds the Matern tables in its first stage and its later passes read
+    them."""
     import torch
 
     from pyscaledvecchia_gb300.likelihood import DeviceProblem
@@ -203,9 +206,9 @@ def test_device_shards_give_the_one_gpu_bits(precision, nshard):
         y = rng.standard_normal(n)
         prob = DeviceProblem(X[order], y[order], np.ones((n, 1)), _nn_groups(nn, m))
         P = d + 2
-        ref = prob.evaluate(theta, 2.5, precision=precision, team_lanes=16)
-        probe = DeviceShard(prob, 0, 0, 2.5, P, precision=precision, team_lanes=16)
-        shards = [DeviceShard(prob, *partition_range(probe.parts, r, nshard), 2.5, P,
+        ref = prob.evaluate(theta, nu, precision=precision, team_lanes=16)
+        probe = DeviceShard(prob, 0, 0, nu, P, precision=precision, team_lanes=16)
+        shards = [DeviceShard(prob, *partition_range(probe.parts, r, nshard), nu, P,
                               precision=precision, team_lanes=16) for r in range(nshard)]
         cm = [s.stage1(theta) for s in shards]
         cmax = torch.stack(cm).max(dim=0).values.contiguous()
