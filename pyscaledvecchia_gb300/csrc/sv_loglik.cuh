@@ -126,7 +126,9 @@ __host__ __device__ inline int split_slot_doubles(int d, int NR, int kc) {
 }
 
 // launch the split-precision kernels over list entries [A.b0, A.b1) (all
-// K <= 32, closed-form nu); lanes = block team width (4, 8, 16 or 32).
+// K <= 32; a closed-form nu or the float32 table of a fixed nu, the blocks
+// of other problems go to the float64 pass); lanes = block team width (4, 8,
+// 16 or 32).
 // launch_block_split: float64 factorisation and solves (the split form);
 // launch_block_split_df: double-float factorisation and solves
 int launch_block_split(const LikArgs& A, int lanes, cudaStream_t st);

@@ -1,5 +1,6 @@
 // Split-precision block kernel of the Vecchia likelihood / score / Fisher
-// evaluation (blocks with K = k+1 <= 32, closed-form nu).
+// evaluation (blocks with K = k+1 <= 32; a closed-form nu or the float32
+// Matern table of a fixed nu).
 //
 // Same per-block record as the float64 kernels (likelihood.py:111-144 of the
 // reference), computed with float64 precision only where conditioning needs

@@ -1,6 +1,7 @@
 // The split-precision block kernel of the Vecchia likelihood / score /
-// Fisher evaluation (blocks with K = k+1 <= 32, closed-form nu): float32
-// assembly, float64 factorisation.
+// Fisher evaluation (blocks with K = k+1 <= 32; a closed-form nu or the
+// float32 Matern table of a fixed nu): float32 assembly, float64
+// factorisation.
 //
 // Same per-block record as the float64 kernels (likelihood.py:111-144 of the
 // reference), with the precision of each step chosen by what conditioning
