@@ -1049,6 +1049,40 @@ def main():
                           "per_entry_bessel_ms": ms_bes,
                           "table_vs_per_entry_bessel": errors_vs(tuple(r_bes), r_tab),
                           "bessel_k": bessel_error(torch, lib, Xo, nn, theta, 0.8)}
+        # estimated nu (the reference's nu=None; log nu in theta at nu = 1.3):
+        # M and g at nu and M at nu +- h (the central difference for dM/dnu)
+        # from the evaluation's three tables; the per-entry Bessel routine (a
+        # batched evaluation without tables) once, as their check
+        nu_e = 1.3
+        th_e = np.concatenate([theta[:-1], [math.log(nu_e)], theta[-1:]])
+        th_e_d = _lib.to_dev(torch, th_e, np.float64)
+        prob.launch(th_e_d, P + 1, None, True, True, 0.0, 0.0, True)
+        torch.cuda.synchronize()
+        ev = []
+        for _ in range(max(2, args.steps // 2)):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            prob.launch(th_e_d, P + 1, None, True, True, 0.0, 0.0, True)
+            e1.record(stream)
+            ev.append((e0, e1))
+        torch.cuda.synchronize()
+        ms_et = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+        r_et = prob.evaluate(th_e, None, estimate_nu=True)
+        BLe = BatchedLikelihood([BatchProblem(Xo, yo, Zo, groups, nu=None, estimate_nu=True)],
+                                matern_tables=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st_e, *r_eb = BLe.evaluate([th_e])[0]
+        torch.cuda.synchronize()
+        ms_eb = (time.perf_counter() - t0) * 1e3
+        del BLe
+        forms["nu_estimated"] = {"nu": nu_e, "float64_ms": ms_et,
+                                 "float64_blocks_per_s": n / (ms_et * 1e-3),
+                                 "kernel": "float64 block kernels, M and g at nu and M at nu +- h "
+                                           "from three Chebyshev tables of the device K_nu",
+                                 "per_entry_bessel_ms": ms_eb,
+                                 "table_vs_per_entry_bessel": errors_vs(tuple(r_eb), r_et)}
 
     peak = measured_peak(lib, torch, "fp64")
     peak32 = measured_peak(lib, torch, "fp32")

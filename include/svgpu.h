@@ -284,9 +284,10 @@ typedef struct sv_batch_desc {
   int32_t need_grad, any_estimate_nu, chunked, precision, team_lanes;
   int32_t theta_stride, out_stride;
   int32_t general_nu;   /* 1: some problem has a fixed nu outside {0.5, 1.5, */
-                        /*    2.5}; the workspace then holds a Matern table  */
-                        /*    per problem (as the one-problem call builds    */
-                        /*    for such a nu), so results match it bit for bit */
+                        /*    2.5} or an estimated nu; the workspace then    */
+                        /*    holds Matern tables per problem (as the        */
+                        /*    one-problem call builds for such a nu), so     */
+                        /*    results match it bit for bit                   */
   double split_rho_min;
   int64_t nblk_max;     /* blocks of the largest problem (sizes the reductions) */
 } sv_batch_desc;

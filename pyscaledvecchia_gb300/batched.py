@@ -152,12 +152,12 @@ class BatchedLikelihood:
         self.dmax = int(self.d.max())
         self.qmax = int(self.q.max())
         self.any_est = bool(self.estimate_nu.any())
-        # a fixed nu without a closed form in some problem: the evaluation
-        # interpolates its Matern from a per-problem table
-        # (matern_tables=False keeps the per-entry Bessel routine: the check
-        # of the tables)
+        # a fixed nu without a closed form, or an estimated nu, in some
+        # problem: the evaluation interpolates its Matern from per-problem
+        # tables (matern_tables=False keeps the per-entry Bessel routine: the
+        # check of the tables)
         self.general_nu = matern_tables and any(
-            not pr.estimate_nu and float(pr.nu) not in (0.5, 1.5, 2.5) for pr in problems)
+            pr.estimate_nu or float(pr.nu) not in (0.5, 1.5, 2.5) for pr in problems)
         self.Pmax = self.dmax + 2 + (1 if self.any_est else 0)
         self.ostride = 1 + self.Pmax + self.Pmax * self.Pmax + self.qmax
 

@@ -42,9 +42,14 @@ struct MaternMode {
   double nu_p, nu_m;   // nu +- h
   double lc_p, lc_m;   // log_coef at nu +- h
   double inv2h;        // 1 / (2h)
-  const double* tab;   // fixed general nu: the table of M and g (or null)
+  const double* tab;   // general nu: the table of M and g (or null)
   int tab_elo;         // its first octave
   double s2n;          // sqrt(2 nu)
+  // estimated nu with tables: those of nu + h and nu - h
+  const double* tab_p;
+  const double* tab_m;
+  int elo_p, elo_m;
+  double s2n_p, s2n_m;
 };
 
 __device__ __forceinline__ void matern_eval(const MaternMode& mm, double r, double& M, double& g,
@@ -54,9 +59,17 @@ __device__ __forceinline__ void matern_eval(const MaternMode& mm, double r, doub
     dMnu = 0.0;
     return;
   }
-  if (mm.tab && !mm.estimate_nu) {
+  if (mm.tab) {
     matern_table_Mg(mm.tab, mm.tab_elo, mm.s2n, mm.nu, mm.log_coef, r, M, g, want_g);
     dMnu = 0.0;
+    if (mm.estimate_nu) {
+      // _matern_general.py:170-176 (central difference in nu), M at nu +- h
+      // from their tables
+      double Mp, Mm, gx;
+      matern_table_Mg(mm.tab_p, mm.elo_p, mm.s2n_p, mm.nu_p, mm.lc_p, r, Mp, gx, false);
+      matern_table_Mg(mm.tab_m, mm.elo_m, mm.s2n_m, mm.nu_m, mm.lc_m, r, Mm, gx, false);
+      dMnu = (Mp - Mm) * mm.inv2h;
+    }
     return;
   }
   if (want_g) {

@@ -32,10 +32,20 @@
 
 namespace sv {
 
-// whether problem D interpolates its Matern from a table: a fixed nu without
-// a closed form, at most 10, whose floor octave the table reaches
-__device__ __forceinline__ bool uses_matern_table(const sv_prob_desc& D) {
-  return !D.estimate_nu && mtab_ok(D.nu);
+// the central difference step of an estimated nu (_matern_general.py:135, nu_fd_h)
+constexpr double kNuFdH = 1e-3;
+
+// the smoothness of problem D at theta th (fixed, or estimated: exp of its
+// entry of theta)
+__device__ __forceinline__ double problem_nu(const sv_prob_desc& D, const double* th) {
+  return D.estimate_nu ? exp(th[1 + D.d]) : D.nu;
+}
+
+// whether problem D interpolates its Matern from tables at smoothness nu: a
+// fixed nu without a closed form, at most 10, whose floor octave the table
+// reaches; an estimated nu whose nu - h and nu + h are in that range
+__device__ __forceinline__ bool uses_matern_table(const sv_prob_desc& D, double nu) {
+  return D.estimate_nu ? mtab_est_ok(nu, kNuFdH) : mtab_ok(nu);
 }
 
 // theta -> per-problem parameters (sigma^2, tau, nu, 1/lambda)
@@ -87,16 +97,24 @@ __global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, in
     mm.estimate_nu = D.estimate_nu;
     mm.nu = nu;
     mm.log_coef = (mm.closed < 0) ? matern_log_coef(nu) : 0.0;
-    const double h = 1e-3;  // _matern_general.py:135 (nu_fd_h)
+    const double h = kNuFdH;
     mm.nu_p = nu + h;
     mm.nu_m = nu - h;
     mm.lc_p = D.estimate_nu ? matern_log_coef(mm.nu_p) : 0.0;
     mm.lc_m = D.estimate_nu ? matern_log_coef(mm.nu_m) : 0.0;
     mm.inv2h = 1.0 / (2.0 * h);
-    // fixed general nu: M and g from the table built for this call
-    mm.tab = (mtabs && uses_matern_table(D)) ? mtabs + (size_t)p * kMtabSlotDoubles : nullptr;
+    // general nu: M and g from the tables built for this call (an estimated
+    // nu also M at nu +- h)
+    mm.tab = (mtabs && uses_matern_table(D, nu)) ? mtabs + (size_t)p * kMtabSlotDoubles : nullptr;
     mm.tab_elo = mm.tab ? mtab_elo(nu) : 0;
     mm.s2n = sqrt(2.0 * nu);
+    const bool est_tab = mm.tab && D.estimate_nu;
+    mm.tab_p = est_tab ? mm.tab + kMtabOffP : nullptr;
+    mm.tab_m = est_tab ? mm.tab + kMtabOffM : nullptr;
+    mm.elo_p = est_tab ? mtab_elo(mm.nu_p) : 0;
+    mm.elo_m = est_tab ? mtab_elo(mm.nu_m) : 0;
+    mm.s2n_p = sqrt(2.0 * mm.nu_p);
+    mm.s2n_m = sqrt(2.0 * mm.nu_m);
     I.mm = mm;
     // split kernels: a closed form, the float32 table, or none
     MaternF32 mf;
@@ -105,24 +123,29 @@ __global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, in
     mf.esw = ftab_switch(nu);
     mf.s2n = (float)mm.s2n;
     mf.tab = nullptr;
-    if (mf.code < 0 && mm.tab && ftabs && ftab_ok(nu)) {
+    if (mf.code < 0 && mm.tab && !D.estimate_nu && ftabs && ftab_ok(nu)) {
       mf.code = 3;
-      mf.tab = (const float4*)(mm.tab + kMtabMaxDoubles);
+      mf.tab = (const float4*)(mm.tab + kFtabOff);
     }
     I.mf32 = mf;
   }
   for (int l = threadIdx.x; l < d; l += blockDim.x) I.invlam[l] = exp(-th[1 + l]);
 }
 
-// the Matern tables of the problems that use one (kMtabMaxDoubles each, at
-// problem p's slot): CTA (interval, p) of kMtabN threads takes the node values
-// e^c M(c), e^c G(c) at the interval's Chebyshev points, then their
-// Chebyshev coefficients ([16 of M, 16 of G] per interval)
-__global__ void k_matern_tables(const sv_prob_desc* descs, double* tabs) {
+// the Matern tables of the problems that use them (kMtabMaxDoubles each, in
+// problem p's slot: nu, and for an estimated nu also nu + h and nu - h):
+// CTA (interval, p, table) of kMtabN threads takes the node values e^c M(c),
+// e^c G(c) at the interval's Chebyshev points, then their Chebyshev
+// coefficients ([16 of M, 16 of G] per interval)
+__global__ void k_matern_tables(const sv_prob_desc* descs, const double* theta, int tstride,
+                                double* tabs) {
   __shared__ double fm[kMtabN], fg[kMtabN];
   const sv_prob_desc& D = descs[blockIdx.y];
-  if (!uses_matern_table(D)) return;
-  const double nu = D.nu;
+  const double nu0 = problem_nu(D, theta + (int64_t)blockIdx.y * tstride);
+  if (!uses_matern_table(D, nu0)) return;
+  const int z = blockIdx.z;  // 0: nu, 1: nu + h, 2: nu - h
+  if (z > 0 && !D.estimate_nu) return;
+  const double nu = z == 0 ? nu0 : z == 1 ? nu0 + kNuFdH : nu0 - kNuFdH;
   const int elo = mtab_elo(nu);
   const int iv = blockIdx.x, j = threadIdx.x;
   if (iv >= mtab_intervals(elo)) return;
@@ -144,25 +167,25 @@ __global__ void k_matern_tables(const sv_prob_desc* descs, double* tabs) {
     ag = fma(fg[i], w, ag);
   }
   const double sc2 = (j == 0 ? 1.0 : 2.0) / kMtabN;
-  double* tab = tabs + (size_t)blockIdx.y * kMtabSlotDoubles;
+  double* tab = tabs + (size_t)blockIdx.y * kMtabSlotDoubles + (z == 0 ? 0 : z == 1 ? kMtabOffP : kMtabOffM);
   tab[(size_t)iv * 2 * kMtabN + j] = am * sc2;
   tab[(size_t)iv * 2 * kMtabN + kMtabN + j] = ag * sc2;
 }
 
-// the float32 tables of the split kernels (after the float64 table in each
-// problem's slot): CTA (interval, p) of kFtabN threads takes the node values
+// the float32 tables of the split kernels (after the float64 tables in each
+// problem's slot; a fixed nu): CTA (interval, p) of kFtabN threads takes the node values
 // F (the deficit D below 2^esw, e^c M above) and e^c G, then their Chebyshev
 // coefficients rounded to float32 ([8 of F, 8 of Q] per interval)
 __global__ void k_matern_ftabs(const sv_prob_desc* descs, double* tabs) {
   __shared__ double ff[kFtabN], fq[kFtabN];
   const sv_prob_desc& D = descs[blockIdx.y];
-  if (!uses_matern_table(D) || !ftab_ok(D.nu)) return;
+  if (D.estimate_nu || !uses_matern_table(D, D.nu) || !ftab_ok(D.nu)) return;
   const int elo = mtab_elo(D.nu);
   const int iv = blockIdx.x, j = threadIdx.x;
   if (iv >= ftab_intervals(elo)) return;
   ftab_node(D.nu, elo, ftab_switch(D.nu), iv, j, ff[j], fq[j]);
   __syncthreads();
-  float* ft = (float*)(tabs + (size_t)blockIdx.y * kMtabSlotDoubles + kMtabMaxDoubles);
+  float* ft = (float*)(tabs + (size_t)blockIdx.y * kMtabSlotDoubles + kFtabOff);
   ft[(size_t)iv * 2 * kFtabN + j] = ftab_coef(ff, j);
   ft[(size_t)iv * 2 * kFtabN + kFtabN + j] = ftab_coef(fq, j);
 }
@@ -1088,8 +1111,8 @@ int run_eval(const EvalCall& C, cudaStream_t st, const ShardStage* sh = nullptr)
     if (S.tabs) {
       // the Matern tables of the problems of fixed general nu
       mtabs = (double*)(ws + W.mtab);
-      k_matern_tables<<<dim3(2 * (kMtabEhi - kMtabEloMin), (unsigned)S.nprob), kMtabN, 0, st>>>(C.probs,
-                                                                                               mtabs);
+      k_matern_tables<<<dim3(2 * (kMtabEhi - kMtabEloMin), (unsigned)S.nprob, S.any_est ? 3 : 1), kMtabN, 0,
+                        st>>>(C.probs, C.theta, C.tstride, mtabs);
       SV_CUDA_TRY(cudaGetLastError());
       if (split) {
         k_matern_ftabs<<<dim3(2 * (kFtabEhi - kMtabEloMin), (unsigned)S.nprob), kFtabN, 0, st>>>(C.probs,
@@ -1198,8 +1221,9 @@ EvalShape single_shape(const sv_loglik_desc* D) {
   // and a fixed nu of the float32 table; another nu runs the float64 kernels
   const bool f32 = matern_closed_code(D->nu) >= 0 || ftab_ok(D->nu);
   S.precision = (D->estimate_nu || !f32) ? 0 : D->precision;
-  // a fixed nu without a closed form: its Matern is interpolated from a table
-  S.tabs = (!D->estimate_nu && mtab_ok(D->nu)) ? 1 : 0;
+  // a fixed nu without a closed form, or an estimated nu: its Matern is
+  // interpolated from tables (built if the evaluation's nu is in their range)
+  S.tabs = (D->estimate_nu || mtab_ok(D->nu)) ? 1 : 0;
   return S;
 }
 

@@ -401,9 +401,14 @@ constexpr int kFtabN = 8;       // Chebyshev terms per interval and function
 constexpr int kFtabEhi = 6;     // the float32 table covers c < 2^6
 constexpr double kFtabNuMax = 8.0;  // larger nu: no float32 table
 constexpr int kFtabMaxFloats = 2 * (kFtabEhi - kMtabEloMin) * 2 * kFtabN;
-// one problem's slot in the table region: the float64 table, then the float32 one
-constexpr int kMtabSlotDoubles = kMtabMaxDoubles + kFtabMaxFloats / 2;
-static_assert((kMtabMaxDoubles * 8) % 16 == 0 && (kMtabSlotDoubles * 8) % 16 == 0,
+// one problem's slot in the table region: the float64 tables of nu, nu + h and
+// nu - h (the last two for an estimated nu's central difference), then the
+// float32 table
+constexpr int kMtabOffP = kMtabMaxDoubles;
+constexpr int kMtabOffM = 2 * kMtabMaxDoubles;
+constexpr int kFtabOff = 3 * kMtabMaxDoubles;
+constexpr int kMtabSlotDoubles = kFtabOff + kFtabMaxFloats / 2;
+static_assert((kFtabOff * 8) % 16 == 0 && (kMtabSlotDoubles * 8) % 16 == 0,
               "the float32 tables are read as float4");
 
 // whether a fixed nu gets the float64 table, and the float32 one
@@ -412,6 +417,11 @@ SV_HD bool mtab_ok(double nu) {
 }
 SV_HD bool ftab_ok(double nu) {
   return mtab_ok(nu) && nu <= kFtabNuMax && fabs(nu - rint(nu)) >= 1e-3;
+}
+// an estimated nu of this evaluation: tables of nu and nu +- h (h the
+// central difference's step) when all three lie in the table's range
+SV_HD bool mtab_est_ok(double nu, double h) {
+  return nu - h > 0.0 && nu + h <= kMtabNuMax && mtab_elo(nu - h) >= kMtabEloMin;
 }
 SV_HD int ftab_intervals(int elo) { return 2 * (kFtabEhi - elo); }
 // the first octave whose F is e^c M (at least 1)

@@ -246,7 +246,7 @@ class DeviceProblem:
         split = (precision in _SPLIT and split_nu(nu, estimate_nu)
                  and self.d + 3 + self.q <= 32)
         n = (1 if warp else 0) + (1 if cta else 0)
-        if matern_table_nu(nu, estimate_nu):
+        if estimate_nu or matern_table_nu(nu):
             n += 2 if split else 1  # the Matern tables: float64, and float32 for the split kernels
         if split and warp:
             n += 1  # coordinate pre-pass

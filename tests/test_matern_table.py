@@ -96,3 +96,72 @@ def test_no_table_above_nu_10():
     assert st == 0 and ll == ll_b
     np.testing.assert_array_equal(g, g_b)
     np.testing.assert_array_equal(F, F_b)
+
+
+def _est_theta(theta, nu):
+    """theta of an estimated-nu evaluation: log nu inserted before log tau."""
+    return np.concatenate([theta[:-1], [math.log(nu)], theta[-1:]])
+
+
+@pytest.mark.parametrize("nu", [0.45, 1.3, 3.7])
+def test_estimated_nu_tables(nu):
+    """An estimated nu interpolates M and g at nu, and M at nu +- h for the
+    central difference dM/dnu (_matern_general.py:170-176), from three tables
+    built for the evaluation's nu: against the per-entry Bessel routine (a
+    batched evaluation built with matern_tables=False) ll within 1e-12, the
+    score and Fisher information within 1e-9 of their largest entries (the
+    difference of two tabulated values over 2h = 2e-3 carries their 1e-15
+    rounding times 500), and the batched evaluation with tables equals the
+    one-problem one bit for bit."""
+    from pyscaledvecchia_gb300.batched import BatchedLikelihood, BatchProblem
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    Xo, yo, Zo, groups, theta = _problem(6, 3000, 4, 20, nu)
+    th = _est_theta(theta, nu)
+    ll_t, g_t, F_t, b_t = DeviceProblem(Xo, yo, Zo, groups).evaluate(th, None, estimate_nu=True)
+    BT = BatchedLikelihood([BatchProblem(Xo, yo, Zo, groups, nu=None, estimate_nu=True)])
+    st, ll_2, g_2, F_2, b_2 = BT.evaluate([th])[0]
+    assert st == 0 and ll_2 == ll_t
+    np.testing.assert_array_equal(g_2, g_t)
+    np.testing.assert_array_equal(F_2, F_t)
+    BL = BatchedLikelihood([BatchProblem(Xo, yo, Zo, groups, nu=None, estimate_nu=True)],
+                           matern_tables=False)
+    st, ll_b, g_b, F_b, b_b = BL.evaluate([th])[0]
+    assert st == 0
+    assert ll_t != ll_b or np.any(g_t != g_b)  # the tables were used
+    assert abs(ll_t - ll_b) <= 1e-12 * abs(ll_b), (ll_t, ll_b)
+    np.testing.assert_allclose(g_t, g_b, rtol=0, atol=1e-9 * np.abs(g_b).max())
+    np.testing.assert_allclose(F_t, F_b, rtol=0, atol=1e-9 * np.abs(F_b).max())
+    np.testing.assert_allclose(b_t, b_b, rtol=1e-11, atol=1e-13)
+
+
+def test_estimated_nu_beyond_the_tables():
+    """An estimated nu whose nu + h exceeds 10 keeps the per-entry Bessel
+    routine: bit for bit the evaluation without tables."""
+    from pyscaledvecchia_gb300.batched import BatchedLikelihood, BatchProblem
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    nu = 10.0
+    Xo, yo, Zo, groups, theta = _problem(7, 1500, 3, 15, nu)
+    th = _est_theta(theta, nu)
+    a = DeviceProblem(Xo, yo, Zo, groups).evaluate(th, None, estimate_nu=True)
+    BL = BatchedLikelihood([BatchProblem(Xo, yo, Zo, groups, nu=None, estimate_nu=True)],
+                           matern_tables=False)
+    st, ll, g, F, b = BL.evaluate([th])[0]
+    assert st == 0 and ll == a[0]
+    np.testing.assert_array_equal(g, a[1])
+    np.testing.assert_array_equal(F, a[2])
+
+
+def test_estimated_nu_tables_against_the_oracle():
+    """The estimated-nu evaluation with tables against the oracle (scipy's kv
+    per entry, the reference's central difference)."""
+    from oracle import oracle
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    nu = 1.3
+    Xo, yo, Zo, groups, theta = _problem(8, 500, 3, 12, nu)
+    th = _est_theta(theta, nu)
+    ll, g, F, b = DeviceProblem(Xo, yo, Zo, groups).evaluate(th, None, estimate_nu=True)
+    ll_o, g_o, F_o, b_o = oracle.vecchia_loglik_np(th, Xo, yo, Zo, groups, None,
+                                                    estimate_nu=True)[:4]
+    assert abs(ll - ll_o) <= 1e-10 * abs(ll_o), (ll, ll_o)
+    np.testing.assert_allclose(g, g_o, rtol=1e-7, atol=1e-7 * np.abs(g_o).max())
+    np.testing.assert_allclose(F, F_o, rtol=1e-7, atol=1e-7 * np.abs(F_o).max())
