@@ -44,7 +44,7 @@ typedef struct CUstream_st* sv_stream_t; /* identical to cudaStream_t */
 
 /* version of this interface: sv_abi_version() returns it; bumped whenever a
  * signature or a structure layout changes */
-#define SV_ABI_VERSION 3
+#define SV_ABI_VERSION 4
 
 const char* sv_status_string(int status);
 int sv_abi_version(void);
@@ -377,6 +377,15 @@ int sv_encoder_adam(float* params, const float* grad, float* m, float* v, uint16
 int sv_matern_eval(const double* r, int64_t n, double nu, int32_t which, int32_t general,
                    double* out, sv_stream_t stream);
 
+/* The Chebyshev table of M and g of a fixed smoothness nu without a closed
+ * form (0 < nu <= 10) that the likelihood builds for such a nu (16-term
+ * series of e^c M(c) and e^c g(c) on half-octave intervals of
+ * c = sqrt(2 nu) r), into device float64[sv_matern_table_doubles()], for
+ * sv_pred_desc.matern_table.  SV_EINVAL for a nu without a table or a
+ * smaller buffer. */
+int64_t sv_matern_table_doubles(void);
+int sv_matern_table(double nu, double* table, int64_t table_doubles, sv_stream_t stream);
+
 /* Modified Bessel function of the second kind K_nu(x) (device Temme/Steed
  * evaluation; stands in for scipy.special.kv on the _matern_general.py path). */
 int sv_bessel_k(const double* x, int64_t n, double nu, double* out, sv_stream_t stream);
@@ -435,6 +444,10 @@ typedef struct sv_pred_desc {
                          /*    d_k / Sigma_kk falls below this (<= 0:     */
                          /*    1e-4), or that does not factor, is redone  */
                          /*    in float64; info[SV_INFO_AUX] counts them  */
+  const double* matern_table; /* general = 1: the Matern table of nu from  */
+                         /*    sv_matern_table (device memory), so that   */
+                         /*    M and g are interpolated as the likelihood */
+                         /*    interpolates them; NULL: K_nu per entry    */
 } sv_pred_desc;
 
 /* One prediction block per target row tgt[b] (noise-free unless

@@ -78,11 +78,12 @@ class PredDesc(ctypes.Structure):
     """Mirror of sv_pred_desc (include/svgpu.h)."""
     _fields_ = [("nall", c_i64), ("nobs", c_i64), ("nblk", c_i64), ("d", c_i32), ("k", c_i32),
                 ("ldnbr", c_i32), ("general", c_i32), ("target_nugget", c_i32),
-                ("precision", c_i32), ("nu", c_dbl), ("split_rho_min", c_dbl)]
+                ("precision", c_i32), ("nu", c_dbl), ("split_rho_min", c_dbl),
+                ("matern_table", c_vp)]
 
 
 # SV_ABI_VERSION of include/svgpu.h that the structures above mirror
-ABI_VERSION = 3
+ABI_VERSION = 4
 
 # name -> (restype, argtypes); every symbol declared in include/svgpu.h
 SIGNATURES = {
@@ -123,6 +124,8 @@ SIGNATURES = {
     "sv_encoder_adam": (c_i32, [c_vp] * 5 + [c_i64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                              ctypes.c_float, c_i32, ctypes.c_float, c_vp]),
     "sv_matern_eval": (c_i32, [c_vp, c_i64, c_dbl, c_i32, c_i32, c_vp, c_vp]),
+    "sv_matern_table_doubles": (c_i64, []),
+    "sv_matern_table": (c_i32, [c_dbl, c_vp, c_i64, c_vp]),
     "sv_bessel_k": (c_i32, [c_vp, c_i64, c_dbl, c_vp, c_vp]),
     "sv_block_cov": (c_i32, [c_vp, c_i64, c_i32, c_i32, c_vp, c_dbl, c_dbl, c_dbl, c_i32, c_i32,
                              c_dbl, c_vp, c_vp, c_vp, c_vp]),

@@ -96,6 +96,13 @@ __global__ void k_matern_eval32(const double* r, int64_t n, double nu, int which
   }
 }
 
+// the float64 Matern table of nu (as the likelihood builds it): CTA
+// (interval) of kMtabN threads
+__global__ void k_matern_table1(double nu, double* tab) {
+  __shared__ double fm[kMtabN], fg[kMtabN];
+  mtab_build_interval(nu, blockIdx.x, fm, fg, tab);
+}
+
 __global__ void k_bessel_k(const double* x, int64_t n, double nu, double* out) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -188,6 +195,15 @@ extern "C" int sv_matern_eval(const double* r, int64_t n, double nu, int32_t whi
   if (grid > 16LL * sv_num_sms()) grid = 16LL * sv_num_sms();
   sv::k_matern_eval<<<(int)grid, 256, 0, (cudaStream_t)stream>>>(r, n, nu, which, general, lc, code,
                                                                   out);
+  SV_CUDA_TRY(cudaGetLastError());
+  return SV_OK;
+}
+
+extern "C" int64_t sv_matern_table_doubles(void) { return sv::kMtabMaxDoubles; }
+
+extern "C" int sv_matern_table(double nu, double* table, int64_t table_doubles, sv_stream_t stream) {
+  if (!table || !sv::mtab_ok(nu) || table_doubles < sv::kMtabMaxDoubles) return SV_EINVAL;
+  sv::k_matern_table1<<<sv::mtab_intervals(sv::mtab_elo(nu)), sv::kMtabN, 0, (cudaStream_t)stream>>>(nu, table);
   SV_CUDA_TRY(cudaGetLastError());
   return SV_OK;
 }

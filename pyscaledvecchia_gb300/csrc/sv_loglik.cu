@@ -146,30 +146,9 @@ __global__ void k_matern_tables(const sv_prob_desc* descs, const double* theta, 
   const int z = blockIdx.z;  // 0: nu, 1: nu + h, 2: nu - h
   if (z > 0 && !D.estimate_nu) return;
   const double nu = z == 0 ? nu0 : z == 1 ? nu0 + kNuFdH : nu0 - kNuFdH;
-  const int elo = mtab_elo(nu);
-  const int iv = blockIdx.x, j = threadIdx.x;
-  if (iv >= mtab_intervals(elo)) return;
-  const double log_coef = matern_log_coef(nu);
-  const int e = elo + iv / 2, half = iv & 1;
-  const double tj = cospi((j + 0.5) / kMtabN);
-  const double m = half ? (tj - kMtabO1) / kMtabS1 : (tj - kMtabO0) / kMtabS0;
-  const double c = ldexp(m, e);
-  double knu, knm1;
-  bessel_k_nu_and_prev(nu, c, knu, knm1);
-  const double sc = exp(c + log_coef + nu * log(c));  // e^c times the prefactor
-  fm[j] = sc * knu;
-  fg[j] = -(2.0 * nu / c) * sc * knm1;
-  __syncthreads();
-  double am = 0.0, ag = 0.0;
-  for (int i = 0; i < kMtabN; ++i) {
-    const double w = cospi((double)j * (i + 0.5) / kMtabN);
-    am = fma(fm[i], w, am);
-    ag = fma(fg[i], w, ag);
-  }
-  const double sc2 = (j == 0 ? 1.0 : 2.0) / kMtabN;
+  if ((int)blockIdx.x >= mtab_intervals(mtab_elo(nu))) return;
   double* tab = tabs + (size_t)blockIdx.y * kMtabSlotDoubles + (z == 0 ? 0 : z == 1 ? kMtabOffP : kMtabOffM);
-  tab[(size_t)iv * 2 * kMtabN + j] = am * sc2;
-  tab[(size_t)iv * 2 * kMtabN + kMtabN + j] = ag * sc2;
+  mtab_build_interval(nu, blockIdx.x, fm, fg, tab);
 }
 
 // the float32 tables of the split kernels (after the float64 tables in each

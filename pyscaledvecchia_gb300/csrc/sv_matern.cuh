@@ -263,6 +263,38 @@ SV_HD void matern_general_MG_c(double c, double nu, double log_coef, double& M, 
 }
 
 #ifdef __CUDACC__
+// node j of interval iv of the float64 table of nu: e^c M(c) and e^c G(c) at
+// the interval's j-th Chebyshev point
+__device__ inline void mtab_node(double nu, int elo, int iv, int j, double& fm, double& fg) {
+  const int e = elo + iv / 2, half = iv & 1;
+  const double tj = cospi((j + 0.5) / kMtabN);
+  const double m = half ? (tj - kMtabO1) / kMtabS1 : (tj - kMtabO0) / kMtabS0;
+  const double c = ldexp(m, e);
+  double knu, knm1;
+  bessel_k_nu_and_prev(nu, c, knu, knm1);
+  const double sc = exp(c + matern_log_coef(nu) + nu * log(c));  // e^c times the prefactor
+  fm = sc * knu;
+  fg = -(2.0 * nu / c) * sc * knm1;
+}
+
+// Chebyshev coefficient j of an interval of the float64 table from its
+// kMtabN node values f
+__device__ inline double mtab_coef(const double* f, int j) {
+  double a = 0.0;
+  for (int i = 0; i < kMtabN; ++i) a = fma(f[i], cospi((double)j * (i + 0.5) / kMtabN), a);
+  return a * ((j == 0 ? 1.0 : 2.0) / kMtabN);
+}
+
+// interval iv of the float64 table of nu into tab (a CTA of kMtabN threads,
+// thread j; fm, fg shared arrays of kMtabN)
+__device__ inline void mtab_build_interval(double nu, int iv, double* fm, double* fg, double* tab) {
+  const int j = threadIdx.x;
+  mtab_node(nu, mtab_elo(nu), iv, j, fm[j], fg[j]);
+  __syncthreads();
+  tab[(size_t)iv * 2 * kMtabN + j] = mtab_coef(fm, j);
+  tab[(size_t)iv * 2 * kMtabN + kMtabN + j] = mtab_coef(fg, j);
+}
+
 __device__ __forceinline__ double mtab_clenshaw(const double* cf, double t) {
   const double t2 = t + t;
   double b1 = 0.0, b2 = 0.0;

@@ -40,6 +40,7 @@ struct PredArgs {
   int split;       // 1: float32 assembly (closed-form nu only)
   double rho_min;  // split: smallest pivot ratio d_k / Sigma_kk kept
   double nu;
+  const double* tab;  // general nu: its Matern table (or null: K_nu per entry)
 };
 
 struct PredPrm {
@@ -59,9 +60,12 @@ __device__ void pred_params(const PredArgs& A, PredPrm* prm) {
     mm.log_coef = A.closed < 0 ? matern_log_coef(A.nu) : 0.0;
     mm.nu_p = mm.nu_m = mm.lc_p = mm.lc_m = 0.0;
     mm.inv2h = 0.0;
-    mm.tab = nullptr;
-    mm.tab_elo = 0;
-    mm.s2n = 0.0;
+    mm.tab = A.closed < 0 ? A.tab : nullptr;
+    mm.tab_elo = mm.tab ? mtab_elo(A.nu) : 0;
+    mm.s2n = sqrt(2.0 * A.nu);
+    mm.tab_p = mm.tab_m = nullptr;
+    mm.elo_p = mm.elo_m = 0;
+    mm.s2n_p = mm.s2n_m = 0.0;
     prm->mm = mm;
   }
   for (int l = threadIdx.x; l < A.d; l += blockDim.x) prm->invlam[l] = exp(-A.theta[1 + l]);
@@ -464,6 +468,7 @@ extern "C" int sv_predict_blocks(const sv_pred_desc* D, const double* theta, con
   if (!(D->nu > 0.0)) return SV_EINVAL;
   const int closed = matern_closed_code(D->nu);
   if (!D->general && closed < 0) return SV_EINVAL;
+  if (D->matern_table && (!D->general || !mtab_ok(D->nu))) return SV_EINVAL;
   if (D->nobs > 0 && !resid && (mean || rhs)) return SV_EINVAL;
   cudaStream_t st = (cudaStream_t)stream;
   int32_t init_info[4] = {0, -1, 0, 0};
@@ -488,6 +493,7 @@ extern "C" int sv_predict_blocks(const sv_pred_desc* D, const double* theta, con
   A.closed = D->general ? -1 : closed;
   A.target_nugget = D->target_nugget;
   A.nu = D->nu;
+  A.tab = D->matern_table;
   if (D->precision < 0 || D->precision > 1) return SV_EINVAL;
   A.split = (D->precision == 1 && A.closed >= 0) ? 1 : 0;
   A.rho_min = D->split_rho_min > 0.0 ? D->split_rho_min : 1e-4;

@@ -290,6 +290,25 @@ class ScaledVecchiaGP:
     def _general(self):
         return self.nu_ not in (0.5, 1.5, 2.5)
 
+    def _matern_table(self):
+        """Device Matern table of a general fitted nu (sv_matern_table: the
+        table the likelihood interpolates M and g from), built once per nu;
+        None for the closed forms and a nu outside the tables' range (K_nu
+        per entry)."""
+        from .likelihood import matern_table_nu
+        nu = float(self.nu_)
+        if not self._general() or not matern_table_nu(nu):
+            return None
+        cache = getattr(self, "_mtab_cache", None)
+        if cache is not None and cache[0] == nu:
+            return cache[1]
+        lib, torch = _lib.device_ready()
+        t = torch.empty(int(lib.sv_matern_table_doubles()), dtype=torch.float64, device="cuda")
+        _lib.check(lib, lib.sv_matern_table(nu, _lib.ptr(t), t.numel(), _lib.stream_handle(torch)),
+                   "sv_matern_table")
+        self._mtab_cache = (nu, t)
+        return t
+
     def _predict_scaled(self, Xs_std, X_tr, y_tr_resid, m, noise_free=True):
         """Marginal Vecchia predictions conditioning on the m nearest training
         inputs.  Exact mean and variance of the Vecchia predictive law."""
@@ -315,6 +334,8 @@ class ScaledVecchiaGP:
         D.d, D.k, D.ldnbr = d, m, m
         D.general, D.nu = int(self._general()), float(self.nu_)
         D.precision = int(self._precision() == "split")
+        mtab = self._matern_table()
+        D.matern_table = mtab.data_ptr() if mtab is not None else None
         th = _lib.to_dev(torch, self._pred_theta(), np.float64)
         info2 = _lib.new_info(torch)
         rc = lib.sv_predict_blocks(D, _lib.ptr(th), _lib.ptr(Xall), _lib.ptr(tgt), _lib.ptr(nbr),
@@ -380,6 +401,8 @@ class ScaledVecchiaGP:
         D.d, D.k, D.ldnbr = d, k, k
         D.general, D.nu = int(self._general()), float(self.nu_)
         D.precision = int(self._precision() == "split")
+        mtab = self._matern_table()
+        D.matern_table = mtab.data_ptr() if mtab is not None else None
         th = _lib.to_dev(torch, self._pred_theta(), np.float64)
         info2 = _lib.new_info(torch)
         rc = lib.sv_predict_blocks(D, _lib.ptr(th), _lib.ptr(Xo), _lib.ptr(tgt), _lib.ptr(nbr),

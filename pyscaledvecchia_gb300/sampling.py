@@ -13,6 +13,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _lib
+from .likelihood import matern_table_nu
 
 __all__ = ["vecchia_prior_sample"]
 
@@ -36,6 +37,13 @@ def vecchia_prior_sample_device(torch, Xo_d, nn_d, theta, nu, eps_d):
     D.general = int(nu not in (0.5, 1.5, 2.5))
     D.target_nugget = 1
     D.nu = float(nu)
+    mtab = None
+    if D.general and matern_table_nu(float(nu)):
+        # M and g interpolated as the likelihood interpolates them
+        mtab = torch.empty(int(lib.sv_matern_table_doubles()), dtype=torch.float64, device="cuda")
+        _lib.check(lib, lib.sv_matern_table(float(nu), _lib.ptr(mtab), mtab.numel(),
+                                            _lib.stream_handle(torch)), "sv_matern_table")
+        D.matern_table = mtab.data_ptr()
     th = _lib.to_dev(torch, np.asarray(theta, dtype=np.float64), np.float64)
     info = _lib.new_info(torch)
     rc = lib.sv_predict_blocks(D, _lib.ptr(th), _lib.ptr(Xo_d), _lib.ptr(tgt), _lib.ptr(nbr),

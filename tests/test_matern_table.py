@@ -165,3 +165,67 @@ def test_estimated_nu_tables_against_the_oracle():
     assert abs(ll - ll_o) <= 1e-10 * abs(ll_o), (ll, ll_o)
     np.testing.assert_allclose(g, g_o, rtol=1e-7, atol=1e-7 * np.abs(g_o).max())
     np.testing.assert_allclose(F, F_o, rtol=1e-7, atol=1e-7 * np.abs(F_o).max())
+
+
+def test_prediction_with_the_table(monkeypatch):
+    """Prediction blocks (sv_predict_blocks) of a general nu interpolate M
+    from the table of sv_matern_table, as the likelihood does: the marginal
+    mean and sd and the joint mean agree with the per-entry Bessel routine
+    to 1e-10, and so do unconditional draws (sampling.vecchia_prior_sample)."""
+    from pyscaledvecchia_gb300 import sampling
+    from pyscaledvecchia_gb300.gp import ScaledVecchiaGP
+    from pyscaledvecchia_gb300.ordering import find_ordered_nn, maximin_order
+    rng = np.random.default_rng(12)
+    X = rng.random((1500, 3))
+    y = np.sin(4 * X[:, 0]) + X[:, 1] + 0.05 * rng.standard_normal(1500)
+    Xq = rng.random((400, 3))
+    gp = ScaledVecchiaGP(nu=0.8, m_est=15, m_pred=60, var_correction=False).fit(X, y)
+    assert gp._matern_table() is not None
+    mu_t, sd_t = gp.predict(Xq, return_std=True)
+    jm_t = gp.predict_joint(Xq)["mean"]
+    gp._matern_table = lambda: None  # K_nu per entry
+    mu_b, sd_b = gp.predict(Xq, return_std=True)
+    jm_b = gp.predict_joint(Xq)["mean"]
+    assert np.any(mu_t != mu_b)  # the table was used
+    np.testing.assert_allclose(mu_t, mu_b, rtol=1e-10, atol=1e-10 * np.abs(mu_b).max())
+    np.testing.assert_allclose(sd_t, sd_b, rtol=1e-10)
+    np.testing.assert_allclose(jm_t, jm_b, rtol=1e-10, atol=1e-10 * np.abs(jm_b).max())
+    th = np.array([0.2, math.log(0.3), math.log(0.6), math.log(0.4), math.log(1e-3)])
+    order = maximin_order(X / np.exp(th[1:4]))
+    Xo = X[order]
+    nn = find_ordered_nn(Xo / np.exp(th[1:4]), 12)
+    eps = rng.standard_normal(1500)
+    y_t = sampling.vecchia_prior_sample(Xo, nn, th, 0.8, eps)
+    monkeypatch.setattr(sampling, "matern_table_nu", lambda nu: False)
+    y_b = sampling.vecchia_prior_sample(Xo, nn, th, 0.8, eps)
+    assert np.any(y_t != y_b)
+    np.testing.assert_allclose(y_t, y_b, rtol=1e-10, atol=1e-10 * np.abs(y_b).max())
+
+
+def test_table_entry_point_checks():
+    """sv_matern_table takes a nu with a table only (no closed form, at most
+    10) and a buffer of sv_matern_table_doubles(); sv_predict_blocks takes a
+    table only for a general nu with one."""
+    import torch
+
+    from pyscaledvecchia_gb300 import _lib
+    lib, _ = _lib.device_ready()
+    nd = int(lib.sv_matern_table_doubles())
+    t = torch.empty(nd, dtype=torch.float64, device="cuda")
+    st = _lib.stream_handle(torch)
+    assert lib.sv_matern_table(0.8, _lib.ptr(t), nd, st) == _lib.SV_OK
+    assert lib.sv_matern_table(2.5, _lib.ptr(t), nd, st) == _lib.SV_EINVAL
+    assert lib.sv_matern_table(12.0, _lib.ptr(t), nd, st) == _lib.SV_EINVAL
+    assert lib.sv_matern_table(0.8, _lib.ptr(t), nd - 1, st) == _lib.SV_EINVAL
+    D = _lib.PredDesc()
+    D.nall, D.nobs, D.nblk, D.d, D.k, D.ldnbr = 4, 4, 1, 2, 1, 1
+    D.general, D.nu, D.matern_table = 0, 2.5, t.data_ptr()
+    x = torch.zeros(8, dtype=torch.float64, device="cuda")
+    th = torch.zeros(4, dtype=torch.float64, device="cuda")
+    tgt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nbr = torch.zeros(1, dtype=torch.int32, device="cuda")
+    info = _lib.new_info(torch)
+    rc = lib.sv_predict_blocks(D, _lib.ptr(th), _lib.ptr(x), _lib.ptr(tgt), _lib.ptr(nbr), None,
+                               None, None, None, None, _lib.ptr(info), st)
+    assert rc == _lib.SV_EINVAL
+    torch.cuda.synchronize()
