@@ -705,7 +705,7 @@ def run_predict(torch, lib, check_oracle=True):
     res["split_vs_float64"] = pred_errors(mu32, sd32, mu64, sd64)
     if check_oracle:
         # the oracle (C restatement of gp.py:242-277, OpenMP on the host's
-        # cores) on every 25th test point: the checker of both forms
+        # cores) on every 25th test point, against which both forms are compared
         from oracle import oracle
         oracle.build()
         oracle.set_threads(os.cpu_count() or 1)

@@ -1,6 +1,6 @@
 """CPU restatement of the reference's fit and marginal prediction.
 
-TEST INFRASTRUCTURE ONLY: used by tests/ as a checker and by ``bench.py``
+TEST INFRASTRUCTURE ONLY: used by tests/ to check the device path and by ``bench.py``
 for its CPU baseline of the fit + predict workload.  The product package
 (pyscaledvecchia_gb300) never imports, loads or calls anything here.
 

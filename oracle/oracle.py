@@ -1,7 +1,7 @@
 """CPU oracle for the scaled Vecchia hot path.
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
-as the checker, and by ``bench.py`` for its CPU baseline.  The product package
+to check the device result, and by ``bench.py`` for its CPU baseline.  The product package
 (pyscaledvecchia_gb300) never imports, loads or calls anything here.
 
 Two layers, both restating the reference implementation
