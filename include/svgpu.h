@@ -369,11 +369,13 @@ int sv_encoder_adam(float* params, const float* grad, float* m, float* v, uint16
  * general = 0: closed forms, nu in {0.5,1.5,2.5}: _covariance.py:49-72.
  * general = 1: Bessel form 2^(1-nu)/Gamma(nu) c^nu K_nu(c), c = sqrt(2nu) r,
  *              r floored at 1e-7: _matern_general.py:87-116.
- * which = 2, 3: the float32 forms the split kernels assemble with, at r
+ * which = 2, 3, 4: the float32 forms the split kernels assemble with, at r
  * rounded to float32 (values of float32, returned as doubles): 2 the
- * correlation deficit D = 1 - M_nu(r), 3 g(r); general = 0 the closed forms,
- * general = 1 the float32 table of a fixed nu (0 < nu <= 8 and at least
- * 1e-3 from an integer, else SV_EINVAL). */
+ * correlation deficit D = 1 - M_nu(r), 3 g(r), 4 dM/dnu of an estimated nu
+ * (the central difference (M_{nu+h} - M_{nu-h}) / 2h, h = 1e-3,
+ * _matern_general.py:170-176); general = 0 the closed forms (which 2, 3),
+ * general = 1 the float32 tables of a general nu (0 < nu <= 8 and at least
+ * 1e-3 from an integer, for which = 4 nu +- h as well; else SV_EINVAL). */
 int sv_matern_eval(const double* r, int64_t n, double nu, int32_t which, int32_t general,
                    double* out, sv_stream_t stream);
 

@@ -200,7 +200,7 @@ class BatchedLikelihood:
         self._lanes = {prec: self.team_lanes for prec in self.precisions}
         for prec in self.precisions:
             if (prec in _SPLIT and self.team_lanes == 0 and self.nwarp > 0
-                    and not self.any_est and self.Pmax + 1 + self.qmax <= 32):
+                    and self.Pmax + 1 + self.qmax <= 32):
                 from . import autotune
                 wp = bprob[wlist]
                 i = int(np.argmax(np.bincount(wp, minlength=self.nprob)))

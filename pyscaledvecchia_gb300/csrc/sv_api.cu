@@ -65,34 +65,46 @@ __global__ void k_matern_eval(const double* r, int64_t n, double nu, int which, 
 }
 
 // the split kernels' float32 Matern at r rounded to float32: which = 2 the
-// deficit D = 1 - M, which = 3 g; a closed form (general = 0) or the float32
-// table of a fixed general nu, which every CTA builds in its shared memory
-// as the likelihood's table kernel builds it in global memory
+// deficit D = 1 - M, which = 3 g, which = 4 dM/dnu of an estimated nu (the
+// central difference at nu +- 1e-3); a closed form (general = 0) or the
+// float32 tables of a general nu, which every CTA builds in its shared
+// memory as the likelihood's table kernel builds them in global memory
 __global__ void k_matern_eval32(const double* r, int64_t n, double nu, int which, int general,
                                 int code, double* out) {
-  __shared__ double fv[2][2 * (kFtabEhi - kMtabEloMin) * kFtabN];
+  __shared__ double fv[3][kFtabIntervals * kFtabN];
   __shared__ __align__(16) float tab[kFtabMaxFloats];
+  __shared__ __align__(16) float dtab[kDtabMaxFloats];
   MaternF32 mf;
   mf.code = general ? 3 : code;
   mf.elo = general ? mtab_elo(nu) : 0;
   mf.esw = ftab_switch(nu);
   mf.s2n = (float)sqrt(2.0 * nu);
   mf.tab = (const float4*)tab;
+  mf.dtab = which == 4 ? (const float4*)dtab : nullptr;
+  mf.nuf = (float)nu;
   if (general) {
     const int nint = ftab_intervals(mf.elo);
-    for (int t = threadIdx.x; t < nint * kFtabN; t += blockDim.x)
+    for (int t = threadIdx.x; t < nint * kFtabN; t += blockDim.x) {
       ftab_node(nu, mf.elo, mf.esw, t / kFtabN, t % kFtabN, fv[0][t], fv[1][t]);
+      if (which == 4) fv[2][t] = ftab_dnu_node(nu, 1e-3, mf.elo, mf.esw, t / kFtabN, t % kFtabN);
+    }
     __syncthreads();
     for (int t = threadIdx.x; t < nint * 2 * kFtabN; t += blockDim.x) {
       const int iv = t / (2 * kFtabN), w = (t / kFtabN) & 1, j = t % kFtabN;
       tab[t] = ftab_coef(fv[w] + iv * kFtabN, j);
     }
+    if (which == 4)
+      for (int t = threadIdx.x; t < nint * kFtabN; t += blockDim.x)
+        dtab[t] = ftab_coef(fv[2] + (t / kFtabN) * kFtabN, t % kFtabN);
     __syncthreads();
   }
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const float rf = (float)r[i];
-    out[i] = which == 2 ? (double)matern_deficit_f32(mf, rf) : (double)matern_g_f32(mf, rf);
+    const float v = which == 2 ? matern_deficit_f32(mf, rf)
+                    : which == 3 ? matern_g_f32(mf, rf)
+                                 : matern_dnu_f32(mf, rf);
+    out[i] = (double)v;
   }
 }
 
@@ -176,11 +188,12 @@ extern "C" int sv_fp64_fma_probe(double* out, int32_t iters, sv_stream_t stream)
 
 extern "C" int sv_matern_eval(const double* r, int64_t n, double nu, int32_t which,
                               int32_t general, double* out, sv_stream_t stream) {
-  if (n < 0 || (n > 0 && (!r || !out)) || which < 0 || which > 3) return SV_EINVAL;
+  if (n < 0 || (n > 0 && (!r || !out)) || which < 0 || which > 4) return SV_EINVAL;
   if (!(nu > 0.0)) return SV_EINVAL;
   const int code = sv::matern_closed_code(nu);
   if (!general && code < 0) return SV_EINVAL;
   if (which >= 2 && general && !sv::ftab_ok(nu)) return SV_EINVAL;
+  if (which == 4 && !(general && sv::ftab_est_ok(nu, 1e-3))) return SV_EINVAL;
   if (n == 0) return SV_OK;
   if (which >= 2) {
     int64_t grid = (n + 255) / 256;

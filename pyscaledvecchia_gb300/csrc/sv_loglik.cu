@@ -116,16 +116,19 @@ __global__ void k_prob_params(const sv_prob_desc* descs, const double* theta, in
     mm.s2n_p = sqrt(2.0 * mm.nu_p);
     mm.s2n_m = sqrt(2.0 * mm.nu_m);
     I.mm = mm;
-    // split kernels: a closed form, the float32 table, or none
+    // split kernels: a closed form, the float32 tables, or none
     MaternF32 mf;
     mf.code = mm.closed;
     mf.elo = mm.tab_elo;
     mf.esw = ftab_switch(nu);
     mf.s2n = (float)mm.s2n;
     mf.tab = nullptr;
-    if (mf.code < 0 && mm.tab && !D.estimate_nu && ftabs && ftab_ok(nu)) {
+    mf.dtab = nullptr;
+    mf.nuf = (float)nu;
+    if (mf.code < 0 && mm.tab && ftabs && (D.estimate_nu ? ftab_est_ok(nu, h) : ftab_ok(nu))) {
       mf.code = 3;
       mf.tab = (const float4*)(mm.tab + kFtabOff);
+      if (D.estimate_nu) mf.dtab = (const float4*)(mm.tab + kDtabOff);
     }
     I.mf32 = mf;
   }
@@ -152,21 +155,27 @@ __global__ void k_matern_tables(const sv_prob_desc* descs, const double* theta, 
 }
 
 // the float32 tables of the split kernels (after the float64 tables in each
-// problem's slot; a fixed nu): CTA (interval, p) of kFtabN threads takes the node values
-// F (the deficit D below 2^esw, e^c M above) and e^c G, then their Chebyshev
-// coefficients rounded to float32 ([8 of F, 8 of Q] per interval)
-__global__ void k_matern_ftabs(const sv_prob_desc* descs, double* tabs) {
-  __shared__ double ff[kFtabN], fq[kFtabN];
+// problem's slot): CTA (interval, p) of kFtabN threads takes the node values
+// F (the deficit D below 2^esw, e^c M above) and e^c G, for an estimated nu
+// also those of dM/dnu, then their Chebyshev coefficients rounded to float32
+// ([8 of F, 8 of Q] per interval; [8 of dM/dnu] per interval after them)
+__global__ void k_matern_ftabs(const sv_prob_desc* descs, const double* theta, int tstride,
+                               double* tabs) {
+  __shared__ double ff[kFtabN], fq[kFtabN], fd[kFtabN];
   const sv_prob_desc& D = descs[blockIdx.y];
-  if (D.estimate_nu || !uses_matern_table(D, D.nu) || !ftab_ok(D.nu)) return;
-  const int elo = mtab_elo(D.nu);
+  const double nu = problem_nu(D, theta + (int64_t)blockIdx.y * tstride);
+  if (!uses_matern_table(D, nu) || !(D.estimate_nu ? ftab_est_ok(nu, kNuFdH) : ftab_ok(nu))) return;
+  const int elo = mtab_elo(nu), esw = ftab_switch(nu);
   const int iv = blockIdx.x, j = threadIdx.x;
   if (iv >= ftab_intervals(elo)) return;
-  ftab_node(D.nu, elo, ftab_switch(D.nu), iv, j, ff[j], fq[j]);
+  ftab_node(nu, elo, esw, iv, j, ff[j], fq[j]);
+  if (D.estimate_nu) fd[j] = ftab_dnu_node(nu, kNuFdH, elo, esw, iv, j);
   __syncthreads();
-  float* ft = (float*)(tabs + (size_t)blockIdx.y * kMtabSlotDoubles + kFtabOff);
+  double* slot = tabs + (size_t)blockIdx.y * kMtabSlotDoubles;
+  float* ft = (float*)(slot + kFtabOff);
   ft[(size_t)iv * 2 * kFtabN + j] = ftab_coef(ff, j);
   ft[(size_t)iv * 2 * kFtabN + kFtabN + j] = ftab_coef(fq, j);
+  if (D.estimate_nu) ((float*)(slot + kDtabOff))[(size_t)iv * kFtabN + j] = ftab_coef(fd, j);
 }
 
 // the problem table of a one-problem evaluation, passed by value
@@ -1044,11 +1053,11 @@ int run_eval(const EvalCall& C, cudaStream_t st, const ShardStage* sh = nullptr)
   }
 
   // split forms (1: float64 factorisation, 2: double-float factorisation):
-  // no estimated nu and at most 32 right-hand sides (d + q <= 29); anything
-  // else runs the float64 kernels.  In a batch, the blocks of a problem whose
-  // nu has neither a closed form nor the float32 table go from the split
-  // kernels to the float64 pass
-  const bool split = (S.precision == 1 || S.precision == 2) && !S.any_est && A.NRmax <= 32;
+  // at most 32 right-hand sides (P + 1 + q); anything else runs the float64
+  // kernels.  The blocks of a problem whose nu (fixed, or estimated at this
+  // theta) has neither a closed form nor the float32 tables go from the
+  // split kernels to the float64 pass
+  const bool split = (S.precision == 1 || S.precision == 2) && A.NRmax <= 32;
   // 16 lanes per block is the fastest team width measured for every K from 6
   // to 31 (d = 3 and 10); 8 and 32 trail by up to 37 % and 12 %
   const int lanes = C.team_lanes > 0 ? C.team_lanes : 16;
@@ -1094,8 +1103,8 @@ int run_eval(const EvalCall& C, cudaStream_t st, const ShardStage* sh = nullptr)
                         st>>>(C.probs, C.theta, C.tstride, mtabs);
       SV_CUDA_TRY(cudaGetLastError());
       if (split) {
-        k_matern_ftabs<<<dim3(2 * (kFtabEhi - kMtabEloMin), (unsigned)S.nprob), kFtabN, 0, st>>>(C.probs,
-                                                                                                 mtabs);
+        k_matern_ftabs<<<dim3(kFtabIntervals, (unsigned)S.nprob), kFtabN, 0, st>>>(C.probs, C.theta, C.tstride,
+                                                                                 mtabs);
         SV_CUDA_TRY(cudaGetLastError());
       }
     }
@@ -1197,9 +1206,10 @@ EvalShape single_shape(const sv_loglik_desc* D) {
   S.need_grad = D->need_grad;
   S.any_est = D->estimate_nu;
   // the split forms assemble in float32 the closed forms (nu 0.5, 1.5, 2.5)
-  // and a fixed nu of the float32 table; another nu runs the float64 kernels
-  const bool f32 = matern_closed_code(D->nu) >= 0 || ftab_ok(D->nu);
-  S.precision = (D->estimate_nu || !f32) ? 0 : D->precision;
+  // and a fixed nu of the float32 table; another fixed nu runs the float64
+  // kernels (an estimated nu is decided on the device at each theta)
+  const bool f32 = D->estimate_nu || matern_closed_code(D->nu) >= 0 || ftab_ok(D->nu);
+  S.precision = f32 ? D->precision : 0;
   // a fixed nu without a closed form, or an estimated nu: its Matern is
   // interpolated from tables (built if the evaluation's nu is in their range)
   S.tabs = (D->estimate_nu || mtab_ok(D->nu)) ? 1 : 0;

@@ -432,15 +432,18 @@ __device__ __forceinline__ float matern_deficit_f32(int code, float r) {
 constexpr int kFtabN = 8;       // Chebyshev terms per interval and function
 constexpr int kFtabEhi = 6;     // the float32 table covers c < 2^6
 constexpr double kFtabNuMax = 8.0;  // larger nu: no float32 table
-constexpr int kFtabMaxFloats = 2 * (kFtabEhi - kMtabEloMin) * 2 * kFtabN;
+constexpr int kFtabIntervals = 2 * (kFtabEhi - kMtabEloMin);
+constexpr int kFtabMaxFloats = kFtabIntervals * 2 * kFtabN;  // F and Q
+constexpr int kDtabMaxFloats = kFtabIntervals * kFtabN;      // dM/dnu
 // one problem's slot in the table region: the float64 tables of nu, nu + h and
-// nu - h (the last two for an estimated nu's central difference), then the
-// float32 table
+// nu - h (the last two for an estimated nu's central difference), the
+// float32 table of D and g, and the float32 table of dM/dnu (an estimated nu)
 constexpr int kMtabOffP = kMtabMaxDoubles;
 constexpr int kMtabOffM = 2 * kMtabMaxDoubles;
 constexpr int kFtabOff = 3 * kMtabMaxDoubles;
-constexpr int kMtabSlotDoubles = kFtabOff + kFtabMaxFloats / 2;
-static_assert((kFtabOff * 8) % 16 == 0 && (kMtabSlotDoubles * 8) % 16 == 0,
+constexpr int kDtabOff = kFtabOff + kFtabMaxFloats / 2;
+constexpr int kMtabSlotDoubles = kDtabOff + kDtabMaxFloats / 2;
+static_assert((kFtabOff * 8) % 16 == 0 && (kDtabOff * 8) % 16 == 0 && (kMtabSlotDoubles * 8) % 16 == 0,
               "the float32 tables are read as float4");
 
 // whether a fixed nu gets the float64 table, and the float32 one
@@ -455,6 +458,9 @@ SV_HD bool ftab_ok(double nu) {
 SV_HD bool mtab_est_ok(double nu, double h) {
   return nu - h > 0.0 && nu + h <= kMtabNuMax && mtab_elo(nu - h) >= kMtabEloMin;
 }
+// an estimated nu of this evaluation in the split forms: float32 tables of
+// nu (D, g) and of dM/dnu, whose node values take the series at nu +- h
+SV_HD bool ftab_est_ok(double nu, double h) { return ftab_ok(nu) && ftab_ok(nu - h) && ftab_ok(nu + h); }
 SV_HD int ftab_intervals(int elo) { return 2 * (kFtabEhi - elo); }
 // the first octave whose F is e^c M (at least 1)
 SV_HD int ftab_switch(double nu) {
@@ -470,6 +476,8 @@ struct MaternF32 {
   int esw;            // its first octave of F = e^c M
   float s2n;          // sqrt(2 nu)
   const float4* tab;  // four float4 per interval: F, then Q (global or shared)
+  const float4* dtab; // estimated nu: two float4 per interval of dM/dnu (or null)
+  float nuf;          // nu (the factor of dSigma_nu = s2 nu dM/dnu)
 };
 
 #ifdef __CUDACC__
@@ -503,6 +511,26 @@ __device__ inline void ftab_node(double nu, int elo, int esw, int iv, int j, dou
   const double ec = exp(c);
   F = e < esw ? matern_deficit_series(c, nu) : ec * M;
   Q = ec * G;
+}
+
+// node j of interval iv of the dM/dnu table of an estimated nu: the
+// reference's central difference (M(nu + h, r) - M(nu - h, r)) / 2h at
+// r = c / sqrt(2 nu) (_matern_general.py:170-176), from the deficits' series
+// below 2^esw (M(nu + h) - M(nu - h) = D(nu - h) - D(nu + h), both accurate
+// however small) and times e^c from the Bessel routine above
+__device__ inline double ftab_dnu_node(double nu, double h, int elo, int esw, int iv, int j) {
+  const int e = elo + iv / 2, half = iv & 1;
+  const double tj = cospi((j + 0.5) / kFtabN);
+  const double m = half ? (tj - kMtabO1) / kMtabS1 : (tj - kMtabO0) / kMtabS0;
+  const double c = ldexp(m, e);
+  const double r = c / sqrt(2.0 * nu);
+  const double nup = nu + h, num = nu - h;
+  const double cp = sqrt(2.0 * nup) * r, cmm = sqrt(2.0 * num) * r;
+  if (e < esw) return (matern_deficit_series(cmm, num) - matern_deficit_series(cp, nup)) / (2.0 * h);
+  double Mp, Mm, G;
+  matern_general_MG_c(cp, nup, matern_log_coef(nup), Mp, G);
+  matern_general_MG_c(cmm, num, matern_log_coef(num), Mm, G);
+  return exp(c) * ((Mp - Mm) / (2.0 * h));
 }
 
 // Chebyshev coefficient j of an interval from its kFtabN node values f
@@ -564,6 +592,19 @@ __device__ __forceinline__ float matern_deficit_f32(const MaternF32& mf, float r
   const float4* p = mf.tab + 4 * iv;
   const float F = ftab_clenshaw(p[0], p[1], t);
   return e < mf.esw ? F : 1.0f - expf(-c) * F;
+}
+
+// dM/dnu of an estimated nu (mf.dtab set; r floored as above: 0 below 1e-7)
+__device__ __forceinline__ float matern_dnu_f32(const MaternF32& mf, float r) {
+  if (r < 1e-7f) return 0.0f;
+  const float c = mf.s2n * r;
+  float t;
+  int e;
+  const int iv = ftab_locate(mf.elo, c, t, e);
+  if (iv < 0) return 0.0f;
+  const float4* p = mf.dtab + 2 * iv;
+  const float F = ftab_clenshaw(p[0], p[1], t);
+  return e < mf.esw ? F : expf(-c) * F;
 }
 
 __device__ __forceinline__ float matern_g_f32(const MaternF32& mf, float r) {

@@ -13,7 +13,9 @@ namespace sv {
 // one pass over the neighbours j with row i's coordinates, the squared
 // differences and the d sums in registers (DR >= d, zero padded); the same
 // roundings in the same order as a pass per l.  store(1 + l, value) writes
-// the value into column 1 + l of the caller's right-hand sides.
+// the value into column 1 + l of the caller's right-hand sides.  An
+// estimated nu (mf.dtab set) also takes its row in the same pass:
+//   R(1 + d, i) = s2 nu sum_{j != i} dM/dnu_ij a_j   (_matern_general.py:177).
 template <int DR, typename Store>
 __device__ __forceinline__ void split_dsig_row(int i, int K, int d, const MaternF32& mf, float s2f,
                                                const float* u, const float* a32, Store store) {
@@ -23,8 +25,9 @@ __device__ __forceinline__ void split_dsig_row(int i, int K, int d, const Matern
     ui[l] = l < d ? u[l * 32 + i] : 0.0f;
     S[l] = 0.0f;
   }
+  float Snu = 0.0f;
   for (int j = 0; j < K; ++j) {
-    if (j == i) continue;  // g_ii a_i (u_i - u_i)^2 adds exactly nothing
+    if (j == i) continue;  // g_ii a_i (u_i - u_i)^2 and dM/dnu_ii add exactly nothing
     float sq[DR];
     float r2 = 0.0f;
 #pragma unroll
@@ -34,7 +37,9 @@ __device__ __forceinline__ void split_dsig_row(int i, int K, int d, const Matern
         r2 = fmaf(df, df, r2);
         sq[l] = df * df;
       }
-    const float c = matern_g_f32(mf, sqrtf(r2)) * a32[j];
+    const float r = sqrtf(r2);
+    const float c = matern_g_f32(mf, r) * a32[j];
+    if (mf.dtab) Snu = fmaf(matern_dnu_f32(mf, r), a32[j], Snu);
 #pragma unroll
     for (int l = 0; l < DR; ++l)
       if (l < d) S[l] = fmaf(c, sq[l], S[l]);
@@ -42,6 +47,7 @@ __device__ __forceinline__ void split_dsig_row(int i, int K, int d, const Matern
 #pragma unroll
   for (int l = 0; l < DR; ++l)
     if (l < d) store(1 + l, -s2f * S[l]);
+  if (mf.dtab) store(1 + d, s2f * mf.nuf * Snu);
 }
 
 // The same for d > 12: row i's g_ij a_j for all j in registers, then one
@@ -50,6 +56,7 @@ template <typename Store>
 __device__ __forceinline__ void split_dsig_row_wide(int i, int K, int d, const MaternF32& mf, float s2f,
                                                     const float* u, const float* a32, Store store) {
   float cj[32];
+  float Snu = 0.0f;
 #pragma unroll
   for (int j = 0; j < 32; ++j) {
     float c = 0.0f;
@@ -59,10 +66,13 @@ __device__ __forceinline__ void split_dsig_row_wide(int i, int K, int d, const M
         const float df = u[l * 32 + i] - u[l * 32 + j];
         r2 = fmaf(df, df, r2);
       }
-      c = matern_g_f32(mf, sqrtf(r2)) * a32[j];
+      const float r = sqrtf(r2);
+      c = matern_g_f32(mf, r) * a32[j];
+      if (mf.dtab) Snu = fmaf(matern_dnu_f32(mf, r), a32[j], Snu);
     }
     cj[j] = c;
   }
+  if (mf.dtab) store(1 + d, s2f * mf.nuf * Snu);
   for (int l = 0; l < d; ++l) {
     const float uil = u[l * 32 + i];
     float s = 0.0f;

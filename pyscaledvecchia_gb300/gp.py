@@ -56,9 +56,10 @@ class ScaledVecchiaGP:
     float32 from centred coordinates and the correlation deficit, the
     factorisation, solves and sums in float64; ill-conditioned blocks are
     redone in float64).  The likelihood takes the split form for the closed
-    forms and for a fixed nu of the library's float32 table (at most 8 and
-    at least 1e-3 from an integer), the prediction blocks for the closed
-    forms; any other nu runs in float64.
+    forms, for a fixed nu of the library's float32 table (at most 8 and at
+    least 1e-3 from an integer) and for an estimated nu whose value and
+    value +- 1e-3 are such (at each iterate), the prediction blocks for the
+    closed forms; any other nu runs in float64.
     """
 
     m_est: int = 30

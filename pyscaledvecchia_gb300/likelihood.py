@@ -44,8 +44,12 @@ def split_nu(nu, estimate_nu=False):
     """Whether the split forms assemble this nu in float32: a closed form
     (0.5, 1.5, 2.5), or a fixed nu of the library's float32 table (at most 8
     and at least 1e-3 from an integer: near an integer the table's series
-    loses its digits).  Any other nu runs the float64 kernels."""
-    if estimate_nu or nu is None:
+    loses its digits).  Any other fixed nu runs the float64 kernels.  An
+    estimated nu takes the split kernels, which decide at each theta (nu,
+    nu - 1e-3 and nu + 1e-3 with float32 tables, or the float64 pass)."""
+    if estimate_nu:
+        return True
+    if nu is None:
         return False
     if float(nu) in (0.5, 1.5, 2.5):
         return True

@@ -5,6 +5,9 @@ for the closed forms and for general smoothness values.  M_nu is the
 reference's Matern (_matern_general.py:92-116):
   M(r) = 2^(1-nu)/Gamma(nu) c^nu K_nu(c),  c = sqrt(2 nu) r,
   g(r) = -(2 nu / c) 2^(1-nu)/Gamma(nu) c^nu K_{nu-1}(c).
+For the general values also dM/dnu as the reference's central difference
+(M_{nu+h}(r) - M_{nu-h}(r)) / 2h, h = 1e-3 (_matern_general.py:170-176),
+what the split kernels assemble an estimated nu's row with.
 Run from the repository root: python tests/golden/make_matern_f32.py"""
 import os
 
@@ -25,6 +28,17 @@ def deficit_and_g(r, nu):
     return float(1 - M), float(g)
 
 
+def matern_M(r, nu):
+    r = mp.mpf(float(r))
+    nu = mp.mpf(nu)
+    c = mp.sqrt(2 * nu) * r
+    return 2 ** (1 - nu) / mp.gamma(nu) * c ** nu * mp.besselk(nu, c)
+
+
+def dnu(r, nu, h=1e-3):
+    return float((matern_M(r, nu + mp.mpf(h)) - matern_M(r, nu - mp.mpf(h))) / (2 * mp.mpf(h)))
+
+
 def main():
     out = {}
     for nu in NUS:
@@ -37,6 +51,8 @@ def main():
         out["r_%g" % nu] = r
         out["D_%g" % nu] = vals[:, 0]
         out["g_%g" % nu] = vals[:, 1]
+        if nu not in (0.5, 1.5, 2.5):
+            out["dnu_%g" % nu] = np.array([dnu(x, nu) for x in r])
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "matern_f32.npz")
     np.savez_compressed(path, nus=np.array(NUS), **out)
     print("wrote", path)

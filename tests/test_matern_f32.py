@@ -79,3 +79,32 @@ def test_no_table_near_integers(nu):
     from pyscaledvecchia_gb300._covariance import _elementwise
     with pytest.raises(ValueError):
         _elementwise(np.array([0.5]), nu, 2, 1)
+
+
+@pytest.mark.gpu
+def test_float32_dnu_against_golden():
+    """dM/dnu of an estimated nu (which = 4): the float32 table of the
+    reference's central difference against 40-digit values.  It changes sign
+    as c grows, so the error is measured against the local scale: the
+    largest |dM/dnu| at the golden points with c within a factor 2; bound 16
+    float32 ulp of that scale (the table's end, c >= 64, gives 0)."""
+    from pyscaledvecchia_gb300._covariance import _elementwise
+    z, nus = _golden()
+    worst = {}
+    for nu in nus:
+        if nu in (0.5, 1.5, 2.5):
+            continue
+        r, dn = z["r_%g" % nu], z["dnu_%g" % nu]
+        if abs(nu - 1e-3 - round(nu - 1e-3)) < 1e-3 or abs(nu + 1e-3 - round(nu + 1e-3)) < 1e-3:
+            with pytest.raises(ValueError):  # nu +- h within 1e-3 of an integer: no table
+                _elementwise(r, nu, 4, 1)
+            continue
+        dd = _elementwise(r, nu, 4, 1)
+        c = np.sqrt(2.0 * nu) * r
+        scale = np.array([np.abs(dn[(c >= ci / 2) & (c <= ci * 2)]).max() for ci in c])
+        inside = c < 64.0
+        e = np.abs(dd - dn)[inside] / scale[inside] / ULP
+        assert e.max() <= 16.0, (nu, float(e.max()), float(c[inside][np.argmax(e)]))
+        assert np.all(np.abs(dd[~inside]) <= 1e-20)
+        worst[nu] = float(e.max())
+    print("worst dnu error in ulp of the local scale:", worst)

@@ -191,3 +191,64 @@ def test_split_general_nu(form):
         np.testing.assert_array_equal(g, one[nu][1])
         np.testing.assert_array_equal(F, one[nu][2])
         assert int(BL.last_info[i, 3]) < Xo.shape[0] // 10
+
+
+@pytest.mark.parametrize("form", SPLIT_FORMS)
+@pytest.mark.parametrize("nu", [0.8, 1.7, 2.0])
+def test_split_estimated_nu(form, nu):
+    """An estimated nu in the split forms: at each theta the split kernels
+    take float32 tables of D and g at nu and of the central difference dM/dnu
+    (nu +- 1e-3) for the extra dSigma_nu a row.  Against the float64 form:
+    the bounds of test_split_matches_float64.  At nu = 2.0 (within 1e-3 of an
+    integer) there are no float32 tables: every block goes to the float64
+    pass (counted as redone) and the result is the float64 form's to 1e-12.
+    A batch of the problem gives the one-problem bits."""
+    from pyscaledvecchia_gb300.batched import BatchedLikelihood, BatchProblem
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    from pyscaledvecchia_gb300.ordering import _nn_groups
+    Xo, y, Z, nn, theta = _inputs(3000, 4, 20, 1e-3, seed=91)
+    th = np.concatenate([theta[:-1], [math.log(nu)], theta[-1:]])
+    groups = _nn_groups(nn, 20)
+    prob = DeviceProblem(Xo, y, Z, groups)
+    a = prob.evaluate(th, None, estimate_nu=True)
+    b = prob.evaluate(th, None, estimate_nu=True, precision=form, team_lanes=16)
+    redone = int(prob.last_info[3])
+    if nu == 2.0:
+        assert redone == Xo.shape[0]
+        assert abs(b[0] - a[0]) <= 1e-12 * abs(a[0]), (b[0], a[0])
+        np.testing.assert_allclose(b[1], a[1], rtol=1e-10, atol=1e-10 * np.abs(a[1]).max())
+        np.testing.assert_allclose(b[2], a[2], rtol=1e-10, atol=1e-10 * np.abs(a[2]).max())
+    else:
+        assert b[0] != a[0]  # the split form ran
+        assert redone < Xo.shape[0] // 10
+        assert abs(b[0] - a[0]) <= 5e-6 * abs(a[0]), (b[0], a[0])
+        assert np.abs(b[1] - a[1]).max() <= 1e-3 * np.abs(a[1]).max()
+        assert np.abs(b[2] - a[2]).max() <= 1e-3 * np.abs(a[2]).max()
+        np.testing.assert_allclose(b[3], a[3], rtol=2e-4, atol=1e-6)
+    BL = BatchedLikelihood([BatchProblem(Xo, y, Z, groups, nu=None, estimate_nu=True)],
+                           precisions=(form,), team_lanes=16)
+    st, ll, g, F, beta = BL.evaluate([th])[0]
+    assert st == 0 and ll == b[0]
+    np.testing.assert_array_equal(g, b[1])
+    np.testing.assert_array_equal(F, b[2])
+
+
+def test_split_estimated_nu_against_oracle(oracle):
+    """The split form with an estimated nu (nu = 1.3) against the oracle
+    (scipy's kv and the reference's central difference), with the bounds of
+    test_split_against_oracle."""
+    from pyscaledvecchia_gb300.likelihood import DeviceProblem
+    from pyscaledvecchia_gb300.ordering import _nn_groups
+    Xo, yo, Zo, nn, theta = _inputs(1500, 3, 15, 1e-3, seed=92)
+    th = np.concatenate([theta[:-1], [math.log(1.3)], theta[-1:]])
+    groups = _nn_groups(nn, 15)
+    prob = DeviceProblem(Xo, yo, Zo, groups)
+    ll, g, F, b = prob.evaluate(th, None, estimate_nu=True, precision="split")
+    assert ll != prob.evaluate(th, None, estimate_nu=True)[0]  # the split form ran
+    ll_o, g_o, F_o, b_o = oracle.vecchia_loglik_np(th, Xo, yo, Zo, groups, None,
+                                                    estimate_nu=True)[:4]
+    assert abs(ll - ll_o) <= 1e-7 * abs(ll_o), (ll, ll_o)
+    sd = np.sqrt(np.diag(F_o))
+    assert np.all(np.abs(g - g_o) <= 1e-3 * sd), np.abs(g - g_o) / sd
+    assert np.abs(F - F_o).max() <= 1e-5 * np.abs(F_o).max()
+    np.testing.assert_allclose(b, b_o, rtol=1e-4, atol=1e-8)
