@@ -16,9 +16,9 @@ namespace sv {
 // the value into column 1 + l of the caller's right-hand sides.  An
 // estimated nu (mf.dtab set) also takes its row in the same pass:
 //   R(1 + d, i) = s2 nu sum_{j != i} dM/dnu_ij a_j   (_matern_general.py:177).
-template <int DR, typename Store>
-__device__ __forceinline__ void split_dsig_row(int i, int K, int d, const MaternF32& mf, float s2f,
-                                               const float* u, const float* a32, Store store) {
+template <int DR, bool EST, typename Store>
+__device__ __forceinline__ void split_dsig_row_t(int i, int K, int d, const MaternF32& mf, float s2f,
+                                                 const float* u, const float* a32, Store store) {
   float ui[DR], S[DR];
 #pragma unroll
   for (int l = 0; l < DR; ++l) {
@@ -39,7 +39,7 @@ __device__ __forceinline__ void split_dsig_row(int i, int K, int d, const Matern
       }
     const float r = sqrtf(r2);
     const float c = matern_g_f32(mf, r) * a32[j];
-    if (mf.dtab) Snu = fmaf(matern_dnu_f32(mf, r), a32[j], Snu);
+    if (EST) Snu = fmaf(matern_dnu_f32(mf, r), a32[j], Snu);
 #pragma unroll
     for (int l = 0; l < DR; ++l)
       if (l < d) S[l] = fmaf(c, sq[l], S[l]);
@@ -47,14 +47,25 @@ __device__ __forceinline__ void split_dsig_row(int i, int K, int d, const Matern
 #pragma unroll
   for (int l = 0; l < DR; ++l)
     if (l < d) store(1 + l, -s2f * S[l]);
-  if (mf.dtab) store(1 + d, s2f * mf.nuf * Snu);
+  if (EST) store(1 + d, s2f * mf.nuf * Snu);
+}
+
+// the pass above, the estimated-nu row taken when mf.dtab is set (one test
+// per row, outside the loop over the neighbours)
+template <int DR, typename Store>
+__device__ __forceinline__ void split_dsig_row(int i, int K, int d, const MaternF32& mf, float s2f,
+                                               const float* u, const float* a32, Store store) {
+  if (mf.dtab)
+    split_dsig_row_t<DR, true>(i, K, d, mf, s2f, u, a32, store);
+  else
+    split_dsig_row_t<DR, false>(i, K, d, mf, s2f, u, a32, store);
 }
 
 // The same for d > 12: row i's g_ij a_j for all j in registers, then one
 // pass per coordinate.
-template <typename Store>
-__device__ __forceinline__ void split_dsig_row_wide(int i, int K, int d, const MaternF32& mf, float s2f,
-                                                    const float* u, const float* a32, Store store) {
+template <bool EST, typename Store>
+__device__ __forceinline__ void split_dsig_row_wide_t(int i, int K, int d, const MaternF32& mf, float s2f,
+                                                      const float* u, const float* a32, Store store) {
   float cj[32];
   float Snu = 0.0f;
 #pragma unroll
@@ -68,11 +79,11 @@ __device__ __forceinline__ void split_dsig_row_wide(int i, int K, int d, const M
       }
       const float r = sqrtf(r2);
       c = matern_g_f32(mf, r) * a32[j];
-      if (mf.dtab) Snu = fmaf(matern_dnu_f32(mf, r), a32[j], Snu);
+      if (EST) Snu = fmaf(matern_dnu_f32(mf, r), a32[j], Snu);
     }
     cj[j] = c;
   }
-  if (mf.dtab) store(1 + d, s2f * mf.nuf * Snu);
+  if (EST) store(1 + d, s2f * mf.nuf * Snu);
   for (int l = 0; l < d; ++l) {
     const float uil = u[l * 32 + i];
     float s = 0.0f;
@@ -85,6 +96,15 @@ __device__ __forceinline__ void split_dsig_row_wide(int i, int K, int d, const M
     }
     store(1 + l, -s2f * s);
   }
+}
+
+template <typename Store>
+__device__ __forceinline__ void split_dsig_row_wide(int i, int K, int d, const MaternF32& mf, float s2f,
+                                                    const float* u, const float* a32, Store store) {
+  if (mf.dtab)
+    split_dsig_row_wide_t<true>(i, K, d, mf, s2f, u, a32, store);
+  else
+    split_dsig_row_wide_t<false>(i, K, d, mf, s2f, u, a32, store);
 }
 
 // L is stored packed by columns with capacity kc (the launch's largest K):
