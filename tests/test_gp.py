@@ -114,6 +114,15 @@ def test_estimated_nu_on_matern_draw():
     assert 0.5 < gp.nu_ < 5.0
     assert gp.nugget_ == pytest.approx(0.02, rel=0.5)
     assert gp.relevance_[0] > gp.relevance_[1]
+    # the split form with nu estimated (float32 tables of D, g and dM/dnu at
+    # each iterate) fits the same model: nu, the nugget and the loglik within
+    # the split form's reach of the float64 fit
+    gs = GP(m_est=25, m_pred=50, nu=None, n_est=500, trend="zero", var_correction=False,
+            random_state=0, precision="split").fit(X, y)
+    assert gs._estimate_nu is True
+    assert gs.nu_ == pytest.approx(gp.nu_, rel=1e-2)
+    assert gs.nugget_ == pytest.approx(gp.nugget_, rel=1e-2)
+    assert abs(gs.loglik_ - gp.loglik_) <= 1e-4 * abs(gp.loglik_)
 
 
 # ---------------------------------------------------------------------------
