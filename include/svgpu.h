@@ -379,12 +379,14 @@ int sv_encoder_adam(float* params, const float* grad, float* m, float* v, uint16
 int sv_matern_eval(const double* r, int64_t n, double nu, int32_t which, int32_t general,
                    double* out, sv_stream_t stream);
 
-/* The Chebyshev table of M and g of a fixed smoothness nu without a closed
+/* The Chebyshev tables of M and g of a fixed smoothness nu without a closed
  * form (0 < nu <= 10) that the likelihood builds for such a nu (16-term
  * series of e^c M(c) and e^c g(c) on half-octave intervals of
- * c = sqrt(2 nu) r), into device float64[sv_matern_table_doubles()], for
+ * c = sqrt(2 nu) r; for nu <= 8 at least 1e-3 from an integer also the
+ * float32 table of the deficit and g the split forms use), into device
+ * float64[sv_matern_table_doubles()] (16-byte aligned), for
  * sv_pred_desc.matern_table.  SV_EINVAL for a nu without a table or a
- * smaller buffer. */
+ * smaller or misaligned buffer. */
 int64_t sv_matern_table_doubles(void);
 int sv_matern_table(double nu, double* table, int64_t table_doubles, sv_stream_t stream);
 
@@ -434,13 +436,14 @@ typedef struct sv_pred_desc {
   int32_t general;  /* 1: Bessel Matern                                */
   int32_t target_nugget; /* 1: the target row carries the nugget too     */
                          /*    (prior / unconditional draws)              */
-  int32_t precision;     /* 0: float64; 1: split (closed-form nu only,   */
-                         /*    float64 otherwise): entries below the      */
-                         /*    diagonal from coordinates centred on the   */
-                         /*    target as float32 (hi, lo) pairs and the   */
-                         /*    float32 correlation deficit, one float64   */
-                         /*    FMA each; diagonal, LDL^T and solves in    */
-                         /*    float64                                    */
+  int32_t precision;     /* 0: float64; 1: split (closed-form nu, or a   */
+                         /*    general nu whose matern_table holds a      */
+                         /*    float32 part; float64 otherwise): entries  */
+                         /*    below the diagonal from coordinates        */
+                         /*    centred on the target as float32 (hi, lo)  */
+                         /*    pairs and the float32 correlation deficit, */
+                         /*    one float64 FMA each; diagonal, LDL^T and  */
+                         /*    solves in float64                          */
   double nu;
   double split_rho_min;  /* split: a block whose smallest pivot ratio     */
                          /*    d_k / Sigma_kk falls below this (<= 0:     */

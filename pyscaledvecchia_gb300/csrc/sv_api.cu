@@ -115,6 +115,17 @@ __global__ void k_matern_table1(double nu, double* tab) {
   mtab_build_interval(nu, blockIdx.x, fm, fg, tab);
 }
 
+// its float32 part (the split prediction blocks): CTA (interval) of kFtabN
+// threads, as the likelihood's float32 tables
+__global__ void k_matern_ftab1(double nu, float* ft) {
+  __shared__ double ff[kFtabN], fq[kFtabN];
+  const int iv = blockIdx.x, j = threadIdx.x;
+  ftab_node(nu, mtab_elo(nu), ftab_switch(nu), iv, j, ff[j], fq[j]);
+  __syncthreads();
+  ft[(size_t)iv * 2 * kFtabN + j] = ftab_coef(ff, j);
+  ft[(size_t)iv * 2 * kFtabN + kFtabN + j] = ftab_coef(fq, j);
+}
+
 __global__ void k_bessel_k(const double* x, int64_t n, double nu, double* out) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -212,12 +223,19 @@ extern "C" int sv_matern_eval(const double* r, int64_t n, double nu, int32_t whi
   return SV_OK;
 }
 
-extern "C" int64_t sv_matern_table_doubles(void) { return sv::kMtabMaxDoubles; }
+extern "C" int64_t sv_matern_table_doubles(void) { return sv::kMtabMaxDoubles + sv::kFtabMaxFloats / 2; }
 
 extern "C" int sv_matern_table(double nu, double* table, int64_t table_doubles, sv_stream_t stream) {
-  if (!table || !sv::mtab_ok(nu) || table_doubles < sv::kMtabMaxDoubles) return SV_EINVAL;
-  sv::k_matern_table1<<<sv::mtab_intervals(sv::mtab_elo(nu)), sv::kMtabN, 0, (cudaStream_t)stream>>>(nu, table);
+  if (!table || !sv::mtab_ok(nu) || table_doubles < sv_matern_table_doubles()) return SV_EINVAL;
+  if ((reinterpret_cast<uintptr_t>(table) & 15) != 0) return SV_EINVAL;
+  cudaStream_t st = (cudaStream_t)stream;
+  sv::k_matern_table1<<<sv::mtab_intervals(sv::mtab_elo(nu)), sv::kMtabN, 0, st>>>(nu, table);
   SV_CUDA_TRY(cudaGetLastError());
+  if (sv::ftab_ok(nu)) {
+    sv::k_matern_ftab1<<<sv::ftab_intervals(sv::mtab_elo(nu)), sv::kFtabN, 0, st>>>(
+        nu, reinterpret_cast<float*>(table + sv::kMtabMaxDoubles));
+    SV_CUDA_TRY(cudaGetLastError());
+  }
   return SV_OK;
 }
 

@@ -40,12 +40,14 @@ struct PredArgs {
   int split;       // 1: float32 assembly (closed-form nu only)
   double rho_min;  // split: smallest pivot ratio d_k / Sigma_kk kept
   double nu;
-  const double* tab;  // general nu: its Matern table (or null: K_nu per entry)
+  const double* tab;    // general nu: its Matern table (or null: K_nu per entry)
+  const float4* ftab;   // general nu, split: the table's float32 part (or null)
 };
 
 struct PredPrm {
   double s2, tau;
   MaternMode mm;
+  MaternF32 mf;  // the split form's float32 Matern: a closed form or the table
   double invlam[64];
 };
 
@@ -67,6 +69,15 @@ __device__ void pred_params(const PredArgs& A, PredPrm* prm) {
     mm.elo_p = mm.elo_m = 0;
     mm.s2n_p = mm.s2n_m = 0.0;
     prm->mm = mm;
+    MaternF32 mf;
+    mf.code = A.closed >= 0 ? A.closed : (A.ftab ? 3 : -1);
+    mf.elo = A.ftab ? mtab_elo(A.nu) : 0;
+    mf.esw = ftab_switch(A.nu);
+    mf.s2n = (float)sqrt(2.0 * A.nu);
+    mf.tab = A.closed >= 0 ? nullptr : A.ftab;
+    mf.dtab = nullptr;
+    mf.nuf = (float)A.nu;
+    prm->mf = mf;
   }
   for (int l = threadIdx.x; l < A.d; l += blockDim.x) prm->invlam[l] = exp(-A.theta[1 + l]);
   __syncthreads();
@@ -114,7 +125,7 @@ __device__ bool pred_split_factor(const PredArgs& A, const PredPrm* prm, int K, 
   for (int i = lane; i < K; i += T) rb[i] = dbits(A.rho_min * (s2 * (1.0 + tau * mask[i])));
   Team<T>::sync();
   if (flag[1]) return false;
-  const int code = A.closed;
+  const MaternF32 mf = prm->mf;
   const int npair = K * (K + 1) / 2;
   for (int t = lane; t < npair; t += T) {
     int i, j;
@@ -133,7 +144,7 @@ __device__ bool pred_split_factor(const PredArgs& A, const PredPrm* prm, int K, 
         const float df = (a.x - c.x) + (a.y - c.y);
         r2 = fmaf(df, df, r2);
       }
-      v = fma(-s2, f2d_int(matern_deficit_f32(code, sqrtf(r2))), s2);
+      v = fma(-s2, f2d_int(matern_deficit_f32(mf, sqrtf(r2))), s2);
     }
     Lp[t] = v;
   }
@@ -494,8 +505,10 @@ extern "C" int sv_predict_blocks(const sv_pred_desc* D, const double* theta, con
   A.target_nugget = D->target_nugget;
   A.nu = D->nu;
   A.tab = D->matern_table;
+  // the float32 part of the table (built where the nu has one)
+  A.ftab = (D->matern_table && ftab_ok(D->nu)) ? (const float4*)(D->matern_table + kMtabMaxDoubles) : nullptr;
   if (D->precision < 0 || D->precision > 1) return SV_EINVAL;
-  A.split = (D->precision == 1 && A.closed >= 0) ? 1 : 0;
+  A.split = (D->precision == 1 && (A.closed >= 0 || A.ftab)) ? 1 : 0;
   A.rho_min = D->split_rho_min > 0.0 ? D->split_rho_min : 1e-4;
   int dev = 0, maxsm = 0;
   cudaGetDevice(&dev);

@@ -110,16 +110,26 @@ def test_split_predictions_small(nu, m):
     assert em.max() < MEAN_TOL_MAX and es.max() < SD_TOL_MAX, (em.max(), es.max())
 
 
-def test_bessel_nu_runs_in_float64():
-    """No float32 form of K_nu: the split setting predicts in float64, bit
-    for bit."""
-    gp, Xte = _small(1.75, n=1500)
-    mu64, sd64 = gp.predict(Xte, return_std=True, m=30)
-    gp.precision = "split"
-    mu32, sd32 = gp.predict(Xte, return_std=True, m=30)
-    np.testing.assert_array_equal(mu32, mu64)
-    np.testing.assert_array_equal(sd32, sd64)
-    assert gp.pred_stats_["redone_float64"] == 0
+@pytest.mark.parametrize("nu", [1.75, 9.3])
+def test_bessel_nu(nu):
+    """A general nu: 1.75 has a float32 table (the split blocks take it,
+    within this file's bounds, warp and CTA blocks); 9.3 has none (above 8),
+    so the split setting predicts in float64, bit for bit."""
+    gp, Xte = _small(nu, n=1500)
+    for m in (30, 60):
+        mu64, sd64 = gp.predict(Xte, return_std=True, m=m)
+        gp.precision = "split"
+        mu32, sd32 = gp.predict(Xte, return_std=True, m=m)
+        gp.precision = "float64"
+        if nu > 8.0:
+            np.testing.assert_array_equal(mu32, mu64)
+            np.testing.assert_array_equal(sd32, sd64)
+            assert gp.pred_stats_["redone_float64"] == 0
+            continue
+        assert np.any(mu32 != mu64)  # the split form ran
+        assert gp.pred_stats_["redone_float64"] < Xte.shape[0] // 10
+        em, es = _errors(mu32, sd32, mu64, sd64)
+        assert em.max() < MEAN_TOL_MAX and es.max() < SD_TOL_MAX, (em.max(), es.max())
 
 
 @pytest.mark.parametrize("m", [20, 60])
@@ -167,3 +177,29 @@ def test_guard_redoes_every_block_in_float64(m):
     # the default threshold keeps most blocks in the split form
     assert split[3] < nte // 2
     assert math.isfinite(float(split[1].sum()))
+
+
+def test_split_predictions_general_nu():
+    """A general fitted nu (0.8): the split prediction blocks take the float32
+    part of the model's Matern table (sv_matern_table) and stay within this
+    file's bounds of the float64 predictions; a nu without a float32 table
+    (2.0, within 1e-3 of an integer) predicts in float64 in both forms."""
+    from pyscaledvecchia_gb300 import ScaledVecchiaGP
+    rng = np.random.default_rng(21)
+    X = rng.random((3000, 3))
+    y = np.sin(4 * X[:, 0]) + X[:, 1] ** 2 + 0.05 * rng.standard_normal(3000)
+    Xq = rng.random((1000, 3))
+    for nu in (0.8, 2.0):
+        gp = ScaledVecchiaGP(nu=nu, m_est=20, m_pred=60, var_correction=False).fit(X, y)
+        mu64, sd64 = gp.predict(Xq, return_std=True)
+        gp.precision = "split"
+        mu, sd = gp.predict(Xq, return_std=True)
+        if nu == 2.0:
+            np.testing.assert_array_equal(mu, mu64)
+            np.testing.assert_array_equal(sd, sd64)
+            continue
+        assert np.any(mu != mu64)  # the split form ran
+        assert gp.pred_stats_["redone_float64"] < 100
+        em, es = _errors(mu, sd, mu64, sd64)
+        assert em.max() <= MEAN_TOL_MAX and np.median(em) <= MEAN_TOL_MEDIAN, (em.max(), np.median(em))
+        assert es.max() <= SD_TOL_MAX, es.max()
