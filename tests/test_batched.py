@@ -89,8 +89,9 @@ def test_batched_float64_equals_single(need_grad):
 
 def test_batched_split_equals_single():
     from pyscaledvecchia_gb300.batched import BatchedLikelihood
-    # closed-form nu, no estimated nu: the split kernels take every block <= 32
-    items = [it for it in _mixed_batch() if not it[0].estimate_nu and it[0].nu in (0.5, 1.5, 2.5)]
+    # every problem of the mixed batch: closed forms, a fixed general nu and
+    # an estimated nu (float32 tables), blocks beyond 32 points (float64)
+    items = _mixed_batch()
     # bit for bit at the same team width (the autotuner may pick another
     # width per problem on its own)
     for lanes in (8, 16):
