@@ -515,15 +515,15 @@ int sv_joint_var_diag(int64_t npred, int64_t nobs, int32_t k, int32_t ldnbr, con
 /* Measurement                                                             */
 /* ---------------------------------------------------------------------- */
 
-/* No reference counterpart: a float64 FMA throughput probe (8 independent
- * chains of `iters` FMAs in each of sv_fp64_probe_threads() threads, one
- * double written per thread to out), used to state the float64 peak that the
- * block kernels are measured against. */
 /* No reference counterpart: *out = 1 when the current device reads ordinary
  * (pageable) host memory coherently through the host's page tables (a
  * Grace-Blackwell chip-to-chip link), else 0. */
 int sv_device_reads_host_memory(int32_t* out);
 
+/* No reference counterpart: a float64 FMA throughput probe (8 independent
+ * chains of `iters` FMAs in each of sv_fp64_probe_threads() threads, one
+ * double written per thread to out), used to state the float64 peak that the
+ * block kernels are measured against. */
 int64_t sv_fp64_probe_threads(void);
 int sv_fp64_fma_probe(double* out, int32_t iters, sv_stream_t stream);
 
