@@ -177,16 +177,16 @@ def test_problem_sharded_fits_give_every_rank_every_model(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("nu", [2.5, 0.8])
+@pytest.mark.parametrize("nu", [2.5, 0.8, None])
 @pytest.mark.parametrize("precision", ["float64", "split"])
 @pytest.mark.parametrize("nshard", [2, 3])
 def test_device_shards_give_the_one_gpu_bits(precision, nshard, nu):
     """Shards of one problem run stage by stage on the one GPU, the exchanges
     done in between (MAX of the chunk tables, SUM of the partial-sum rows):
     the result is sv_vecchia_loglik's bit for bit, for a problem whose
-    duplicated rows need chunk-wide jitter as well; at nu = 0.8 each shard
-    builds the Matern tables in its first stage and its later passes read
-    them."""
+    duplicated rows need chunk-wide jitter as well; at nu = 0.8 and with nu
+    estimated (None: nu = 1.3 in theta) each shard builds the Matern tables
+    in its first stage and its later passes read them."""
     import torch
 
     from pyscaledvecchia_gb300.likelihood import DeviceProblem
@@ -200,15 +200,17 @@ def test_device_shards_give_the_one_gpu_bits(precision, nshard, nu):
             X[6000:6300] = X[300:600]
             tau = 1e-20
         lam = np.exp(rng.uniform(math.log(0.1), math.log(2.0), d))
-        theta = np.concatenate([[math.log(1.7)], np.log(lam), [math.log(tau)]])
+        est = nu is None
+        theta = np.concatenate([[math.log(1.7)], np.log(lam), [math.log(1.3)] if est else [],
+                                [math.log(tau)]])
         order = maximin_order(X / lam)
         nn = find_ordered_nn((X / lam)[order], m)
         y = rng.standard_normal(n)
         prob = DeviceProblem(X[order], y[order], np.ones((n, 1)), _nn_groups(nn, m))
-        P = d + 2
-        ref = prob.evaluate(theta, nu, precision=precision, team_lanes=16)
-        probe = DeviceShard(prob, 0, 0, nu, P, precision=precision, team_lanes=16)
-        shards = [DeviceShard(prob, *partition_range(probe.parts, r, nshard), nu, P,
+        P = d + 3 if est else d + 2
+        ref = prob.evaluate(theta, nu, estimate_nu=est, precision=precision, team_lanes=16)
+        probe = DeviceShard(prob, 0, 0, nu, P, estimate_nu=est, precision=precision, team_lanes=16)
+        shards = [DeviceShard(prob, *partition_range(probe.parts, r, nshard), nu, P, estimate_nu=est,
                               precision=precision, team_lanes=16) for r in range(nshard)]
         cm = [s.stage1(theta) for s in shards]
         cmax = torch.stack(cm).max(dim=0).values.contiguous()
