@@ -161,10 +161,11 @@ typedef struct sv_loglik_desc {
                         /*   products, float64 LDL^T, solves, log-determinant  */
                         /*   and sums; 2 = split with a double-float (float32  */
                         /*   pair) factorisation and solves.  The split forms  */
-                        /*   take k+1 <= 32 blocks of a closed-form nu or a    */
-                        /*   fixed nu of the float32 table (0 < nu <= 8, at    */
-                        /*   least 1e-3 from an integer); other blocks run in  */
-                        /*   float64                                           */
+                        /*   take k+1 <= 32 blocks of a closed-form nu or of   */
+                        /*   a general nu with float32 tables (0 < nu <= 8,    */
+                        /*   at least 1e-3 from an integer; an estimated nu    */
+                        /*   at theta, with nu +- 1e-3 too); other blocks run  */
+                        /*   in float64                                        */
   int32_t team_lanes;   /* split forms: lanes per block (4, 8, 16, 32; 0 = 16) */
   double split_rho_min; /* split forms: blocks whose smallest pivot ratio     */
                         /*   L_kk^2 / Sigma_kk is below this (0 = 1e-4) are    */
