@@ -86,6 +86,8 @@ class ScaledVecchiaGP:
     d_: int = field(default=None, init=False, repr=False)
     _estimate_nu: bool = field(default=False, init=False, repr=False)
     _nu_fit: float = field(default=None, init=False, repr=False)
+    # (nu, device Matern table) of the last general nu predicted with
+    _mtab_cache: tuple = field(default=None, init=False, repr=False, compare=False)
 
     def _precision(self):
         if self.precision not in ("float64", "split"):
