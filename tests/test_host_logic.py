@@ -75,3 +75,30 @@ def test_chunk_ids_number_chunks_group_by_group():
     assert ids[0] == 0 and ids[1] == 1
     big = ids[2:]
     np.testing.assert_array_equal(big, 2 + np.arange(1000) // 346)
+
+
+def test_matern_table_gates_follow_the_library():
+    """The host's gates (which fixed nu gets Matern tables, which takes the
+    split forms) use the library's limits: the float64 tables up to
+    kMtabNuMax, the float32 ones up to kFtabNuMax and at least 1e-3 from an
+    integer (csrc/sv_matern.cuh), an estimated nu always (decided on the
+    device at each theta)."""
+    import os
+    import re
+
+    from pyscaledvecchia_gb300.likelihood import matern_table_nu, split_nu
+    src = open(os.path.join(os.path.dirname(__file__), os.pardir, "pyscaledvecchia_gb300",
+                            "csrc", "sv_matern.cuh")).read()
+    mtab_max = float(re.search(r"kMtabNuMax = ([0-9.]+);", src).group(1))
+    ftab_max = float(re.search(r"kFtabNuMax = ([0-9.]+);", src).group(1))
+    assert (mtab_max, ftab_max) == (10.0, 8.0)
+    for nu in (0.5, 1.5, 2.5):
+        assert not matern_table_nu(nu) and split_nu(nu)
+    assert matern_table_nu(0.8) and split_nu(0.8)
+    assert matern_table_nu(mtab_max) and not matern_table_nu(mtab_max + 0.5)
+    assert split_nu(ftab_max - 0.5) and not split_nu(ftab_max + 0.5)
+    assert matern_table_nu(2.0) and not split_nu(2.0)          # within 1e-3 of an integer
+    assert not split_nu(1.0005) and split_nu(1.002)
+    assert not matern_table_nu(1e-12)                         # below the tables' first octave
+    assert not matern_table_nu(0.8, estimate_nu=True)         # estimated: built per theta
+    assert split_nu(None, estimate_nu=True) and not split_nu(None)
